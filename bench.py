@@ -1,0 +1,353 @@
+"""Benchmark: powder-averaged FIDs on one GB300 (workload c1 by default).
+
+Workload c1: 13C + 6 1H, IK-0 level 3 basis (dim 1156), T1/T2 relaxation,
+1000-orientation zcwn grid, 2048 steps of 5 us (seeded synthetic system).
+A step is one full powder run: every orientation's FID (2049 points) and
+their weighted FP64 sum.
+
+Reported:
+  value  orientation-FIDs/s of the FP32 exact path, inputs resident in HBM,
+         CUDA events on the engine stream around each step, L2 flushed
+         between steps (256 MiB write);
+  e2e    the same metric through the C ABI with host buffers
+         (spx_upload_system + spx_run_powder: H2D of I/Q/R/states/grid,
+         D2H of the powder FID inside the timed region);
+  roofline / cpu_baseline / clocks / gpu_launches as described in the design doc.
+
+--impl reference times the reference algorithm (the oracle's restatement of
+Spinach's default CPU branch, propagator.m + P*rho) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'powder FIDs/sec at <=1e-5 rel err vs FP64: FP32 exact, surrogate vs plain FP64'
+UNIT = 'FIDs/s'
+FID_NOTE = 'one FID = one orientation over all time steps; a powder FID of c1 is 1000 of them'
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+def dist_env():
+    return int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)), int(os.environ.get('LOCAL_RANK', 0))
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get('hbm_gbs', 6800.0), 'measured'
+    return 6800.0, 'fallback'
+
+
+def profile_traffic(name='powder_chebyshev_c1.md'):
+    """Per-launch DRAM bytes of the propagation kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, 'profiles', name)
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            if line.startswith('dram_bytes_per_full_launch:'):
+                try:
+                    return float(line.split(':', 1)[1].split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+class ClockSampler:
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), f'--query-gpu={self.FIELDS}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ''
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in (self.out or '').splitlines():
+            parts = [x.strip() for x in line.split(',')]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith('active'):
+                    reasons.add(nm)
+        if not sm:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unsampled'], 'samples': 0}
+        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(mx), 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU reference (oracle restatement of the reference's default CPU branch)
+# ---------------------------------------------------------------------------
+_CPU = {}
+
+
+def _cpu_init(wname):
+    os.environ['OPENBLAS_NUM_THREADS'] = '1'
+    os.environ['OMP_NUM_THREADS'] = '1'
+    sys.path.insert(0, os.path.join(ROOT, 'tests'))
+    from spinach_gb300 import workloads as W
+    from oracle_cases import oracle_system
+    from oracle import spinach_ref as R
+    w = getattr(W, wname)()
+    ss, I, Q = oracle_system(w)
+    par = dict(rho0=R.state(ss, *w.rho0), coil=R.state(ss, *w.coil), sweep=1 / w.dt, npoints=w.nsteps + 1)
+    _CPU.update(w=w, ss=ss, I=I, Q=Q, par=par, R=R, grid=W.zcwn_grid(w.n_orient))
+
+
+def _cpu_one(o):
+    R, g = _CPU['R'], _CPU['grid']
+    par = dict(_CPU['par'])
+    if o < 0:                       # warm-up sample: a few steps only
+        par['npoints'] = 9
+        o = -o - 1
+    R.powder_orientation_fid(_CPU['ss'], _CPU['I'], _CPU['Q'], par, (g[0][o], g[1][o], g[2][o]))
+    return o
+
+
+def cpu_pool(wname, cores):
+    ctx = mp.get_context('spawn')
+    return ctx.Pool(cores, initializer=_cpu_init, initargs=(wname,))
+
+
+def time_cpu(pool, cores, n_orient, start):
+    idx = [(start + i * 37) % n_orient for i in range(cores)]
+    t = time.perf_counter()
+    pool.map(_cpu_one, idx, chunksize=1)
+    return time.perf_counter() - t, len(idx)
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    pool = cpu_pool(args.workload, cores)
+    try:
+        for i in range(args.warmup):
+            pool.map(_cpu_one, [-(k + 1) for k in range(cores)], chunksize=1)
+        tot_t, tot_n = 0.0, 0
+        for s in range(args.steps):
+            t, n = time_cpu(pool, cores, 1000, s * cores)
+            tot_t += t
+            tot_n += n
+    finally:
+        pool.terminate()
+    v = tot_n / tot_t
+    line = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': UNIT, 'n_gpus': args.gpus,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * tot_t / args.steps,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'complex f64',
+            'data': 'synthetic (seeded workload c1)',
+            'config': {'workload': 'c1: 13C+6x1H, IK-0(3) dim 1156, T1/T2, 1000-orientation zcwn grid, 2048 steps of 5 us',
+                       'fid_unit': FID_NOTE, 'branch': 'propagator.m chopped Taylor + squaring, then P*rho (evolution.m:537-566)'},
+            'cpu_baseline': {'value': v, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+                             'sample': f'{cores} orientations per step (one per core), all 2048 steps'},
+            'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    from spinach_gb300 import engine as E, workloads as W
+    from spinach_gb300.build import build_library
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('gloo')
+    torch.cuda.set_device(local)
+    build_library()
+    w = getattr(W, args.workload)()
+    L = W.build(w)
+    grid = W.zcwn_grid(w.n_orient)
+    eng = E.Engine(local)
+    eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
+    prec = E.FP64 if args.precision == 'fp64' else E.FP32
+    dev = torch.device('cuda', local)
+    stream = torch.cuda.ExternalStream(eng.stream, device=dev)
+    with torch.cuda.stream(stream):
+        g = torch.tensor(np.stack(grid), dtype=torch.float64, device=dev).contiguous()
+        d_fid = torch.zeros(2 * (w.nsteps + 1), dtype=torch.float64, device=dev)
+        flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device=dev)
+    no = w.n_orient
+    ptr = [g[i].data_ptr() for i in range(4)]
+
+    def step():
+        eng.run_device(ptr[0], ptr[1], ptr[2], ptr[3], no, w.dt, w.nsteps, d_fid.data_ptr(), precision=prec)
+
+    for _ in range(args.warmup):
+        step()
+    eng.synchronize()
+    # timed region: per-step events, L2 flushed between steps (not timed)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    kernel_ms = []
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                evs[i][0].record(stream)
+            step()
+            with torch.cuda.stream(stream):
+                evs[i][1].record(stream)
+            st = eng.stats()             # synchronises; kernel time from the engine's own events
+            kernel_ms.append(st['kernel_ms'])
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    t_total = sum(step_ms) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_total], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt[0])
+    value = world * no * args.steps / t_total
+    stats = eng.stats()
+    fid32 = d_fid.cpu().numpy().view(np.complex128).copy()
+
+    # FP64 reference on the same GPU and inputs (the plain FP64 path)
+    t0 = time.perf_counter()
+    r64 = eng.run(*grid, w.dt, w.nsteps, precision=E.FP64)
+    fp64_s = time.perf_counter() - t0
+    rel_err = float(np.linalg.norm(fid32 - r64.fid) / np.linalg.norm(r64.fid)) if prec == E.FP32 else 0.0
+
+    # e2e through the C ABI with host buffers (upload + run incl. copies)
+    h2d = (sum(A.nnz * 16 + (A.shape[0] + 1) * 8 + A.nnz * 8 for A in [L.I, L.R, *L.terms.values()])
+           + 2 * L.dim * 16 + 4 * no * 8)
+    d2h = (w.nsteps + 1) * 16
+    e2e_t = []
+    for i in range(max(1, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
+        res = eng.run(*grid, w.dt, w.nsteps, precision=prec)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e = no / statistics.median(e2e_t)
+
+    # roofline of the dominant kernel (powder_chebyshev_kernel)
+    nnz, n = stats['nnz'], stats['dim']
+    bytes_per_mv = (12 if prec == E.FP32 else 20) * nnz + 16 * n
+    alg_bytes = bytes_per_mv * stats['matvecs']
+    k_ms = statistics.mean(kernel_ms)
+    achieved = alg_bytes / (k_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = profile_traffic()
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    fma_per_mv = 2 * (nnz - n) * (2 if prec == E.FP32 else 1) + 8 * n
+    clk = clk.summary()
+    clock_hz = (clk['sm_mhz'] or 1900.0) * 1e6
+    fma_rate = fma_per_mv * stats['matvecs'] / (k_ms / 1e3)
+    fma_peak = sm_count * 128 * clock_hz * (1 if prec == E.FP32 else 1 / 64)
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline and world == 1:
+            cores = os.cpu_count() or 1
+            pool = cpu_pool(args.workload, cores)
+            try:
+                pool.map(_cpu_one, [-(k + 1) for k in range(cores)], chunksize=1)
+                t, nn = time_cpu(pool, cores, no, 0)
+            finally:
+                pool.terminate()
+            cpu = {'value': nn / t, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+                   'sample': f'{nn} orientations of c1 (one per core, all 2048 steps), '
+                             'oracle restatement of propagator.m + P*rho in FP64'}
+        line = {
+            'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': statistics.mean(step_ms), 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'complex f32 (values hi+lo f32, FP64 powder sum)'
+            if prec == E.FP32 else 'complex f64',
+            'data': 'synthetic (seeded workload, no dataset)',
+            'config': {'workload': 'c1: 13C+6x1H, IK-0(3) dim 1156, T1/T2, 1000-orientation zcwn grid, '
+                                   '2048 steps of 5 us', 'fid_unit': FID_NOTE, 'l2': 'flushed between steps (256 MiB)',
+                       'precision': args.precision, 'chunk_steps': stats['chunk_steps'],
+                       'series_terms_max': stats['max_terms'], 'threads': stats['threads'],
+                       'parallelism': f'orientations over CTAs; {world} replica(s)'},
+            'rel_err_vs_fp64_gpu': rel_err,
+            'fp64_gpu': {'value': no / fp64_s, 'unit': UNIT, 'kernel_ms': r64.stats['kernel_ms']},
+            'e2e': {'value': e2e, 'unit': UNIT, 'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h)},
+            'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                         'frac': achieved / peak, 'traffic': traffic, 'peak_source': peak_kind,
+                         'kernel': 'powder_chebyshev_kernel', 'kernel_ms': k_ms,
+                         'algorithmic_bytes': alg_bytes, 'matvecs': stats['matvecs'],
+                         'fp32_fma_frac': fma_rate / fma_peak if prec == E.FP32 else None},
+            'cpu_baseline': cpu,
+            'clocks': clk,
+            'gpu_launches': 3 * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--workload', default='c1')
+    ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64'])
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,158 @@
+/*
+ * spinach_gpu.h -- C ABI of the GB300 powder-FID engine.
+ *
+ * Replaces, on one GPU, the static powder path of Spinach:
+ *   [fid,grid] = powder(spin_system, @acquire, parameters, assumptions)
+ *     kernel/contexts/powder.m:99-309   (orientation loop and weighted sum)
+ *     kernel/orientation.m:29-57        (H = I + sum D(k,m) Q{r}{k,m}, Hermitised)
+ *     kernel/relaxation.m:72-93         (R, added as L = H + 1i*R, acquire.m:48)
+ *     experiments/acquire.m:42-73       (dt = 1/sweep, nsteps = npoints-1)
+ *     kernel/evolution.m:503-587        (observable: fid(n) = coil'*rho(n))
+ *     kernel/propagator.m / krylov.m / step.m  (action of exp(-1i*L*dt))
+ *
+ * The caller (a MATLAB MEX gateway, Python ctypes, C or C++) passes the
+ * matrices that kernel/hamiltonian.m returns once per powder call: the
+ * isotropic part I and the non-empty rotational-basis terms Q{r}{k,m}, all
+ * in MATLAB's own sparse layout (CSC, 0-based row indices, interleaved
+ * complex double).  Inputs are read-only and owned by the caller; every
+ * output buffer is caller-allocated.  No C++ exception crosses this ABI;
+ * every entry point returns an spx_status.
+ *
+ * Threading: one handle per host thread.  A handle owns one CUDA stream and
+ * its device buffers; calls on one handle are serialised by the caller.
+ */
+#ifndef SPINACH_GPU_H
+#define SPINACH_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SPX_OK = 0,
+    SPX_ERR_INVALID_ARGUMENT = 1,   /* bad sizes, NULL pointers, non-finite input */
+    SPX_ERR_NO_SYSTEM = 2,          /* spx_run_powder before spx_upload_system */
+    SPX_ERR_CUDA = 3,               /* a CUDA runtime call failed */
+    SPX_ERR_UNSUPPORTED = 4,        /* input outside this engine's scope */
+    SPX_ERR_SERIES = 5,             /* the device series did not converge (status word set) */
+    SPX_ERR_NORM = 6,               /* |L*dt| too large (kernel/step.m:230-233 analogue) */
+    SPX_ERR_OUT_OF_MEMORY = 7,
+    SPX_ERR_INTERNAL = 8
+} spx_status;
+
+typedef enum { SPX_FP32 = 0, SPX_FP64 = 1 } spx_precision;
+
+/* One sparse matrix in MATLAB CSC layout (mxGetJc / mxGetIr / mxGetComplexDoubles). */
+typedef struct {
+    int64_t n;                 /* rows == columns */
+    const int64_t *colptr;     /* n+1 entries, colptr[0] == 0 */
+    const int64_t *rowidx;     /* colptr[n] entries, 0-based */
+    const double *values;      /* 2*colptr[n] doubles, interleaved (re, im) */
+} spx_csc;
+
+/* Run options.  Zero-initialise and set what you need; zeros mean "auto". */
+typedef struct {
+    int32_t precision;         /* spx_precision: storage/arithmetic of the propagation */
+    int32_t chunk_steps;       /* time steps covered by one series expansion, 0 = auto */
+    int32_t threads;           /* CTA size, 0 = auto */
+    int32_t reserved0;
+    double series_tol;         /* truncation tolerance of the series, 0 = auto */
+    double reserved1;
+} spx_options;
+
+/* Statistics of the last spx_run_powder* call on a handle. */
+typedef struct {
+    int64_t n_orientations;
+    int64_t nsteps;
+    int64_t matvecs;           /* Liouvillian actions executed, summed over orientations */
+    int64_t orientations_failed;
+    int32_t chunk_steps;
+    int32_t max_terms;         /* largest series length used by any orientation */
+    int32_t threads;
+    int32_t precision;
+    double kernel_ms;          /* propagation kernel, CUDA events on the handle stream */
+    double reduce_ms;          /* powder summation kernel */
+    double min_half_width;     /* smallest / largest spectral half-width seen (rad/s) */
+    double max_half_width;
+    int64_t dim;
+    int64_t nnz;               /* stored Liouvillian non-zeros (diagonal included) */
+    int64_t ell_entries;       /* padded sliced-ELL entries (off-diagonal) */
+    int32_t value_streams;     /* per-non-zero value streams combined per orientation */
+    int32_t real_offdiag;      /* 1 if off-diagonal Liouvillian values are real */
+} spx_stats;
+
+typedef struct spx_handle spx_handle;
+
+/* Create a handle bound to CUDA device `device` (cudaSetDevice semantics). */
+spx_status spx_create(spx_handle **handle, int device);
+
+/* Release every device buffer and the stream of a handle.  NULL is a no-op. */
+spx_status spx_destroy(spx_handle *handle);
+
+/*
+ * Upload one spin system: the isotropic part I, n_terms rotational-basis
+ * terms Q{rank}{k,m} (rank 1 or 2, 0-based k, m in 0..2*rank), the
+ * relaxation superoperator R (diagonal; may be NULL for no relaxation), and
+ * the initial state rho0 and detection state coil (2*n doubles each,
+ * interleaved complex).  Replaces any previously uploaded system.
+ * The Liouvillian of an orientation is L = (H+H')/2 + 1i*R with
+ * H = I + sum_t D^{rank_t}(alpha,beta,gamma)(k_t,m_t) Q_t.
+ */
+spx_status spx_upload_system(spx_handle *handle, const spx_csc *I,
+                             int32_t n_terms, const int32_t *rank,
+                             const int32_t *k, const int32_t *m,
+                             const spx_csc *Q, const spx_csc *R,
+                             const double *rho0, const double *coil);
+
+/*
+ * Powder-averaged FID over an orientation grid (host buffers).  alphas,
+ * betas, gammas, weights: n_orient doubles.  fid: 2*(nsteps+1) doubles
+ * (interleaved complex), fid = sum_n weights(n) * fid_n.  fids_per_orient:
+ * optional (NULL to skip), 2*(nsteps+1)*n_orient doubles, orientation-major
+ * (the parameters.sum_up=false output of powder.m:291-297).
+ */
+spx_status spx_run_powder(spx_handle *handle, int64_t n_orient,
+                          const double *alphas, const double *betas,
+                          const double *gammas, const double *weights,
+                          double dt, int64_t nsteps, const spx_options *opt,
+                          double *fid, double *fids_per_orient);
+
+/*
+ * Same computation with every array already in device memory of the
+ * handle's device (inputs n_orient doubles each; d_fid 2*(nsteps+1)
+ * doubles).  Work is enqueued on the handle's stream and the call returns
+ * without synchronising; spx_stats timings are filled at the next
+ * synchronising call (spx_synchronize, spx_run_powder, spx_get_stats).
+ */
+spx_status spx_run_powder_device(spx_handle *handle, int64_t n_orient,
+                                 const double *d_alphas, const double *d_betas,
+                                 const double *d_gammas, const double *d_weights,
+                                 double dt, int64_t nsteps, const spx_options *opt,
+                                 double *d_fid);
+
+/* Wait for all work on the handle's stream; returns the device status. */
+spx_status spx_synchronize(spx_handle *handle);
+
+/* The handle's cudaStream_t, for callers that time or order work around it. */
+void *spx_get_stream(spx_handle *handle);
+
+/* Statistics of the last run (synchronises). */
+spx_status spx_get_stats(spx_handle *handle, spx_stats *stats);
+
+/* Static text of a status code. */
+const char *spx_status_string(spx_status status);
+
+/* Detail of the last error on a handle (empty string if none). */
+const char *spx_last_error(const spx_handle *handle);
+
+/* Library version string. */
+const char *spx_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPINACH_GPU_H */

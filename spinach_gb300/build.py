@@ -1,0 +1,35 @@
+"""In-tree build of the engine library for sm_103a (nvcc, no cmake)."""
+from __future__ import annotations
+
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+SOURCES = [os.path.join(HERE, 'csrc', 'engine.cu')]
+DEPS = SOURCES + [os.path.join(HERE, 'csrc', 'kernels.cuh'), os.path.join(ROOT, 'include', 'spinach_gpu.h')]
+LIB = os.path.join(HERE, 'lib', 'libspinach_gpu.so')
+NVCC_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a', '-O3', '-lineinfo', '-std=c++17',
+              '-Xcompiler', '-fPIC', '-shared', '-diag-suppress', '550']
+
+
+def build_library(force: bool = False, verbose: bool = False) -> str:
+    """Compile libspinach_gpu.so if it is missing or older than its sources."""
+    if not force and os.path.exists(LIB):
+        t = os.path.getmtime(LIB)
+        if all(os.path.getmtime(d) <= t for d in DEPS):
+            return LIB
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    nvcc = os.environ.get('NVCC', 'nvcc')
+    cmd = [nvcc, *NVCC_FLAGS, '-I', os.path.join(ROOT, 'include'), *SOURCES, '-o', LIB + '.tmp']
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError('nvcc failed:\n' + res.stdout + res.stderr)
+    if verbose:
+        print(res.stdout + res.stderr)
+    os.replace(LIB + '.tmp', LIB)
+    return LIB
+
+
+if __name__ == '__main__':
+    print(build_library(force=True, verbose=True))

@@ -1,0 +1,742 @@
+// C ABI of the GB300 powder-FID engine (declared in include/spinach_gpu.h).
+//
+// Host part: converts the caller's CSC matrices (the I and Q{r}{k,m} that
+// kernel/hamiltonian.m returns) into Hermitised value streams on one union
+// sparsity pattern, reorders the basis by row length into a 32-row sliced
+// ELL layout, uploads it once, and launches the propagation and powder-sum
+// kernels of kernels.cuh for every orientation grid.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "spinach_gpu.h"
+#include "kernels.cuh"
+
+namespace {
+
+struct SpxError : std::runtime_error {
+    spx_status code;
+    SpxError(spx_status c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define SPX_CUDA(call)                                                                    \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            throw SpxError(e_ == cudaErrorMemoryAllocation ? SPX_ERR_OUT_OF_MEMORY         \
+                                                           : SPX_ERR_CUDA,                \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));          \
+        }                                                                                 \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void reserve(size_t count) {
+        if (count <= n && p) return;
+        release();
+        SPX_CUDA(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)));
+        n = count;
+    }
+    void upload(const std::vector<T> &v, cudaStream_t s) {
+        reserve(v.size());
+        if (!v.empty()) SPX_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+};
+
+struct Cplx {
+    double re = 0.0, im = 0.0;
+};
+
+}  // namespace
+
+struct spx_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::string err;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+
+    // uploaded system
+    bool have_system = false;
+    int n = 0, n_pad = 0, nslices = 0, ell_len = 0, nstreams = 0, nterms = 0;
+    bool cplx = false;
+    int64_t nnz = 0;
+    double g_upper = 0.0;      // upper bound of the spectral radius of H over all orientations
+    double max_im_diag = 0.0;
+    DevBuf<int> d_slice_off, d_stream_coef, d_term_rkm;
+    DevBuf<uint16_t> d_ell_col;
+    DevBuf<double> d_ell_re, d_ell_im;
+    DevBuf<double2> d_diag, d_rho0, d_coil;
+
+    // run buffers
+    DevBuf<double> d_grid;       // alpha | beta | gamma | weight
+    DevBuf<double> d_table;
+    DevBuf<unsigned char> d_fids;
+    DevBuf<double2> d_part, d_fid;
+    DevBuf<int> d_status, d_kused;
+    DevBuf<long long> d_matvecs;
+    DevBuf<double> d_halfwidth;
+
+    // last run
+    spx_stats stats{};
+    bool stats_pending = false;
+    int64_t last_norient = 0;
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Upload: CSC -> Hermitised streams -> sliced ELL
+// ---------------------------------------------------------------------------
+void check_csc(const spx_csc *A, int64_t n, const char *name) {
+    if (!A) throw SpxError(SPX_ERR_INVALID_ARGUMENT, std::string(name) + " is NULL");
+    if (A->n != n) throw SpxError(SPX_ERR_INVALID_ARGUMENT, std::string(name) + " has the wrong dimension");
+    if (!A->colptr) throw SpxError(SPX_ERR_INVALID_ARGUMENT, std::string(name) + ": NULL colptr");
+    const int64_t nnz = A->colptr[n];
+    if (A->colptr[0] != 0 || nnz < 0) throw SpxError(SPX_ERR_INVALID_ARGUMENT, std::string(name) + ": bad colptr");
+    if (nnz > 0 && (!A->rowidx || !A->values))
+        throw SpxError(SPX_ERR_INVALID_ARGUMENT, std::string(name) + ": NULL rowidx/values");
+    for (int64_t c = 0; c < n; ++c)
+        if (A->colptr[c + 1] < A->colptr[c]) throw SpxError(SPX_ERR_INVALID_ARGUMENT, std::string(name) + ": colptr decreases");
+    for (int64_t p = 0; p < nnz; ++p) {
+        if (A->rowidx[p] < 0 || A->rowidx[p] >= n)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, std::string(name) + ": row index out of range");
+        if (!std::isfinite(A->values[2 * p]) || !std::isfinite(A->values[2 * p + 1]))
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, std::string(name) + ": non-finite value");
+    }
+}
+
+template <class F>
+void for_each_entry(const spx_csc *A, F f) {
+    for (int64_t c = 0; c < A->n; ++c)
+        for (int64_t p = A->colptr[c]; p < A->colptr[c + 1]; ++p)
+            f(A->rowidx[p], c, Cplx{A->values[2 * p], A->values[2 * p + 1]});
+}
+
+void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32_t *rank,
+                   const int32_t *kk, const int32_t *mm, const spx_csc *Q, const spx_csc *R,
+                   const double *rho0, const double *coil) {
+    if (!I) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "I is NULL");
+    const int64_t n = I->n;
+    if (n < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "dimension must be positive");
+    if (n > 65535) throw SpxError(SPX_ERR_UNSUPPORTED, "Liouville dimension above 65535");
+    if (n_terms < 0 || n_terms > (spx::kMaxCoef - 1) / 2)
+        throw SpxError(SPX_ERR_UNSUPPORTED, "too many rotational-basis terms");
+    if (n_terms > 0 && (!rank || !kk || !mm || !Q)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL term arrays");
+    if (!rho0 || !coil) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "rho0/coil is NULL");
+    check_csc(I, n, "I");
+    for (int t = 0; t < n_terms; ++t) {
+        if (rank[t] < 1 || rank[t] > 2) throw SpxError(SPX_ERR_UNSUPPORTED, "only spherical ranks 1 and 2 are supported");
+        if (kk[t] < 0 || kk[t] > 2 * rank[t] || mm[t] < 0 || mm[t] > 2 * rank[t])
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "term projection index out of range");
+        check_csc(&Q[t], n, "Q");
+    }
+    if (R) check_csc(R, n, "R");
+    for (int64_t i = 0; i < 2 * n; ++i)
+        if (!std::isfinite(rho0[i]) || !std::isfinite(coil[i]))
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite rho0/coil");
+
+    // union pattern (structurally symmetric, full diagonal)
+    std::vector<int64_t> keys;
+    keys.reserve((size_t)n * 4);
+    for (int64_t i = 0; i < n; ++i) keys.push_back(i * n + i);
+    auto add_pattern = [&](const spx_csc *A) {
+        for_each_entry(A, [&](int64_t r, int64_t c, Cplx) {
+            keys.push_back(r * n + c);
+            keys.push_back(c * n + r);
+        });
+    };
+    add_pattern(I);
+    for (int t = 0; t < n_terms; ++t) add_pattern(&Q[t]);
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    const size_t nk = keys.size();
+    auto pos = [&](int64_t r, int64_t c) -> size_t {
+        return (size_t)(std::lower_bound(keys.begin(), keys.end(), r * n + c) - keys.begin());
+    };
+
+    // streams: 0 = Ih + iR (coefficient 1), then S_t, A_t per term
+    const int nst_all = 1 + 2 * n_terms;
+    std::vector<std::vector<Cplx>> st(nst_all, std::vector<Cplx>(nk));
+    for_each_entry(I, [&](int64_t r, int64_t c, Cplx v) {
+        Cplx &a = st[0][pos(r, c)];
+        a.re += 0.5 * v.re; a.im += 0.5 * v.im;
+        Cplx &b = st[0][pos(c, r)];
+        b.re += 0.5 * v.re; b.im -= 0.5 * v.im;
+    });
+    for (int t = 0; t < n_terms; ++t) {
+        auto &S = st[1 + 2 * t];
+        auto &A = st[2 + 2 * t];
+        for_each_entry(&Q[t], [&](int64_t r, int64_t c, Cplx v) {
+            const size_t p = pos(r, c), q = pos(c, r);
+            // S = (Q + Q^H)/2,  A = 1i (Q - Q^H)/2
+            S[p].re += 0.5 * v.re; S[p].im += 0.5 * v.im;
+            S[q].re += 0.5 * v.re; S[q].im -= 0.5 * v.im;
+            A[p].re -= 0.5 * v.im; A[p].im += 0.5 * v.re;
+            A[q].re -= 0.5 * v.im; A[q].im -= 0.5 * v.re;
+        });
+    }
+    double max_im_diag = 0.0;
+    if (R) {
+        for_each_entry(R, [&](int64_t r, int64_t c, Cplx v) {
+            if (r != c) {
+                if (v.re != 0.0 || v.im != 0.0)
+                    throw SpxError(SPX_ERR_UNSUPPORTED, "only diagonal relaxation superoperators are supported");
+                return;
+            }
+            Cplx &a = st[0][pos(r, r)];      // L = H + 1i*R
+            a.re -= v.im;
+            a.im += v.re;
+        });
+    }
+    // scale of everything, real/complex off-diagonal decision
+    double vmax = 0.0;
+    for (auto &s : st)
+        for (auto &v : s) vmax = std::max(vmax, std::max(std::fabs(v.re), std::fabs(v.im)));
+    const double im_tol = 1e-14 * vmax;
+    bool cplx = false;
+    for (auto &s : st)
+        for (size_t p = 0; p < nk && !cplx; ++p) {
+            const int64_t r = keys[p] / n, c = keys[p] % n;
+            if (r != c && std::fabs(s[p].im) > im_tol) cplx = true;
+        }
+    // drop all-zero streams
+    std::vector<int> keep;
+    for (int s = 0; s < nst_all; ++s) {
+        bool nz = (s == 0);
+        for (size_t p = 0; p < nk && !nz; ++p) nz = (st[s][p].re != 0.0 || st[s][p].im != 0.0);
+        if (nz) keep.push_back(s);
+    }
+    const int nst = (int)keep.size();
+
+    // rows: count off-diagonals, order by count (descending, stable)
+    std::vector<int> cnt(n, 0);
+    for (size_t p = 0; p < nk; ++p) {
+        const int64_t r = keys[p] / n, c = keys[p] % n;
+        if (r != c) ++cnt[r];
+    }
+    std::vector<int> perm(n);  // new -> old
+    for (int i = 0; i < n; ++i) perm[i] = i;
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return cnt[a] > cnt[b]; });
+    std::vector<int> inv(n);
+    for (int i = 0; i < n; ++i) inv[perm[i]] = i;
+    const int nslices = (int)((n + 31) / 32), n_pad = nslices * 32;
+    std::vector<int> slice_off(nslices + 1, 0);
+    for (int s = 0; s < nslices; ++s) {
+        int w = 0;
+        for (int l = 0; l < 32; ++l) {
+            const int row = s * 32 + l;
+            if (row < n) w = std::max(w, cnt[perm[row]]);
+        }
+        slice_off[s + 1] = slice_off[s] + 32 * w;
+    }
+    const int ell_len = slice_off[nslices];
+    // row start of each old row in the key list
+    std::vector<size_t> rstart(n + 1, 0);
+    for (size_t p = 0; p < nk; ++p) rstart[keys[p] / n + 1]++;
+    for (int64_t i = 0; i < n; ++i) rstart[i + 1] += rstart[i];
+
+    std::vector<uint16_t> ell_col(std::max(ell_len, 1), 0);
+    std::vector<double> ell_re((size_t)nst * std::max(ell_len, 1), 0.0), ell_im;
+    if (cplx) ell_im.assign((size_t)nst * std::max(ell_len, 1), 0.0);
+    std::vector<double2> diag((size_t)nst * n_pad, make_double2(0.0, 0.0));
+    double g_upper = 0.0;
+    for (int s = 0; s < nslices; ++s) {
+        for (int l = 0; l < 32; ++l) {
+            const int row = s * 32 + l;
+            int c = 0;
+            double rowsum = 0.0;
+            if (row < n) {
+                const int old = perm[row];
+                for (size_t p = rstart[old]; p < rstart[old + 1]; ++p) {
+                    const int64_t oc = keys[p] % n;
+                    if (oc == old) {
+                        for (int q = 0; q < nst; ++q) {
+                            const Cplx v = st[keep[q]][p];
+                            diag[(size_t)q * n_pad + row] = make_double2(v.re, v.im);
+                            rowsum += (keep[q] == 0) ? std::fabs(v.re) : std::hypot(v.re, v.im);
+                        }
+                        continue;
+                    }
+                    const size_t e = (size_t)slice_off[s] + (size_t)c * 32 + l;
+                    ell_col[e] = (uint16_t)inv[oc];
+                    for (int q = 0; q < nst; ++q) {
+                        const Cplx v = st[keep[q]][p];
+                        ell_re[(size_t)q * ell_len + e] = v.re;
+                        if (cplx) ell_im[(size_t)q * ell_len + e] = v.im;
+                        rowsum += std::hypot(v.re, v.im);
+                    }
+                    ++c;
+                }
+            }
+            // padding entries point at the row itself with zero value
+            const int w = (slice_off[s + 1] - slice_off[s]) / 32;
+            for (; c < w; ++c) ell_col[(size_t)slice_off[s] + (size_t)c * 32 + l] = (uint16_t)std::min(row, n_pad - 1);
+            g_upper = std::max(g_upper, rowsum);
+        }
+    }
+    for (int i = 0; i < n; ++i) max_im_diag = std::max(max_im_diag, std::fabs(diag[i].y));
+    std::vector<int> stream_coef(nst);
+    for (int q = 0; q < nst; ++q) stream_coef[q] = keep[q];     // slot in the coefficient vector
+    std::vector<int> term_rkm(3 * std::max(n_terms, 1), 0);
+    for (int t = 0; t < n_terms; ++t) {
+        term_rkm[3 * t] = rank[t];
+        term_rkm[3 * t + 1] = kk[t];
+        term_rkm[3 * t + 2] = mm[t];
+    }
+    std::vector<double2> r0(n_pad, make_double2(0, 0)), cl(n_pad, make_double2(0, 0));
+    for (int i = 0; i < n; ++i) {
+        r0[inv[i]] = make_double2(rho0[2 * i], rho0[2 * i + 1]);
+        cl[inv[i]] = make_double2(coil[2 * i], coil[2 * i + 1]);
+    }
+
+    SPX_CUDA(cudaSetDevice(h->device));
+    h->have_system = false;
+    h->d_slice_off.upload(slice_off, h->stream);
+    h->d_ell_col.upload(ell_col, h->stream);
+    h->d_ell_re.upload(ell_re, h->stream);
+    if (cplx) h->d_ell_im.upload(ell_im, h->stream); else h->d_ell_im.release();
+    h->d_diag.upload(diag, h->stream);
+    h->d_stream_coef.upload(stream_coef, h->stream);
+    h->d_term_rkm.upload(term_rkm, h->stream);
+    h->d_rho0.upload(r0, h->stream);
+    h->d_coil.upload(cl, h->stream);
+    SPX_CUDA(cudaStreamSynchronize(h->stream));
+    h->n = (int)n;
+    h->n_pad = n_pad;
+    h->nslices = nslices;
+    h->ell_len = ell_len;
+    h->nstreams = nst;
+    h->nterms = n_terms;
+    h->cplx = cplx;
+    h->nnz = (int64_t)nk;
+    h->g_upper = g_upper;
+    h->max_im_diag = max_im_diag;
+    h->have_system = true;
+}
+
+// ---------------------------------------------------------------------------
+// Launch configuration
+// ---------------------------------------------------------------------------
+struct Config {
+    int threads, rmax, M, Kmax, grid;
+    size_t smem;
+    double tol;
+};
+
+double host_series_terms(double x, double lg, double tol) {
+    if (!(x > 0.0)) return 1;
+    const double ltol = std::log(tol);
+    int k = std::max(1, (int)std::ceil(x) + 1);
+    while (k < 200000) {
+        const double lt = -0.5 * std::log(2.0 * M_PI * k) + k * std::log(M_E * x / (2.0 * k)) + k * lg;
+        if (lt < ltol) break;
+        ++k;
+    }
+    return k;
+}
+
+template <bool F64, bool CPLX>
+size_t smem_bytes(const spx_handle *h, int Kmax, int M, int threads) {
+    spx::SmemLayout<F64, CPLX> L(h->n_pad, h->nslices, h->ell_len, Kmax, M, threads);
+    return L.total;
+}
+
+size_t smem_for(const spx_handle *h, bool f64, int Kmax, int M, int threads) {
+    if (f64) return h->cplx ? smem_bytes<true, true>(h, Kmax, M, threads) : smem_bytes<true, false>(h, Kmax, M, threads);
+    return h->cplx ? smem_bytes<false, true>(h, Kmax, M, threads) : smem_bytes<false, false>(h, Kmax, M, threads);
+}
+
+template <bool F64, bool CPLX, int RMAX>
+const void *kernel_ptr() {
+    return reinterpret_cast<const void *>(&spx::powder_chebyshev_kernel<F64, CPLX, RMAX>);
+}
+
+const void *select_kernel(bool f64, bool cplx, int rmax) {
+#define SPX_SEL(F, C)                                  \
+    switch (rmax) {                                    \
+        case 1: return kernel_ptr<F, C, 1>();          \
+        case 2: return kernel_ptr<F, C, 2>();          \
+        case 4: return kernel_ptr<F, C, 4>();          \
+        default: return kernel_ptr<F, C, 8>();         \
+    }
+    if (f64) {
+        if (cplx) { SPX_SEL(true, true) } else { SPX_SEL(true, false) }
+    } else {
+        if (cplx) { SPX_SEL(false, true) } else { SPX_SEL(false, false) }
+    }
+#undef SPX_SEL
+}
+
+Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps, const spx_options &opt,
+                     int kmax_override) {
+    Config c{};
+    const bool f64 = opt.precision == SPX_FP64;
+    c.tol = opt.series_tol > 0 ? opt.series_tol : (f64 ? 1e-16 : 1e-11);
+    // warps: about four 32-row slices per lane, at most 16 warps
+    int nwarps = std::min(16, std::max(1, (h->nslices + 3) / 4));
+    if (opt.threads > 0) nwarps = std::max(1, std::min(16, opt.threads / 32));
+    const int rows = (h->nslices + nwarps - 1) / nwarps;
+    if (rows > 8) throw SpxError(SPX_ERR_UNSUPPORTED, "Liouville dimension too large for the register-resident kernel");
+    c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 8;
+    c.threads = nwarps * 32;
+    // chunk: about 150 series terms per chunk from an estimate of the half-width
+    const double s_est = std::max(h->g_upper / 1.5, 1e-300);
+    int M = opt.chunk_steps;
+    if (M <= 0) {
+        const double target = 150.0 / (s_est * dt);
+        M = 4;
+        while (M * 2 <= target && M < 256) M *= 2;
+    }
+    M = (int)std::min<int64_t>(M, nsteps + 1);
+    M = std::max(M, 1);
+    c.M = M;
+    const double xu = h->g_upper * M * dt;
+    const double lg = (h->g_upper > 0) ? 2.0 * h->max_im_diag / (h->g_upper / 4.0) : 0.0;
+    int K = (int)host_series_terms(xu, std::min(lg, 0.05), c.tol) + 16;
+    if (kmax_override > 0) K = std::max(K, kmax_override);
+    c.Kmax = std::min(K, 8192);
+    c.smem = smem_for(h, f64, c.Kmax, c.M, c.threads);
+    if (c.smem > h->smem_optin)
+        throw SpxError(SPX_ERR_UNSUPPORTED, "system does not fit the shared-memory budget of one SM (" +
+                                                std::to_string(c.smem) + " bytes)");
+    const void *kfn = select_kernel(f64, h->cplx, c.rmax);
+    SPX_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem));
+    int per_sm = 0;
+    SPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, c.threads, c.smem));
+    per_sm = std::max(per_sm, 1);
+    c.grid = (int)std::min<int64_t>(n_orient, (int64_t)h->sm_count * per_sm);
+    return c;
+}
+
+void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be,
+                   const double *d_ga, const double *d_w, double dt, int64_t nsteps,
+                   const spx_options &opt, double2 *d_out, const Config &c) {
+    const bool f64 = opt.precision == SPX_FP64;
+    const size_t npts = (size_t)nsteps + 1;
+    const size_t vec_bytes = f64 ? sizeof(double2) : sizeof(float2);
+    h->d_fids.reserve(npts * n_orient * vec_bytes);
+    h->d_table.reserve((size_t)c.grid * c.Kmax * (c.M + 1));
+    h->d_status.reserve(n_orient);
+    h->d_kused.reserve(n_orient);
+    h->d_matvecs.reserve(n_orient);
+    h->d_halfwidth.reserve(n_orient);
+
+    spx::DevSystem sys{};
+    sys.n = h->n; sys.n_pad = h->n_pad; sys.nslices = h->nslices; sys.ell_len = h->ell_len;
+    sys.slice_off = h->d_slice_off.p; sys.ell_col = h->d_ell_col.p;
+    sys.ell_re = h->d_ell_re.p; sys.ell_im = h->cplx ? h->d_ell_im.p : nullptr;
+    sys.diag = h->d_diag.p; sys.stream_coef = h->d_stream_coef.p; sys.nstreams = h->nstreams;
+    sys.ncoef = 1 + 2 * h->nterms; sys.nterms = h->nterms; sys.term_rkm = h->d_term_rkm.p;
+    sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag;
+    spx::DevRun run{};
+    run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
+    run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
+    run.lanczos_its = 32; run.fids = h->d_fids.p; run.table = h->d_table.p;
+    run.status = h->d_status.p; run.matvecs = h->d_matvecs.p; run.halfwidth = h->d_halfwidth.p;
+    run.kused = h->d_kused.p;
+
+    const void *kfn = select_kernel(f64, h->cplx, c.rmax);
+    void *args[] = {&sys, &run};
+    SPX_CUDA(cudaEventRecord(h->ev[0], h->stream));
+    SPX_CUDA(cudaLaunchKernel(kfn, dim3(c.grid), dim3(c.threads), args, c.smem, h->stream));
+    SPX_CUDA(cudaEventRecord(h->ev[1], h->stream));
+    // deterministic FP64 powder sum: fixed groups of orientations, fixed order
+    const int group = 64;
+    const int ngroups = (int)((n_orient + group - 1) / group);
+    h->d_part.reserve((size_t)ngroups * npts);
+    const dim3 pb(256), pg((unsigned)((npts + 255) / 256), (unsigned)ngroups);
+    if (f64)
+        spx::powder_partial_kernel<double2><<<pg, pb, 0, h->stream>>>(
+            reinterpret_cast<const double2 *>(h->d_fids.p), d_w, (int)n_orient, (int)npts, group, h->d_part.p);
+    else
+        spx::powder_partial_kernel<float2><<<pg, pb, 0, h->stream>>>(
+            reinterpret_cast<const float2 *>(h->d_fids.p), d_w, (int)n_orient, (int)npts, group, h->d_part.p);
+    SPX_CUDA(cudaGetLastError());
+    spx::powder_combine_kernel<<<dim3((unsigned)((npts + 255) / 256)), dim3(256), 0, h->stream>>>(
+        h->d_part.p, ngroups, (int)npts, d_out);
+    SPX_CUDA(cudaGetLastError());
+    SPX_CUDA(cudaEventRecord(h->ev[2], h->stream));
+
+    h->stats = spx_stats{};
+    h->stats.n_orientations = n_orient;
+    h->stats.nsteps = nsteps;
+    h->stats.chunk_steps = c.M;
+    h->stats.threads = c.threads;
+    h->stats.precision = opt.precision;
+    h->stats.dim = h->n;
+    h->stats.nnz = h->nnz;
+    h->stats.ell_entries = h->ell_len;
+    h->stats.value_streams = h->nstreams;
+    h->stats.real_offdiag = h->cplx ? 0 : 1;
+    h->stats_pending = true;
+    h->last_norient = n_orient;
+}
+
+// Synchronise, read per-orientation status and fill the statistics.
+spx_status finish_run(spx_handle *h) {
+    SPX_CUDA(cudaStreamSynchronize(h->stream));
+    if (!h->stats_pending) return SPX_OK;
+    h->stats_pending = false;
+    const int64_t no = h->last_norient;
+    std::vector<int> status(no), kused(no);
+    std::vector<long long> mv(no);
+    std::vector<double> hw(no);
+    SPX_CUDA(cudaMemcpy(status.data(), h->d_status.p, no * sizeof(int), cudaMemcpyDeviceToHost));
+    SPX_CUDA(cudaMemcpy(kused.data(), h->d_kused.p, no * sizeof(int), cudaMemcpyDeviceToHost));
+    SPX_CUDA(cudaMemcpy(mv.data(), h->d_matvecs.p, no * sizeof(long long), cudaMemcpyDeviceToHost));
+    SPX_CUDA(cudaMemcpy(hw.data(), h->d_halfwidth.p, no * sizeof(double), cudaMemcpyDeviceToHost));
+    float ms0 = 0, ms1 = 0;
+    SPX_CUDA(cudaEventElapsedTime(&ms0, h->ev[0], h->ev[1]));
+    SPX_CUDA(cudaEventElapsedTime(&ms1, h->ev[1], h->ev[2]));
+    h->stats.kernel_ms = ms0;
+    h->stats.reduce_ms = ms1;
+    int64_t failed = 0, matvecs = 0;
+    int maxk = 0;
+    double hmin = INFINITY, hmax = 0.0;
+    int first_bad = -1, first_code = 0;
+    for (int64_t o = 0; o < no; ++o) {
+        if (status[o] != spx::kDevOk) {
+            ++failed;
+            if (first_bad < 0) { first_bad = (int)o; first_code = status[o]; }
+        }
+        matvecs += mv[o];
+        maxk = std::max(maxk, kused[o]);
+        hmin = std::min(hmin, hw[o]);
+        hmax = std::max(hmax, hw[o]);
+    }
+    h->stats.matvecs = matvecs;
+    h->stats.max_terms = maxk;
+    h->stats.orientations_failed = failed;
+    h->stats.min_half_width = hmin;
+    h->stats.max_half_width = hmax;
+    if (failed) {
+        static const char *why[] = {"ok", "series longer than the coefficient table", "state norm grew (spectral bound violated)",
+                                    "non-finite state", "launch configuration has too few threads"};
+        const char *w = (first_code >= 0 && first_code <= 4) ? why[first_code] : "unknown device status";
+        throw SpxError(SPX_ERR_SERIES, std::to_string(failed) + " orientation(s) failed, first #" +
+                                           std::to_string(first_bad) + ": " + w);
+    }
+    return SPX_OK;
+}
+
+void validate_run(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps) {
+    if (!h->have_system) throw SpxError(SPX_ERR_NO_SYSTEM, "no spin system uploaded");
+    if (n_orient < 1 || n_orient > (1LL << 30)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "bad orientation count");
+    if (!(dt > 0.0) || !std::isfinite(dt)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
+    if (nsteps < 0 || nsteps > (1LL << 28)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "bad step count");
+    if (h->g_upper * dt > 1e4)
+        throw SpxError(SPX_ERR_NORM, "|L*dt| exceeds 1e4: check L and dt (kernel/step.m:230-233)");
+}
+
+template <class F>
+spx_status guarded(spx_handle *h, F f) {
+    try {
+        f();
+        if (h) h->err.clear();
+        return SPX_OK;
+    } catch (const SpxError &e) {
+        if (h) h->err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        if (h) h->err = "host allocation failed";
+        return SPX_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception &e) {
+        if (h) h->err = e.what();
+        return SPX_ERR_INTERNAL;
+    } catch (...) {
+        if (h) h->err = "unknown failure";
+        return SPX_ERR_INTERNAL;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+spx_status spx_create(spx_handle **handle, int device) {
+    if (!handle) return SPX_ERR_INVALID_ARGUMENT;
+    *handle = nullptr;
+    spx_handle *h = new (std::nothrow) spx_handle();
+    if (!h) return SPX_ERR_OUT_OF_MEMORY;
+    const spx_status st = guarded(h, [&] {
+        int ndev = 0;
+        SPX_CUDA(cudaGetDeviceCount(&ndev));
+        if (device < 0 || device >= ndev) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "no such CUDA device");
+        h->device = device;
+        SPX_CUDA(cudaSetDevice(device));
+        SPX_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        for (auto &e : h->ev) SPX_CUDA(cudaEventCreate(&e));
+        SPX_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device));
+        int optin = 0;
+        SPX_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+        h->smem_optin = (size_t)optin;
+    });
+    if (st != SPX_OK) {
+        spx_destroy(h);
+        return st;
+    }
+    *handle = h;
+    return SPX_OK;
+}
+
+spx_status spx_destroy(spx_handle *h) {
+    if (!h) return SPX_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto &e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return SPX_OK;
+}
+
+spx_status spx_upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32_t *rank,
+                             const int32_t *k, const int32_t *m, const spx_csc *Q, const spx_csc *R,
+                             const double *rho0, const double *coil) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] { upload_system(h, I, n_terms, rank, k, m, Q, R, rho0, coil); });
+}
+
+spx_status spx_run_powder(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
+                          const double *gammas, const double *weights, double dt, int64_t nsteps,
+                          const spx_options *opt, double *fid, double *fids_per_orient) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        validate_run(h, n_orient, dt, nsteps);
+        if (!alphas || !betas || !gammas || !weights || !fid)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL grid or output pointer");
+        for (int64_t o = 0; o < n_orient; ++o)
+            if (!std::isfinite(alphas[o]) || !std::isfinite(betas[o]) || !std::isfinite(gammas[o]) ||
+                !std::isfinite(weights[o]))
+                throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite grid entry");
+        spx_options o{};
+        if (opt) o = *opt;
+        if (o.precision != SPX_FP32 && o.precision != SPX_FP64)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
+        SPX_CUDA(cudaSetDevice(h->device));
+        h->d_grid.reserve(4 * (size_t)n_orient);
+        double *g = h->d_grid.p;
+        const size_t b = (size_t)n_orient * sizeof(double);
+        SPX_CUDA(cudaMemcpyAsync(g, alphas, b, cudaMemcpyHostToDevice, h->stream));
+        SPX_CUDA(cudaMemcpyAsync(g + n_orient, betas, b, cudaMemcpyHostToDevice, h->stream));
+        SPX_CUDA(cudaMemcpyAsync(g + 2 * n_orient, gammas, b, cudaMemcpyHostToDevice, h->stream));
+        SPX_CUDA(cudaMemcpyAsync(g + 3 * n_orient, weights, b, cudaMemcpyHostToDevice, h->stream));
+        h->d_fid.reserve((size_t)nsteps + 1);
+        Config c = choose_config(h, n_orient, dt, nsteps, o, 0);
+        launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o, h->d_fid.p, c);
+        spx_status st = SPX_OK;
+        try {
+            finish_run(h);
+        } catch (const SpxError &e) {
+            // one retry with a wider coefficient table if that was the only problem
+            std::vector<int> status(n_orient), kused(n_orient);
+            SPX_CUDA(cudaMemcpy(status.data(), h->d_status.p, n_orient * sizeof(int), cudaMemcpyDeviceToHost));
+            SPX_CUDA(cudaMemcpy(kused.data(), h->d_kused.p, n_orient * sizeof(int), cudaMemcpyDeviceToHost));
+            bool only_table = true;
+            int kneed = 0;
+            for (int64_t i = 0; i < n_orient; ++i) {
+                if (status[i] != spx::kDevOk && status[i] != spx::kDevTableTooSmall) only_table = false;
+                kneed = std::max(kneed, kused[i]);
+            }
+            if (!only_table) throw;
+            c = choose_config(h, n_orient, dt, nsteps, o, kneed + 8);
+            launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o, h->d_fid.p, c);
+            st = finish_run(h);
+        }
+        (void)st;
+        SPX_CUDA(cudaMemcpy(fid, h->d_fid.p, ((size_t)nsteps + 1) * sizeof(double2), cudaMemcpyDeviceToHost));
+        if (fids_per_orient) {
+            const size_t cnt = ((size_t)nsteps + 1) * n_orient;
+            if (o.precision == SPX_FP64) {
+                SPX_CUDA(cudaMemcpy(fids_per_orient, h->d_fids.p, cnt * sizeof(double2), cudaMemcpyDeviceToHost));
+            } else {
+                std::vector<float2> tmp(cnt);
+                SPX_CUDA(cudaMemcpy(tmp.data(), h->d_fids.p, cnt * sizeof(float2), cudaMemcpyDeviceToHost));
+                for (size_t i = 0; i < cnt; ++i) {
+                    fids_per_orient[2 * i] = tmp[i].x;
+                    fids_per_orient[2 * i + 1] = tmp[i].y;
+                }
+            }
+        }
+    });
+}
+
+spx_status spx_run_powder_device(spx_handle *h, int64_t n_orient, const double *d_alphas, const double *d_betas,
+                                 const double *d_gammas, const double *d_weights, double dt, int64_t nsteps,
+                                 const spx_options *opt, double *d_fid) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        validate_run(h, n_orient, dt, nsteps);
+        if (!d_alphas || !d_betas || !d_gammas || !d_weights || !d_fid)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL device pointer");
+        spx_options o{};
+        if (opt) o = *opt;
+        if (o.precision != SPX_FP32 && o.precision != SPX_FP64)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
+        SPX_CUDA(cudaSetDevice(h->device));
+        const Config c = choose_config(h, n_orient, dt, nsteps, o, 0);
+        launch_powder(h, n_orient, d_alphas, d_betas, d_gammas, d_weights, dt, nsteps, o,
+                      reinterpret_cast<double2 *>(d_fid), c);
+    });
+}
+
+spx_status spx_synchronize(spx_handle *h) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        SPX_CUDA(cudaSetDevice(h->device));
+        finish_run(h);
+    });
+}
+
+void *spx_get_stream(spx_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+spx_status spx_get_stats(spx_handle *h, spx_stats *stats) {
+    if (!h || !stats) return SPX_ERR_INVALID_ARGUMENT;
+    const spx_status st = guarded(h, [&] {
+        SPX_CUDA(cudaSetDevice(h->device));
+        finish_run(h);
+    });
+    *stats = h->stats;
+    return st;
+}
+
+const char *spx_status_string(spx_status s) {
+    switch (s) {
+        case SPX_OK: return "success";
+        case SPX_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case SPX_ERR_NO_SYSTEM: return "no spin system uploaded";
+        case SPX_ERR_CUDA: return "CUDA runtime error";
+        case SPX_ERR_UNSUPPORTED: return "unsupported input";
+        case SPX_ERR_SERIES: return "series did not converge";
+        case SPX_ERR_NORM: return "|L*dt| too large";
+        case SPX_ERR_OUT_OF_MEMORY: return "out of memory";
+        case SPX_ERR_INTERNAL: return "internal error";
+    }
+    return "unknown status";
+}
+
+const char *spx_last_error(const spx_handle *h) { return h ? h->err.c_str() : "NULL handle"; }
+
+const char *spx_version(void) { return "spinach-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

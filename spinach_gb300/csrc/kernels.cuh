@@ -1,0 +1,791 @@
+// Device code of the GB300 powder-FID engine.
+//
+// One CTA owns one orientation at a time (persistent grid, orientations
+// strided over CTAs).  For each orientation it
+//   1. forms the Wigner-D coefficients of its Euler angles in FP64
+//      (kernel/utilities/wigner.m:45-77) and assembles the Hermitised
+//      Liouvillian L = Ih + sum_t Re(D_t) S_t + Im(D_t) A_t + 1i R on the
+//      shared sparsity pattern straight into shared memory
+//      (kernel/orientation.m:38-57, kernel/contexts/powder.m:235,263,
+//      experiments/acquire.m:48);
+//   2. bounds the spectrum of the Hermitian part with a short Lanczos run
+//      (clamped by Gershgorin discs) and rescales L to L~ = (L - c)/s;
+//   3. tabulates Bessel coefficients J_k(s*j*dt) for one chunk of M steps;
+//   4. propagates the state chunk by chunk with the Chebyshev expansion
+//      exp(-1i*L*t) = e^{-1i c t} sum_k (2-d_k0) (-1i)^k J_k(s t) T_k(L~),
+//      reading the detection moments mu_k = coil' T_k(L~) rho at every term
+//      (fused coil projection, kernel/evolution.m:564 / krylov.m:154) and
+//      reconstructing the M FID points of the chunk from them.
+// This replaces the reference's per-step action of exp(-1i*L*dt)
+// (kernel/propagator.m:34-211 followed by P*rho, or kernel/step.m:204-375);
+// the series is exact to the chosen tolerance, so the FID is the same
+// quantity the reference computes.
+//
+// FP32 mode stores Liouvillian values and series coefficients as hi+lo float
+// pairs (about 48 significant bits) and state vectors as complex float: the
+// value rounding, not the vector rounding, is what drifts the phase over
+// thousands of steps.  FP64 mode stores everything in double.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+namespace spx {
+
+constexpr int kMaxCoef = 128;     // 1 + 2 * (number of rotational-basis terms)
+constexpr int kMaxLanczos = 48;
+constexpr int kRedSlots = 64;
+
+enum DeviceStatus : int {
+    kDevOk = 0,
+    kDevTableTooSmall = 1,   // series longer than the scratch table
+    kDevDiverged = 2,        // state norm grew: spectral bound violated
+    kDevNonFinite = 3,
+    kDevTooManyRows = 4,
+};
+
+struct __align__(8) SplitR { float hi, lo; };
+struct __align__(16) SplitC { float rh, ih, rl, il; };
+
+// ---------------------------------------------------------------------------
+// Precision policies
+// ---------------------------------------------------------------------------
+template <bool F64, bool CPLX> struct Prec;
+template <> struct Prec<false, false> { using Vec = float2;  using Val = SplitR; using Dg = SplitC; using Real = float; };
+template <> struct Prec<false, true>  { using Vec = float2;  using Val = SplitC; using Dg = SplitC; using Real = float; };
+template <> struct Prec<true, false>  { using Vec = double2; using Val = double; using Dg = double2; using Real = double; };
+template <> struct Prec<true, true>   { using Vec = double2; using Val = double2; using Dg = double2; using Real = double; };
+
+__device__ __forceinline__ void pack(SplitR &o, double re, double) {
+    o.hi = (float)re; o.lo = (float)(re - (double)o.hi);
+}
+__device__ __forceinline__ void pack(SplitC &o, double re, double im) {
+    o.rh = (float)re; o.ih = (float)im;
+    o.rl = (float)(re - (double)o.rh); o.il = (float)(im - (double)o.ih);
+}
+__device__ __forceinline__ void pack(double &o, double re, double) { o = re; }
+__device__ __forceinline__ void pack(double2 &o, double re, double im) { o = make_double2(re, im); }
+
+__device__ __forceinline__ double2 unpack(const SplitR &v) { return make_double2((double)v.hi + (double)v.lo, 0.0); }
+__device__ __forceinline__ double2 unpack(const SplitC &v) {
+    return make_double2((double)v.rh + (double)v.rl, (double)v.ih + (double)v.il);
+}
+__device__ __forceinline__ double2 unpack(const double &v) { return make_double2(v, 0.0); }
+__device__ __forceinline__ double2 unpack(const double2 &v) { return v; }
+
+// y += v * x  (value times complex state)
+__device__ __forceinline__ void mac(float2 &y, const SplitR &v, const float2 x) {
+    y.x = fmaf(v.hi, x.x, y.x); y.y = fmaf(v.hi, x.y, y.y);
+    y.x = fmaf(v.lo, x.x, y.x); y.y = fmaf(v.lo, x.y, y.y);
+}
+__device__ __forceinline__ void mac(float2 &y, const SplitC &v, const float2 x) {
+    y.x = fmaf(v.rh, x.x, y.x); y.x = fmaf(-v.ih, x.y, y.x);
+    y.y = fmaf(v.rh, x.y, y.y); y.y = fmaf(v.ih, x.x, y.y);
+    y.x = fmaf(v.rl, x.x, y.x); y.x = fmaf(-v.il, x.y, y.x);
+    y.y = fmaf(v.rl, x.y, y.y); y.y = fmaf(v.il, x.x, y.y);
+}
+__device__ __forceinline__ void mac(double2 &y, const double &v, const double2 x) {
+    y.x = fma(v, x.x, y.x); y.y = fma(v, x.y, y.y);
+}
+__device__ __forceinline__ void mac(double2 &y, const double2 &v, const double2 x) {
+    y.x = fma(v.x, x.x, y.x); y.x = fma(-v.y, x.y, y.x);
+    y.y = fma(v.x, x.y, y.y); y.y = fma(v.y, x.x, y.y);
+}
+
+template <class V> __device__ __forceinline__ V vzero();
+template <> __device__ __forceinline__ float2 vzero<float2>() { return make_float2(0.f, 0.f); }
+template <> __device__ __forceinline__ double2 vzero<double2>() { return make_double2(0.0, 0.0); }
+
+__device__ __forceinline__ float2 tovec(double2 a, float2) { return make_float2((float)a.x, (float)a.y); }
+__device__ __forceinline__ double2 tovec(double2 a, double2) { return a; }
+__device__ __forceinline__ double2 tod(float2 a) { return make_double2(a.x, a.y); }
+__device__ __forceinline__ double2 tod(double2 a) { return a; }
+
+// conj(a) * b accumulated
+__device__ __forceinline__ void cdot_acc(float2 &s, const float2 a, const float2 b) {
+    s.x = fmaf(a.x, b.x, s.x); s.x = fmaf(a.y, b.y, s.x);
+    s.y = fmaf(a.x, b.y, s.y); s.y = fmaf(-a.y, b.x, s.y);
+}
+__device__ __forceinline__ void cdot_acc(double2 &s, const double2 a, const double2 b) {
+    s.x = fma(a.x, b.x, s.x); s.x = fma(a.y, b.y, s.x);
+    s.y = fma(a.x, b.y, s.y); s.y = fma(-a.y, b.x, s.y);
+}
+
+template <class V> __device__ __forceinline__ V warp_sum(V v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_min_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide reductions through a shared scratch of kRedSlots doubles.
+// Every thread of the block must call them (they contain __syncthreads).
+__device__ double block_sum(double v, double *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum_d(v);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    for (int w = 0; w < nw; ++w) r += red[w];
+    return r;
+}
+__device__ double block_max(double v, double *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_max_d(v);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double r = -CUDART_INF;
+    for (int w = 0; w < nw; ++w) r = fmax(r, red[w]);
+    return r;
+}
+__device__ double block_min(double v, double *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_min_d(v);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double r = CUDART_INF;
+    for (int w = 0; w < nw; ++w) r = fmin(r, red[w]);
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// System and run descriptors (device pointers)
+// ---------------------------------------------------------------------------
+struct DevSystem {
+    int n;              // Liouville dimension
+    int n_pad;          // nslices * 32
+    int nslices;        // 32-row slices of the sliced-ELL layout
+    int ell_len;        // padded off-diagonal entries
+    const int *slice_off;       // nslices + 1 (entries)
+    const uint16_t *ell_col;    // ell_len
+    const double *ell_re;       // nstreams * ell_len
+    const double *ell_im;       // nstreams * ell_len, or nullptr (real off-diagonal)
+    const double2 *diag;        // nstreams * n_pad
+    const int *stream_coef;     // nstreams: slot in the per-orientation coefficient vector
+    int nstreams;
+    int ncoef;                  // 1 + 2 * nterms
+    int nterms;
+    const int *term_rkm;        // 3 * nterms: rank, k, m (0-based k, m)
+    const double2 *rho0;        // n_pad (sliced order)
+    const double2 *coil;        // n_pad (sliced order)
+    double max_im_diag;         // largest |Im L_ii| (relaxation), rad/s
+};
+
+struct DevRun {
+    int n_orient;
+    const double *alpha, *beta, *gamma;
+    double dt;
+    int nsteps;
+    int M;              // time steps per chunk
+    int Kmax;           // width of the Bessel table
+    double tol;         // series truncation tolerance
+    int lanczos_its;
+    void *fids;         // n_orient * (nsteps + 1) complex (precision of the run)
+    double *table;      // gridDim.x * Kmax * (M + 1) doubles, per-CTA scratch
+    int *status;        // n_orient
+    long long *matvecs; // n_orient
+    double *halfwidth;  // n_orient
+    int *kused;         // n_orient
+};
+
+// ---------------------------------------------------------------------------
+// Wigner D (Brink & Satchler convention, rows/cols from +l to -l), FP64.
+// Written from the closed forms d^1 and d^2 of the small-d matrices.
+// ---------------------------------------------------------------------------
+__device__ void wigner_element(int rank, int k, int m, double a, double b, double g,
+                               double &re, double &im) {
+    // projections: row k -> p = rank - k, column m -> q = rank - m
+    const int p = rank - k, q = rank - m;
+    const double cb = cos(b), sb = sin(b);
+    double d = 0.0;
+    if (rank == 1) {
+        const double s2 = sqrt(0.5);
+        const double t[3][3] = {{(1 + cb) / 2, -sb * s2, (1 - cb) / 2},
+                                {sb * s2, cb, -sb * s2},
+                                {(1 - cb) / 2, sb * s2, (1 + cb) / 2}};
+        d = t[k][m];
+    } else if (rank == 2) {
+        const double c2 = cos(b / 2), s2 = sin(b / 2);
+        const double c4 = c2 * c2 * c2 * c2, s4 = s2 * s2 * s2 * s2;
+        const double r38 = sqrt(3.0 / 8.0), r32 = sqrt(1.5);
+        const double t[5][5] = {
+            {c4, -sb * (1 + cb) / 2, r38 * sb * sb, -sb * (1 - cb) / 2, s4},
+            {sb * (1 + cb) / 2, (2 * cb - 1) * (1 + cb) / 2, -r32 * sb * cb, (2 * cb + 1) * (1 - cb) / 2, sb * (cb - 1) / 2},
+            {r38 * sb * sb, r32 * sb * cb, (3 * cb * cb - 1) / 2, -r32 * sb * cb, r38 * sb * sb},
+            {-sb * (cb - 1) / 2, (2 * cb + 1) * (1 - cb) / 2, r32 * sb * cb, (2 * cb - 1) * (1 + cb) / 2, -sb * (cb + 1) / 2},
+            {s4, sb * (1 - cb) / 2, r38 * sb * sb, sb * (1 + cb) / 2, c4}};
+        d = t[k][m];
+    }
+    // D(p,q) = exp(-i p a) d(p,q) exp(-i q g)
+    const double ph = -(p * a + q * g);
+    re = d * cos(ph);
+    im = d * sin(ph);
+}
+
+// Extreme eigenvalues of a symmetric tridiagonal matrix by Sturm bisection.
+__device__ int sturm_count(const double *al, const double *be, int m, double x) {
+    int cnt = 0;
+    double q = al[0] - x;
+    if (q < 0) ++cnt;
+    for (int i = 1; i < m; ++i) {
+        const double den = (q == 0.0) ? 1e-300 : q;
+        q = al[i] - x - be[i - 1] * be[i - 1] / den;
+        if (q < 0) ++cnt;
+    }
+    return cnt;
+}
+__device__ void tridiag_extremes(const double *al, const double *be, int m, double &lo, double &hi) {
+    double glo = CUDART_INF, ghi = -CUDART_INF;
+    for (int i = 0; i < m; ++i) {
+        double r = 0.0;
+        if (i > 0) r += fabs(be[i - 1]);
+        if (i < m - 1) r += fabs(be[i]);
+        glo = fmin(glo, al[i] - r);
+        ghi = fmax(ghi, al[i] + r);
+    }
+    double a = glo, b = ghi;
+    for (int it = 0; it < 100 && b - a > 1e-13 * fmax(fabs(a), fabs(b)) + 1e-300; ++it) {
+        const double x = 0.5 * (a + b);
+        if (sturm_count(al, be, m, x) >= 1) b = x; else a = x;
+    }
+    lo = b;
+    a = glo; b = ghi;
+    for (int it = 0; it < 100 && b - a > 1e-13 * fmax(fabs(a), fabs(b)) + 1e-300; ++it) {
+        const double x = 0.5 * (a + b);
+        if (sturm_count(al, be, m, x) >= m) b = x; else a = x;
+    }
+    hi = a;
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory layout of the propagation kernel
+// ---------------------------------------------------------------------------
+template <bool F64, bool CPLX>
+struct SmemLayout {
+    using P = Prec<F64, CPLX>;
+    size_t coef, red, alpha, beta, slice_off, ell_col, ell_val, diag, xa, xb, part, atau, mu, phase, rec, total;
+    __host__ __device__ static size_t align(size_t x) { return (x + 15) & ~size_t(15); }
+    __host__ __device__ SmemLayout(int n_pad, int nslices, int ell_len, int Kmax, int M, int nthreads) {
+        size_t o = 0;
+        coef = o; o = align(o + sizeof(double) * kMaxCoef);
+        red = o; o = align(o + sizeof(double) * kRedSlots);
+        alpha = o; o = align(o + sizeof(double) * kMaxLanczos);
+        beta = o; o = align(o + sizeof(double) * kMaxLanczos);
+        slice_off = o; o = align(o + sizeof(int) * (nslices + 1));
+        ell_col = o; o = align(o + sizeof(uint16_t) * ell_len);
+        ell_val = o; o = align(o + sizeof(typename P::Val) * ell_len);
+        diag = o; o = align(o + sizeof(typename P::Dg) * n_pad);
+        xa = o; o = align(o + sizeof(typename P::Vec) * n_pad);
+        xb = o; o = align(o + sizeof(typename P::Vec) * n_pad);
+        part = o; o = align(o + sizeof(typename P::Vec) * 64);
+        atau = o; o = align(o + sizeof(typename P::Dg) * Kmax);
+        mu = o; o = align(o + sizeof(typename P::Vec) * Kmax);
+        phase = o; o = align(o + sizeof(typename P::Vec) * (M + 1));
+        rec = o; o = align(o + sizeof(typename P::Vec) * (nthreads > M ? nthreads : M));
+        total = o;
+    }
+};
+
+// Number of Chebyshev/Bessel terms after which |J_k(x)| * e^{k*lg} < tol
+// (Debye-type bound (e x / 2k)^k / sqrt(2 pi k), conservative for k > x).
+__device__ int series_terms(double x, double lg, double tol, int kcap) {
+    if (!(x > 0.0)) return 1;
+    const double ltol = log(tol);
+    int k = max(1, (int)ceil(x) + 1);
+    while (k < kcap) {
+        const double lt = -0.5 * log(2.0 * CUDART_PI * k) + k * log(2.718281828459045 * x / (2.0 * k)) + k * lg;
+        if (lt < ltol) break;
+        ++k;
+    }
+    return k;
+}
+
+// Columns j = 0..M of the table T[k][j] = (2 - delta_k0) J_k(half * j * dt),
+// k < K, by Miller's backward recurrence J_{k-1} = (2k/x) J_k - J_{k+1},
+// normalised with J_0 + 2 sum J_2k = 1.  Rescaling is only needed above the
+// stored range; tiny arguments use the leading terms of the power series.
+__device__ void bessel_columns(double *table, int M, int K, double half, double dt) {
+    for (int j = threadIdx.x; j <= M; j += blockDim.x) {
+        double *col = table + j;
+        const size_t ld = (size_t)(M + 1);
+        const double x = half * j * dt;
+        if (x < 1e-6) {
+            for (int k = 0; k < K; ++k) col[k * ld] = 0.0;
+            col[0] = 1.0 - 0.25 * x * x;
+            if (K > 1) col[ld] = 2.0 * 0.5 * x;
+            if (K > 2) col[2 * ld] = 2.0 * 0.125 * x * x;
+            continue;
+        }
+        const int kneed = min(K, series_terms(x, 0.0, 1e-40, K + 64) + 1);
+        const int base = max(kneed, (int)ceil(x));
+        int kst = base + 20 + (int)sqrt(160.0 * base);
+        kst += kst & 1;
+        double jp1 = 0.0, jk = 1e-30, norm = 0.0;
+        for (int k = kst; k >= 1; --k) {
+            const double jm1 = (2.0 * k / x) * jk - jp1;
+            jp1 = jk;
+            jk = jm1;                                   // J_{k-1}, unnormalised
+            const int km1 = k - 1;
+            if (km1 > 0 && (km1 & 1) == 0) norm += 2.0 * jk;
+            if (km1 < kneed) {
+                col[km1 * ld] = jk;
+            } else if (fabs(jk) > 1e200) {
+                jk *= 1e-200; jp1 *= 1e-200; norm *= 1e-200;
+            }
+        }
+        norm += jk;                                     // + J_0
+        const double inv = 1.0 / norm;
+        col[0] = col[0] * inv;
+        for (int k = 1; k < kneed; ++k) col[k * ld] = 2.0 * col[k * ld] * inv;
+        for (int k = kneed; k < K; ++k) col[k * ld] = 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The propagation kernel
+// ---------------------------------------------------------------------------
+template <bool F64, bool CPLX, int RMAX>
+__global__ void __launch_bounds__(512)
+powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
+    using P = Prec<F64, CPLX>;
+    using Vec = typename P::Vec;
+    using Val = typename P::Val;
+    using Dg = typename P::Dg;
+    using Real = typename P::Real;
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    const SmemLayout<F64, CPLX> L(sys.n_pad, sys.nslices, sys.ell_len, run.Kmax, run.M, blockDim.x);
+    double *s_coef = reinterpret_cast<double *>(smem + L.coef);
+    double *s_red = reinterpret_cast<double *>(smem + L.red);
+    double *s_al = reinterpret_cast<double *>(smem + L.alpha);
+    double *s_be = reinterpret_cast<double *>(smem + L.beta);
+    int *s_soff = reinterpret_cast<int *>(smem + L.slice_off);
+    uint16_t *s_col = reinterpret_cast<uint16_t *>(smem + L.ell_col);
+    Val *s_val = reinterpret_cast<Val *>(smem + L.ell_val);
+    Dg *s_diag = reinterpret_cast<Dg *>(smem + L.diag);
+    Vec *s_xa = reinterpret_cast<Vec *>(smem + L.xa);
+    Vec *s_xb = reinterpret_cast<Vec *>(smem + L.xb);
+    Vec *s_part = reinterpret_cast<Vec *>(smem + L.part);
+    Dg *s_atau = reinterpret_cast<Dg *>(smem + L.atau);
+    Vec *s_mu = reinterpret_cast<Vec *>(smem + L.mu);
+    Vec *s_phase = reinterpret_cast<Vec *>(smem + L.phase);
+    Vec *s_rec = reinterpret_cast<Vec *>(smem + L.rec);
+    __shared__ double s_scalar[8];
+    __shared__ int s_int[4];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int n = sys.n;
+    const int M = run.M;
+    const int nsteps = run.nsteps;
+    double *table = run.table + (size_t)blockIdx.x * run.Kmax * (M + 1);
+    const int rows_per_lane = (sys.nslices + nwarps - 1) / nwarps;
+
+    // Static pattern: copy once per CTA.
+    for (int i = tid; i <= sys.nslices; i += blockDim.x) s_soff[i] = sys.slice_off[i];
+    for (int e = tid; e < sys.ell_len; e += blockDim.x) s_col[e] = sys.ell_col[e];
+
+    for (int o = blockIdx.x; o < run.n_orient; o += gridDim.x) {
+        if (rows_per_lane > RMAX) {                  // launch configuration error
+            if (tid == 0) run.status[o] = kDevTooManyRows;
+            continue;
+        }
+        // ---- 1. rotational coefficients (FP64) --------------------------------
+        __syncthreads();
+        for (int t = tid; t < sys.nterms; t += blockDim.x) {
+            double re, im;
+            wigner_element(sys.term_rkm[3 * t], sys.term_rkm[3 * t + 1], sys.term_rkm[3 * t + 2],
+                           run.alpha[o], run.beta[o], run.gamma[o], re, im);
+            s_coef[1 + 2 * t] = re;
+            s_coef[2 + 2 * t] = im;
+        }
+        if (tid == 0) s_coef[0] = 1.0;
+        __syncthreads();
+
+        // ---- 2. assemble L(Omega) in FP64, store in working precision ---------
+        double gmax = -CUDART_INF, gmin = CUDART_INF;
+        for (int e = tid; e < sys.ell_len; e += blockDim.x) {
+            double re = 0.0, im = 0.0;
+            for (int s = 0; s < sys.nstreams; ++s) {
+                const double c = s_coef[sys.stream_coef[s]];
+                re = fma(c, sys.ell_re[(size_t)s * sys.ell_len + e], re);
+                if (CPLX) im = fma(c, sys.ell_im[(size_t)s * sys.ell_len + e], im);
+            }
+            pack(s_val[e], re, im);
+        }
+        for (int i = tid; i < sys.n_pad; i += blockDim.x) {
+            double re = 0.0, im = 0.0;
+            for (int s = 0; s < sys.nstreams; ++s) {
+                const double c = s_coef[sys.stream_coef[s]];
+                const double2 d = sys.diag[(size_t)s * sys.n_pad + i];
+                re = fma(c, d.x, re);
+                im = fma(c, d.y, im);
+            }
+            pack(s_diag[i], re, im);
+        }
+        __syncthreads();
+        // Gershgorin interval of the Hermitian part (real diagonal + off-diagonal)
+        for (int r = 0; r < rows_per_lane; ++r) {
+            const int sl = warp + r * nwarps;
+            if (sl >= sys.nslices) break;
+            const int row = sl * 32 + lane;
+            if (row >= n) continue;
+            const int off = s_soff[sl], w = (s_soff[sl + 1] - off) >> 5;
+            double rad = 0.0;
+            for (int c = 0; c < w; ++c) {
+                const double2 v = unpack(s_val[off + c * 32 + lane]);
+                rad += sqrt(v.x * v.x + v.y * v.y);
+            }
+            const double dr = unpack(s_diag[row]).x;
+            gmax = fmax(gmax, dr + rad);
+            gmin = fmin(gmin, dr - rad);
+        }
+        gmax = block_max(gmax, s_red);
+        gmin = block_min(gmin, s_red);
+        double imax = 0.0;
+        for (int i = tid; i < n; i += blockDim.x) imax = fmax(imax, fabs(unpack(s_diag[i]).y));
+        imax = block_max(imax, s_red);
+
+        // ---- 3. Lanczos bounds on the Hermitian part ---------------------------
+        Vec q_prev[RMAX], q_cur[RMAX];
+        double nrm2 = 0.0;
+#pragma unroll
+        for (int r = 0; r < RMAX; ++r) {
+            const int row = (warp + r * nwarps) * 32 + lane;
+            const bool own = (r < rows_per_lane) && (warp + r * nwarps < sys.nslices) && row < n;
+            const double v = own ? 1.0 + 0.37 * sin(1.7 * row + 0.3) : 0.0;
+            q_cur[r] = tovec(make_double2(v, 0.0), Vec());
+            q_prev[r] = vzero<Vec>();
+            nrm2 += v * v;
+        }
+        nrm2 = block_sum(nrm2, s_red);
+        {
+            const double inv = 1.0 / sqrt(nrm2);
+#pragma unroll
+            for (int r = 0; r < RMAX; ++r) {
+                if (r >= rows_per_lane) break;
+                const int sl = warp + r * nwarps;
+                if (sl >= sys.nslices) break;
+                q_cur[r].x *= inv; q_cur[r].y *= inv;
+                s_xa[sl * 32 + lane] = q_cur[r];
+            }
+        }
+        int m_eff = 0;
+        double beta_prev = 0.0;
+        const int lits = min(run.lanczos_its, min(kMaxLanczos, n));
+        for (int j = 0; j < lits; ++j) {
+            __syncthreads();
+            Vec wv[RMAX];
+            double alpha_p = 0.0;
+#pragma unroll
+            for (int r = 0; r < RMAX; ++r) {
+                wv[r] = vzero<Vec>();
+                if (r >= rows_per_lane) continue;
+                const int sl = warp + r * nwarps;
+                if (sl >= sys.nslices) continue;
+                const int row = sl * 32 + lane;
+                if (row >= n) continue;
+                const int off = s_soff[sl], w = (s_soff[sl + 1] - off) >> 5;
+                Vec y = vzero<Vec>();
+                for (int c = 0; c < w; ++c) {
+                    const int e = off + c * 32 + lane;
+                    mac(y, s_val[e], s_xa[s_col[e]]);
+                }
+                const double dr = unpack(s_diag[row]).x;
+                y.x += (Real)dr * q_cur[r].x;
+                y.y += (Real)dr * q_cur[r].y;
+                y.x -= (Real)beta_prev * q_prev[r].x;
+                y.y -= (Real)beta_prev * q_prev[r].y;
+                wv[r] = y;
+                alpha_p += (double)q_cur[r].x * y.x + (double)q_cur[r].y * y.y;
+            }
+            const double alpha = block_sum(alpha_p, s_red);
+            double b2 = 0.0;
+#pragma unroll
+            for (int r = 0; r < RMAX; ++r) {
+                wv[r].x -= (Real)alpha * q_cur[r].x;
+                wv[r].y -= (Real)alpha * q_cur[r].y;
+                b2 += (double)wv[r].x * wv[r].x + (double)wv[r].y * wv[r].y;
+            }
+            const double beta = sqrt(block_sum(b2, s_red));
+            if (tid == 0) { s_al[j] = alpha; s_be[j] = beta; }
+            m_eff = j + 1;
+            if (!(beta > 1e-12 * (fabs(alpha) + 1e-300))) break;   // invariant subspace
+            const double inv = 1.0 / beta;
+#pragma unroll
+            for (int r = 0; r < RMAX; ++r) {
+                q_prev[r] = q_cur[r];
+                q_cur[r].x = wv[r].x * (Real)inv;
+                q_cur[r].y = wv[r].y * (Real)inv;
+                if (r < rows_per_lane) {
+                    const int sl = warp + r * nwarps;
+                    if (sl < sys.nslices) s_xb[sl * 32 + lane] = q_cur[r];
+                }
+            }
+            Vec *t = s_xa; s_xa = s_xb; s_xb = t;
+            beta_prev = beta;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double tlo, thi;
+            tridiag_extremes(s_al, s_be, m_eff, tlo, thi);
+            const double bl = fabs(s_be[m_eff - 1]);
+            double hi = fmin(thi + bl, gmax), lo = fmax(tlo - bl, gmin);
+            if (!(hi >= lo)) { hi = gmax; lo = gmin; }
+            const double width = hi - lo;
+            const double scale = fmax(fabs(hi), fabs(lo));
+            const double half = 0.5 * width * 1.01 + 1e-9 * scale + 1e-30;
+            s_scalar[0] = 0.5 * (hi + lo);   // centre c
+            s_scalar[1] = half;              // half-width s
+            // series length for the chunk (x = s*M*dt) incl. growth from Im(L)
+            const double x = half * M * run.dt;
+            const double lg = 2.0 * imax / half;
+            int K = max(2, series_terms(x, lg, run.tol, run.Kmax + 1)) + 2;
+            s_int[0] = K;
+            s_int[1] = (K > run.Kmax) ? 1 : 0;
+        }
+        __syncthreads();
+        const double cen = s_scalar[0], half = s_scalar[1];
+        const int K = s_int[0];
+        if (s_int[1]) {
+            if (tid == 0) { run.status[o] = kDevTableTooSmall; run.kused[o] = K; run.halfwidth[o] = half; }
+            continue;
+        }
+
+        // ---- 4. rescale to L~ = (L - c)/s -------------------------------------
+        {
+            const double inv = 1.0 / half;
+            for (int e = tid; e < sys.ell_len; e += blockDim.x) {
+                const double2 v = unpack(s_val[e]);
+                pack(s_val[e], v.x * inv, v.y * inv);
+            }
+            for (int i = tid; i < sys.n_pad; i += blockDim.x) {
+                const double2 d = unpack(s_diag[i]);
+                pack(s_diag[i], (d.x - cen) * inv, d.y * inv);
+            }
+        }
+
+        // ---- 5. Bessel table J_k(s j dt), j = 0..M --------------------------
+        bessel_columns(table, M, K, half, run.dt);
+        __syncthreads();
+        // series coefficients of one chunk (tau = M dt), centre phase folded in
+        {
+            const double tau = M * run.dt;
+            const double pr = cos(-cen * tau), pi_ = sin(-cen * tau);
+            for (int k = tid; k < K; k += blockDim.x) {
+                const double jv = table[(size_t)k * (M + 1) + M];
+                // (-i)^k * e^{-i c tau} * jv   (factor 2 for k>0 is already in the table)
+                double re, im;
+                switch (k & 3) {
+                    case 0: re = pr; im = pi_; break;
+                    case 1: re = pi_; im = -pr; break;
+                    case 2: re = -pr; im = -pi_; break;
+                    default: re = -pi_; im = pr; break;
+                }
+                pack(s_atau[k], re * jv, im * jv);
+            }
+            for (int j = tid; j < M; j += blockDim.x) {
+                const double ph = -cen * j * run.dt;
+                s_phase[j] = tovec(make_double2(cos(ph), sin(ph)), Vec());
+            }
+        }
+
+        // ---- 6. chunked Chebyshev propagation with fused coil projection -------
+        Vec t_prev[RMAX], t_cur[RMAX], acc[RMAX], cc[RMAX];
+#pragma unroll
+        for (int r = 0; r < RMAX; ++r) {
+            t_prev[r] = vzero<Vec>(); t_cur[r] = vzero<Vec>(); acc[r] = vzero<Vec>(); cc[r] = vzero<Vec>();
+            if (r < rows_per_lane) {
+                const int sl = warp + r * nwarps;
+                if (sl < sys.nslices) {
+                    const int row = sl * 32 + lane;
+                    t_cur[r] = tovec(sys.rho0[row], Vec());
+                    cc[r] = tovec(sys.coil[row], Vec());
+                }
+            }
+        }
+        const int nchunks = (nsteps + M) / M;        // ceil((nsteps+1)/M)
+        Vec *fid_out = reinterpret_cast<Vec *>(run.fids) + (size_t)o * (nsteps + 1);
+        int status = kDevOk;
+        for (int a = 0; a < nchunks && status == kDevOk; ++a) {
+            const bool advance = (a + 1 < nchunks);
+            double start_max = 0.0;
+            // k = 0: t0 = rho
+            {
+                Vec mom = vzero<Vec>();
+#pragma unroll
+                for (int r = 0; r < RMAX; ++r) {
+                    if (r >= rows_per_lane) break;
+                    const int sl = warp + r * nwarps;
+                    if (sl >= sys.nslices) break;
+                    s_xa[sl * 32 + lane] = t_cur[r];
+                    cdot_acc(mom, cc[r], t_cur[r]);
+                    acc[r] = vzero<Vec>();
+                    mac(acc[r], s_atau[0], t_cur[r]);
+                    start_max += (double)t_cur[r].x * t_cur[r].x + (double)t_cur[r].y * t_cur[r].y;
+                    t_prev[r] = vzero<Vec>();
+                }
+                mom = warp_sum(mom);
+                if (lane == 0) s_part[warp] = mom;
+            }
+            __syncthreads();
+            if (warp == 0) {
+                Vec v = (lane < nwarps) ? s_part[lane] : vzero<Vec>();
+                v = warp_sum(v);
+                if (lane == 0) s_mu[0] = v;
+            }
+            // k = 1 .. K-1: t_k = (k==1 ? 1 : 2) L~ t_{k-1} - t_{k-2}
+            for (int k = 1; k < K; ++k) {
+                Vec *src = (k & 1) ? s_xa : s_xb;
+                Vec *dst = (k & 1) ? s_xb : s_xa;
+                Vec *part = s_part + ((k & 1) ? 32 : 0);
+                const Real two = (k == 1) ? (Real)1 : (Real)2;
+                Vec mom = vzero<Vec>();
+#pragma unroll
+                for (int r = 0; r < RMAX; ++r) {
+                    if (r >= rows_per_lane) break;
+                    const int sl = warp + r * nwarps;
+                    if (sl >= sys.nslices) break;
+                    const int row = sl * 32 + lane;
+                    const int off = s_soff[sl], w = (s_soff[sl + 1] - off) >> 5;
+                    Vec y = vzero<Vec>();
+                    mac(y, s_diag[row], t_cur[r]);
+                    for (int c = 0; c < w; ++c) {
+                        const int e = off + c * 32 + lane;
+                        mac(y, s_val[e], src[s_col[e]]);
+                    }
+                    Vec tn;
+                    tn.x = two * y.x - t_prev[r].x;
+                    tn.y = two * y.y - t_prev[r].y;
+                    t_prev[r] = t_cur[r];
+                    t_cur[r] = tn;
+                    dst[row] = tn;
+                    cdot_acc(mom, cc[r], tn);
+                    if (advance) mac(acc[r], s_atau[k], tn);
+                }
+                mom = warp_sum(mom);
+                if (lane == 0) part[warp] = mom;
+                __syncthreads();
+                if (warp == 0) {
+                    Vec v = (lane < nwarps) ? part[lane] : vzero<Vec>();
+                    v = warp_sum(v);
+                    if (lane == 0) s_mu[k] = v;
+                }
+            }
+            __syncthreads();
+            // FID points of this chunk: f_j = ph_j * sum_k J_k(s j dt) (-i)^k mu_k
+            {
+                const int parts = max(1, (int)blockDim.x / M);
+                const int kper = (K + parts - 1) / parts;
+                for (int jj = tid; jj < M * parts; jj += blockDim.x) {
+                    const int j = jj % M, pidx = jj / M;
+                    const int k0 = pidx * kper, k1 = min(K, k0 + kper);
+                    Vec f = vzero<Vec>();
+                    for (int k = k0; k < k1; ++k) {
+                        const Real jv = (Real)table[(size_t)k * (M + 1) + j];
+                        const Vec mu = s_mu[k];
+                        Real re, im;
+                        switch (k & 3) {
+                            case 0: re = mu.x; im = mu.y; break;
+                            case 1: re = mu.y; im = -mu.x; break;
+                            case 2: re = -mu.x; im = -mu.y; break;
+                            default: re = -mu.y; im = mu.x; break;
+                        }
+                        f.x += jv * re;
+                        f.y += jv * im;
+                    }
+                    s_rec[jj] = f;
+                }
+                __syncthreads();
+                for (int j = tid; j < M; j += blockDim.x) {
+                    Vec f = vzero<Vec>();
+                    for (int pidx = 0; pidx < parts; ++pidx) {
+                        const Vec g = s_rec[pidx * M + j];
+                        f.x += g.x; f.y += g.y;
+                    }
+                    const Vec ph = s_phase[j];
+                    Vec out;
+                    out.x = ph.x * f.x - ph.y * f.y;
+                    out.y = ph.x * f.y + ph.y * f.x;
+                    const int nidx = a * M + j;
+                    if (nidx <= nsteps) fid_out[nidx] = out;
+                }
+            }
+            // next chunk starts from the accumulated state; guard against a
+            // violated spectral bound (the series would then grow, not decay)
+            double end_n2 = 0.0;
+#pragma unroll
+            for (int r = 0; r < RMAX; ++r) {
+                if (r >= rows_per_lane) break;
+                if (advance) t_cur[r] = acc[r];
+                end_n2 += (double)t_cur[r].x * t_cur[r].x + (double)t_cur[r].y * t_cur[r].y;
+            }
+            end_n2 = block_sum(end_n2, s_red);
+            start_max = block_sum(start_max, s_red);
+            if (!isfinite(end_n2)) status = kDevNonFinite;
+            else if (end_n2 > 16.0 * start_max + 1e-300) status = kDevDiverged;
+        }
+        if (tid == 0) {
+            run.status[o] = status;
+            run.kused[o] = K;
+            run.halfwidth[o] = half;
+            run.matvecs[o] = (long long)nchunks * (K - 1);
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Weighted powder sum (kernel/contexts/powder.m:280-287) in FP64.
+// Deterministic: each output point sums its orientations in grid order,
+// split into fixed groups that are combined in fixed order.
+// ---------------------------------------------------------------------------
+template <class Vec>
+__global__ void powder_partial_kernel(const Vec *__restrict__ fids, const double *__restrict__ w,
+                                      int n_orient, int npts, int group, double2 *__restrict__ part) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = blockIdx.y;
+    if (t >= npts) return;
+    const int o0 = g * group, o1 = min(n_orient, o0 + group);
+    double2 s = make_double2(0.0, 0.0);
+    for (int o = o0; o < o1; ++o) {
+        const double2 v = tod(fids[(size_t)o * npts + t]);
+        s.x = fma(w[o], v.x, s.x);
+        s.y = fma(w[o], v.y, s.y);
+    }
+    part[(size_t)g * npts + t] = s;
+}
+
+__global__ void powder_combine_kernel(const double2 *__restrict__ part, int ngroups, int npts,
+                                      double2 *__restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npts) return;
+    double2 s = make_double2(0.0, 0.0);
+    for (int g = 0; g < ngroups; ++g) {
+        const double2 v = part[(size_t)g * npts + t];
+        s.x += v.x; s.y += v.y;
+    }
+    out[t] = s;
+}
+
+}  // namespace spx

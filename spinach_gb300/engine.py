@@ -1,0 +1,196 @@
+"""ctypes binding of the C ABI in include/spinach_gpu.h.
+
+The shared library is built in-tree (``spinach_gb300/lib/libspinach_gpu.so``)
+by ``spinach_gb300.build``.  There is no CPU fallback: constructing an
+``Engine`` without the library, or without a CUDA device, raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+import scipy.sparse as sp
+
+LIB_PATH = os.path.join(os.path.dirname(__file__), 'lib', 'libspinach_gpu.so')
+
+FP32, FP64 = 0, 1
+
+
+class SpxCsc(C.Structure):
+    _fields_ = [('n', C.c_int64), ('colptr', C.POINTER(C.c_int64)),
+                ('rowidx', C.POINTER(C.c_int64)), ('values', C.POINTER(C.c_double))]
+
+
+class SpxOptions(C.Structure):
+    _fields_ = [('precision', C.c_int32), ('chunk_steps', C.c_int32), ('threads', C.c_int32),
+                ('reserved0', C.c_int32), ('series_tol', C.c_double), ('reserved1', C.c_double)]
+
+
+class SpxStats(C.Structure):
+    _fields_ = [('n_orientations', C.c_int64), ('nsteps', C.c_int64), ('matvecs', C.c_int64),
+                ('orientations_failed', C.c_int64), ('chunk_steps', C.c_int32),
+                ('max_terms', C.c_int32), ('threads', C.c_int32), ('precision', C.c_int32),
+                ('kernel_ms', C.c_double), ('reduce_ms', C.c_double),
+                ('min_half_width', C.c_double), ('max_half_width', C.c_double),
+                ('dim', C.c_int64), ('nnz', C.c_int64), ('ell_entries', C.c_int64),
+                ('value_streams', C.c_int32), ('real_offdiag', C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# Every entry point of include/spinach_gpu.h with its ctypes signature.
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+SIGNATURES = {
+    'spx_create': (C.c_int, [C.POINTER(_P), C.c_int]),
+    'spx_destroy': (C.c_int, [_P]),
+    'spx_upload_system': (C.c_int, [_P, C.POINTER(SpxCsc), C.c_int32, C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(SpxCsc),
+                                    C.POINTER(SpxCsc), _D, _D]),
+    'spx_run_powder': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64,
+                                 C.POINTER(SpxOptions), _D, _D]),
+    'spx_run_powder_device': (C.c_int, [_P, C.c_int64, _P, _P, _P, _P, C.c_double, C.c_int64,
+                                        C.POINTER(SpxOptions), _P]),
+    'spx_synchronize': (C.c_int, [_P]),
+    'spx_get_stream': (_P, [_P]),
+    'spx_get_stats': (C.c_int, [_P, C.POINTER(SpxStats)]),
+    'spx_status_string': (C.c_char_p, [C.c_int]),
+    'spx_last_error': (C.c_char_p, [_P]),
+    'spx_version': (C.c_char_p, []),
+}
+
+
+class SpxError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f'spinach_gpu error {code}: {message}')
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the engine library and bind every declared entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f'{path} is missing: build it with spinach_gb300.build.build_library()')
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+class _CscHolder:
+    """Keeps numpy buffers of one MATLAB-layout CSC matrix alive."""
+
+    def __init__(self, A, n: int):
+        A = sp.csc_matrix(A, shape=(n, n)).astype(np.complex128)
+        A.sort_indices()
+        self.colptr = np.ascontiguousarray(A.indptr, dtype=np.int64)
+        self.rowidx = np.ascontiguousarray(A.indices, dtype=np.int64)
+        self.values = np.ascontiguousarray(A.data.view(np.float64) if A.nnz else np.zeros(2))
+        self.struct = SpxCsc(n, self.colptr.ctypes.data_as(C.POINTER(C.c_int64)),
+                             self.rowidx.ctypes.data_as(C.POINTER(C.c_int64)), _dptr(self.values))
+
+
+@dataclass
+class PowderResult:
+    fid: np.ndarray                    # (nsteps+1,) complex128
+    fids: np.ndarray | None            # (n_orient, nsteps+1) complex128 or None
+    stats: dict
+
+
+class Engine:
+    """One device handle with one uploaded spin system."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        self._check(self.lib.spx_create(C.byref(h), device), None)
+        self.h = h
+        self.dim = None
+
+    def _check(self, status: int, handle):
+        if status != 0:
+            detail = self.lib.spx_last_error(handle).decode() if handle else ''
+            raise SpxError(status, f'{self.lib.spx_status_string(status).decode()}: {detail}')
+
+    def close(self):
+        if getattr(self, 'h', None):
+            self.lib.spx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, I, terms: dict, R=None, rho0=None, coil=None):
+        """Upload ``I`` and the rotational-basis terms ``{(rank, k, m): Q}`` (0-based
+        k, m), the relaxation superoperator ``R`` (or None), and the states."""
+        n = I.shape[0]
+        keys = sorted(terms)
+        self._holders = [_CscHolder(I, n)] + [_CscHolder(terms[k], n) for k in keys]
+        Qarr = (SpxCsc * max(1, len(keys)))(*[h.struct for h in self._holders[1:]])
+        rank = np.array([k[0] for k in keys] or [0], np.int32)
+        kk = np.array([k[1] for k in keys] or [0], np.int32)
+        mm = np.array([k[2] for k in keys] or [0], np.int32)
+        Rh = _CscHolder(R, n) if R is not None else None
+        rho0 = np.ascontiguousarray(np.asarray(rho0, np.complex128).view(np.float64))
+        coil = np.ascontiguousarray(np.asarray(coil, np.complex128).view(np.float64))
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+        self._check(self.lib.spx_upload_system(
+            self.h, C.byref(self._holders[0].struct), len(keys), ip(rank), ip(kk), ip(mm), Qarr,
+            C.byref(Rh.struct) if Rh else None, _dptr(rho0), _dptr(coil)), self.h)
+        self.dim = n
+
+    def run(self, alphas, betas, gammas, weights, dt: float, nsteps: int, precision: int = FP32,
+            per_orientation: bool = False, chunk_steps: int = 0, threads: int = 0,
+            series_tol: float = 0.0) -> PowderResult:
+        al = np.ascontiguousarray(alphas, np.float64)
+        be = np.ascontiguousarray(betas, np.float64)
+        ga = np.ascontiguousarray(gammas, np.float64)
+        w = np.ascontiguousarray(weights, np.float64)
+        no = al.size
+        fid = np.zeros(2 * (nsteps + 1))
+        fids = np.zeros(2 * (nsteps + 1) * no) if per_orientation else None
+        opt = SpxOptions(precision, chunk_steps, threads, 0, series_tol, 0.0)
+        self._check(self.lib.spx_run_powder(self.h, no, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
+                                            float(dt), int(nsteps), C.byref(opt), _dptr(fid),
+                                            _dptr(fids) if fids is not None else None), self.h)
+        return PowderResult(fid.view(np.complex128), None if fids is None else
+                            fids.view(np.complex128).reshape(no, nsteps + 1), self.stats())
+
+    def run_device(self, d_alphas: int, d_betas: int, d_gammas: int, d_weights: int, n_orient: int,
+                   dt: float, nsteps: int, d_fid: int, precision: int = FP32, chunk_steps: int = 0,
+                   threads: int = 0, series_tol: float = 0.0):
+        """Enqueue a run on device-resident buffers (raw device pointers); no sync."""
+        opt = SpxOptions(precision, chunk_steps, threads, 0, series_tol, 0.0)
+        self._check(self.lib.spx_run_powder_device(self.h, n_orient, d_alphas, d_betas, d_gammas,
+                                                   d_weights, float(dt), int(nsteps), C.byref(opt),
+                                                   d_fid), self.h)
+
+    def synchronize(self):
+        self._check(self.lib.spx_synchronize(self.h), self.h)
+
+    @property
+    def stream(self) -> int:
+        return self.lib.spx_get_stream(self.h) or 0
+
+    def stats(self) -> dict:
+        st = SpxStats()
+        self._check(self.lib.spx_get_stats(self.h, C.byref(st)), self.h)
+        return st.as_dict()

@@ -1,0 +1,47 @@
+"""Generate the FP64 oracle fixtures used by the GPU parity tests.
+
+Run from the repository root:  python tests/golden/make_golden.py
+Writes tests/golden/*.npz.  Inputs are the seeded workloads of
+spinach_gb300.workloads; FIDs come from the oracle (oracle/spinach_ref.py).
+"""
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from spinach_gb300 import workloads as W  # noqa: E402
+from oracle_cases import oracle_powder  # noqa: E402
+
+
+def save(name, **kw):
+    np.savez_compressed(os.path.join(HERE, name), **kw)
+    print('wrote', name, {k: getattr(v, 'shape', v) for k, v in kw.items()})
+
+
+def main():
+    t = time.time()
+    # c0: full 200-point grid, 1024 steps, default tolerances (expm branch, dim < 200)
+    w = W.c0()
+    g = W.zcwn_grid(w.n_orient)
+    fid = oracle_powder(w, g)
+    save('c0_powder_fp64.npz', fid=fid, seed=w.seed, nsteps=w.nsteps, n_orient=w.n_orient)
+    # c1: three orientations, 2048 steps; Krylov branch (step.m) and propagator branch
+    w = W.c1()
+    al, be, ga, wt = W.zcwn_grid(w.n_orient)
+    sel = np.array([0, 333, 777])
+    sub = (al[sel], be[sel], ga[sel], np.full(sel.size, 1.0 / sel.size))
+    fk = oracle_powder(w, sub, krylov=True, sum_up=False)
+    save('c1_orient_krylov_fp64.npz', sel=sel, fids=np.array(fk), seed=w.seed, nsteps=w.nsteps)
+    fp = oracle_powder(w, (sub[0][:1], sub[1][:1], sub[2][:1], np.ones(1)), krylov=False, sum_up=False)
+    save('c1_orient_propagator_fp64.npz', sel=sel[:1], fids=np.array(fp), seed=w.seed, nsteps=w.nsteps)
+    print('done in', round(time.time() - t, 1), 's')
+
+
+if __name__ == '__main__':
+    main()
