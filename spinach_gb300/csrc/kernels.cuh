@@ -554,7 +554,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             if (!(hi >= lo)) { hi = gmax; lo = gmin; }
             const double width = hi - lo;
             const double scale = fmax(fabs(hi), fabs(lo));
-            const double half = 0.5 * width * 1.01 + 1e-9 * scale + 1e-30;
+            // the width must also cover the dissipative (imaginary) extent of L
+            const double half = fmax(0.5 * width * 1.01 + 1e-9 * scale, imax) + 1e-30;
             s_scalar[0] = 0.5 * (hi + lo);   // centre c
             s_scalar[1] = half;              // half-width s
             // series length for the chunk (x = s*M*dt) incl. growth from Im(L)
