@@ -430,7 +430,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
 
 void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be,
                    const double *d_ga, const double *d_w, double dt, int64_t nsteps,
-                   const spx_options &opt, double2 *d_out, const Config &c) {
+                   const spx_options &opt, double2 *d_out, const Config &c, int safe_bounds = 0) {
     const bool f64 = opt.precision == SPX_FP64;
     const size_t npts = (size_t)nsteps + 1;
     const size_t vec_bytes = f64 ? sizeof(double2) : sizeof(float2);
@@ -451,7 +451,7 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     spx::DevRun run{};
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
-    run.lanczos_its = 32; run.fids = h->d_fids.p; run.table = h->d_table.p;
+    run.lanczos_its = 32; run.safe_bounds = safe_bounds; run.fids = h->d_fids.p; run.table = h->d_table.p;
     run.status = h->d_status.p; run.matvecs = h->d_matvecs.p; run.halfwidth = h->d_halfwidth.p;
     run.kused = h->d_kused.p;
 
@@ -648,19 +648,21 @@ spx_status spx_run_powder(spx_handle *h, int64_t n_orient, const double *alphas,
         try {
             finish_run(h);
         } catch (const SpxError &e) {
-            // one retry with a wider coefficient table if that was the only problem
+            // one retry: a wider coefficient table if that was the only problem,
+            // otherwise the conservative spectral bound
             std::vector<int> status(n_orient), kused(n_orient);
             SPX_CUDA(cudaMemcpy(status.data(), h->d_status.p, n_orient * sizeof(int), cudaMemcpyDeviceToHost));
             SPX_CUDA(cudaMemcpy(kused.data(), h->d_kused.p, n_orient * sizeof(int), cudaMemcpyDeviceToHost));
-            bool only_table = true;
+            bool retriable = true;
             int kneed = 0;
             for (int64_t i = 0; i < n_orient; ++i) {
-                if (status[i] != spx::kDevOk && status[i] != spx::kDevTableTooSmall) only_table = false;
+                if (status[i] == spx::kDevTooManyRows) retriable = false;
                 kneed = std::max(kneed, kused[i]);
             }
-            if (!only_table) throw;
-            c = choose_config(h, n_orient, dt, nsteps, o, kneed + 8);
-            launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o, h->d_fid.p, c);
+            if (!retriable) throw;
+            c = choose_config(h, n_orient, dt, nsteps, o, 2 * kneed + 16);
+            launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o,
+                          h->d_fid.p, c, 1);
             st = finish_run(h);
         }
         (void)st;

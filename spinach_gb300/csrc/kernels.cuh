@@ -201,6 +201,7 @@ struct DevRun {
     int Kmax;           // width of the Bessel table
     double tol;         // series truncation tolerance
     int lanczos_its;
+    int safe_bounds;    // 1: theta + beta Lanczos bound clamped by Gershgorin
     void *fids;         // n_orient * (nsteps + 1) complex (precision of the run)
     double *table;      // gridDim.x * Kmax * (M + 1) doubles, per-CTA scratch
     int *status;        // n_orient
@@ -276,6 +277,36 @@ __device__ void tridiag_extremes(const double *al, const double *be, int m, doub
         if (sturm_count(al, be, m, x) >= m) b = x; else a = x;
     }
     hi = a;
+}
+
+// |last component| of the normalised eigenvector of the tridiagonal matrix for
+// eigenvalue theta, by three steps of inverse iteration (Thomas algorithm).
+__device__ double ritz_last_component(const double *al, const double *be, int m, double theta) {
+    if (m <= 1) return 1.0;
+    double y[kMaxLanczos], c[kMaxLanczos], d[kMaxLanczos];
+    const double shift = theta + 1e-10 * (fabs(theta) + 1e-300);
+    for (int i = 0; i < m; ++i) y[i] = 1.0;
+    for (int it = 0; it < 3; ++it) {
+        // solve (T - shift) x = y
+        double den = al[0] - shift;
+        if (den == 0.0) den = 1e-300;
+        c[0] = be[0] / den;
+        d[0] = y[0] / den;
+        for (int i = 1; i < m; ++i) {
+            den = (al[i] - shift) - be[i - 1] * c[i - 1];
+            if (den == 0.0) den = 1e-300;
+            c[i] = (i < m - 1) ? be[i] / den : 0.0;
+            d[i] = (y[i] - be[i - 1] * d[i - 1]) / den;
+        }
+        y[m - 1] = d[m - 1];
+        for (int i = m - 2; i >= 0; --i) y[i] = d[i] - c[i] * y[i + 1];
+        double nrm = 0.0;
+        for (int i = 0; i < m; ++i) nrm += y[i] * y[i];
+        nrm = sqrt(nrm);
+        if (!(nrm > 0.0) || !isfinite(nrm)) return 1.0;
+        for (int i = 0; i < m; ++i) y[i] /= nrm;
+    }
+    return fabs(y[m - 1]);
 }
 
 // ---------------------------------------------------------------------------
@@ -550,7 +581,21 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             double tlo, thi;
             tridiag_extremes(s_al, s_be, m_eff, tlo, thi);
             const double bl = fabs(s_be[m_eff - 1]);
-            double hi = fmin(thi + bl, gmax), lo = fmax(tlo - bl, gmin);
+            double hi, lo;
+            if (run.safe_bounds) {
+                // theta +- beta_m (Zhou-Saad upper bound), clamped by Gershgorin
+                hi = fmin(thi + bl, gmax);
+                lo = fmax(tlo - bl, gmin);
+            } else {
+                // Ritz value plus its residual |beta_m * y_m| and 2% of the width;
+                // the propagation checks the norm and the host retries with the
+                // safe bound if this was too tight
+                const double rhi = bl * ritz_last_component(s_al, s_be, m_eff, thi);
+                const double rlo = bl * ritz_last_component(s_al, s_be, m_eff, tlo);
+                const double wid = thi - tlo;
+                hi = fmin(thi + rhi + 0.02 * wid, gmax);
+                lo = fmax(tlo - rlo - 0.02 * wid, gmin);
+            }
             if (!(hi >= lo)) { hi = gmax; lo = gmin; }
             const double width = hi - lo;
             const double scale = fmax(fabs(hi), fabs(lo));
@@ -610,6 +655,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 s_phase[j] = tovec(make_double2(cos(ph), sin(ph)), Vec());
             }
         }
+        __syncthreads();          // coefficients and phases visible before the first term
 
         // ---- 6. chunked Chebyshev propagation with fused coil projection -------
         Vec t_prev[RMAX], t_cur[RMAX], acc[RMAX], cc[RMAX];

@@ -1,0 +1,89 @@
+"""Oracle vs an independent Zeeman-basis model, and the product-side
+spin-system builder vs the oracle's literal restatement."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import spinach_ref as R
+from oracle.kron_model import KronModel
+from oracle_cases import oracle_system, rel_err
+from spinach_gb300 import spin_system as S, workloads as W
+
+
+def _c0_like(relax):
+    w = W.c0()
+    if relax:
+        rng = np.random.default_rng(11)
+        w.r1 = list(rng.uniform(1, 50, 3))
+        w.r2 = list(rng.uniform(100, 900, 3))
+    return w
+
+
+@pytest.mark.parametrize('relax', [False, True])
+def test_full_basis_fid_matches_kron_model(relax):
+    """Basis-invariance: full spherical-tensor basis vs Zeeman Liouville space."""
+    w = _c0_like(relax)
+    ss, I, Q = oracle_system(w)
+    km = KronModel(ss)
+    rho_st, coil_st = R.state(ss, *w.rho0), R.state(ss, *w.coil)
+    # state(...,'exact') is the Hilbert operator applied to the unit state E/sqrt(d)
+    rho_h = km.spin_op(*w.rho0) / np.sqrt(km.dim)
+    coil_h = km.spin_op(*w.coil) / np.sqrt(km.dim)
+    assert abs(np.vdot(coil_st, rho_st) - np.vdot(coil_h.ravel(), rho_h.ravel())) < 1e-14
+    par = dict(rho0=rho_st, coil=coil_st, sweep=1 / w.dt, npoints=129)
+    for ang in [(0.0, 0.7, 1.3), (0.0, 2.1, 5.0), (0.4, 1.0, -0.3)]:
+        f_st = R.powder_orientation_fid(ss, I, Q, par, ang)
+        f_kr = km.fid(ang, rho_h, coil_h, w.dt, 128)
+        # both models form rotating-frame offsets as differences of ~4e9 rad/s
+        # lab-frame numbers: 1e-16 * 4e9 rad/s * 1.3 ms is ~5e-10 of phase
+        assert rel_err(f_st, f_kr) < 1e-8, ang
+
+
+@pytest.mark.parametrize('wl', ['c0', 'c4'])
+def test_builder_matches_oracle_operators(wl):
+    w = getattr(W, wl)()
+    if wl == 'c4':            # keep the CPU suite fast: electron, 14N, three protons
+        w.isotopes = w.isotopes[:5]
+        w.zeeman_eigs, w.zeeman_euler = w.zeeman_eigs[:5], w.zeeman_euler[:5]
+        w.coupling_eigs = {k: v for k, v in w.coupling_eigs.items() if max(k) < 5}
+        w.r1, w.r2 = w.r1[:5], w.r2[:5]
+    ss, I, Q = oracle_system(w)
+    L = W.build(w)
+    assert L.dim == ss.basis.shape[0]
+    scale = max(abs(I).max(), max(abs(q).max() for r in Q for row in Q[r] for q in row if q.nnz))
+    assert abs(L.I - I).max() <= 1e-14 * scale
+    for r in Q:
+        for k in range(2 * r + 1):
+            for m in range(2 * r + 1):
+                ref = Q[r][k][m]
+                got = L.terms.get((r, k, m))
+                if got is None:
+                    assert ref.nnz == 0 or abs(ref).max() <= 1e-14 * scale
+                else:
+                    assert abs(got - ref).max() <= 1e-14 * scale
+    assert np.abs(L.rho0 - R.state(ss, *w.rho0)).max() < 1e-15
+    assert np.abs(L.coil - R.state(ss, *w.coil)).max() < 1e-15
+    assert np.abs(L.R.diagonal() - R.relaxation(ss).diagonal()).max() < 1e-12
+
+
+def test_builder_matches_oracle_c1_basis():
+    w = W.c1()
+    ss, I, Q = oracle_system(w)
+    L = W.build(w)
+    assert L.dim == 1156 == ss.basis.shape[0]
+    assert abs(L.I - I).max() <= 1e-14 * abs(I).max()
+    for (r, k, m), q in L.terms.items():
+        assert abs(q - Q[r][k][m]).max() <= 1e-14 * abs(Q[r][k][m]).max()
+
+
+def test_ik1_basis_dimension_of_epr_radical():
+    """IK-1 level 3 on the electron-centred coupling graph of e + 14N + 10 1H."""
+    w = W.c4()
+    ss = W.spin_system_of(w)
+    b = S.build_basis(ss, 'IK-1', 3)
+    assert b.dim == 2736
+    ss_o = R.create(dict(isotopes=w.isotopes, magnet=w.magnet),
+                    dict(zeeman=dict(eigs=w.zeeman_eigs, euler=w.zeeman_euler),
+                         coupling=dict(eigs=w.coupling_eigs, euler=w.coupling_euler)))
+    ss_o = R.basis(ss_o, dict(approximation='IK-1', level=3, space_level=1))
+    assert np.array_equal(ss_o.basis, b.codes)
