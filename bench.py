@@ -246,6 +246,12 @@ def run_gpu(args):
     if world > 1:
         dist.barrier()
     step_ms = [a.elapsed_time(b) for a, b in evs]
+    if args.profile_only:
+        if rank == 0:
+            print(json.dumps({'profile_only': True, 'ms_per_step': statistics.mean(step_ms),
+                              'kernel_ms': statistics.mean(kernel_ms), 'stats': eng.stats()}), flush=True)
+        eng.close()
+        return
     t_total = sum(step_ms) / 1e3
     if world > 1:
         tt = torch.tensor([t_total], dtype=torch.float64)
@@ -340,6 +346,8 @@ def main():
     ap.add_argument('--workload', default='c1')
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--profile-only', action='store_true',
+                    help='warm-up and timed powder runs only (for ncu captures); no FP64/e2e/CPU legs')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

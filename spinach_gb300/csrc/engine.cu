@@ -92,7 +92,7 @@ struct spx_handle {
     DevBuf<double> d_table;
     DevBuf<unsigned char> d_fids;
     DevBuf<double2> d_part, d_fid;
-    DevBuf<int> d_status, d_kused;
+    DevBuf<int> d_status, d_kused, d_mused;
     DevBuf<long long> d_matvecs;
     DevBuf<double> d_halfwidth;
 
@@ -339,6 +339,8 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
 // ---------------------------------------------------------------------------
 struct Config {
     int threads, rmax, M, Kmax, grid;
+    bool fixed;
+    double chunk_x;
     size_t smem;
     double tol;
 };
@@ -399,18 +401,15 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     if (rows > 8) throw SpxError(SPX_ERR_UNSUPPORTED, "Liouville dimension too large for the register-resident kernel");
     c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 8;
     c.threads = nwarps * 32;
-    // chunk: about 150 series terms per chunk from an estimate of the half-width
-    const double s_est = std::max(h->g_upper / 1.5, 1e-300);
-    int M = opt.chunk_steps;
-    if (M <= 0) {
-        const double target = 150.0 / (s_est * dt);
-        M = 4;
-        while (M * 2 <= target && M < 256) M *= 2;
-    }
+    // chunk: each orientation picks a power-of-two step count whose series
+    // argument s*M*dt is about chunk_x (kernel side); M here is the cap.
+    c.fixed = opt.chunk_steps > 0;
+    c.chunk_x = f64 ? 150.0 : 150.0;
+    int M = c.fixed ? opt.chunk_steps : 256;
     M = (int)std::min<int64_t>(M, nsteps + 1);
     M = std::max(M, 1);
     c.M = M;
-    const double xu = h->g_upper * M * dt;
+    const double xu = c.fixed ? std::max(h->g_upper * M * dt, 1.0) : c.chunk_x;
     const double lg = (h->g_upper > 0) ? 2.0 * h->max_im_diag / (h->g_upper / 4.0) : 0.0;
     int K = (int)host_series_terms(xu, std::min(lg, 0.05), c.tol) + 16;
     if (kmax_override > 0) K = std::max(K, kmax_override);
@@ -438,6 +437,7 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     h->d_table.reserve((size_t)c.grid * c.Kmax * (c.M + 1));
     h->d_status.reserve(n_orient);
     h->d_kused.reserve(n_orient);
+    h->d_mused.reserve(n_orient);
     h->d_matvecs.reserve(n_orient);
     h->d_halfwidth.reserve(n_orient);
 
@@ -451,9 +451,11 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     spx::DevRun run{};
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
+    run.fixed_chunk = c.fixed ? 1 : 0; run.chunk_x = c.chunk_x;
     run.lanczos_its = 32; run.safe_bounds = safe_bounds; run.fids = h->d_fids.p; run.table = h->d_table.p;
     run.status = h->d_status.p; run.matvecs = h->d_matvecs.p; run.halfwidth = h->d_halfwidth.p;
     run.kused = h->d_kused.p;
+    run.mused = h->d_mused.p;
 
     const void *kfn = select_kernel(f64, h->cplx, c.rmax);
     void *args[] = {&sys, &run};
@@ -498,11 +500,12 @@ spx_status finish_run(spx_handle *h) {
     if (!h->stats_pending) return SPX_OK;
     h->stats_pending = false;
     const int64_t no = h->last_norient;
-    std::vector<int> status(no), kused(no);
+    std::vector<int> status(no), kused(no), mused(no);
     std::vector<long long> mv(no);
     std::vector<double> hw(no);
     SPX_CUDA(cudaMemcpy(status.data(), h->d_status.p, no * sizeof(int), cudaMemcpyDeviceToHost));
     SPX_CUDA(cudaMemcpy(kused.data(), h->d_kused.p, no * sizeof(int), cudaMemcpyDeviceToHost));
+    SPX_CUDA(cudaMemcpy(mused.data(), h->d_mused.p, no * sizeof(int), cudaMemcpyDeviceToHost));
     SPX_CUDA(cudaMemcpy(mv.data(), h->d_matvecs.p, no * sizeof(long long), cudaMemcpyDeviceToHost));
     SPX_CUDA(cudaMemcpy(hw.data(), h->d_halfwidth.p, no * sizeof(double), cudaMemcpyDeviceToHost));
     float ms0 = 0, ms1 = 0;
@@ -511,7 +514,7 @@ spx_status finish_run(spx_handle *h) {
     h->stats.kernel_ms = ms0;
     h->stats.reduce_ms = ms1;
     int64_t failed = 0, matvecs = 0;
-    int maxk = 0;
+    int maxk = 0, maxm = 0;
     double hmin = INFINITY, hmax = 0.0;
     int first_bad = -1, first_code = 0;
     for (int64_t o = 0; o < no; ++o) {
@@ -521,11 +524,13 @@ spx_status finish_run(spx_handle *h) {
         }
         matvecs += mv[o];
         maxk = std::max(maxk, kused[o]);
+        maxm = std::max(maxm, mused[o]);
         hmin = std::min(hmin, hw[o]);
         hmax = std::max(hmax, hw[o]);
     }
     h->stats.matvecs = matvecs;
     h->stats.max_terms = maxk;
+    h->stats.chunk_steps = maxm;
     h->stats.orientations_failed = failed;
     h->stats.min_half_width = hmin;
     h->stats.max_half_width = hmax;

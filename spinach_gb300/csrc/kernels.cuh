@@ -197,7 +197,9 @@ struct DevRun {
     const double *alpha, *beta, *gamma;
     double dt;
     int nsteps;
-    int M;              // time steps per chunk
+    int M;              // largest time-step count per chunk (table height - 1)
+    int fixed_chunk;    // 1: every orientation uses M; 0: choose per orientation
+    double chunk_x;     // target series argument s*M*dt of one chunk
     int Kmax;           // width of the Bessel table
     double tol;         // series truncation tolerance
     int lanczos_its;
@@ -208,6 +210,7 @@ struct DevRun {
     long long *matvecs; // n_orient
     double *halfwidth;  // n_orient
     int *kused;         // n_orient
+    int *mused;         // n_orient: time steps per chunk used
 };
 
 // ---------------------------------------------------------------------------
@@ -337,6 +340,24 @@ struct SmemLayout {
         total = o;
     }
 };
+
+// acc += a * t.  In FP32 mode the sum is compensated (Kahan): the chunk-end
+// state is a sum of ~100 terms of size up to ~1 and would otherwise carry
+// sqrt(K)*eps of rounding into every later chunk.
+template <bool F64, class Vec, class Cf>
+__device__ __forceinline__ void acc_add(Vec &acc, Vec &comp, const Cf &a, const Vec t) {
+    Vec p = vzero<Vec>();
+    mac(p, a, t);
+    if (F64) {
+        acc.x += p.x; acc.y += p.y;
+    } else {
+        const auto yx = p.x - comp.x, yy = p.y - comp.y;
+        const auto sx = acc.x + yx, sy = acc.y + yy;
+        comp.x = (sx - acc.x) - yx;
+        comp.y = (sy - acc.y) - yy;
+        acc.x = sx; acc.y = sy;
+    }
+}
 
 // Number of Chebyshev/Bessel terms after which |J_k(x)| * e^{k*lg} < tol
 // (Debye-type bound (e x / 2k)^k / sqrt(2 pi k), conservative for k > x).
@@ -603,8 +624,17 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             const double half = fmax(0.5 * width * 1.01 + 1e-9 * scale, imax) + 1e-30;
             s_scalar[0] = 0.5 * (hi + lo);   // centre c
             s_scalar[1] = half;              // half-width s
-            // series length for the chunk (x = s*M*dt) incl. growth from Im(L)
-            const double x = half * M * run.dt;
+            // chunk length: about chunk_x series argument per chunk, power of two
+            int Mo = M;
+            if (!run.fixed_chunk) {
+                const double target = run.chunk_x / (half * run.dt);
+                Mo = 1;
+                while (Mo * 2 <= target && Mo * 2 <= M) Mo *= 2;
+            }
+            Mo = min(Mo, nsteps + 1);
+            s_int[2] = Mo;
+            // series length for the chunk (x = s*Mo*dt) incl. growth from Im(L)
+            const double x = half * Mo * run.dt;
             const double lg = 2.0 * imax / half;
             int K = max(2, series_terms(x, lg, run.tol, run.Kmax + 1)) + 2;
             s_int[0] = K;
@@ -613,6 +643,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         __syncthreads();
         const double cen = s_scalar[0], half = s_scalar[1];
         const int K = s_int[0];
+        const int Mo = s_int[2];
         if (s_int[1]) {
             if (tid == 0) { run.status[o] = kDevTableTooSmall; run.kused[o] = K; run.halfwidth[o] = half; }
             continue;
@@ -632,14 +663,14 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         }
 
         // ---- 5. Bessel table J_k(s j dt), j = 0..M --------------------------
-        bessel_columns(table, M, K, half, run.dt);
+        bessel_columns(table, Mo, K, half, run.dt);
         __syncthreads();
         // series coefficients of one chunk (tau = M dt), centre phase folded in
         {
-            const double tau = M * run.dt;
+            const double tau = Mo * run.dt;
             const double pr = cos(-cen * tau), pi_ = sin(-cen * tau);
             for (int k = tid; k < K; k += blockDim.x) {
-                const double jv = table[(size_t)k * (M + 1) + M];
+                const double jv = table[(size_t)k * (Mo + 1) + Mo];
                 // (-i)^k * e^{-i c tau} * jv   (factor 2 for k>0 is already in the table)
                 double re, im;
                 switch (k & 3) {
@@ -650,7 +681,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 }
                 pack(s_atau[k], re * jv, im * jv);
             }
-            for (int j = tid; j < M; j += blockDim.x) {
+            for (int j = tid; j < Mo; j += blockDim.x) {
                 const double ph = -cen * j * run.dt;
                 s_phase[j] = tovec(make_double2(cos(ph), sin(ph)), Vec());
             }
@@ -658,10 +689,11 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         __syncthreads();          // coefficients and phases visible before the first term
 
         // ---- 6. chunked Chebyshev propagation with fused coil projection -------
-        Vec t_prev[RMAX], t_cur[RMAX], acc[RMAX], cc[RMAX];
+        Vec t_prev[RMAX], t_cur[RMAX], acc[RMAX], comp[RMAX], cc[RMAX];
 #pragma unroll
         for (int r = 0; r < RMAX; ++r) {
-            t_prev[r] = vzero<Vec>(); t_cur[r] = vzero<Vec>(); acc[r] = vzero<Vec>(); cc[r] = vzero<Vec>();
+            t_prev[r] = vzero<Vec>(); t_cur[r] = vzero<Vec>(); acc[r] = vzero<Vec>(); comp[r] = vzero<Vec>();
+            cc[r] = vzero<Vec>();
             if (r < rows_per_lane) {
                 const int sl = warp + r * nwarps;
                 if (sl < sys.nslices) {
@@ -671,7 +703,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 }
             }
         }
-        const int nchunks = (nsteps + M) / M;        // ceil((nsteps+1)/M)
+        const int nchunks = (nsteps + Mo) / Mo;      // ceil((nsteps+1)/Mo)
         Vec *fid_out = reinterpret_cast<Vec *>(run.fids) + (size_t)o * (nsteps + 1);
         int status = kDevOk;
         for (int a = 0; a < nchunks && status == kDevOk; ++a) {
@@ -688,6 +720,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     s_xa[sl * 32 + lane] = t_cur[r];
                     cdot_acc(mom, cc[r], t_cur[r]);
                     acc[r] = vzero<Vec>();
+                    comp[r] = vzero<Vec>();
                     mac(acc[r], s_atau[0], t_cur[r]);
                     start_max += (double)t_cur[r].x * t_cur[r].x + (double)t_cur[r].y * t_cur[r].y;
                     t_prev[r] = vzero<Vec>();
@@ -728,7 +761,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     t_cur[r] = tn;
                     dst[row] = tn;
                     cdot_acc(mom, cc[r], tn);
-                    if (advance) mac(acc[r], s_atau[k], tn);
+                    if (advance) acc_add<F64>(acc[r], comp[r], s_atau[k], tn);
                 }
                 mom = warp_sum(mom);
                 if (lane == 0) part[warp] = mom;
@@ -742,14 +775,14 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             __syncthreads();
             // FID points of this chunk: f_j = ph_j * sum_k J_k(s j dt) (-i)^k mu_k
             {
-                const int parts = max(1, (int)blockDim.x / M);
+                const int parts = max(1, (int)blockDim.x / Mo);
                 const int kper = (K + parts - 1) / parts;
-                for (int jj = tid; jj < M * parts; jj += blockDim.x) {
-                    const int j = jj % M, pidx = jj / M;
+                for (int jj = tid; jj < Mo * parts; jj += blockDim.x) {
+                    const int j = jj % Mo, pidx = jj / Mo;
                     const int k0 = pidx * kper, k1 = min(K, k0 + kper);
                     Vec f = vzero<Vec>();
                     for (int k = k0; k < k1; ++k) {
-                        const Real jv = (Real)table[(size_t)k * (M + 1) + j];
+                        const Real jv = (Real)table[(size_t)k * (Mo + 1) + j];
                         const Vec mu = s_mu[k];
                         Real re, im;
                         switch (k & 3) {
@@ -764,17 +797,17 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     s_rec[jj] = f;
                 }
                 __syncthreads();
-                for (int j = tid; j < M; j += blockDim.x) {
+                for (int j = tid; j < Mo; j += blockDim.x) {
                     Vec f = vzero<Vec>();
                     for (int pidx = 0; pidx < parts; ++pidx) {
-                        const Vec g = s_rec[pidx * M + j];
+                        const Vec g = s_rec[pidx * Mo + j];
                         f.x += g.x; f.y += g.y;
                     }
                     const Vec ph = s_phase[j];
                     Vec out;
                     out.x = ph.x * f.x - ph.y * f.y;
                     out.y = ph.x * f.y + ph.y * f.x;
-                    const int nidx = a * M + j;
+                    const int nidx = a * Mo + j;
                     if (nidx <= nsteps) fid_out[nidx] = out;
                 }
             }
@@ -795,6 +828,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         if (tid == 0) {
             run.status[o] = status;
             run.kused[o] = K;
+            run.mused[o] = Mo;
             run.halfwidth[o] = half;
             run.matvecs[o] = (long long)nchunks * (K - 1);
         }
