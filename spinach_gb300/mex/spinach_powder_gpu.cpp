@@ -1,0 +1,235 @@
+// MATLAB MEX gateway to the GB300 powder-FID engine.
+//
+//   fid          = spinach_powder_gpu(I, Q, R, rho0, coil, grid, dt, nsteps)
+//   [fid, fids]  = spinach_powder_gpu(I, Q, R, rho0, coil, grid, dt, nsteps, opts)
+//
+// I, Q     the outputs of [I,Q]=hamiltonian(spin_system) (kernel/hamiltonian.m:44):
+//          I sparse dim x dim, Q a 1x2 cell {Q1 (3x3 cell), Q2 (5x5 cell)} of sparse
+//          matrices; empty entries are skipped as orientation.m:45-52 does.
+// R        relaxation(spin_system) (diagonal sparse) or [].
+// rho0     initial state, coil detection state (dense or sparse columns).
+// grid     struct with alphas, betas, gammas, weights (a kernel/grids/*.mat file).
+// dt       1/parameters.sweep,  nsteps  parameters.npoints-1  (acquire.m:70-71).
+// opts     optional struct: precision ('double' default, or 'single').
+// fid      (nsteps+1) x 1 complex: sum_n weights(n) fid_n (powder.m:280-287).
+// fids     (nsteps+1) x n_orient complex, the sum_up=false output (powder.m:291-297).
+//
+// Conventions follow etc/mex/prune_cpu.cpp: -R2018a interleaved complex API,
+// 0-based mwIndex CSC arrays, inputs read-only, outputs from mxCreate*, and a
+// grumble() that reports errors through mexErrMsgIdAndTxt.  Because
+// mexErrMsgIdAndTxt does not return, every call runs in a scope whose RAII
+// owners are released before the error is raised.  The engine handle (one
+// CUDA context and stream) persists across calls and is released by mexAtExit.
+#include "mex.h"
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "spinach_gpu.h"
+
+namespace {
+
+spx_handle *g_handle = nullptr;
+
+void release_handle() {
+    if (g_handle) spx_destroy(g_handle);
+    g_handle = nullptr;
+}
+
+struct CscCopy {
+    std::vector<int64_t> colptr, rowidx;
+    std::vector<double> values;
+    spx_csc view{};
+};
+
+struct GatewayError {
+    std::string id, msg;
+};
+
+void fill_csc(const mxArray *A, int64_t n, const char *name, CscCopy &out) {
+    if (!mxIsSparse(A) || !mxIsDouble(A))
+        throw GatewayError{"Spinach:spinach_powder_gpu:input", std::string(name) + " must be a sparse double matrix."};
+    if ((int64_t)mxGetM(A) != n || (int64_t)mxGetN(A) != n)
+        throw GatewayError{"Spinach:spinach_powder_gpu:input", std::string(name) + " has the wrong dimension."};
+    const mwIndex *jc = mxGetJc(A);
+    const mwIndex *ir = mxGetIr(A);
+    const int64_t nnz = (int64_t)jc[n];
+    out.colptr.assign(jc, jc + n + 1);
+    out.rowidx.assign(ir, ir + nnz);
+    out.values.assign(2 * (size_t)nnz, 0.0);
+    if (mxIsComplex(A)) {
+        const mxComplexDouble *v = mxGetComplexDoubles(A);
+        for (int64_t p = 0; p < nnz; ++p) {
+            out.values[2 * p] = v[p].real;
+            out.values[2 * p + 1] = v[p].imag;
+        }
+    } else {
+        const mxDouble *v = mxGetDoubles(A);
+        for (int64_t p = 0; p < nnz; ++p) out.values[2 * p] = v[p];
+    }
+    out.view.n = n;
+    out.view.colptr = out.colptr.data();
+    out.view.rowidx = out.rowidx.data();
+    out.view.values = out.values.data();
+}
+
+std::vector<double> column(const mxArray *A, int64_t n, const char *name) {
+    if (!mxIsDouble(A) || (int64_t)mxGetNumberOfElements(A) != n)
+        throw GatewayError{"Spinach:spinach_powder_gpu:input", std::string(name) + " must be a double vector of length dim."};
+    std::vector<double> out(2 * (size_t)n, 0.0);
+    if (mxIsSparse(A)) {
+        const mwIndex *jc = mxGetJc(A), *ir = mxGetIr(A);
+        const int64_t nnz = (int64_t)jc[1];
+        if (mxIsComplex(A)) {
+            const mxComplexDouble *v = mxGetComplexDoubles(A);
+            for (int64_t p = 0; p < nnz; ++p) { out[2 * ir[p]] = v[p].real; out[2 * ir[p] + 1] = v[p].imag; }
+        } else {
+            const mxDouble *v = mxGetDoubles(A);
+            for (int64_t p = 0; p < nnz; ++p) out[2 * ir[p]] = v[p];
+        }
+    } else if (mxIsComplex(A)) {
+        const mxComplexDouble *v = mxGetComplexDoubles(A);
+        for (int64_t i = 0; i < n; ++i) { out[2 * i] = v[i].real; out[2 * i + 1] = v[i].imag; }
+    } else {
+        const mxDouble *v = mxGetDoubles(A);
+        for (int64_t i = 0; i < n; ++i) out[2 * i] = v[i];
+    }
+    return out;
+}
+
+std::vector<double> grid_field(const mxArray *g, const char *name, int64_t &count) {
+    const mxArray *f = mxGetField(g, 0, name);
+    if (!f || !mxIsDouble(f) || mxIsComplex(f) || mxIsSparse(f))
+        throw GatewayError{"Spinach:spinach_powder_gpu:grid", std::string("grid.") + name + " must be a real double vector."};
+    const int64_t n = (int64_t)mxGetNumberOfElements(f);
+    if (count >= 0 && n != count)
+        throw GatewayError{"Spinach:spinach_powder_gpu:grid", "grid fields must have equal lengths."};
+    count = n;
+    const mxDouble *v = mxGetDoubles(f);
+    return std::vector<double>(v, v + n);
+}
+
+double scalar(const mxArray *A, const char *name) {
+    if (!mxIsDouble(A) || mxIsComplex(A) || mxGetNumberOfElements(A) != 1)
+        throw GatewayError{"Spinach:spinach_powder_gpu:input", std::string(name) + " must be a real scalar."};
+    return mxGetScalar(A);
+}
+
+// static grumble(): argument-count and type checks (etc/mex/prune_cpu.cpp:199-223 style)
+void grumble(int nlhs, int nrhs, const mxArray *prhs[]) {
+    if (nrhs < 8 || nrhs > 9)
+        throw GatewayError{"Spinach:spinach_powder_gpu:nrhs", "eight or nine input arguments are required."};
+    if (nlhs > 2) throw GatewayError{"Spinach:spinach_powder_gpu:nlhs", "at most two outputs are returned."};
+    if (!mxIsCell(prhs[1]) || mxGetNumberOfElements(prhs[1]) != 2)
+        throw GatewayError{"Spinach:spinach_powder_gpu:Q", "Q must be the 1x2 cell returned by hamiltonian()."};
+    if (!mxIsStruct(prhs[5])) throw GatewayError{"Spinach:spinach_powder_gpu:grid", "grid must be a struct."};
+    if (nrhs == 9 && !mxIsStruct(prhs[8]))
+        throw GatewayError{"Spinach:spinach_powder_gpu:opts", "opts must be a struct."};
+}
+
+void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
+    grumble(nlhs, nrhs, prhs);
+    const int64_t n = (int64_t)mxGetM(prhs[0]);
+    CscCopy I;
+    fill_csc(prhs[0], n, "I", I);
+    // non-empty rotational-basis terms Q{r}{k,m}
+    std::vector<CscCopy> terms;
+    std::vector<int32_t> rank, kk, mm;
+    terms.reserve(34);
+    for (int r = 1; r <= 2; ++r) {
+        const mxArray *Qr = mxGetCell(prhs[1], r - 1);
+        if (!Qr || !mxIsCell(Qr) || (int)mxGetM(Qr) != 2 * r + 1 || (int)mxGetN(Qr) != 2 * r + 1)
+            throw GatewayError{"Spinach:spinach_powder_gpu:Q", "Q{r} must be a (2r+1)x(2r+1) cell."};
+        for (int m = 0; m < 2 * r + 1; ++m)
+            for (int k = 0; k < 2 * r + 1; ++k) {
+                const mxArray *A = mxGetCell(Qr, (mwIndex)(k + m * (2 * r + 1)));   // column-major {k,m}
+                if (!A || !mxIsSparse(A) || mxGetJc(A)[mxGetN(A)] == 0) continue;
+                terms.emplace_back();
+                fill_csc(A, n, "Q{r}{k,m}", terms.back());
+                rank.push_back(r);
+                kk.push_back(k);
+                mm.push_back(m);
+            }
+    }
+    std::vector<spx_csc> qv;
+    for (auto &t : terms) qv.push_back(t.view);
+    CscCopy R;
+    const bool have_R = !mxIsEmpty(prhs[2]);
+    if (have_R) fill_csc(prhs[2], n, "R", R);
+    const std::vector<double> rho0 = column(prhs[3], n, "rho0");
+    const std::vector<double> coil = column(prhs[4], n, "coil");
+    int64_t no = -1;
+    const std::vector<double> al = grid_field(prhs[5], "alphas", no);
+    const std::vector<double> be = grid_field(prhs[5], "betas", no);
+    const std::vector<double> ga = grid_field(prhs[5], "gammas", no);
+    const std::vector<double> wt = grid_field(prhs[5], "weights", no);
+    const double dt = scalar(prhs[6], "dt");
+    const double ns = scalar(prhs[7], "nsteps");
+    if (ns < 0 || ns != (double)(int64_t)ns)
+        throw GatewayError{"Spinach:spinach_powder_gpu:nsteps", "nsteps must be a non-negative integer."};
+    const int64_t nsteps = (int64_t)ns;
+    spx_options opt{};
+    opt.precision = SPX_FP64;
+    if (nrhs == 9) {
+        const mxArray *p = mxGetField(prhs[8], 0, "precision");
+        if (p) {
+            char buf[16] = {0};
+            if (!mxIsChar(p) || mxGetString(p, buf, sizeof buf) != 0)
+                throw GatewayError{"Spinach:spinach_powder_gpu:opts", "opts.precision must be 'single' or 'double'."};
+            if (std::strcmp(buf, "single") == 0) opt.precision = SPX_FP32;
+            else if (std::strcmp(buf, "double") != 0)
+                throw GatewayError{"Spinach:spinach_powder_gpu:opts", "opts.precision must be 'single' or 'double'."};
+        }
+    }
+    if (!g_handle) {
+        spx_status st = spx_create(&g_handle, 0);
+        if (st != SPX_OK)
+            throw GatewayError{"Spinach:spinach_powder_gpu:device", std::string("GPU engine unavailable: ") + spx_status_string(st)};
+        mexAtExit(release_handle);
+    }
+    spx_status st = spx_upload_system(g_handle, &I.view, (int32_t)rank.size(), rank.data(), kk.data(), mm.data(),
+                                      qv.data(), have_R ? &R.view : nullptr, rho0.data(), coil.data());
+    if (st != SPX_OK)
+        throw GatewayError{"Spinach:spinach_powder_gpu:upload", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
+    plhs[0] = mxCreateDoubleMatrix((mwSize)(nsteps + 1), 1, mxCOMPLEX);
+    double *per = nullptr;
+    std::vector<double> per_buf;
+    if (nlhs > 1) {
+        per_buf.assign(2 * (size_t)(nsteps + 1) * (size_t)no, 0.0);
+        per = per_buf.data();
+    }
+    std::vector<double> fid(2 * (size_t)(nsteps + 1));
+    st = spx_run_powder(g_handle, no, al.data(), be.data(), ga.data(), wt.data(), dt, nsteps, &opt, fid.data(), per);
+    if (st != SPX_OK)
+        throw GatewayError{"Spinach:spinach_powder_gpu:run", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
+    mxComplexDouble *out = mxGetComplexDoubles(plhs[0]);
+    for (int64_t i = 0; i <= nsteps; ++i) { out[i].real = fid[2 * i]; out[i].imag = fid[2 * i + 1]; }
+    if (nlhs > 1) {
+        plhs[1] = mxCreateDoubleMatrix((mwSize)(nsteps + 1), (mwSize)no, mxCOMPLEX);
+        mxComplexDouble *o2 = mxGetComplexDoubles(plhs[1]);
+        for (size_t i = 0; i < (size_t)(nsteps + 1) * (size_t)no; ++i) { o2[i].real = per[2 * i]; o2[i].imag = per[2 * i + 1]; }
+    }
+}
+
+}  // namespace
+
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
+    // mexErrMsgIdAndTxt does not return: the message is copied into static
+    // storage and every owner of run() is destroyed before it is raised.
+    static char id[128], msg[1024];
+    bool failed = false;
+    try {
+        run(nlhs, plhs, nrhs, prhs);
+    } catch (const GatewayError &e) {
+        std::snprintf(id, sizeof id, "%s", e.id.c_str());
+        std::snprintf(msg, sizeof msg, "%s", e.msg.c_str());
+        failed = true;
+    } catch (const std::exception &e) {
+        std::snprintf(id, sizeof id, "%s", "Spinach:spinach_powder_gpu:internal");
+        std::snprintf(msg, sizeof msg, "%s", e.what());
+        failed = true;
+    }
+    if (failed) mexErrMsgIdAndTxt(id, "%s", msg);
+}

@@ -1,0 +1,128 @@
+// Drives spinach_powder_gpu.cpp through the mx stand-in and the recording
+// engine: argument marshalling, Q{r}{k,m} enumeration, real->complex and
+// sparse->dense conversion, options and error identifiers.
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "mex.h"
+
+struct Recorded {
+    int64_t n;
+    std::vector<int64_t> I_colptr, I_rowidx;
+    std::vector<double> I_values;
+    std::vector<int> rank, k, m;
+    std::vector<std::vector<double>> Q_values;
+    bool have_R;
+    std::vector<double> R_values, rho0, coil, grid;
+    double dt;
+    int64_t nsteps, n_orient;
+    int precision;
+    bool want_per;
+    int fail_run;
+};
+extern Recorded g_rec;
+void stub_run_atexit();
+
+static int failures = 0;
+#define CHECK(c) do { if (!(c)) { std::printf("FAIL line %d: %s\n", __LINE__, #c); ++failures; } } while (0)
+
+static mxArray *sparse(size_t n, const std::vector<size_t> &rows, const std::vector<size_t> &cols,
+                       const std::vector<double> &re, const std::vector<double> &im) {
+    mxArray *a = new mxArray;
+    a->kind = mxArray::Sparse; a->m = n; a->n = n; a->complex = !im.empty();
+    a->jc.assign(n + 1, 0);
+    for (size_t c : cols) a->jc[c + 1]++;
+    for (size_t c = 0; c < n; ++c) a->jc[c + 1] += a->jc[c];
+    std::vector<size_t> fill(a->jc.begin(), a->jc.end() - 1);
+    a->ir.assign(rows.size(), 0);
+    if (a->complex) a->cx.assign(rows.size(), mxComplexDouble{0, 0}); else a->re.assign(rows.size(), 0);
+    for (size_t p = 0; p < rows.size(); ++p) {
+        size_t q = fill[cols[p]]++;
+        a->ir[q] = rows[p];
+        if (a->complex) a->cx[q] = mxComplexDouble{re[p], im[p]}; else a->re[q] = re[p];
+    }
+    return a;
+}
+static mxArray *empty_sparse(size_t n) { return sparse(n, {}, {}, {}, {}); }
+static mxArray *cell(size_t m, size_t n) {
+    mxArray *a = new mxArray; a->kind = mxArray::Cell; a->m = m; a->n = n; a->cells.assign(m * n, nullptr); return a;
+}
+static mxArray *dense(std::vector<double> v) {
+    mxArray *a = new mxArray; a->m = v.size(); a->n = 1; a->re = v; return a;
+}
+static mxArray *scalar(double v) { return dense({v}); }
+static mxArray *str(const char *s) { mxArray *a = new mxArray; a->kind = mxArray::Char; a->m = 1; a->n = 1; a->str = s; return a; }
+static mxArray *strct() { mxArray *a = new mxArray; a->kind = mxArray::Struct; a->m = 1; a->n = 1; return a; }
+
+int main() {
+    const size_t n = 4;
+    mxArray *I = sparse(n, {0, 1, 3}, {0, 1, 2}, {1.5, -2.0, 0.25}, {});
+    mxArray *Q = cell(1, 2);
+    Q->cells[0] = cell(3, 3);
+    Q->cells[1] = cell(5, 5);
+    for (auto &c : Q->cells[0]->cells) c = empty_sparse(n);
+    for (auto &c : Q->cells[1]->cells) c = empty_sparse(n);
+    Q->cells[0]->cells[0 + 2 * 3] = sparse(n, {1}, {2}, {3.0}, {4.0});      // Q{1}{1,3}
+    Q->cells[1]->cells[2 + 0 * 5] = sparse(n, {0, 3}, {3, 0}, {5.0, 6.0}, {});   // Q{2}{3,1}
+    Q->cells[1]->cells[2 + 4 * 5] = sparse(n, {2}, {2}, {7.0}, {-1.0});   // Q{2}{3,5}
+    mxArray *R = sparse(n, {0, 1, 2, 3}, {0, 1, 2, 3}, {0, -1, -2, -3}, {});
+    mxArray *rho0 = sparse(n, {2}, {0}, {0.5}, {});
+    rho0->n = 1; rho0->jc.assign({0, 1});
+    mxArray *coil = new mxArray; coil->m = n; coil->n = 1; coil->complex = true;
+    coil->cx = {{0, 0}, {1, 2}, {0, 0}, {3, -4}};
+    mxArray *grid = strct();
+    grid->fields["alphas"] = dense({0, 0, 0});
+    grid->fields["betas"] = dense({0.1, 0.2, 0.3});
+    grid->fields["gammas"] = dense({1, 2, 3});
+    grid->fields["weights"] = dense({0.2, 0.3, 0.5});
+    mxArray *opts = strct();
+    opts->fields["precision"] = str("single");
+    const mxArray *prhs[9] = {I, Q, R, rho0, coil, grid, scalar(1e-5), scalar(5), opts};
+    mxArray *plhs[2] = {nullptr, nullptr};
+    mexFunction(2, plhs, 9, prhs);
+    CHECK(g_rec.n == 4);
+    CHECK((g_rec.I_colptr == std::vector<int64_t>{0, 1, 2, 3, 3}));
+    CHECK((g_rec.I_rowidx == std::vector<int64_t>{0, 1, 3}));
+    CHECK((g_rec.I_values == std::vector<double>{1.5, 0, -2.0, 0, 0.25, 0}));
+    CHECK((g_rec.rank == std::vector<int>{1, 2, 2}));
+    CHECK((g_rec.k == std::vector<int>{0, 2, 2}));
+    CHECK((g_rec.m == std::vector<int>{2, 0, 4}));
+    CHECK(g_rec.Q_values.size() == 3 && (g_rec.Q_values[0] == std::vector<double>{3.0, 4.0}));
+    CHECK((g_rec.Q_values[1] == std::vector<double>{6.0, 0.0, 5.0, 0.0}));
+    CHECK(g_rec.have_R && g_rec.R_values.size() == 8 && g_rec.R_values[6] == -3.0);
+    CHECK((g_rec.rho0 == std::vector<double>{0, 0, 0, 0, 0.5, 0, 0, 0}));
+    CHECK((g_rec.coil == std::vector<double>{0, 0, 1, 2, 0, 0, 3, -4}));
+    CHECK(g_rec.n_orient == 3 && g_rec.grid[5] == 0.2 && g_rec.grid[11] == 0.5);
+    CHECK(g_rec.dt == 1e-5 && g_rec.nsteps == 5 && g_rec.precision == 1 - 1 && g_rec.want_per);
+    CHECK(plhs[0] && plhs[0]->m == 6 && plhs[0]->n == 1 && plhs[0]->complex);
+    CHECK(plhs[0]->cx[3].real == 3.0 && plhs[0]->cx[3].imag == -1.5);
+    CHECK(plhs[1] && plhs[1]->m == 6 && plhs[1]->n == 3 && plhs[1]->cx[6 + 2].real == 102.0);
+    // default precision is double, one output
+    const mxArray *p8[8] = {I, Q, mxCreateDoubleMatrix(0, 0, mxREAL), dense({0, 1, 0, 0}), coil, grid, scalar(2e-5), scalar(0)};
+    mxArray *o1[1] = {nullptr};
+    mexFunction(1, o1, 8, p8);
+    CHECK(g_rec.precision == 1 && !g_rec.have_R && !g_rec.want_per && o1[0]->m == 1);
+    // error identifiers
+    auto expect = [&](int nl, int nr, const mxArray **pr, const char *id) {
+        mxArray *o[2] = {nullptr, nullptr};
+        try {
+            mexFunction(nl, o, nr, pr);
+            std::printf("FAIL: no error for %s\n", id);
+            ++failures;
+        } catch (const MexError &e) {
+            if (e.id != id) { std::printf("FAIL: got %s, want %s\n", e.id.c_str(), id); ++failures; }
+        }
+    };
+    expect(1, 3, prhs, "Spinach:spinach_powder_gpu:nrhs");
+    const mxArray *badq[8] = {I, grid, R, rho0, coil, grid, scalar(1e-5), scalar(5)};
+    expect(1, 8, badq, "Spinach:spinach_powder_gpu:Q");
+    const mxArray *badn[8] = {I, Q, R, rho0, coil, grid, scalar(1e-5), scalar(2.5)};
+    expect(1, 8, badn, "Spinach:spinach_powder_gpu:nsteps");
+    g_rec.fail_run = 1;
+    expect(1, 8, p8, "Spinach:spinach_powder_gpu:run");
+    stub_run_atexit();
+    std::printf(failures ? "FAILED %d\n" : "PASS\n", failures);
+    return failures ? 1 : 0;
+}
