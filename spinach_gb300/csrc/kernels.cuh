@@ -46,16 +46,17 @@ enum DeviceStatus : int {
 };
 
 struct __align__(8) SplitR { float hi, lo; };
+struct CAcc;
 struct __align__(16) SplitC { float rh, ih, rl, il; };
 
 // ---------------------------------------------------------------------------
 // Precision policies
 // ---------------------------------------------------------------------------
 template <bool F64, bool CPLX> struct Prec;
-template <> struct Prec<false, false> { using Vec = float2;  using Val = SplitR; using Dg = SplitC; using Real = float; };
-template <> struct Prec<false, true>  { using Vec = float2;  using Val = SplitC; using Dg = SplitC; using Real = float; };
-template <> struct Prec<true, false>  { using Vec = double2; using Val = double; using Dg = double2; using Real = double; };
-template <> struct Prec<true, true>   { using Vec = double2; using Val = double2; using Dg = double2; using Real = double; };
+template <> struct Prec<false, false> { using Vec = float2;  using Val = SplitR; using Dg = SplitC; using Real = float; using Acc = CAcc; };
+template <> struct Prec<false, true>  { using Vec = float2;  using Val = SplitC; using Dg = SplitC; using Real = float; using Acc = CAcc; };
+template <> struct Prec<true, false>  { using Vec = double2; using Val = double; using Dg = double2; using Real = double; using Acc = double2; };
+template <> struct Prec<true, true>   { using Vec = double2; using Val = double2; using Dg = double2; using Real = double; using Acc = double2; };
 
 __device__ __forceinline__ void pack(SplitR &o, double re, double) {
     o.hi = (float)re; o.lo = (float)(re - (double)o.hi);
@@ -135,6 +136,76 @@ __device__ __forceinline__ double warp_min_d(double v) {
     for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
+
+// ---------------------------------------------------------------------------
+// Compensated FP32 accumulation (error-free transformations).  The product
+// error comes from fmaf(a, b, -round(a*b)); sums use TwoSum.  The _rn
+// intrinsics keep the compiler from contracting the pieces into FMAs, which
+// would break the error bookkeeping.
+// ---------------------------------------------------------------------------
+struct CAcc { float2 hi, lo; };
+
+__device__ __forceinline__ void two_sum_into(float &hi, float &lo, float p) {
+    const float s = __fadd_rn(hi, p);
+    const float bp = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
+// hi/lo += a * b with the product error kept
+__device__ __forceinline__ void prod_into(float &hi, float &lo, float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);
+    two_sum_into(hi, lo, p);
+    lo = __fadd_rn(lo, e);
+}
+__device__ __forceinline__ void cmac(CAcc &y, const SplitR &v, const float2 x) {
+    prod_into(y.hi.x, y.lo.x, v.hi, x.x);
+    prod_into(y.hi.y, y.lo.y, v.hi, x.y);
+    y.lo.x = __fmaf_rn(v.lo, x.x, y.lo.x);
+    y.lo.y = __fmaf_rn(v.lo, x.y, y.lo.y);
+}
+__device__ __forceinline__ void cmac(CAcc &y, const SplitC &v, const float2 x) {
+    prod_into(y.hi.x, y.lo.x, v.rh, x.x);
+    prod_into(y.hi.x, y.lo.x, -v.ih, x.y);
+    prod_into(y.hi.y, y.lo.y, v.rh, x.y);
+    prod_into(y.hi.y, y.lo.y, v.ih, x.x);
+    y.lo.x = __fmaf_rn(v.rl, x.x, y.lo.x);
+    y.lo.x = __fmaf_rn(-v.il, x.y, y.lo.x);
+    y.lo.y = __fmaf_rn(v.rl, x.y, y.lo.y);
+    y.lo.y = __fmaf_rn(v.il, x.x, y.lo.y);
+}
+// conj(a) * b accumulated with compensation
+__device__ __forceinline__ void cdot_comp(CAcc &s, const float2 a, const float2 b) {
+    prod_into(s.hi.x, s.lo.x, a.x, b.x);
+    prod_into(s.hi.x, s.lo.x, a.y, b.y);
+    prod_into(s.hi.y, s.lo.y, a.x, b.y);
+    prod_into(s.hi.y, s.lo.y, -a.y, b.x);
+}
+__device__ __forceinline__ void cmac(double2 &y, const double &v, const double2 x) { mac(y, v, x); }
+__device__ __forceinline__ void cmac(double2 &y, const double2 &v, const double2 x) { mac(y, v, x); }
+__device__ __forceinline__ void cdot_comp(double2 &s, const double2 a, const double2 b) { cdot_acc(s, a, b); }
+
+template <class A> __device__ __forceinline__ A azero();
+template <> __device__ __forceinline__ CAcc azero<CAcc>() {
+    CAcc a; a.hi = make_float2(0.f, 0.f); a.lo = make_float2(0.f, 0.f); return a;
+}
+template <> __device__ __forceinline__ double2 azero<double2>() { return make_double2(0.0, 0.0); }
+
+// t_new = two * y - t_prev, rounded once from the compensated value
+__device__ __forceinline__ float2 recur(const CAcc &y, float two, const float2 tp) {
+    float2 t;
+    t.x = __fmaf_rn(two, y.lo.x, __fmaf_rn(two, y.hi.x, -tp.x));
+    t.y = __fmaf_rn(two, y.lo.y, __fmaf_rn(two, y.hi.y, -tp.y));
+    return t;
+}
+__device__ __forceinline__ double2 recur(const double2 &y, double two, const double2 tp) {
+    return make_double2(two * y.x - tp.x, two * y.y - tp.y);
+}
+__device__ __forceinline__ float2 collapse(const CAcc &a) {
+    return make_float2(__fadd_rn(a.hi.x, a.lo.x), __fadd_rn(a.hi.y, a.lo.y));
+}
+__device__ __forceinline__ double2 collapse(const double2 &a) { return a; }
 
 // Block-wide reductions through a shared scratch of kRedSlots doubles.
 // Every thread of the block must call them (they contain __syncthreads).
@@ -373,45 +444,43 @@ __device__ int series_terms(double x, double lg, double tol, int kcap) {
     return k;
 }
 
-// Columns j = 0..M of the table T[k][j] = (2 - delta_k0) J_k(half * j * dt),
-// k < K, by Miller's backward recurrence J_{k-1} = (2k/x) J_k - J_{k+1},
-// normalised with J_0 + 2 sum J_2k = 1.  Rescaling is only needed above the
-// stored range; tiny arguments use the leading terms of the power series.
-__device__ void bessel_columns(double *table, int M, int K, double half, double dt) {
-    for (int j = threadIdx.x; j <= M; j += blockDim.x) {
-        double *col = table + j;
-        const size_t ld = (size_t)(M + 1);
-        const double x = half * j * dt;
-        if (x < 1e-6) {
-            for (int k = 0; k < K; ++k) col[k * ld] = 0.0;
-            col[0] = 1.0 - 0.25 * x * x;
-            if (K > 1) col[ld] = 2.0 * 0.5 * x;
-            if (K > 2) col[2 * ld] = 2.0 * 0.125 * x * x;
-            continue;
-        }
-        const int kneed = min(K, series_terms(x, 0.0, 1e-40, K + 64) + 1);
-        const int base = max(kneed, (int)ceil(x));
-        int kst = base + 20 + (int)sqrt(160.0 * base);
-        kst += kst & 1;
-        double jp1 = 0.0, jk = 1e-30, norm = 0.0;
-        for (int k = kst; k >= 1; --k) {
-            const double jm1 = (2.0 * k / x) * jk - jp1;
-            jp1 = jk;
-            jk = jm1;                                   // J_{k-1}, unnormalised
-            const int km1 = k - 1;
-            if (km1 > 0 && (km1 & 1) == 0) norm += 2.0 * jk;
-            if (km1 < kneed) {
-                col[km1 * ld] = jk;
-            } else if (fabs(jk) > 1e200) {
-                jk *= 1e-200; jp1 *= 1e-200; norm *= 1e-200;
-            }
-        }
-        norm += jk;                                     // + J_0
-        const double inv = 1.0 / norm;
-        col[0] = col[0] * inv;
-        for (int k = 1; k < kneed; ++k) col[k * ld] = 2.0 * col[k * ld] * inv;
-        for (int k = kneed; k < K; ++k) col[k * ld] = 0.0;
+// Column j of the table T[k][j] = (2 - delta_k0) J_k(half * j * dt), k < K,
+// by Miller's backward recurrence J_{k-1} = (2k/x) J_k - J_{k+1}, normalised
+// with J_0 + 2 sum J_2k = 1.  Rescaling is only needed above the stored range;
+// tiny arguments use the leading terms of the power series.
+__device__ void bessel_column(double *table, int M, int j, int K, double half, double dt) {
+    double *col = table + j;
+    const size_t ld = (size_t)(M + 1);
+    const double x = half * j * dt;
+    if (x < 1e-6) {
+        for (int k = 0; k < K; ++k) col[k * ld] = 0.0;
+        col[0] = 1.0 - 0.25 * x * x;
+        if (K > 1) col[ld] = 2.0 * 0.5 * x;
+        if (K > 2) col[2 * ld] = 2.0 * 0.125 * x * x;
+        return;
     }
+    const int kneed = min(K, series_terms(x, 0.0, 1e-40, K + 64) + 1);
+    const int base = max(kneed, (int)ceil(x));
+    int kst = base + 20 + (int)sqrt(160.0 * base);
+    kst += kst & 1;
+    double jp1 = 0.0, jk = 1e-30, norm = 0.0;
+    for (int k = kst; k >= 1; --k) {
+        const double jm1 = (2.0 * k / x) * jk - jp1;
+        jp1 = jk;
+        jk = jm1;                                   // J_{k-1}, unnormalised
+        const int km1 = k - 1;
+        if (km1 > 0 && (km1 & 1) == 0) norm += 2.0 * jk;
+        if (km1 < kneed) {
+            col[km1 * ld] = jk;
+        } else if (fabs(jk) > 1e200) {
+            jk *= 1e-200; jp1 *= 1e-200; norm *= 1e-200;
+        }
+    }
+    norm += jk;                                     // + J_0
+    const double inv = 1.0 / norm;
+    col[0] = col[0] * inv;
+    for (int k = 1; k < kneed; ++k) col[k * ld] = 2.0 * col[k * ld] * inv;
+    for (int k = kneed; k < K; ++k) col[k * ld] = 0.0;
 }
 
 // ---------------------------------------------------------------------------
@@ -425,6 +494,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     using Val = typename P::Val;
     using Dg = typename P::Dg;
     using Real = typename P::Real;
+    using Acc = typename P::Acc;
 
     extern __shared__ __align__(16) unsigned char smem[];
     const SmemLayout<F64, CPLX> L(sys.n_pad, sys.nslices, sys.ell_len, run.Kmax, run.M, blockDim.x);
@@ -636,7 +706,16 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             // series length for the chunk (x = s*Mo*dt) incl. growth from Im(L)
             const double x = half * Mo * run.dt;
             const double lg = 2.0 * imax / half;
-            int K = max(2, series_terms(x, lg, run.tol, run.Kmax + 1)) + 2;
+            // bound first (Debye-type, loose for k ~ x), then the exact tail
+            // from the Bessel column of the chunk end itself
+            const int Kb = min(run.Kmax, max(2, series_terms(x, lg, run.tol, run.Kmax + 1)) + 2);
+            bessel_column(table, Mo, Mo, Kb, half, run.dt);
+            int K = 2;
+            for (int k = Kb - 1; k >= 2; --k) {
+                if (fabs(table[(size_t)k * (Mo + 1) + Mo]) * exp(k * lg) > run.tol) { K = k + 1; break; }
+            }
+            K = min(K + 2, Kb);
+            if (Kb >= run.Kmax && series_terms(x, lg, run.tol, run.Kmax + 1) + 2 > run.Kmax && K >= Kb - 2) K = run.Kmax + 1;
             s_int[0] = K;
             s_int[1] = (K > run.Kmax) ? 1 : 0;
         }
@@ -663,7 +742,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         }
 
         // ---- 5. Bessel table J_k(s j dt), j = 0..M --------------------------
-        bessel_columns(table, Mo, K, half, run.dt);
+        for (int j = tid; j < Mo; j += blockDim.x) bessel_column(table, Mo, j, K, half, run.dt);
         __syncthreads();
         // series coefficients of one chunk (tau = M dt), centre phase folded in
         {
@@ -711,21 +790,21 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             double start_max = 0.0;
             // k = 0: t0 = rho
             {
-                Vec mom = vzero<Vec>();
+                Acc macc = azero<Acc>();
 #pragma unroll
                 for (int r = 0; r < RMAX; ++r) {
                     if (r >= rows_per_lane) break;
                     const int sl = warp + r * nwarps;
                     if (sl >= sys.nslices) break;
                     s_xa[sl * 32 + lane] = t_cur[r];
-                    cdot_acc(mom, cc[r], t_cur[r]);
+                    cdot_comp(macc, cc[r], t_cur[r]);
                     acc[r] = vzero<Vec>();
                     comp[r] = vzero<Vec>();
                     mac(acc[r], s_atau[0], t_cur[r]);
                     start_max += (double)t_cur[r].x * t_cur[r].x + (double)t_cur[r].y * t_cur[r].y;
                     t_prev[r] = vzero<Vec>();
                 }
-                mom = warp_sum(mom);
+                const Vec mom = warp_sum(collapse(macc));
                 if (lane == 0) s_part[warp] = mom;
             }
             __syncthreads();
@@ -740,7 +819,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 Vec *dst = (k & 1) ? s_xb : s_xa;
                 Vec *part = s_part + ((k & 1) ? 32 : 0);
                 const Real two = (k == 1) ? (Real)1 : (Real)2;
-                Vec mom = vzero<Vec>();
+                Acc macc = azero<Acc>();
 #pragma unroll
                 for (int r = 0; r < RMAX; ++r) {
                     if (r >= rows_per_lane) break;
@@ -748,22 +827,20 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     if (sl >= sys.nslices) break;
                     const int row = sl * 32 + lane;
                     const int off = s_soff[sl], w = (s_soff[sl + 1] - off) >> 5;
-                    Vec y = vzero<Vec>();
-                    mac(y, s_diag[row], t_cur[r]);
+                    Acc y = azero<Acc>();
+                    cmac(y, s_diag[row], t_cur[r]);
                     for (int c = 0; c < w; ++c) {
                         const int e = off + c * 32 + lane;
-                        mac(y, s_val[e], src[s_col[e]]);
+                        cmac(y, s_val[e], src[s_col[e]]);
                     }
-                    Vec tn;
-                    tn.x = two * y.x - t_prev[r].x;
-                    tn.y = two * y.y - t_prev[r].y;
+                    const Vec tn = recur(y, two, t_prev[r]);
                     t_prev[r] = t_cur[r];
                     t_cur[r] = tn;
                     dst[row] = tn;
-                    cdot_acc(mom, cc[r], tn);
+                    cdot_comp(macc, cc[r], tn);
                     if (advance) acc_add<F64>(acc[r], comp[r], s_atau[k], tn);
                 }
-                mom = warp_sum(mom);
+                Vec mom = warp_sum(collapse(macc));
                 if (lane == 0) part[warp] = mom;
                 __syncthreads();
                 if (warp == 0) {
