@@ -133,6 +133,31 @@ spx_status spx_run_powder_device(spx_handle *handle, int64_t n_orient,
                                  double dt, int64_t nsteps, const spx_options *opt,
                                  double *d_fid);
 
+/*
+ * Powder run that allocates nothing (no counterpart in the reference).
+ *
+ * For callers that cannot allocate device memory while they run: a host that
+ * reserves all GPU memory up front (for example a MATLAB session whose
+ * gpuArray pool already holds it, or instrument software that budgets memory
+ * at start-up) and code that must not trigger the implicit device-wide
+ * synchronisation a cudaMalloc/cudaFree can cause.  Uses the system already
+ * uploaded on the handle; the grid (d_alphas, d_betas, d_gammas, d_weights:
+ * n_orient doubles each) and d_fid (2*(nsteps+1) doubles) are caller-owned
+ * device memory.  Every intermediate lives in one static device array of
+ * SPX_NOALLOC_SCRATCH_BYTES per GPU (held from library load until process
+ * exit); runs needing more return SPX_ERR_UNSUPPORTED before any work is
+ * queued.  Chunks are capped at 64 steps.  The first call on a device looks up
+ * the array's address and should therefore come before any stream capture.
+ * The call blocks until the run has finished.  Calls share the array: calls
+ * that overlap on the GPU (other threads or handles on the same device) race.
+ */
+#define SPX_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+spx_status spx_run_powder_noalloc(spx_handle *handle, int64_t n_orient,
+                                  const double *d_alphas, const double *d_betas,
+                                  const double *d_gammas, const double *d_weights,
+                                  double dt, int64_t nsteps, int32_t precision,
+                                  double *d_fid);
+
 /* Wait for all work on the handle's stream; returns the device status. */
 spx_status spx_synchronize(spx_handle *handle);
 

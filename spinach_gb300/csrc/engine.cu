@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -390,7 +391,7 @@ const void *select_kernel(bool f64, bool cplx, int rmax) {
 }
 
 Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps, const spx_options &opt,
-                     int kmax_override) {
+                     int kmax_override, int m_cap = 256) {
     Config c{};
     const bool f64 = opt.precision == SPX_FP64;
     c.tol = opt.series_tol > 0 ? opt.series_tol : (f64 ? 1e-16 : 1e-11);
@@ -405,7 +406,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     // argument s*M*dt is about chunk_x (kernel side); M here is the cap.
     c.fixed = opt.chunk_steps > 0;
     c.chunk_x = f64 ? 150.0 : 150.0;
-    int M = c.fixed ? opt.chunk_steps : 256;
+    int M = c.fixed ? opt.chunk_steps : m_cap;
     M = (int)std::min<int64_t>(M, nsteps + 1);
     M = std::max(M, 1);
     c.M = M;
@@ -574,9 +575,132 @@ spx_status guarded(spx_handle *h, F f) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// No-allocation variant: all intermediates in one static device array
+// ---------------------------------------------------------------------------
+constexpr int kNoallocChunkCap = 64;
+
+__global__ void status_any_kernel(const int *status, int n, int *flag) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (status[i] != spx::kDevOk) atomicOr(flag, 1);
+}
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[SPX_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+std::mutex g_noalloc_mutex;
+void *g_noalloc_address[256] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (host code only sees a stand-in symbol, never the device address).
+void *noalloc_scratch(int device) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (device < 0 || device >= 256) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+    if (!g_noalloc_address[device]) {
+        void *ptr = nullptr;
+        SPX_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+        if (!ptr) throw SpxError(SPX_ERR_CUDA, "no device address for the static scratch array");
+        g_noalloc_address[device] = ptr;
+    }
+    return g_noalloc_address[device];
+}
+
+void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be,
+                        const double *d_ga, const double *d_w, double dt, int64_t nsteps, int32_t precision,
+                        double *d_fid) {
+    validate_run(h, n_orient, dt, nsteps);
+    if (!d_al || !d_be || !d_ga || !d_w || !d_fid) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL device pointer");
+    if (precision != SPX_FP32 && precision != SPX_FP64) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
+    SPX_CUDA(cudaSetDevice(h->device));
+    spx_options opt{};
+    opt.precision = precision;
+    const Config c = choose_config(h, n_orient, dt, nsteps, opt, 0, kNoallocChunkCap);
+    const bool f64 = precision == SPX_FP64;
+    const size_t npts = (size_t)nsteps + 1;
+    const int group = 64;
+    const int ngroups = (int)((n_orient + group - 1) / group);
+    // carve the scratch: sizes first, then check, then addresses
+    const size_t sizes[8] = {
+        (size_t)c.grid * c.Kmax * (c.M + 1) * sizeof(double),        // Bessel tables
+        npts * (size_t)n_orient * (f64 ? sizeof(double2) : sizeof(float2)),   // per-orientation FIDs
+        (size_t)ngroups * npts * sizeof(double2),                     // FP64 partial sums
+        (size_t)n_orient * sizeof(int), (size_t)n_orient * sizeof(int), (size_t)n_orient * sizeof(int),
+        (size_t)n_orient * sizeof(long long) + (size_t)n_orient * sizeof(double),
+        sizeof(int)};
+    size_t offs[8], total = 0;
+    for (int i = 0; i < 8; ++i) {
+        offs[i] = total;
+        total += (sizes[i] + 255) & ~(size_t)255;
+    }
+    if (total > SPX_NOALLOC_SCRATCH_BYTES)
+        throw SpxError(SPX_ERR_UNSUPPORTED, "this run needs " + std::to_string(total) +
+                                                " bytes of scratch; spx_run_powder_noalloc holds " +
+                                                std::to_string((size_t)SPX_NOALLOC_SCRATCH_BYTES) +
+                                                " (use spx_run_powder_device for larger runs)");
+    unsigned char *base = static_cast<unsigned char *>(noalloc_scratch(h->device));
+    int *flag = reinterpret_cast<int *>(base + offs[7]);
+    spx::DevSystem sys{};
+    sys.n = h->n; sys.n_pad = h->n_pad; sys.nslices = h->nslices; sys.ell_len = h->ell_len;
+    sys.slice_off = h->d_slice_off.p; sys.ell_col = h->d_ell_col.p;
+    sys.ell_re = h->d_ell_re.p; sys.ell_im = h->cplx ? h->d_ell_im.p : nullptr;
+    sys.diag = h->d_diag.p; sys.stream_coef = h->d_stream_coef.p; sys.nstreams = h->nstreams;
+    sys.ncoef = 1 + 2 * h->nterms; sys.nterms = h->nterms; sys.term_rkm = h->d_term_rkm.p;
+    sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag;
+    spx::DevRun run{};
+    run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
+    run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
+    run.fixed_chunk = c.fixed ? 1 : 0; run.chunk_x = c.chunk_x;
+    run.lanczos_its = 32; run.safe_bounds = 0;
+    run.table = reinterpret_cast<double *>(base + offs[0]);
+    run.fids = base + offs[1];
+    run.status = reinterpret_cast<int *>(base + offs[3]);
+    run.kused = reinterpret_cast<int *>(base + offs[4]);
+    run.mused = reinterpret_cast<int *>(base + offs[5]);
+    run.matvecs = reinterpret_cast<long long *>(base + offs[6]);
+    run.halfwidth = reinterpret_cast<double *>(base + offs[6] + (size_t)n_orient * sizeof(long long));
+    double2 *part = reinterpret_cast<double2 *>(base + offs[2]);
+    // the only value that must start at zero is the failure flag
+    SPX_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
+    const void *kfn = select_kernel(f64, h->cplx, c.rmax);
+    void *args[] = {&sys, &run};
+    SPX_CUDA(cudaLaunchKernel(kfn, dim3(c.grid), dim3(c.threads), args, c.smem, h->stream));
+    const dim3 pb(256), pg((unsigned)((npts + 255) / 256), (unsigned)ngroups);
+    if (f64)
+        spx::powder_partial_kernel<double2><<<pg, pb, 0, h->stream>>>(
+            reinterpret_cast<const double2 *>(run.fids), d_w, (int)n_orient, (int)npts, group, part);
+    else
+        spx::powder_partial_kernel<float2><<<pg, pb, 0, h->stream>>>(
+            reinterpret_cast<const float2 *>(run.fids), d_w, (int)n_orient, (int)npts, group, part);
+    SPX_CUDA(cudaGetLastError());
+    spx::powder_combine_kernel<<<dim3((unsigned)((npts + 255) / 256)), dim3(256), 0, h->stream>>>(
+        part, ngroups, (int)npts, reinterpret_cast<double2 *>(d_fid));
+    SPX_CUDA(cudaGetLastError());
+    status_any_kernel<<<dim3(64), dim3(256), 0, h->stream>>>(run.status, (int)n_orient, flag);
+    SPX_CUDA(cudaGetLastError());
+    int failed = 0;
+    SPX_CUDA(cudaMemcpyAsync(&failed, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    SPX_CUDA(cudaStreamSynchronize(h->stream));
+    if (failed)
+        throw SpxError(SPX_ERR_SERIES, "at least one orientation failed its series checks; "
+                                       "spx_run_powder retries such runs with conservative bounds");
+}
+
 }  // namespace
 
 extern "C" {
+
+spx_status spx_run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_alphas,
+                                  const double *d_betas, const double *d_gammas, const double *d_weights,
+                                  double dt, int64_t nsteps, int32_t precision, double *d_fid) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        run_powder_noalloc(h, n_orient, d_alphas, d_betas, d_gammas, d_weights, dt, nsteps, precision, d_fid);
+    });
+}
+
 
 spx_status spx_create(spx_handle **handle, int device) {
     if (!handle) return SPX_ERR_INVALID_ARGUMENT;

@@ -54,6 +54,8 @@ SIGNATURES = {
                                  C.POINTER(SpxOptions), _D, _D]),
     'spx_run_powder_device': (C.c_int, [_P, C.c_int64, _P, _P, _P, _P, C.c_double, C.c_int64,
                                         C.POINTER(SpxOptions), _P]),
+    'spx_run_powder_noalloc': (C.c_int, [_P, C.c_int64, _P, _P, _P, _P, C.c_double, C.c_int64,
+                                         C.c_int32, _P]),
     'spx_synchronize': (C.c_int, [_P]),
     'spx_get_stream': (_P, [_P]),
     'spx_get_stats': (C.c_int, [_P, C.POINTER(SpxStats)]),
@@ -182,6 +184,14 @@ class Engine:
         self._check(self.lib.spx_run_powder_device(self.h, n_orient, d_alphas, d_betas, d_gammas,
                                                    d_weights, float(dt), int(nsteps), C.byref(opt),
                                                    d_fid), self.h)
+
+    def run_noalloc(self, d_alphas: int, d_betas: int, d_gammas: int, d_weights: int, n_orient: int,
+                    dt: float, nsteps: int, d_fid: int, precision: int = FP32):
+        """Blocking run that allocates no memory: every intermediate lives in the
+        library's static device scratch array (spx_run_powder_noalloc)."""
+        self._check(self.lib.spx_run_powder_noalloc(self.h, n_orient, d_alphas, d_betas, d_gammas,
+                                                     d_weights, float(dt), int(nsteps), int(precision),
+                                                     d_fid), self.h)
 
     def synchronize(self):
         self._check(self.lib.spx_synchronize(self.h), self.h)
