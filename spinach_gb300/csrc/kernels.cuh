@@ -403,7 +403,7 @@ struct SmemLayout {
         diag = o; o = align(o + sizeof(typename P::Dg) * n_pad);
         xa = o; o = align(o + sizeof(typename P::Vec) * n_pad);
         xb = o; o = align(o + sizeof(typename P::Vec) * n_pad);
-        part = o; o = align(o + sizeof(typename P::Vec) * 64);
+        part = o; o = align(o + sizeof(typename P::Vec) * (size_t)Kmax * (nthreads / 32));
         atau = o; o = align(o + sizeof(typename P::Dg) * Kmax);
         mu = o; o = align(o + sizeof(typename P::Vec) * Kmax);
         phase = o; o = align(o + sizeof(typename P::Vec) * (M + 1));
@@ -768,18 +768,26 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         __syncthreads();          // coefficients and phases visible before the first term
 
         // ---- 6. chunked Chebyshev propagation with fused coil projection -------
+        // Each lane owns up to RMAX rows (one per 32-row slice of its warp); the
+        // rows advance together, entry index outer and rows inner, so their
+        // accumulations are independent dependency chains.
         Vec t_prev[RMAX], t_cur[RMAX], acc[RMAX], comp[RMAX], cc[RMAX];
+        int r_row[RMAX], r_off[RMAX], r_w[RMAX];
+        int nr = 0, wmax = 0;
 #pragma unroll
         for (int r = 0; r < RMAX; ++r) {
             t_prev[r] = vzero<Vec>(); t_cur[r] = vzero<Vec>(); acc[r] = vzero<Vec>(); comp[r] = vzero<Vec>();
             cc[r] = vzero<Vec>();
-            if (r < rows_per_lane) {
-                const int sl = warp + r * nwarps;
-                if (sl < sys.nslices) {
-                    const int row = sl * 32 + lane;
-                    t_cur[r] = tovec(sys.rho0[row], Vec());
-                    cc[r] = tovec(sys.coil[row], Vec());
-                }
+            r_row[r] = 0; r_off[r] = 0; r_w[r] = 0;
+            const int sl = warp + r * nwarps;
+            if (r < rows_per_lane && sl < sys.nslices) {
+                nr = r + 1;
+                r_row[r] = sl * 32 + lane;
+                r_off[r] = s_soff[sl] + lane;
+                r_w[r] = (s_soff[sl + 1] - s_soff[sl]) >> 5;
+                wmax = max(wmax, r_w[r]);
+                t_cur[r] = tovec(sys.rho0[r_row[r]], Vec());
+                cc[r] = tovec(sys.coil[r_row[r]], Vec());
             }
         }
         const int nchunks = (nsteps + Mo) / Mo;      // ceil((nsteps+1)/Mo)
@@ -790,64 +798,67 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             double start_max = 0.0;
             // k = 0: t0 = rho
             {
-                Acc macc = azero<Acc>();
+                Vec mom = vzero<Vec>();
 #pragma unroll
                 for (int r = 0; r < RMAX; ++r) {
-                    if (r >= rows_per_lane) break;
-                    const int sl = warp + r * nwarps;
-                    if (sl >= sys.nslices) break;
-                    s_xa[sl * 32 + lane] = t_cur[r];
-                    cdot_comp(macc, cc[r], t_cur[r]);
-                    acc[r] = vzero<Vec>();
-                    comp[r] = vzero<Vec>();
-                    mac(acc[r], s_atau[0], t_cur[r]);
-                    start_max += (double)t_cur[r].x * t_cur[r].x + (double)t_cur[r].y * t_cur[r].y;
-                    t_prev[r] = vzero<Vec>();
+                    if (r < nr) {
+                        s_xa[r_row[r]] = t_cur[r];
+                        cdot_acc(mom, cc[r], t_cur[r]);
+                        acc[r] = vzero<Vec>();
+                        comp[r] = vzero<Vec>();
+                        mac(acc[r], s_atau[0], t_cur[r]);
+                        start_max += (double)t_cur[r].x * t_cur[r].x + (double)t_cur[r].y * t_cur[r].y;
+                        t_prev[r] = vzero<Vec>();
+                    }
                 }
-                const Vec mom = warp_sum(collapse(macc));
+                mom = warp_sum(mom);
                 if (lane == 0) s_part[warp] = mom;
             }
             __syncthreads();
-            if (warp == 0) {
-                Vec v = (lane < nwarps) ? s_part[lane] : vzero<Vec>();
-                v = warp_sum(v);
-                if (lane == 0) s_mu[0] = v;
-            }
             // k = 1 .. K-1: t_k = (k==1 ? 1 : 2) L~ t_{k-1} - t_{k-2}
             for (int k = 1; k < K; ++k) {
-                Vec *src = (k & 1) ? s_xa : s_xb;
+                const Vec *src = (k & 1) ? s_xa : s_xb;
                 Vec *dst = (k & 1) ? s_xb : s_xa;
-                Vec *part = s_part + ((k & 1) ? 32 : 0);
                 const Real two = (k == 1) ? (Real)1 : (Real)2;
-                Acc macc = azero<Acc>();
+                Acc y[RMAX];
 #pragma unroll
                 for (int r = 0; r < RMAX; ++r) {
-                    if (r >= rows_per_lane) break;
-                    const int sl = warp + r * nwarps;
-                    if (sl >= sys.nslices) break;
-                    const int row = sl * 32 + lane;
-                    const int off = s_soff[sl], w = (s_soff[sl + 1] - off) >> 5;
-                    Acc y = azero<Acc>();
-                    cmac(y, s_diag[row], t_cur[r]);
-                    for (int c = 0; c < w; ++c) {
-                        const int e = off + c * 32 + lane;
-                        cmac(y, s_val[e], src[s_col[e]]);
+                    y[r] = azero<Acc>();
+                    if (r < nr) cmac(y[r], s_diag[r_row[r]], t_cur[r]);
+                }
+                for (int c = 0; c < wmax; ++c) {
+#pragma unroll
+                    for (int r = 0; r < RMAX; ++r) {
+                        if (r < nr && c < r_w[r]) {
+                            const int e = r_off[r] + c * 32;
+                            cmac(y[r], s_val[e], src[s_col[e]]);
+                        }
                     }
-                    const Vec tn = recur(y, two, t_prev[r]);
-                    t_prev[r] = t_cur[r];
-                    t_cur[r] = tn;
-                    dst[row] = tn;
-                    cdot_comp(macc, cc[r], tn);
-                    if (advance) acc_add<F64>(acc[r], comp[r], s_atau[k], tn);
                 }
-                Vec mom = warp_sum(collapse(macc));
-                if (lane == 0) part[warp] = mom;
+                Vec mom = vzero<Vec>();
+#pragma unroll
+                for (int r = 0; r < RMAX; ++r) {
+                    if (r < nr) {
+                        const Vec tn = recur(y[r], two, t_prev[r]);
+                        t_prev[r] = t_cur[r];
+                        t_cur[r] = tn;
+                        dst[r_row[r]] = tn;
+                        cdot_acc(mom, cc[r], tn);
+                        if (advance) acc_add<F64>(acc[r], comp[r], s_atau[k], tn);
+                    }
+                }
+                mom = warp_sum(mom);
+                if (lane == 0) s_part[k * nwarps + warp] = mom;
                 __syncthreads();
-                if (warp == 0) {
-                    Vec v = (lane < nwarps) ? part[lane] : vzero<Vec>();
-                    v = warp_sum(v);
-                    if (lane == 0) s_mu[k] = v;
+            }
+            // moments: sum the per-warp partials of every term
+            for (int k = tid; k < K; k += blockDim.x) {
+                Vec v = vzero<Vec>();
+                for (int w2 = 0; w2 < nwarps; ++w2) {
+                    const Vec q = s_part[k * nwarps + w2];
+                    v.x += q.x; v.y += q.y;
                 }
+                s_mu[k] = v;
             }
             __syncthreads();
             // FID points of this chunk: f_j = ph_j * sum_k J_k(s j dt) (-i)^k mu_k
