@@ -773,7 +773,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         // accumulations are independent dependency chains.
         Vec t_prev[RMAX], t_cur[RMAX], acc[RMAX], comp[RMAX], cc[RMAX];
         int r_row[RMAX], r_off[RMAX], r_w[RMAX];
-        int nr = 0, wmax = 0;
+        int nr = 0;
 #pragma unroll
         for (int r = 0; r < RMAX; ++r) {
             t_prev[r] = vzero<Vec>(); t_cur[r] = vzero<Vec>(); acc[r] = vzero<Vec>(); comp[r] = vzero<Vec>();
@@ -785,7 +785,6 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 r_row[r] = sl * 32 + lane;
                 r_off[r] = s_soff[sl] + lane;
                 r_w[r] = (s_soff[sl + 1] - s_soff[sl]) >> 5;
-                wmax = max(wmax, r_w[r]);
                 t_cur[r] = tovec(sys.rho0[r_row[r]], Vec());
                 cc[r] = tovec(sys.coil[r_row[r]], Vec());
             }
@@ -826,12 +825,22 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     y[r] = azero<Acc>();
                     if (r < nr) cmac(y[r], s_diag[r_row[r]], t_cur[r]);
                 }
-                for (int c = 0; c < wmax; ++c) {
+                // a lane's slices come in non-increasing width, so entry c is
+                // shared by rows 0..seg-1 while c < width of row seg-1: run each
+                // segment with a compile-time row count (branch-free bodies)
+                {
+                    int c = 0;
 #pragma unroll
-                    for (int r = 0; r < RMAX; ++r) {
-                        if (r < nr && c < r_w[r]) {
-                            const int e = r_off[r] + c * 32;
-                            cmac(y[r], s_val[e], src[s_col[e]]);
+                    for (int seg = RMAX; seg >= 1; --seg) {
+                        if (seg <= nr) {
+                            const int cend = r_w[seg - 1];
+                            for (; c < cend; ++c) {
+#pragma unroll
+                                for (int r = 0; r < seg; ++r) {
+                                    const int e = r_off[r] + c * 32;
+                                    cmac(y[r], s_val[e], src[s_col[e]]);
+                                }
+                            }
                         }
                     }
                 }
