@@ -22,9 +22,11 @@
 // quantity the reference computes.
 //
 // FP32 mode stores Liouvillian values and series coefficients as hi+lo float
-// pairs (about 48 significant bits) and state vectors as complex float: the
-// value rounding, not the vector rounding, is what drifts the phase over
-// thousands of steps.  FP64 mode stores everything in double.
+// pairs (about 48 significant bits), keeps state vectors in complex float, and
+// sums every matvec row with a compensated (TwoSum) accumulator in packed
+// f32x2 (re, im) arithmetic: rounding each term at most once is what keeps the
+// phase from drifting over thousands of steps.  FP64 mode stores everything in
+// double.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -45,46 +47,71 @@ enum DeviceStatus : int {
     kDevTooManyRows = 4,
 };
 
-struct __align__(8) SplitR { float hi, lo; };
-struct CAcc;
-struct __align__(16) SplitC { float rh, ih, rl, il; };
+// FP32 shared-memory value layouts, pre-packed for f32x2 arithmetic:
+//   PackR  real off-diagonal value v = hi + lo as (hi, hi, lo, lo)
+//   PackC  complex value: h = (re_hi, re_hi, -im_hi, im_hi), l = same for lo parts
+//   PackD  diagonal d: h = (re_hi, re_hi, -im, im), l = (re_lo, re_lo, 0, 0)
+//   PackA  complex series coefficient, laid out as PackC
+struct __align__(16) PackR { float4 v; };
+struct __align__(16) PackC { float4 h, l; };
+struct __align__(16) PackD { float4 h, l; };
+typedef PackC PackA;
 
 // ---------------------------------------------------------------------------
 // Precision policies
 // ---------------------------------------------------------------------------
 template <bool F64, bool CPLX> struct Prec;
-template <> struct Prec<false, false> { using Vec = float2;  using Val = SplitR; using Dg = SplitC; using Real = float; using Acc = CAcc; };
-template <> struct Prec<false, true>  { using Vec = float2;  using Val = SplitC; using Dg = SplitC; using Real = float; using Acc = CAcc; };
-template <> struct Prec<true, false>  { using Vec = double2; using Val = double; using Dg = double2; using Real = double; using Acc = double2; };
-template <> struct Prec<true, true>   { using Vec = double2; using Val = double2; using Dg = double2; using Real = double; using Acc = double2; };
+template <> struct Prec<false, false> { using Vec = float2;  using Val = PackR;  using Dg = PackD;   using Af = PackA;   using Real = float;  using Acc = float2; };
+template <> struct Prec<false, true>  { using Vec = float2;  using Val = PackC;  using Dg = PackD;   using Af = PackA;   using Real = float;  using Acc = float2; };
+template <> struct Prec<true, false>  { using Vec = double2; using Val = double;  using Dg = double2; using Af = double2; using Real = double; using Acc = double2; };
+template <> struct Prec<true, true>   { using Vec = double2; using Val = double2; using Dg = double2; using Af = double2; using Real = double; using Acc = double2; };
 
-__device__ __forceinline__ void pack(SplitR &o, double re, double) {
-    o.hi = (float)re; o.lo = (float)(re - (double)o.hi);
+__device__ __forceinline__ void split(double v, float &hi, float &lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
 }
-__device__ __forceinline__ void pack(SplitC &o, double re, double im) {
-    o.rh = (float)re; o.ih = (float)im;
-    o.rl = (float)(re - (double)o.rh); o.il = (float)(im - (double)o.ih);
+__device__ __forceinline__ void pack(PackR &o, double re, double) {
+    float h, l;
+    split(re, h, l);
+    o.v = make_float4(h, h, l, l);
 }
+__device__ __forceinline__ void pack(PackC &o, double re, double im) {
+    float rh, rl, ih, il;
+    split(re, rh, rl);
+    split(im, ih, il);
+    o.h = make_float4(rh, rh, -ih, ih);
+    o.l = make_float4(rl, rl, -il, il);
+}
+__device__ __forceinline__ void pack(PackD &o, double re, double im) {
+    float rh, rl;
+    split(re, rh, rl);
+    const float fi = (float)im;
+    o.h = make_float4(rh, rh, -fi, fi);
+    o.l = make_float4(rl, rl, 0.f, 0.f);
+}
+__device__ __forceinline__ double2 unpack(const PackR &v) { return make_double2((double)v.v.x + (double)v.v.z, 0.0); }
+__device__ __forceinline__ double2 unpack(const PackC &v) {
+    return make_double2((double)v.h.x + (double)v.l.x, (double)v.h.w + (double)v.l.w);
+}
+__device__ __forceinline__ double2 unpack(const PackD &v) { return make_double2((double)v.h.x + (double)v.l.x, (double)v.h.w); }
 __device__ __forceinline__ void pack(double &o, double re, double) { o = re; }
 __device__ __forceinline__ void pack(double2 &o, double re, double im) { o = make_double2(re, im); }
 
-__device__ __forceinline__ double2 unpack(const SplitR &v) { return make_double2((double)v.hi + (double)v.lo, 0.0); }
-__device__ __forceinline__ double2 unpack(const SplitC &v) {
-    return make_double2((double)v.rh + (double)v.rl, (double)v.ih + (double)v.il);
-}
 __device__ __forceinline__ double2 unpack(const double &v) { return make_double2(v, 0.0); }
 __device__ __forceinline__ double2 unpack(const double2 &v) { return v; }
 
-// y += v * x  (value times complex state)
-__device__ __forceinline__ void mac(float2 &y, const SplitR &v, const float2 x) {
-    y.x = fmaf(v.hi, x.x, y.x); y.y = fmaf(v.hi, x.y, y.y);
-    y.x = fmaf(v.lo, x.x, y.x); y.y = fmaf(v.lo, x.y, y.y);
+// y += v * x  (value times complex state; plain arithmetic, used outside the
+// propagation loop and in the FP64 path)
+__device__ __forceinline__ void mac(float2 &y, const PackR &v, const float2 x) {
+    y.x = fmaf(v.v.x, x.x, y.x); y.y = fmaf(v.v.x, x.y, y.y);
+    y.x = fmaf(v.v.z, x.x, y.x); y.y = fmaf(v.v.z, x.y, y.y);
 }
-__device__ __forceinline__ void mac(float2 &y, const SplitC &v, const float2 x) {
-    y.x = fmaf(v.rh, x.x, y.x); y.x = fmaf(-v.ih, x.y, y.x);
-    y.y = fmaf(v.rh, x.y, y.y); y.y = fmaf(v.ih, x.x, y.y);
-    y.x = fmaf(v.rl, x.x, y.x); y.x = fmaf(-v.il, x.y, y.x);
-    y.y = fmaf(v.rl, x.y, y.y); y.y = fmaf(v.il, x.x, y.y);
+__device__ __forceinline__ void mac(float2 &y, const PackC &v, const float2 x) {
+    // h = (re, re, -im, im): re*x + (-im*x.y, im*x.x)
+    y.x = fmaf(v.h.x, x.x, y.x); y.y = fmaf(v.h.y, x.y, y.y);
+    y.x = fmaf(v.h.z, x.y, y.x); y.y = fmaf(v.h.w, x.x, y.y);
+    y.x = fmaf(v.l.x, x.x, y.x); y.y = fmaf(v.l.y, x.y, y.y);
+    y.x = fmaf(v.l.z, x.y, y.x); y.y = fmaf(v.l.w, x.x, y.y);
 }
 __device__ __forceinline__ void mac(double2 &y, const double &v, const double2 x) {
     y.x = fma(v, x.x, y.x); y.y = fma(v, x.y, y.y);
@@ -138,74 +165,57 @@ __device__ __forceinline__ double warp_min_d(double v) {
 }
 
 // ---------------------------------------------------------------------------
-// Compensated FP32 accumulation (error-free transformations).  The product
-// error comes from fmaf(a, b, -round(a*b)); sums use TwoSum.  The _rn
-// intrinsics keep the compiler from contracting the pieces into FMAs, which
-// would break the error bookkeeping.
+// Packed f32x2 arithmetic (sm_100+ PTX add/sub/mul/fma.rn.f32x2).  A complex
+// float is one 64-bit register pair (re, im).  Inline PTX is never contracted
+// or reassociated by the compiler, which the TwoSum bookkeeping relies on.
 // ---------------------------------------------------------------------------
-struct CAcc { float2 hi, lo; };
+typedef unsigned long long f2x;
 
-__device__ __forceinline__ void two_sum_into(float &hi, float &lo, float p) {
-    const float s = __fadd_rn(hi, p);
-    const float bp = __fsub_rn(s, hi);
-    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
-    hi = s;
-    lo = __fadd_rn(lo, err);
+__device__ __forceinline__ f2x f2pk(float a, float b) {
+    f2x r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
 }
-// hi/lo += a * b with the product error kept
-__device__ __forceinline__ void prod_into(float &hi, float &lo, float a, float b) {
-    const float p = __fmul_rn(a, b);
-    const float e = __fmaf_rn(a, b, -p);
-    two_sum_into(hi, lo, p);
-    lo = __fadd_rn(lo, e);
+__device__ __forceinline__ float2 f2up(f2x v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
 }
-__device__ __forceinline__ void cmac(CAcc &y, const SplitR &v, const float2 x) {
-    prod_into(y.hi.x, y.lo.x, v.hi, x.x);
-    prod_into(y.hi.y, y.lo.y, v.hi, x.y);
-    y.lo.x = __fmaf_rn(v.lo, x.x, y.lo.x);
-    y.lo.y = __fmaf_rn(v.lo, x.y, y.lo.y);
+__device__ __forceinline__ f2x add2(f2x a, f2x b) { f2x r; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
+__device__ __forceinline__ f2x sub2(f2x a, f2x b) { f2x r; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) { f2x r; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+    f2x r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
 }
-__device__ __forceinline__ void cmac(CAcc &y, const SplitC &v, const float2 x) {
-    prod_into(y.hi.x, y.lo.x, v.rh, x.x);
-    prod_into(y.hi.x, y.lo.x, -v.ih, x.y);
-    prod_into(y.hi.y, y.lo.y, v.rh, x.y);
-    prod_into(y.hi.y, y.lo.y, v.ih, x.x);
-    y.lo.x = __fmaf_rn(v.rl, x.x, y.lo.x);
-    y.lo.x = __fmaf_rn(-v.il, x.y, y.lo.x);
-    y.lo.y = __fmaf_rn(v.rl, x.y, y.lo.y);
-    y.lo.y = __fmaf_rn(v.il, x.x, y.lo.y);
+__device__ __forceinline__ f2x swap2(f2x a) { const float2 f = f2up(a); return f2pk(f.y, f.x); }
+__device__ __forceinline__ f2x lo2(const float4 &v) { return f2pk(v.x, v.y); }
+__device__ __forceinline__ f2x hi2(const float4 &v) { return f2pk(v.z, v.w); }
+
+// Y + Z += P with Y the running sum and Z collecting its rounding errors (TwoSum)
+__device__ __forceinline__ void two_sum2(f2x &Y, f2x &Z, f2x P) {
+    const f2x S = add2(Y, P);
+    const f2x B = sub2(S, Y);
+    const f2x E = add2(sub2(Y, sub2(S, B)), sub2(P, B));
+    Y = S;
+    Z = add2(Z, E);
 }
-// conj(a) * b accumulated with compensation
-__device__ __forceinline__ void cdot_comp(CAcc &s, const float2 a, const float2 b) {
-    prod_into(s.hi.x, s.lo.x, a.x, b.x);
-    prod_into(s.hi.x, s.lo.x, a.y, b.y);
-    prod_into(s.hi.y, s.lo.y, a.x, b.y);
-    prod_into(s.hi.y, s.lo.y, -a.y, b.x);
+// a * t for a packed complex coefficient (PackC/PackA layout), hi and lo parts
+__device__ __forceinline__ f2x cmul_pk(const PackC &a, f2x T) {
+    const f2x TS = swap2(T);
+    f2x P = mul2(lo2(a.h), T);
+    P = fma2(hi2(a.h), TS, P);
+    P = fma2(lo2(a.l), T, P);
+    return fma2(hi2(a.l), TS, P);
 }
+
+// FP64 helpers of the generic propagation loop
 __device__ __forceinline__ void cmac(double2 &y, const double &v, const double2 x) { mac(y, v, x); }
 __device__ __forceinline__ void cmac(double2 &y, const double2 &v, const double2 x) { mac(y, v, x); }
-__device__ __forceinline__ void cdot_comp(double2 &s, const double2 a, const double2 b) { cdot_acc(s, a, b); }
-
-template <class A> __device__ __forceinline__ A azero();
-template <> __device__ __forceinline__ CAcc azero<CAcc>() {
-    CAcc a; a.hi = make_float2(0.f, 0.f); a.lo = make_float2(0.f, 0.f); return a;
-}
-template <> __device__ __forceinline__ double2 azero<double2>() { return make_double2(0.0, 0.0); }
-
-// t_new = two * y - t_prev, rounded once from the compensated value
-__device__ __forceinline__ float2 recur(const CAcc &y, float two, const float2 tp) {
-    float2 t;
-    t.x = __fmaf_rn(two, y.lo.x, __fmaf_rn(two, y.hi.x, -tp.x));
-    t.y = __fmaf_rn(two, y.lo.y, __fmaf_rn(two, y.hi.y, -tp.y));
-    return t;
-}
 __device__ __forceinline__ double2 recur(const double2 &y, double two, const double2 tp) {
     return make_double2(two * y.x - tp.x, two * y.y - tp.y);
 }
-__device__ __forceinline__ float2 collapse(const CAcc &a) {
-    return make_float2(__fadd_rn(a.hi.x, a.lo.x), __fadd_rn(a.hi.y, a.lo.y));
-}
-__device__ __forceinline__ double2 collapse(const double2 &a) { return a; }
 
 // Block-wide reductions through a shared scratch of kRedSlots doubles.
 // Every thread of the block must call them (they contain __syncthreads).
@@ -404,7 +414,7 @@ struct SmemLayout {
         xa = o; o = align(o + sizeof(typename P::Vec) * n_pad);
         xb = o; o = align(o + sizeof(typename P::Vec) * n_pad);
         part = o; o = align(o + sizeof(typename P::Vec) * (size_t)Kmax * (nthreads / 32));
-        atau = o; o = align(o + sizeof(typename P::Dg) * Kmax);
+        atau = o; o = align(o + sizeof(typename P::Af) * Kmax);
         mu = o; o = align(o + sizeof(typename P::Vec) * Kmax);
         phase = o; o = align(o + sizeof(typename P::Vec) * (M + 1));
         rec = o; o = align(o + sizeof(typename P::Vec) * (nthreads > M ? nthreads : M));
@@ -412,23 +422,8 @@ struct SmemLayout {
     }
 };
 
-// acc += a * t.  In FP32 mode the sum is compensated (Kahan): the chunk-end
-// state is a sum of ~100 terms of size up to ~1 and would otherwise carry
-// sqrt(K)*eps of rounding into every later chunk.
-template <bool F64, class Vec, class Cf>
-__device__ __forceinline__ void acc_add(Vec &acc, Vec &comp, const Cf &a, const Vec t) {
-    Vec p = vzero<Vec>();
-    mac(p, a, t);
-    if (F64) {
-        acc.x += p.x; acc.y += p.y;
-    } else {
-        const auto yx = p.x - comp.x, yy = p.y - comp.y;
-        const auto sx = acc.x + yx, sy = acc.y + yy;
-        comp.x = (sx - acc.x) - yx;
-        comp.y = (sy - acc.y) - yy;
-        acc.x = sx; acc.y = sy;
-    }
-}
+// acc += a * t (FP64 propagation loop)
+__device__ __forceinline__ void acc_add64(double2 &acc, const double2 &a, const double2 t) { mac(acc, a, t); }
 
 // Number of Chebyshev/Bessel terms after which |J_k(x)| * e^{k*lg} < tol
 // (Debye-type bound (e x / 2k)^k / sqrt(2 pi k), conservative for k > x).
@@ -495,6 +490,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     using Dg = typename P::Dg;
     using Real = typename P::Real;
     using Acc = typename P::Acc;
+    using Af = typename P::Af;
 
     extern __shared__ __align__(16) unsigned char smem[];
     const SmemLayout<F64, CPLX> L(sys.n_pad, sys.nslices, sys.ell_len, run.Kmax, run.M, blockDim.x);
@@ -509,7 +505,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     Vec *s_xa = reinterpret_cast<Vec *>(smem + L.xa);
     Vec *s_xb = reinterpret_cast<Vec *>(smem + L.xb);
     Vec *s_part = reinterpret_cast<Vec *>(smem + L.part);
-    Dg *s_atau = reinterpret_cast<Dg *>(smem + L.atau);
+    Af *s_atau = reinterpret_cast<Af *>(smem + L.atau);
     Vec *s_mu = reinterpret_cast<Vec *>(smem + L.mu);
     Vec *s_phase = reinterpret_cast<Vec *>(smem + L.phase);
     Vec *s_rec = reinterpret_cast<Vec *>(smem + L.rec);
@@ -770,14 +766,13 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         // ---- 6. chunked Chebyshev propagation with fused coil projection -------
         // Each lane owns up to RMAX rows (one per 32-row slice of its warp); the
         // rows advance together, entry index outer and rows inner, so their
-        // accumulations are independent dependency chains.
-        Vec t_prev[RMAX], t_cur[RMAX], acc[RMAX], comp[RMAX], cc[RMAX];
+        // accumulations are independent dependency chains.  A lane's slices come
+        // in non-increasing width, so entry c is shared by rows 0..seg-1 while
+        // c < width of row seg-1: each segment runs with a compile-time row count.
         int r_row[RMAX], r_off[RMAX], r_w[RMAX];
         int nr = 0;
 #pragma unroll
         for (int r = 0; r < RMAX; ++r) {
-            t_prev[r] = vzero<Vec>(); t_cur[r] = vzero<Vec>(); acc[r] = vzero<Vec>(); comp[r] = vzero<Vec>();
-            cc[r] = vzero<Vec>();
             r_row[r] = 0; r_off[r] = 0; r_w[r] = 0;
             const int sl = warp + r * nwarps;
             if (r < rows_per_lane && sl < sys.nslices) {
@@ -785,18 +780,34 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 r_row[r] = sl * 32 + lane;
                 r_off[r] = s_soff[sl] + lane;
                 r_w[r] = (s_soff[sl + 1] - s_soff[sl]) >> 5;
-                t_cur[r] = tovec(sys.rho0[r_row[r]], Vec());
-                cc[r] = tovec(sys.coil[r_row[r]], Vec());
             }
         }
         const int nchunks = (nsteps + Mo) / Mo;      // ceil((nsteps+1)/Mo)
         Vec *fid_out = reinterpret_cast<Vec *>(run.fids) + (size_t)o * (nsteps + 1);
         int status = kDevOk;
+        [[maybe_unused]] Vec t_prev[RMAX], t_cur[RMAX], acc[RMAX], cc[RMAX];
+        [[maybe_unused]] f2x tp[RMAX], tc[RMAX], ac[RMAX], cp[RMAX], crr[RMAX], cim[RMAX];
+#pragma unroll
+        for (int r = 0; r < RMAX; ++r) {
+            const double2 x0 = r < nr ? sys.rho0[r_row[r]] : make_double2(0.0, 0.0);
+            const double2 c0 = r < nr ? sys.coil[r_row[r]] : make_double2(0.0, 0.0);
+            if constexpr (F64) {
+                t_prev[r] = vzero<Vec>(); acc[r] = vzero<Vec>();
+                t_cur[r] = tovec(x0, Vec());
+                cc[r] = tovec(c0, Vec());
+            } else {
+                tp[r] = 0ull; ac[r] = 0ull; cp[r] = 0ull;
+                tc[r] = f2pk((float)x0.x, (float)x0.y);
+                // conj(c) * t = (cr tr + ci ti, cr ti - ci tr) = crr*t + cim*swap(t)
+                crr[r] = f2pk((float)c0.x, (float)c0.x);
+                cim[r] = f2pk((float)c0.y, -(float)c0.y);
+            }
+        }
         for (int a = 0; a < nchunks && status == kDevOk; ++a) {
             const bool advance = (a + 1 < nchunks);
-            double start_max = 0.0;
-            // k = 0: t0 = rho
-            {
+            double start_n2 = 0.0, end_n2 = 0.0;
+            if constexpr (F64) {
+                // k = 0: t0 = rho
                 Vec mom = vzero<Vec>();
 #pragma unroll
                 for (int r = 0; r < RMAX; ++r) {
@@ -804,31 +815,25 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                         s_xa[r_row[r]] = t_cur[r];
                         cdot_acc(mom, cc[r], t_cur[r]);
                         acc[r] = vzero<Vec>();
-                        comp[r] = vzero<Vec>();
-                        mac(acc[r], s_atau[0], t_cur[r]);
-                        start_max += (double)t_cur[r].x * t_cur[r].x + (double)t_cur[r].y * t_cur[r].y;
+                        acc_add64(acc[r], s_atau[0], t_cur[r]);
+                        start_n2 += t_cur[r].x * t_cur[r].x + t_cur[r].y * t_cur[r].y;
                         t_prev[r] = vzero<Vec>();
                     }
                 }
                 mom = warp_sum(mom);
                 if (lane == 0) s_part[warp] = mom;
-            }
-            __syncthreads();
-            // k = 1 .. K-1: t_k = (k==1 ? 1 : 2) L~ t_{k-1} - t_{k-2}
-            for (int k = 1; k < K; ++k) {
-                const Vec *src = (k & 1) ? s_xa : s_xb;
-                Vec *dst = (k & 1) ? s_xb : s_xa;
-                const Real two = (k == 1) ? (Real)1 : (Real)2;
-                Acc y[RMAX];
+                __syncthreads();
+                // k = 1 .. K-1: t_k = (k==1 ? 1 : 2) L~ t_{k-1} - t_{k-2}
+                for (int k = 1; k < K; ++k) {
+                    const Vec *src = (k & 1) ? s_xa : s_xb;
+                    Vec *dst = (k & 1) ? s_xb : s_xa;
+                    const Real two = (k == 1) ? (Real)1 : (Real)2;
+                    Acc y[RMAX];
 #pragma unroll
-                for (int r = 0; r < RMAX; ++r) {
-                    y[r] = azero<Acc>();
-                    if (r < nr) cmac(y[r], s_diag[r_row[r]], t_cur[r]);
-                }
-                // a lane's slices come in non-increasing width, so entry c is
-                // shared by rows 0..seg-1 while c < width of row seg-1: run each
-                // segment with a compile-time row count (branch-free bodies)
-                {
+                    for (int r = 0; r < RMAX; ++r) {
+                        y[r] = vzero<Vec>();
+                        if (r < nr) cmac(y[r], s_diag[r_row[r]], t_cur[r]);
+                    }
                     int c = 0;
 #pragma unroll
                     for (int seg = RMAX; seg >= 1; --seg) {
@@ -843,22 +848,129 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                             }
                         }
                     }
+                    mom = vzero<Vec>();
+#pragma unroll
+                    for (int r = 0; r < RMAX; ++r) {
+                        if (r < nr) {
+                            const Vec tn = recur(y[r], two, t_prev[r]);
+                            t_prev[r] = t_cur[r];
+                            t_cur[r] = tn;
+                            dst[r_row[r]] = tn;
+                            cdot_acc(mom, cc[r], tn);
+                            if (advance) acc_add64(acc[r], s_atau[k], tn);
+                        }
+                    }
+                    mom = warp_sum(mom);
+                    if (lane == 0) s_part[k * nwarps + warp] = mom;
+                    __syncthreads();
                 }
-                Vec mom = vzero<Vec>();
 #pragma unroll
                 for (int r = 0; r < RMAX; ++r) {
                     if (r < nr) {
-                        const Vec tn = recur(y[r], two, t_prev[r]);
-                        t_prev[r] = t_cur[r];
-                        t_cur[r] = tn;
-                        dst[r_row[r]] = tn;
-                        cdot_acc(mom, cc[r], tn);
-                        if (advance) acc_add<F64>(acc[r], comp[r], s_atau[k], tn);
+                        if (advance) t_cur[r] = acc[r];
+                        end_n2 += t_cur[r].x * t_cur[r].x + t_cur[r].y * t_cur[r].y;
                     }
                 }
-                mom = warp_sum(mom);
-                if (lane == 0) s_part[k * nwarps + warp] = mom;
+            } else {
+                // ---- FP32: packed (re, im) pairs, compensated row sums ----
+                const f2x TWO = f2pk(2.f, 2.f), ONE = f2pk(1.f, 1.f);
+                f2x MOM = 0ull;
+#pragma unroll
+                for (int r = 0; r < RMAX; ++r) {
+                    if (r < nr) {
+                        const f2x T = tc[r];
+                        reinterpret_cast<f2x *>(s_xa)[r_row[r]] = T;
+                        MOM = fma2(crr[r], T, MOM);
+                        MOM = fma2(cim[r], swap2(T), MOM);
+                        ac[r] = cmul_pk(s_atau[0], T);
+                        cp[r] = 0ull;
+                        tp[r] = 0ull;
+                        const float2 t = f2up(T);
+                        start_n2 += (double)t.x * t.x + (double)t.y * t.y;
+                    }
+                }
+                {
+                    float2 m = warp_sum(f2up(MOM));
+                    if (lane == 0) s_part[warp] = m;
+                }
                 __syncthreads();
+                for (int k = 1; k < K; ++k) {
+                    const f2x *src = reinterpret_cast<const f2x *>((k & 1) ? s_xa : s_xb);
+                    f2x *dst = reinterpret_cast<f2x *>((k & 1) ? s_xb : s_xa);
+                    const f2x TW = (k == 1) ? ONE : TWO;
+                    f2x Y[RMAX], Z[RMAX];
+#pragma unroll
+                    for (int r = 0; r < RMAX; ++r) {
+                        Y[r] = 0ull;
+                        Z[r] = 0ull;
+                        if (r < nr) {
+                            const PackD d = s_diag[r_row[r]];
+                            const f2x X = tc[r];
+                            two_sum2(Y[r], Z[r], mul2(lo2(d.h), X));
+                            two_sum2(Y[r], Z[r], mul2(hi2(d.h), swap2(X)));
+                            Z[r] = fma2(lo2(d.l), X, Z[r]);
+                        }
+                    }
+                    int c = 0;
+#pragma unroll
+                    for (int seg = RMAX; seg >= 1; --seg) {
+                        if (seg <= nr) {
+                            const int cend = r_w[seg - 1];
+                            for (; c < cend; ++c) {
+#pragma unroll
+                                for (int r = 0; r < seg; ++r) {
+                                    const int e = r_off[r] + c * 32;
+                                    const f2x X = src[s_col[e]];
+                                    if constexpr (CPLX) {
+                                        const PackC v = s_val[e];
+                                        const f2x XS = swap2(X);
+                                        two_sum2(Y[r], Z[r], mul2(lo2(v.h), X));
+                                        two_sum2(Y[r], Z[r], mul2(hi2(v.h), XS));
+                                        Z[r] = fma2(lo2(v.l), X, Z[r]);
+                                        Z[r] = fma2(hi2(v.l), XS, Z[r]);
+                                    } else {
+                                        const PackR v = s_val[e];
+                                        two_sum2(Y[r], Z[r], mul2(lo2(v.v), X));
+                                        Z[r] = fma2(hi2(v.v), X, Z[r]);
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    MOM = 0ull;
+#pragma unroll
+                    for (int r = 0; r < RMAX; ++r) {
+                        if (r < nr) {
+                            // t_k = TW * (Y + Z) - t_{k-2}, rounded once from the compensated sum
+                            const f2x T = sub2(fma2(TW, Y[r], mul2(TW, Z[r])), tp[r]);
+                            tp[r] = tc[r];
+                            tc[r] = T;
+                            dst[r_row[r]] = T;
+                            MOM = fma2(crr[r], T, MOM);
+                            MOM = fma2(cim[r], swap2(T), MOM);
+                            if (advance) {
+                                // Kahan-compensated chunk-end sum acc += a_k t_k
+                                const f2x Yk = sub2(cmul_pk(s_atau[k], T), cp[r]);
+                                const f2x S = add2(ac[r], Yk);
+                                cp[r] = sub2(sub2(S, ac[r]), Yk);
+                                ac[r] = S;
+                            }
+                        }
+                    }
+                    {
+                        float2 m = warp_sum(f2up(MOM));
+                        if (lane == 0) s_part[k * nwarps + warp] = m;
+                    }
+                    __syncthreads();
+                }
+#pragma unroll
+                for (int r = 0; r < RMAX; ++r) {
+                    if (r < nr) {
+                        if (advance) tc[r] = ac[r];
+                        const float2 t = f2up(tc[r]);
+                        end_n2 += (double)t.x * t.x + (double)t.y * t.y;
+                    }
+                }
             }
             // moments: sum the per-warp partials of every term
             for (int k = tid; k < K; k += blockDim.x) {
@@ -908,19 +1020,12 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     if (nidx <= nsteps) fid_out[nidx] = out;
                 }
             }
-            // next chunk starts from the accumulated state; guard against a
-            // violated spectral bound (the series would then grow, not decay)
-            double end_n2 = 0.0;
-#pragma unroll
-            for (int r = 0; r < RMAX; ++r) {
-                if (r >= rows_per_lane) break;
-                if (advance) t_cur[r] = acc[r];
-                end_n2 += (double)t_cur[r].x * t_cur[r].x + (double)t_cur[r].y * t_cur[r].y;
-            }
+            // guard against a violated spectral bound (the series would then
+            // grow; a dissipative L can only shrink the state)
             end_n2 = block_sum(end_n2, s_red);
-            start_max = block_sum(start_max, s_red);
+            start_n2 = block_sum(start_n2, s_red);
             if (!isfinite(end_n2)) status = kDevNonFinite;
-            else if (end_n2 > 16.0 * start_max + 1e-300) status = kDevDiverged;
+            else if (end_n2 > 16.0 * start_n2 + 1e-300) status = kDevDiverged;
         }
         if (tid == 0) {
             run.status[o] = status;
