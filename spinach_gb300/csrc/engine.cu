@@ -396,16 +396,16 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     const bool f64 = opt.precision == SPX_FP64;
     c.tol = opt.series_tol > 0 ? opt.series_tol : (f64 ? 1e-16 : 1e-11);
     // warps: about four 32-row slices per lane, at most 16 warps
-    int nwarps = std::min(16, std::max(1, (h->nslices + 3) / 4));
+    int nwarps = std::min(16, std::max(1, (2 * h->nslices + 4) / 5));   // ~2.5 slices per warp
     if (opt.threads > 0) nwarps = std::max(1, std::min(16, opt.threads / 32));
     const int rows = (h->nslices + nwarps - 1) / nwarps;
-    if (rows > 8) throw SpxError(SPX_ERR_UNSUPPORTED, "Liouville dimension too large for the register-resident kernel");
+    if (rows > 8 || nwarps > 32) throw SpxError(SPX_ERR_UNSUPPORTED, "Liouville dimension too large for the register-resident kernel");
     c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 8;
     c.threads = nwarps * 32;
     // chunk: each orientation picks a power-of-two step count whose series
     // argument s*M*dt is about chunk_x (kernel side); M here is the cap.
     c.fixed = opt.chunk_steps > 0;
-    c.chunk_x = f64 ? 150.0 : 150.0;
+    c.chunk_x = 300.0;
     int M = c.fixed ? opt.chunk_steps : m_cap;
     M = (int)std::min<int64_t>(M, nsteps + 1);
     M = std::max(M, 1);

@@ -517,14 +517,37 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     const int M = run.M;
     const int nsteps = run.nsteps;
     double *table = run.table + (size_t)blockIdx.x * run.Kmax * (M + 1);
-    const int rows_per_lane = (sys.nslices + nwarps - 1) / nwarps;
-
     // Static pattern: copy once per CTA.
     for (int i = tid; i <= sys.nslices; i += blockDim.x) s_soff[i] = sys.slice_off[i];
     for (int e = tid; e < sys.ell_len; e += blockDim.x) s_col[e] = sys.ell_col[e];
+    // Slices to warps, longest-processing-time first: slices are stored in
+    // non-increasing width, each goes to the least-loaded warp with room, so a
+    // warp's slices also come in non-increasing width.  Cost ~ width + 5.
+    __shared__ short s_wsl[32 * 8];
+    __shared__ int s_wcnt[32];
+    __shared__ int s_wload[32];
+    __syncthreads();
+    if (tid == 0) {
+        for (int w = 0; w < nwarps; ++w) { s_wcnt[w] = 0; s_wload[w] = 0; }
+        bool fits = true;
+        for (int sl = 0; sl < sys.nslices; ++sl) {
+            const int cost = ((s_soff[sl + 1] - s_soff[sl]) >> 5) + 5;
+            int best = -1;
+            for (int w = 0; w < nwarps; ++w)
+                if (s_wcnt[w] < RMAX && (best < 0 || s_wload[w] < s_wload[best])) best = w;
+            if (best < 0) { fits = false; break; }
+            s_wsl[best * RMAX + s_wcnt[best]] = (short)sl;
+            ++s_wcnt[best];
+            s_wload[best] += cost;
+        }
+        s_wload[0] = fits ? 1 : 0;          // reused as the "assignment fits" flag
+    }
+    __syncthreads();
+    const bool assignment_ok = s_wload[0] != 0;
+    const int rows_per_lane = s_wcnt[warp];
 
     for (int o = blockIdx.x; o < run.n_orient; o += gridDim.x) {
-        if (rows_per_lane > RMAX) {                  // launch configuration error
+        if (!assignment_ok) {                        // launch configuration error
             if (tid == 0) run.status[o] = kDevTooManyRows;
             continue;
         }
@@ -564,8 +587,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         __syncthreads();
         // Gershgorin interval of the Hermitian part (real diagonal + off-diagonal)
         for (int r = 0; r < rows_per_lane; ++r) {
-            const int sl = warp + r * nwarps;
-            if (sl >= sys.nslices) break;
+            const int sl = s_wsl[warp * RMAX + r];
             const int row = sl * 32 + lane;
             if (row >= n) continue;
             const int off = s_soff[sl], w = (s_soff[sl + 1] - off) >> 5;
@@ -589,8 +611,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         double nrm2 = 0.0;
 #pragma unroll
         for (int r = 0; r < RMAX; ++r) {
-            const int row = (warp + r * nwarps) * 32 + lane;
-            const bool own = (r < rows_per_lane) && (warp + r * nwarps < sys.nslices) && row < n;
+            const int row = (r < rows_per_lane) ? s_wsl[warp * RMAX + r] * 32 + lane : n;
+            const bool own = row < n;
             const double v = own ? 1.0 + 0.37 * sin(1.7 * row + 0.3) : 0.0;
             q_cur[r] = tovec(make_double2(v, 0.0), Vec());
             q_prev[r] = vzero<Vec>();
@@ -602,8 +624,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 #pragma unroll
             for (int r = 0; r < RMAX; ++r) {
                 if (r >= rows_per_lane) break;
-                const int sl = warp + r * nwarps;
-                if (sl >= sys.nslices) break;
+                const int sl = s_wsl[warp * RMAX + r];
                 q_cur[r].x *= inv; q_cur[r].y *= inv;
                 s_xa[sl * 32 + lane] = q_cur[r];
             }
@@ -619,8 +640,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             for (int r = 0; r < RMAX; ++r) {
                 wv[r] = vzero<Vec>();
                 if (r >= rows_per_lane) continue;
-                const int sl = warp + r * nwarps;
-                if (sl >= sys.nslices) continue;
+                const int sl = s_wsl[warp * RMAX + r];
                 const int row = sl * 32 + lane;
                 if (row >= n) continue;
                 const int off = s_soff[sl], w = (s_soff[sl + 1] - off) >> 5;
@@ -655,10 +675,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 q_prev[r] = q_cur[r];
                 q_cur[r].x = wv[r].x * (Real)inv;
                 q_cur[r].y = wv[r].y * (Real)inv;
-                if (r < rows_per_lane) {
-                    const int sl = warp + r * nwarps;
-                    if (sl < sys.nslices) s_xb[sl * 32 + lane] = q_cur[r];
-                }
+                if (r < rows_per_lane) s_xb[s_wsl[warp * RMAX + r] * 32 + lane] = q_cur[r];
             }
             Vec *t = s_xa; s_xa = s_xb; s_xb = t;
             beta_prev = beta;
@@ -774,8 +791,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 #pragma unroll
         for (int r = 0; r < RMAX; ++r) {
             r_row[r] = 0; r_off[r] = 0; r_w[r] = 0;
-            const int sl = warp + r * nwarps;
-            if (r < rows_per_lane && sl < sys.nslices) {
+            if (r < rows_per_lane) {
+                const int sl = s_wsl[warp * RMAX + r];
                 nr = r + 1;
                 r_row[r] = sl * 32 + lane;
                 r_off[r] = s_soff[sl] + lane;
