@@ -403,20 +403,27 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 8;
     c.threads = nwarps * 32;
     // chunk: each orientation picks a power-of-two step count whose series
-    // argument s*M*dt is about chunk_x (kernel side); M here is the cap.
+    // argument s*M*dt is about chunk_x (kernel side); M here is the cap.  The
+    // longest target whose shared-memory layout fits one SM is used.
     c.fixed = opt.chunk_steps > 0;
-    c.chunk_x = 300.0;
-    int M = c.fixed ? opt.chunk_steps : m_cap;
-    M = (int)std::min<int64_t>(M, nsteps + 1);
-    M = std::max(M, 1);
-    c.M = M;
-    const double xu = c.fixed ? std::max(h->g_upper * M * dt, 1.0) : c.chunk_x;
     const double lg = (h->g_upper > 0) ? 2.0 * h->max_im_diag / (h->g_upper / 4.0) : 0.0;
-    int K = (int)host_series_terms(xu, std::min(lg, 0.05), c.tol) + 16;
-    if (kmax_override > 0) K = std::max(K, kmax_override);
-    c.Kmax = std::min(K, 8192);
-    c.smem = smem_for(h, f64, c.Kmax, c.M, c.threads);
-    if (c.smem > h->smem_optin)
+    const double targets[] = {300.0, 200.0, 150.0, 100.0, 60.0, 30.0};
+    bool placed = false;
+    for (double tx : targets) {
+        c.chunk_x = tx;
+        int M = c.fixed ? opt.chunk_steps : m_cap;
+        M = (int)std::min<int64_t>(M, nsteps + 1);
+        M = std::max(M, 1);
+        c.M = M;
+        const double xu = c.fixed ? std::max(h->g_upper * M * dt, 1.0) : c.chunk_x;
+        int K = (int)host_series_terms(xu, std::min(lg, 0.05), c.tol) + 16;
+        if (kmax_override > 0) K = std::max(K, kmax_override);
+        c.Kmax = std::min(K, 8192);
+        c.smem = smem_for(h, f64, c.Kmax, c.M, c.threads);
+        if (c.smem <= h->smem_optin) { placed = true; break; }
+        if (c.fixed) break;
+    }
+    if (!placed)
         throw SpxError(SPX_ERR_UNSUPPORTED, "system does not fit the shared-memory budget of one SM (" +
                                                 std::to_string(c.smem) + " bytes)");
     const void *kfn = select_kernel(f64, h->cplx, c.rmax);
