@@ -413,7 +413,7 @@ struct SmemLayout {
         diag = o; o = align(o + sizeof(typename P::Dg) * n_pad);
         xa = o; o = align(o + sizeof(typename P::Vec) * n_pad);
         xb = o; o = align(o + sizeof(typename P::Vec) * n_pad);
-        part = o; o = align(o + sizeof(typename P::Vec) * 64);
+        part = o; o = align(o + sizeof(typename P::Vec) * (size_t)Kmax * (nthreads / 32));
         atau = o; o = align(o + sizeof(typename P::Af) * Kmax);
         mu = o; o = align(o + sizeof(typename P::Vec) * Kmax);
         phase = o; o = align(o + sizeof(typename P::Vec) * (M + 1));
@@ -476,16 +476,6 @@ __device__ void bessel_column(double *table, int M, int j, int K, double half, d
     col[0] = col[0] * inv;
     for (int k = 1; k < kneed; ++k) col[k * ld] = 2.0 * col[k * ld] * inv;
     for (int k = kneed; k < K; ++k) col[k * ld] = 0.0;
-}
-
-// Moments: every warp leaves its partial of term k in part[(k&1)*32 + warp];
-// during the next term one warp (rotating over k) sums them into mu[k].
-template <class Vec>
-__device__ __forceinline__ void reduce_moment(const Vec *part, Vec *mu, int k, int warp, int lane, int nwarps) {
-    if (warp != k % nwarps) return;
-    Vec v = (lane < nwarps) ? part[(k & 1) * 32 + lane] : vzero<Vec>();
-    v = warp_sum(v);
-    if (lane == 0) mu[k] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -888,11 +878,9 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                         }
                     }
                     mom = warp_sum(mom);
-                    if (lane == 0) s_part[(k & 1) * 32 + warp] = mom;
-                    reduce_moment(s_part, s_mu, k - 1, warp, lane, nwarps);
+                    if (lane == 0) s_part[k * nwarps + warp] = mom;
                     __syncthreads();
                 }
-                reduce_moment(s_part, s_mu, K - 1, warp, lane, nwarps);
 #pragma unroll
                 for (int r = 0; r < RMAX; ++r) {
                     if (r < nr) {
@@ -988,12 +976,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     }
                     {
                         float2 m = warp_sum(f2up(MOM));
-                        if (lane == 0) s_part[(k & 1) * 32 + warp] = m;
+                        if (lane == 0) s_part[k * nwarps + warp] = m;
                     }
-                    reduce_moment(s_part, s_mu, k - 1, warp, lane, nwarps);
                     __syncthreads();
                 }
-                reduce_moment(s_part, s_mu, K - 1, warp, lane, nwarps);
 #pragma unroll
                 for (int r = 0; r < RMAX; ++r) {
                     if (r < nr) {
@@ -1003,7 +989,16 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     }
                 }
             }
-            __syncthreads();          // every moment mu_k is in s_mu
+            // moments: sum the per-warp partials of every term
+            for (int k = tid; k < K; k += blockDim.x) {
+                Vec v = vzero<Vec>();
+                for (int w2 = 0; w2 < nwarps; ++w2) {
+                    const Vec q = s_part[k * nwarps + w2];
+                    v.x += q.x; v.y += q.y;
+                }
+                s_mu[k] = v;
+            }
+            __syncthreads();
             // FID points of this chunk: f_j = ph_j * sum_k J_k(s j dt) (-i)^k mu_k
             {
                 const int parts = max(1, (int)blockDim.x / Mo);
