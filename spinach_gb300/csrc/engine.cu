@@ -396,7 +396,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     const bool f64 = opt.precision == SPX_FP64;
     c.tol = opt.series_tol > 0 ? opt.series_tol : (f64 ? 1e-16 : 1e-11);
     // warps: about four 32-row slices per lane, at most 16 warps
-    int nwarps = std::min(16, std::max(1, (2 * h->nslices + 4) / 5));   // ~2.5 slices per warp
+    int nwarps = std::min(16, std::max(1, (h->nslices + 2) / 3));       // ~3 slices per warp
     if (opt.threads > 0) nwarps = std::max(1, std::min(16, opt.threads / 32));
     const int rows = (h->nslices + nwarps - 1) / nwarps;
     if (rows > 8 || nwarps > 32) throw SpxError(SPX_ERR_UNSUPPORTED, "Liouville dimension too large for the register-resident kernel");
