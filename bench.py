@@ -204,9 +204,11 @@ def run_gpu(args):
         dist.init_process_group('gloo')
     torch.cuda.set_device(local)
     build_library()
+    from spinach_gb300.shard import combine_partial_fids, max_over_ranks, shard_grid
     w = getattr(W, args.workload)()
     L = W.build(w)
-    grid = W.zcwn_grid(w.n_orient)
+    # weak scaling: the grid grows with the ranks and each rank owns one block of it
+    grid = shard_grid(W.zcwn_grid(w.n_orient * world), rank, world)
     eng = E.Engine(local)
     eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
     prec = E.FP64 if args.precision == 'fp64' else E.FP32
@@ -216,7 +218,7 @@ def run_gpu(args):
         g = torch.tensor(np.stack(grid), dtype=torch.float64, device=dev).contiguous()
         d_fid = torch.zeros(2 * (w.nsteps + 1), dtype=torch.float64, device=dev)
         flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device=dev)
-    no = w.n_orient
+    no = grid[0].size
     ptr = [g[i].data_ptr() for i in range(4)]
 
     def step():
@@ -252,19 +254,17 @@ def run_gpu(args):
                               'kernel_ms': statistics.mean(kernel_ms), 'stats': eng.stats()}), flush=True)
         eng.close()
         return
-    t_total = sum(step_ms) / 1e3
-    if world > 1:
-        tt = torch.tensor([t_total], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt[0])
+    t_total = max_over_ranks(sum(step_ms) / 1e3)
     value = world * no * args.steps / t_total
     stats = eng.stats()
-    fid32 = d_fid.cpu().numpy().view(np.complex128).copy()
+    # the powder FID of the whole grid: rank-ordered FP64 sum of the partials
+    fid32 = combine_partial_fids(d_fid.cpu().numpy().view(np.complex128).copy())
 
     # FP64 reference on the same GPU and inputs (the plain FP64 path)
     t0 = time.perf_counter()
     r64 = eng.run(*grid, w.dt, w.nsteps, precision=E.FP64)
     fp64_s = time.perf_counter() - t0
+    r64.fid = combine_partial_fids(r64.fid)
     rel_err = float(np.linalg.norm(fid32 - r64.fid) / np.linalg.norm(r64.fid)) if prec == E.FP32 else 0.0
 
     # e2e through the C ABI with host buffers (upload + run incl. copies)
@@ -317,7 +317,7 @@ def run_gpu(args):
                                    '2048 steps of 5 us', 'fid_unit': FID_NOTE, 'l2': 'flushed between steps (256 MiB)',
                        'precision': args.precision, 'chunk_steps': stats['chunk_steps'],
                        'series_terms_max': stats['max_terms'], 'threads': stats['threads'],
-                       'parallelism': f'orientations over CTAs; {world} replica(s)'},
+                       'parallelism': f'orientations over CTAs; {world} rank(s), one grid block each'},
             'rel_err_vs_fp64_gpu': rel_err,
             'fp64_gpu': {'value': no / fp64_s, 'unit': UNIT, 'kernel_ms': r64.stats['kernel_ms']},
             'e2e': {'value': e2e, 'unit': UNIT, 'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h)},
