@@ -185,3 +185,19 @@ def build(w: Workload) -> Liouvillian:
     H = ssm.rotational_hamiltonian(ss, basis, w.assumptions, fac)
     R = sp.diags(ssm.relaxation_diagonal(ss, basis)).tocsr().astype(complex)
     return Liouvillian(H.iso, H.aniso, R, fac.state(*w.rho0), fac.state(*w.coil), basis.dim)
+
+
+def c4_small(seed: int = 4, n_protons: int = 2) -> Workload:
+    """The c4 radical cut to ``n_protons`` protons in the full basis (parity-test size)."""
+    w = c4(seed)
+    keep = 2 + n_protons
+    w.name = f'c4_small{n_protons}'
+    w.isotopes = w.isotopes[:keep]
+    w.zeeman_eigs = w.zeeman_eigs[:keep]
+    w.zeeman_euler = w.zeeman_euler[:keep]
+    w.coupling_eigs = {k: v for k, v in w.coupling_eigs.items() if max(k) < keep}
+    w.coupling_euler = {k: v for k, v in w.coupling_euler.items() if max(k) < keep}
+    w.r1, w.r2 = w.r1[:keep], w.r2[:keep]
+    w.approximation, w.level = 'none', 0
+    w.nsteps, w.n_orient = 256, 8
+    return w
