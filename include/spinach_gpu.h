@@ -158,6 +158,39 @@ spx_status spx_run_powder_noalloc(spx_handle *handle, int64_t n_orient,
                                   double dt, int64_t nsteps, int32_t precision,
                                   double *d_fid);
 
+/*
+ * Orientation surrogate (no counterpart in the reference; the features follow
+ * kernel/utilities/spher_harmon.m).  A multilayer perceptron over the
+ * (lmax+1)^2 real spherical harmonics of (beta, gamma): `layers` hidden layers
+ * of `hidden` GELU units and n_out linear outputs, FP32 master weights with
+ * BF16 copies used in every product (FP32 accumulation).  Parameters are laid
+ * out layer by layer as W (out x in, row-major) then b (out).  Every pointer
+ * named d_* is device memory of the surrogate's device; h_* is host memory.
+ */
+typedef struct spx_surrogate spx_surrogate;
+spx_status spx_surrogate_create(spx_surrogate **s, int device, int32_t lmax,
+                                int32_t hidden, int32_t layers, int32_t n_out,
+                                uint64_t seed);
+spx_status spx_surrogate_destroy(spx_surrogate *s);
+int64_t spx_surrogate_num_params(const spx_surrogate *s);
+/* n x (lmax+1)^2 features, row-major: per l, Re Y_l0 then Re/Im Y_lm, m = 1..l. */
+spx_status spx_surrogate_features(spx_surrogate *s, int64_t n, const double *d_beta,
+                                  const double *d_gamma, float *d_features);
+/* Full-batch Adam on the mean squared error against d_targets (n x n_out),
+ * cosine-decayed learning rate; h_loss_per_epoch may be NULL. */
+spx_status spx_surrogate_train(spx_surrogate *s, int64_t n, const double *d_beta,
+                               const double *d_gamma, const float *d_targets,
+                               int32_t epochs, float lr, float *h_loss_per_epoch);
+spx_status spx_surrogate_predict(spx_surrogate *s, int64_t n, const double *d_beta,
+                                 const double *d_gamma, float *d_out);
+/* One forward and backward pass: loss and the gradient of every parameter. */
+spx_status spx_surrogate_gradients(spx_surrogate *s, int64_t n, const double *d_beta,
+                                   const double *d_gamma, const float *d_targets,
+                                   float *h_grad, float *h_loss);
+spx_status spx_surrogate_get_params(spx_surrogate *s, float *h_params);
+spx_status spx_surrogate_set_params(spx_surrogate *s, const float *h_params);
+const char *spx_surrogate_last_error(const spx_surrogate *s);
+
 /* Wait for all work on the handle's stream; returns the device status. */
 spx_status spx_synchronize(spx_handle *handle);
 

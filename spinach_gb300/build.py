@@ -6,7 +6,7 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-SOURCES = [os.path.join(HERE, 'csrc', 'engine.cu')]
+SOURCES = [os.path.join(HERE, 'csrc', 'engine.cu'), os.path.join(HERE, 'csrc', 'surrogate.cu')]
 DEPS = SOURCES + [os.path.join(HERE, 'csrc', 'kernels.cuh'), os.path.join(ROOT, 'include', 'spinach_gpu.h')]
 LIB = os.path.join(HERE, 'lib', 'libspinach_gpu.so')
 NVCC_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a', '-O3', '-lineinfo', '-std=c++17',
@@ -21,12 +21,21 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
             return LIB
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     nvcc = os.environ.get('NVCC', 'nvcc')
-    cmd = [nvcc, *NVCC_FLAGS, '-I', os.path.join(ROOT, 'include'), *SOURCES, '-o', LIB + '.tmp']
-    res = subprocess.run(cmd, capture_output=True, text=True)
+    inc = ['-I', os.path.join(ROOT, 'include')]
+    objs, procs = [], []
+    for src in SOURCES:                       # translation units compile in parallel
+        obj = os.path.join(os.path.dirname(LIB), os.path.basename(src) + '.o')
+        objs.append(obj)
+        procs.append(subprocess.Popen([nvcc, *NVCC_FLAGS, '-c', *inc, src, '-o', obj],
+                                      stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
+    logs = [p.communicate()[0] for p in procs]
+    if any(p.returncode for p in procs):
+        raise RuntimeError('nvcc failed:\n' + '\n'.join(logs))
+    res = subprocess.run([nvcc, *NVCC_FLAGS, *objs, '-o', LIB + '.tmp'], capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError('nvcc failed:\n' + res.stdout + res.stderr)
+        raise RuntimeError('nvcc link failed:\n' + res.stdout + res.stderr)
     if verbose:
-        print(res.stdout + res.stderr)
+        print('\n'.join(logs) + res.stdout + res.stderr)
     os.replace(LIB + '.tmp', LIB)
     return LIB
 

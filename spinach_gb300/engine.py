@@ -56,6 +56,19 @@ SIGNATURES = {
                                         C.POINTER(SpxOptions), _P]),
     'spx_run_powder_noalloc': (C.c_int, [_P, C.c_int64, _P, _P, _P, _P, C.c_double, C.c_int64,
                                          C.c_int32, _P]),
+    'spx_surrogate_create': (C.c_int, [C.POINTER(_P), C.c_int, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                       C.c_uint64]),
+    'spx_surrogate_destroy': (C.c_int, [_P]),
+    'spx_surrogate_num_params': (C.c_int64, [_P]),
+    'spx_surrogate_features': (C.c_int, [_P, C.c_int64, _P, _P, _P]),
+    'spx_surrogate_train': (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_int32, C.c_float,
+                                      C.POINTER(C.c_float)]),
+    'spx_surrogate_predict': (C.c_int, [_P, C.c_int64, _P, _P, _P]),
+    'spx_surrogate_gradients': (C.c_int, [_P, C.c_int64, _P, _P, _P, C.POINTER(C.c_float),
+                                          C.POINTER(C.c_float)]),
+    'spx_surrogate_get_params': (C.c_int, [_P, C.POINTER(C.c_float)]),
+    'spx_surrogate_set_params': (C.c_int, [_P, C.POINTER(C.c_float)]),
+    'spx_surrogate_last_error': (C.c_char_p, [_P]),
     'spx_synchronize': (C.c_int, [_P]),
     'spx_get_stream': (_P, [_P]),
     'spx_get_stats': (C.c_int, [_P, C.POINTER(SpxStats)]),
@@ -204,3 +217,66 @@ class Engine:
         st = SpxStats()
         self._check(self.lib.spx_get_stats(self.h, C.byref(st)), self.h)
         return st.as_dict()
+
+
+class Surrogate:
+    """Device MLP over spherical-harmonic features of (beta, gamma) (spx_surrogate_*).
+
+    Device buffers are passed as raw pointers (ints), e.g. torch ``data_ptr()``."""
+
+    def __init__(self, device: int = 0, lmax: int = 12, hidden: int = 256, layers: int = 4,
+                 n_out: int = 128, seed: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        st = self.lib.spx_surrogate_create(C.byref(h), device, lmax, hidden, layers, n_out, seed)
+        if st != 0:
+            raise SpxError(st, self.lib.spx_status_string(st).decode())
+        self.h = h
+        self.lmax, self.hidden, self.layers, self.n_out = lmax, hidden, layers, n_out
+        self.n_in = (lmax + 1) ** 2
+        self.n_params = int(self.lib.spx_surrogate_num_params(h))
+
+    def _check(self, st):
+        if st != 0:
+            raise SpxError(st, f'{self.lib.spx_status_string(st).decode()}: '
+                               f'{self.lib.spx_surrogate_last_error(self.h).decode()}')
+
+    def close(self):
+        if getattr(self, 'h', None):
+            self.lib.spx_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def features(self, n, d_beta, d_gamma, d_out):
+        self._check(self.lib.spx_surrogate_features(self.h, n, d_beta, d_gamma, d_out))
+
+    def train(self, n, d_beta, d_gamma, d_targets, epochs: int, lr: float) -> np.ndarray:
+        loss = np.zeros(epochs, np.float32)
+        self._check(self.lib.spx_surrogate_train(self.h, n, d_beta, d_gamma, d_targets, epochs, lr,
+                                                 loss.ctypes.data_as(C.POINTER(C.c_float))))
+        return loss
+
+    def predict(self, n, d_beta, d_gamma, d_out):
+        self._check(self.lib.spx_surrogate_predict(self.h, n, d_beta, d_gamma, d_out))
+
+    def gradients(self, n, d_beta, d_gamma, d_targets):
+        g = np.zeros(self.n_params, np.float32)
+        loss = np.zeros(1, np.float32)
+        self._check(self.lib.spx_surrogate_gradients(self.h, n, d_beta, d_gamma, d_targets,
+                                                     g.ctypes.data_as(C.POINTER(C.c_float)),
+                                                     loss.ctypes.data_as(C.POINTER(C.c_float))))
+        return float(loss[0]), g
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, np.float32)
+        self._check(self.lib.spx_surrogate_get_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
+        return p
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        self._check(self.lib.spx_surrogate_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
