@@ -4,7 +4,8 @@ network that predicts FIDs at the orientations of a dense grid.
 Steps (all on one GPU; torch holds device buffers and runs the SVD):
   1. exact FP32 FIDs at the coarse grid (the engine's propagation kernel,
      per-orientation output as in kernel/contexts/powder.m:291-297),
-  2. complex SVD time basis of those FIDs, ``rank`` right singular vectors,
+  2. time basis: the ``rank`` leading right singular vectors of those FIDs
+     (randomised range finder on the device),
   3. the MLP of spx_surrogate_* (spherical-harmonic features of (beta, gamma),
      BF16 weights, FP32 accumulation) is trained on the GPU to map an
      orientation to the 2*rank real coefficients (centred, one global scale),
@@ -47,6 +48,27 @@ def _xyz(beta, gamma):
     return np.stack([np.sin(b) * np.cos(g), np.sin(b) * np.sin(g), np.cos(b)], 1)
 
 
+def _time_basis(F, rank: int, seed: int, oversample: int = 16, power: int = 3):
+    """Leading right singular vectors of F (n x T) by a randomised range finder
+    with power iterations (Halko, Martinsson and Tropp, SIAM Rev. 53 (2011) 217,
+    algorithms 4.4 and 5.1), on the device: a few products with F instead of a full SVD."""
+    import torch
+    n, T = F.shape
+    k = min(rank + oversample, n, T)
+    g = torch.Generator(device=F.device).manual_seed(seed)
+    Om = torch.randn(n, k, generator=g, device=F.device, dtype=torch.float32).to(F.dtype)
+    Y = F.conj().T @ Om                                  # (T, k): range of F^H
+    Q, _ = torch.linalg.qr(Y)
+    for _ in range(power):
+        Q, _ = torch.linalg.qr(F @ Q)
+        Q, _ = torch.linalg.qr(F.conj().T @ Q)
+    Bs = F @ Q                                           # (n, k) = F restricted to span(Q)
+    _, _, Wh = torch.linalg.svd(Bs, full_matrices=False)
+    V = Q @ Wh.conj().T                                  # (T, k) right singular vectors
+    r = min(rank, k)
+    return V[:, :r].conj().T.contiguous()
+
+
 class SurrogatePowder:
     """Surrogate-assisted powder FID on an uploaded engine."""
 
@@ -58,6 +80,7 @@ class SurrogatePowder:
         self.dev = torch.device('cuda', device)
         self.rank = rank
         self.net = E.Surrogate(device, lmax, hidden, layers, 2 * rank, seed)
+        self.seed = seed
 
     def run(self, coarse_grid, dense_grid, holdout_idx, dt: float, nsteps: int, epochs: int = 1500,
             lr: float = 1e-3, tol: float = 1e-5, precision: int = E.FP32) -> SurrogateResult:
@@ -75,9 +98,8 @@ class SurrogatePowder:
 
         t0 = time.perf_counter()
         F = torch.from_numpy(coarse.fids).to(self.dev, torch.complex64)
-        _, _, Vh = torch.linalg.svd(F, full_matrices=False)
-        r = min(self.rank, Vh.shape[0])
-        B = Vh[:r]                                                  # (r, nsteps+1)
+        B = _time_basis(F, self.rank, self.seed)                    # (r, nsteps+1)
+        r = B.shape[0]
         coef = F @ B.conj().T                                       # (n_coarse, r)
         T = torch.cat([coef.real, coef.imag], 1)
         if r < self.rank:
