@@ -58,7 +58,8 @@ typedef struct {
     int32_t precision;         /* spx_precision: storage/arithmetic of the propagation */
     int32_t chunk_steps;       /* time steps covered by one series expansion, 0 = auto */
     int32_t threads;           /* CTA size, 0 = auto */
-    int32_t reserved0;
+    int32_t cluster;           /* CTAs sharing one orientation (1, 2, 4, 8), 0 = auto:
+                                  the smallest whose per-CTA share of L fits shared memory */
     double series_tol;         /* truncation tolerance of the series, 0 = auto */
     double reserved1;
 } spx_options;
@@ -82,6 +83,8 @@ typedef struct {
     int64_t ell_entries;       /* padded sliced-ELL entries (off-diagonal) */
     int32_t value_streams;     /* per-non-zero value streams combined per orientation */
     int32_t real_offdiag;      /* 1 if off-diagonal Liouvillian values are real */
+    int32_t cluster;           /* CTAs that shared one orientation (thread-block cluster size) */
+    int32_t smem_bytes;        /* dynamic shared memory of each CTA */
 } spx_stats;
 
 typedef struct spx_handle spx_handle;

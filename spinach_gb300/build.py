@@ -6,8 +6,10 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-SOURCES = [os.path.join(HERE, 'csrc', 'engine.cu'), os.path.join(HERE, 'csrc', 'surrogate.cu')]
-DEPS = SOURCES + [os.path.join(HERE, 'csrc', 'kernels.cuh'), os.path.join(ROOT, 'include', 'spinach_gpu.h')]
+SOURCES = [os.path.join(HERE, 'csrc', f) for f in
+           ('engine.cu', 'surrogate.cu', 'kern_f32r.cu', 'kern_f32c.cu', 'kern_f64r.cu', 'kern_f64c.cu')]
+DEPS = SOURCES + [os.path.join(HERE, 'csrc', 'kernels.cuh'), os.path.join(HERE, 'csrc', 'kern_inst.inc'),
+                  os.path.join(ROOT, 'include', 'spinach_gpu.h')]
 LIB = os.path.join(HERE, 'lib', 'libspinach_gpu.so')
 NVCC_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a', '-O3', '-lineinfo', '-std=c++17',
               '-Xcompiler', '-fPIC', '-shared', '-diag-suppress', '550']

@@ -84,6 +84,7 @@ struct spx_handle {
     double g_upper = 0.0;      // upper bound of the spectral radius of H over all orientations
     double max_im_diag = 0.0;
     DevBuf<int> d_slice_off, d_stream_coef, d_term_rkm;
+    std::vector<int> slice_off_host;
     DevBuf<uint16_t> d_ell_col;
     DevBuf<double> d_ell_re, d_ell_im;
     DevBuf<double2> d_diag, d_rho0, d_coil;
@@ -313,6 +314,7 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
     SPX_CUDA(cudaSetDevice(h->device));
     h->have_system = false;
     h->d_slice_off.upload(slice_off, h->stream);
+    h->slice_off_host = slice_off;
     h->d_ell_col.upload(ell_col, h->stream);
     h->d_ell_re.upload(ell_re, h->stream);
     if (cplx) h->d_ell_im.upload(ell_im, h->stream); else h->d_ell_im.release();
@@ -344,6 +346,9 @@ struct Config {
     double chunk_x;
     size_t smem;
     double tol;
+    int cl = 1;                                   // CTAs per cluster
+    int slices[spx::kMaxCluster + 1] = {};        // row blocks of the cluster's CTAs
+    int nsl_loc = 0, ell_loc = 0;                 // largest block (slices, ELL entries)
 };
 
 double host_series_terms(double x, double lg, double tol) {
@@ -359,80 +364,164 @@ double host_series_terms(double x, double lg, double tol) {
 }
 
 template <bool F64, bool CPLX>
-size_t smem_bytes(const spx_handle *h, int Kmax, int M, int threads) {
-    spx::SmemLayout<F64, CPLX> L(h->n_pad, h->nslices, h->ell_len, Kmax, M, threads);
+size_t smem_bytes(const spx_handle *h, int nsl_loc, int ell_loc, int Kmax, int M, int threads) {
+    spx::SmemLayout<F64, CPLX> L(h->n_pad, nsl_loc, ell_loc, Kmax, M, threads);
     return L.total;
 }
 
-size_t smem_for(const spx_handle *h, bool f64, int Kmax, int M, int threads) {
-    if (f64) return h->cplx ? smem_bytes<true, true>(h, Kmax, M, threads) : smem_bytes<true, false>(h, Kmax, M, threads);
-    return h->cplx ? smem_bytes<false, true>(h, Kmax, M, threads) : smem_bytes<false, false>(h, Kmax, M, threads);
+size_t smem_for(const spx_handle *h, bool f64, int nsl_loc, int ell_loc, int Kmax, int M, int threads) {
+    if (f64)
+        return h->cplx ? smem_bytes<true, true>(h, nsl_loc, ell_loc, Kmax, M, threads)
+                       : smem_bytes<true, false>(h, nsl_loc, ell_loc, Kmax, M, threads);
+    return h->cplx ? smem_bytes<false, true>(h, nsl_loc, ell_loc, Kmax, M, threads)
+                   : smem_bytes<false, false>(h, nsl_loc, ell_loc, Kmax, M, threads);
 }
 
-template <bool F64, bool CPLX, int RMAX>
-const void *kernel_ptr() {
-    return reinterpret_cast<const void *>(&spx::powder_chebyshev_kernel<F64, CPLX, RMAX>);
+}  // namespace
+// Kernel addresses from the translation units that instantiate them
+// (kern_f32r.cu, kern_f32c.cu, kern_f64r.cu, kern_f64c.cu).
+const void *spx_kernel_f32r(int rmax, bool cluster);
+const void *spx_kernel_f32c(int rmax, bool cluster);
+const void *spx_kernel_f64r(int rmax, bool cluster);
+const void *spx_kernel_f64c(int rmax, bool cluster);
+namespace {
+
+// Single-CTA kernels for RMAX 1, 2, 4, 8; cluster kernels for RMAX 1, 2, 4.
+const void *select_kernel(bool f64, bool cplx, int rmax, bool clu) {
+    if (f64) return cplx ? spx_kernel_f64c(rmax, clu) : spx_kernel_f64r(rmax, clu);
+    return cplx ? spx_kernel_f32c(rmax, clu) : spx_kernel_f32r(rmax, clu);
 }
 
-const void *select_kernel(bool f64, bool cplx, int rmax) {
-#define SPX_SEL(F, C)                                  \
-    switch (rmax) {                                    \
-        case 1: return kernel_ptr<F, C, 1>();          \
-        case 2: return kernel_ptr<F, C, 2>();          \
-        case 4: return kernel_ptr<F, C, 4>();          \
-        default: return kernel_ptr<F, C, 8>();         \
+// Split the slices into cl contiguous blocks of about equal cost (ELL entries
+// plus a per-row share); returns false if cl exceeds the slice count.
+bool partition_slices(const spx_handle *h, int cl, Config &c) {
+    if (cl > h->nslices) return false;
+    const std::vector<int> &off = h->slice_off_host;
+    auto cost = [&](int sl) { return (double)(off[sl + 1] - off[sl]) + 32.0 * 4; };
+    double total = 0;
+    for (int sl = 0; sl < h->nslices; ++sl) total += cost(sl);
+    c.cl = cl;
+    c.slices[0] = 0;
+    double acc = 0;
+    int r = 1;
+    for (int sl = 0; sl < h->nslices && r < cl; ++sl) {
+        acc += cost(sl);
+        // cut once the running cost reaches r/cl of the total, leaving a slice for every later block
+        if (acc >= total * r / cl || h->nslices - (sl + 1) == cl - r) c.slices[r++] = sl + 1;
     }
-    if (f64) {
-        if (cplx) { SPX_SEL(true, true) } else { SPX_SEL(true, false) }
-    } else {
-        if (cplx) { SPX_SEL(false, true) } else { SPX_SEL(false, false) }
+    c.slices[cl] = h->nslices;
+    c.nsl_loc = 0;
+    c.ell_loc = 0;
+    for (int j = 0; j < cl; ++j) {
+        if (c.slices[j + 1] <= c.slices[j]) return false;
+        c.nsl_loc = std::max(c.nsl_loc, c.slices[j + 1] - c.slices[j]);
+        c.ell_loc = std::max(c.ell_loc, off[c.slices[j + 1]] - off[c.slices[j]]);
     }
-#undef SPX_SEL
+    return true;
 }
 
 Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps, const spx_options &opt,
                      int kmax_override, int m_cap = 256) {
     Config c{};
     const bool f64 = opt.precision == SPX_FP64;
+    if (opt.cluster != 0 && opt.cluster != 1 && opt.cluster != 2 && opt.cluster != 4 && opt.cluster != 8)
+        throw SpxError(SPX_ERR_INVALID_ARGUMENT, "cluster must be 0 (auto), 1, 2, 4 or 8");
     c.tol = opt.series_tol > 0 ? opt.series_tol : (f64 ? 1e-16 : 1e-11);
-    // warps: about four 32-row slices per lane, at most 16 warps
-    int nwarps = std::min(16, std::max(1, (h->nslices + 2) / 3));       // ~3 slices per warp
-    if (opt.threads > 0) nwarps = std::max(1, std::min(16, opt.threads / 32));
-    const int rows = (h->nslices + nwarps - 1) / nwarps;
-    if (rows > 8 || nwarps > 32) throw SpxError(SPX_ERR_UNSUPPORTED, "Liouville dimension too large for the register-resident kernel");
-    c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 8;
-    c.threads = nwarps * 32;
     // chunk: each orientation picks a power-of-two step count whose series
     // argument s*M*dt is about chunk_x (kernel side); M here is the cap.  The
-    // longest target whose shared-memory layout fits one SM is used.
+    // first layout that fits one SM's shared memory is used: one CTA per
+    // orientation with the longest chunk target, else clusters of 2, 4, 8 CTAs
+    // sharing an orientation (rows split between them).
     c.fixed = opt.chunk_steps > 0;
     const double lg = (h->g_upper > 0) ? 2.0 * h->max_im_diag / (h->g_upper / 4.0) : 0.0;
     const double targets[] = {300.0, 200.0, 150.0, 100.0, 60.0, 30.0};
     bool placed = false;
-    for (double tx : targets) {
-        c.chunk_x = tx;
-        int M = c.fixed ? opt.chunk_steps : m_cap;
-        M = (int)std::min<int64_t>(M, nsteps + 1);
-        M = std::max(M, 1);
-        c.M = M;
-        const double xu = c.fixed ? std::max(h->g_upper * M * dt, 1.0) : c.chunk_x;
-        int K = (int)host_series_terms(xu, std::min(lg, 0.05), c.tol) + 16;
-        if (kmax_override > 0) K = std::max(K, kmax_override);
-        c.Kmax = std::min(K, 8192);
-        c.smem = smem_for(h, f64, c.Kmax, c.M, c.threads);
-        if (c.smem <= h->smem_optin) { placed = true; break; }
-        if (c.fixed) break;
+    const int cls[] = {1, 2, 4, 8};
+    for (int cl : cls) {
+        if (opt.cluster > 0 && cl != opt.cluster) continue;       // cluster size set by the caller
+        if (!partition_slices(h, cl, c)) continue;
+        // warps: about three 32-row slices per warp, at most 16 warps
+        int nwarps = std::min(16, std::max(1, (c.nsl_loc + 2) / 3));
+        if (opt.threads > 0) nwarps = std::max(1, std::min(16, opt.threads / 32));
+        const int rows = (c.nsl_loc + nwarps - 1) / nwarps;
+        if (rows > (cl > 1 ? 4 : 8)) continue;
+        c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 8;
+        c.threads = nwarps * 32;
+        // dynamic shared memory may use what the kernel's static arrays leave
+        cudaFuncAttributes fa{};
+        SPX_CUDA(cudaFuncGetAttributes(&fa, select_kernel(f64, h->cplx, c.rmax, cl > 1)));
+        const size_t budget = h->smem_optin > fa.sharedSizeBytes ? h->smem_optin - fa.sharedSizeBytes : 0;
+        for (double tx : targets) {
+            c.chunk_x = tx;
+            int M = c.fixed ? opt.chunk_steps : m_cap;
+            M = (int)std::min<int64_t>(M, nsteps + 1);
+            M = std::max(M, 1);
+            c.M = M;
+            const double xu = c.fixed ? std::max(h->g_upper * M * dt, 1.0) : c.chunk_x;
+            int K = (int)host_series_terms(xu, std::min(lg, 0.05), c.tol) + 16;
+            if (kmax_override > 0) K = std::max(K, kmax_override);
+            c.Kmax = std::min(K, 8192);
+            c.smem = smem_for(h, f64, c.nsl_loc, c.ell_loc, c.Kmax, c.M, c.threads);
+            if (c.smem <= budget) { placed = true; break; }
+            if (c.fixed) break;
+        }
+        if (placed) break;
     }
     if (!placed)
-        throw SpxError(SPX_ERR_UNSUPPORTED, "system does not fit the shared-memory budget of one SM (" +
-                                                std::to_string(c.smem) + " bytes)");
-    const void *kfn = select_kernel(f64, h->cplx, c.rmax);
+        throw SpxError(SPX_ERR_UNSUPPORTED, "system does not fit the shared memory of a cluster of 8 SMs (" +
+                                                std::to_string(c.smem) + " bytes per SM)");
+    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1);
     SPX_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem));
-    int per_sm = 0;
-    SPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, c.threads, c.smem));
-    per_sm = std::max(per_sm, 1);
-    c.grid = (int)std::min<int64_t>(n_orient, (int64_t)h->sm_count * per_sm);
+    if (c.cl == 1) {
+        int per_sm = 0;
+        SPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, c.threads, c.smem));
+        per_sm = std::max(per_sm, 1);
+        c.grid = (int)std::min<int64_t>(n_orient, (int64_t)h->sm_count * per_sm);
+    } else {
+        cudaLaunchConfig_t lc{};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)c.cl;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        lc.gridDim = dim3((unsigned)(c.cl * h->sm_count));
+        lc.blockDim = dim3((unsigned)c.threads);
+        lc.dynamicSmemBytes = c.smem;
+        lc.attrs = at;
+        lc.numAttrs = 1;
+        int nclusters = 0;
+        SPX_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, kfn, &lc));
+        if (nclusters < 1) throw SpxError(SPX_ERR_UNSUPPORTED, "no cluster of " + std::to_string(c.cl) + " CTAs fits");
+        c.grid = (int)std::min<int64_t>(n_orient, nclusters) * c.cl;
+    }
     return c;
+}
+
+// Launch the propagation kernel (plain or cluster launch) on the handle's stream.
+void launch_chebyshev(spx_handle *h, bool f64, const Config &c, spx::DevSystem &sys, spx::DevRun &run) {
+    run.cl = c.cl;
+    run.nsl_loc = c.nsl_loc;
+    run.ell_loc = c.ell_loc;
+    for (int j = 0; j <= spx::kMaxCluster; ++j) run.cl_slices[j] = j <= c.cl ? c.slices[j] : 0;
+    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1);
+    void *args[] = {&sys, &run};
+    if (c.cl == 1) {
+        SPX_CUDA(cudaLaunchKernel(kfn, dim3(c.grid), dim3(c.threads), args, c.smem, h->stream));
+        return;
+    }
+    cudaLaunchConfig_t lc{};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)c.cl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    lc.gridDim = dim3((unsigned)c.grid);
+    lc.blockDim = dim3((unsigned)c.threads);
+    lc.dynamicSmemBytes = c.smem;
+    lc.stream = h->stream;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    SPX_CUDA(cudaLaunchKernelExC(&lc, kfn, args));
 }
 
 void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be,
@@ -465,10 +554,8 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     run.kused = h->d_kused.p;
     run.mused = h->d_mused.p;
 
-    const void *kfn = select_kernel(f64, h->cplx, c.rmax);
-    void *args[] = {&sys, &run};
     SPX_CUDA(cudaEventRecord(h->ev[0], h->stream));
-    SPX_CUDA(cudaLaunchKernel(kfn, dim3(c.grid), dim3(c.threads), args, c.smem, h->stream));
+    launch_chebyshev(h, f64, c, sys, run);
     SPX_CUDA(cudaEventRecord(h->ev[1], h->stream));
     // deterministic FP64 powder sum: fixed groups of orientations, fixed order
     const int group = 64;
@@ -498,6 +585,8 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     h->stats.ell_entries = h->ell_len;
     h->stats.value_streams = h->nstreams;
     h->stats.real_offdiag = h->cplx ? 0 : 1;
+    h->stats.cluster = c.cl;
+    h->stats.smem_bytes = (int32_t)c.smem;
     h->stats_pending = true;
     h->last_norient = n_orient;
 }
@@ -671,9 +760,7 @@ void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, con
     double2 *part = reinterpret_cast<double2 *>(base + offs[2]);
     // the only value that must start at zero is the failure flag
     SPX_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
-    const void *kfn = select_kernel(f64, h->cplx, c.rmax);
-    void *args[] = {&sys, &run};
-    SPX_CUDA(cudaLaunchKernel(kfn, dim3(c.grid), dim3(c.threads), args, c.smem, h->stream));
+    launch_chebyshev(h, f64, c, sys, run);
     const dim3 pb(256), pg((unsigned)((npts + 255) / 256), (unsigned)ngroups);
     if (f64)
         spx::powder_partial_kernel<double2><<<pg, pb, 0, h->stream>>>(

@@ -38,6 +38,7 @@ namespace spx {
 constexpr int kMaxCoef = 128;     // 1 + 2 * (number of rotational-basis terms)
 constexpr int kMaxLanczos = 48;
 constexpr int kRedSlots = 64;
+constexpr int kMaxCluster = 8;    // portable cluster size
 
 enum DeviceStatus : int {
     kDevOk = 0,
@@ -66,57 +67,57 @@ template <> struct Prec<false, true>  { using Vec = float2;  using Val = PackC; 
 template <> struct Prec<true, false>  { using Vec = double2; using Val = double;  using Dg = double2; using Af = double2; using Real = double; using Acc = double2; };
 template <> struct Prec<true, true>   { using Vec = double2; using Val = double2; using Dg = double2; using Af = double2; using Real = double; using Acc = double2; };
 
-__device__ __forceinline__ void split(double v, float &hi, float &lo) {
+static __device__ __forceinline__ void split(double v, float &hi, float &lo) {
     hi = (float)v;
     lo = (float)(v - (double)hi);
 }
-__device__ __forceinline__ void pack(PackR &o, double re, double) {
+static __device__ __forceinline__ void pack(PackR &o, double re, double) {
     float h, l;
     split(re, h, l);
     o.v = make_float4(h, h, l, l);
 }
-__device__ __forceinline__ void pack(PackC &o, double re, double im) {
+static __device__ __forceinline__ void pack(PackC &o, double re, double im) {
     float rh, rl, ih, il;
     split(re, rh, rl);
     split(im, ih, il);
     o.h = make_float4(rh, rh, -ih, ih);
     o.l = make_float4(rl, rl, -il, il);
 }
-__device__ __forceinline__ void pack(PackD &o, double re, double im) {
+static __device__ __forceinline__ void pack(PackD &o, double re, double im) {
     float rh, rl;
     split(re, rh, rl);
     const float fi = (float)im;
     o.h = make_float4(rh, rh, -fi, fi);
     o.l = make_float4(rl, rl, 0.f, 0.f);
 }
-__device__ __forceinline__ double2 unpack(const PackR &v) { return make_double2((double)v.v.x + (double)v.v.z, 0.0); }
-__device__ __forceinline__ double2 unpack(const PackC &v) {
+static __device__ __forceinline__ double2 unpack(const PackR &v) { return make_double2((double)v.v.x + (double)v.v.z, 0.0); }
+static __device__ __forceinline__ double2 unpack(const PackC &v) {
     return make_double2((double)v.h.x + (double)v.l.x, (double)v.h.w + (double)v.l.w);
 }
-__device__ __forceinline__ double2 unpack(const PackD &v) { return make_double2((double)v.h.x + (double)v.l.x, (double)v.h.w); }
-__device__ __forceinline__ void pack(double &o, double re, double) { o = re; }
-__device__ __forceinline__ void pack(double2 &o, double re, double im) { o = make_double2(re, im); }
+static __device__ __forceinline__ double2 unpack(const PackD &v) { return make_double2((double)v.h.x + (double)v.l.x, (double)v.h.w); }
+static __device__ __forceinline__ void pack(double &o, double re, double) { o = re; }
+static __device__ __forceinline__ void pack(double2 &o, double re, double im) { o = make_double2(re, im); }
 
-__device__ __forceinline__ double2 unpack(const double &v) { return make_double2(v, 0.0); }
-__device__ __forceinline__ double2 unpack(const double2 &v) { return v; }
+static __device__ __forceinline__ double2 unpack(const double &v) { return make_double2(v, 0.0); }
+static __device__ __forceinline__ double2 unpack(const double2 &v) { return v; }
 
 // y += v * x  (value times complex state; plain arithmetic, used outside the
 // propagation loop and in the FP64 path)
-__device__ __forceinline__ void mac(float2 &y, const PackR &v, const float2 x) {
+static __device__ __forceinline__ void mac(float2 &y, const PackR &v, const float2 x) {
     y.x = fmaf(v.v.x, x.x, y.x); y.y = fmaf(v.v.x, x.y, y.y);
     y.x = fmaf(v.v.z, x.x, y.x); y.y = fmaf(v.v.z, x.y, y.y);
 }
-__device__ __forceinline__ void mac(float2 &y, const PackC &v, const float2 x) {
+static __device__ __forceinline__ void mac(float2 &y, const PackC &v, const float2 x) {
     // h = (re, re, -im, im): re*x + (-im*x.y, im*x.x)
     y.x = fmaf(v.h.x, x.x, y.x); y.y = fmaf(v.h.y, x.y, y.y);
     y.x = fmaf(v.h.z, x.y, y.x); y.y = fmaf(v.h.w, x.x, y.y);
     y.x = fmaf(v.l.x, x.x, y.x); y.y = fmaf(v.l.y, x.y, y.y);
     y.x = fmaf(v.l.z, x.y, y.x); y.y = fmaf(v.l.w, x.x, y.y);
 }
-__device__ __forceinline__ void mac(double2 &y, const double &v, const double2 x) {
+static __device__ __forceinline__ void mac(double2 &y, const double &v, const double2 x) {
     y.x = fma(v, x.x, y.x); y.y = fma(v, x.y, y.y);
 }
-__device__ __forceinline__ void mac(double2 &y, const double2 &v, const double2 x) {
+static __device__ __forceinline__ void mac(double2 &y, const double2 &v, const double2 x) {
     y.x = fma(v.x, x.x, y.x); y.x = fma(-v.y, x.y, y.x);
     y.y = fma(v.x, x.y, y.y); y.y = fma(v.y, x.x, y.y);
 }
@@ -125,17 +126,17 @@ template <class V> __device__ __forceinline__ V vzero();
 template <> __device__ __forceinline__ float2 vzero<float2>() { return make_float2(0.f, 0.f); }
 template <> __device__ __forceinline__ double2 vzero<double2>() { return make_double2(0.0, 0.0); }
 
-__device__ __forceinline__ float2 tovec(double2 a, float2) { return make_float2((float)a.x, (float)a.y); }
-__device__ __forceinline__ double2 tovec(double2 a, double2) { return a; }
-__device__ __forceinline__ double2 tod(float2 a) { return make_double2(a.x, a.y); }
-__device__ __forceinline__ double2 tod(double2 a) { return a; }
+static __device__ __forceinline__ float2 tovec(double2 a, float2) { return make_float2((float)a.x, (float)a.y); }
+static __device__ __forceinline__ double2 tovec(double2 a, double2) { return a; }
+static __device__ __forceinline__ double2 tod(float2 a) { return make_double2(a.x, a.y); }
+static __device__ __forceinline__ double2 tod(double2 a) { return a; }
 
 // conj(a) * b accumulated
-__device__ __forceinline__ void cdot_acc(float2 &s, const float2 a, const float2 b) {
+static __device__ __forceinline__ void cdot_acc(float2 &s, const float2 a, const float2 b) {
     s.x = fmaf(a.x, b.x, s.x); s.x = fmaf(a.y, b.y, s.x);
     s.y = fmaf(a.x, b.y, s.y); s.y = fmaf(-a.y, b.x, s.y);
 }
-__device__ __forceinline__ void cdot_acc(double2 &s, const double2 a, const double2 b) {
+static __device__ __forceinline__ void cdot_acc(double2 &s, const double2 a, const double2 b) {
     s.x = fma(a.x, b.x, s.x); s.x = fma(a.y, b.y, s.x);
     s.y = fma(a.x, b.y, s.y); s.y = fma(-a.y, b.x, s.y);
 }
@@ -148,17 +149,17 @@ template <class V> __device__ __forceinline__ V warp_sum(V v) {
     }
     return v;
 }
-__device__ __forceinline__ double warp_sum_d(double v) {
+static __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
-__device__ __forceinline__ double warp_max_d(double v) {
+static __device__ __forceinline__ double warp_max_d(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
-__device__ __forceinline__ double warp_min_d(double v) {
+static __device__ __forceinline__ double warp_min_d(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
@@ -171,30 +172,30 @@ __device__ __forceinline__ double warp_min_d(double v) {
 // ---------------------------------------------------------------------------
 typedef unsigned long long f2x;
 
-__device__ __forceinline__ f2x f2pk(float a, float b) {
+static __device__ __forceinline__ f2x f2pk(float a, float b) {
     f2x r;
     asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
     return r;
 }
-__device__ __forceinline__ float2 f2up(f2x v) {
+static __device__ __forceinline__ float2 f2up(f2x v) {
     float2 r;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
     return r;
 }
-__device__ __forceinline__ f2x add2(f2x a, f2x b) { f2x r; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
-__device__ __forceinline__ f2x sub2(f2x a, f2x b) { f2x r; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
-__device__ __forceinline__ f2x mul2(f2x a, f2x b) { f2x r; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
-__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+static __device__ __forceinline__ f2x add2(f2x a, f2x b) { f2x r; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
+static __device__ __forceinline__ f2x sub2(f2x a, f2x b) { f2x r; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
+static __device__ __forceinline__ f2x mul2(f2x a, f2x b) { f2x r; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
+static __device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
     f2x r;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
     return r;
 }
-__device__ __forceinline__ f2x swap2(f2x a) { const float2 f = f2up(a); return f2pk(f.y, f.x); }
-__device__ __forceinline__ f2x lo2(const float4 &v) { return f2pk(v.x, v.y); }
-__device__ __forceinline__ f2x hi2(const float4 &v) { return f2pk(v.z, v.w); }
+static __device__ __forceinline__ f2x swap2(f2x a) { const float2 f = f2up(a); return f2pk(f.y, f.x); }
+static __device__ __forceinline__ f2x lo2(const float4 &v) { return f2pk(v.x, v.y); }
+static __device__ __forceinline__ f2x hi2(const float4 &v) { return f2pk(v.z, v.w); }
 
 // Y + Z += P with Y the running sum and Z collecting its rounding errors (TwoSum)
-__device__ __forceinline__ void two_sum2(f2x &Y, f2x &Z, f2x P) {
+static __device__ __forceinline__ void two_sum2(f2x &Y, f2x &Z, f2x P) {
     const f2x S = add2(Y, P);
     const f2x B = sub2(S, Y);
     const f2x E = add2(sub2(Y, sub2(S, B)), sub2(P, B));
@@ -202,7 +203,7 @@ __device__ __forceinline__ void two_sum2(f2x &Y, f2x &Z, f2x P) {
     Z = add2(Z, E);
 }
 // a * t for a packed complex coefficient (PackC/PackA layout), hi and lo parts
-__device__ __forceinline__ f2x cmul_pk(const PackC &a, f2x T) {
+static __device__ __forceinline__ f2x cmul_pk(const PackC &a, f2x T) {
     const f2x TS = swap2(T);
     f2x P = mul2(lo2(a.h), T);
     P = fma2(hi2(a.h), TS, P);
@@ -211,15 +212,15 @@ __device__ __forceinline__ f2x cmul_pk(const PackC &a, f2x T) {
 }
 
 // FP64 helpers of the generic propagation loop
-__device__ __forceinline__ void cmac(double2 &y, const double &v, const double2 x) { mac(y, v, x); }
-__device__ __forceinline__ void cmac(double2 &y, const double2 &v, const double2 x) { mac(y, v, x); }
-__device__ __forceinline__ double2 recur(const double2 &y, double two, const double2 tp) {
+static __device__ __forceinline__ void cmac(double2 &y, const double &v, const double2 x) { mac(y, v, x); }
+static __device__ __forceinline__ void cmac(double2 &y, const double2 &v, const double2 x) { mac(y, v, x); }
+static __device__ __forceinline__ double2 recur(const double2 &y, double two, const double2 tp) {
     return make_double2(two * y.x - tp.x, two * y.y - tp.y);
 }
 
 // Block-wide reductions through a shared scratch of kRedSlots doubles.
 // Every thread of the block must call them (they contain __syncthreads).
-__device__ double block_sum(double v, double *red) {
+static __device__ double block_sum(double v, double *red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     v = warp_sum_d(v);
     __syncthreads();
@@ -229,7 +230,7 @@ __device__ double block_sum(double v, double *red) {
     for (int w = 0; w < nw; ++w) r += red[w];
     return r;
 }
-__device__ double block_max(double v, double *red) {
+static __device__ double block_max(double v, double *red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     v = warp_max_d(v);
     __syncthreads();
@@ -239,7 +240,7 @@ __device__ double block_max(double v, double *red) {
     for (int w = 0; w < nw; ++w) r = fmax(r, red[w]);
     return r;
 }
-__device__ double block_min(double v, double *red) {
+static __device__ double block_min(double v, double *red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     v = warp_min_d(v);
     __syncthreads();
@@ -248,6 +249,88 @@ __device__ double block_min(double v, double *red) {
     double r = CUDART_INF;
     for (int w = 0; w < nw; ++w) r = fmin(r, red[w]);
     return r;
+}
+
+// ---------------------------------------------------------------------------
+// Thread-block clusters (distributed shared memory).  A cluster of CL CTAs
+// shares one orientation: each CTA owns a contiguous block of 32-row slices,
+// keeps a full replica of the Chebyshev vectors and pushes the rows it
+// computes into every peer's replica; hardware cluster barriers order the
+// pushes before the next product reads them.
+// ---------------------------------------------------------------------------
+static __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+static __device__ __forceinline__ int cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return (int)r;
+}
+static __device__ __forceinline__ uint32_t cluster_addr(uint32_t local, int rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
+}
+static __device__ __forceinline__ void st_cluster(uint32_t a, unsigned long long v) {
+    asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(a), "l"(v) : "memory");
+}
+static __device__ __forceinline__ void st_cluster(uint32_t a, double v) {
+    asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+static __device__ __forceinline__ double ld_cluster_f64(uint32_t a) {
+    double v;
+    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a) : "memory");
+    return v;
+}
+static __device__ __forceinline__ int ld_cluster_s32(uint32_t a) {
+    int v;
+    asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
+}
+// all threads of all CTAs of the cluster; release/acquire orders shared::cluster stores
+template <bool CLU> __device__ __forceinline__ void csync() {
+    if constexpr (!CLU) {
+        __syncthreads();
+    } else {
+        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    }
+}
+// write v at the same shared-memory location of every other CTA of the cluster
+template <bool CLU> __device__ __forceinline__ void push_peers(const void *p, unsigned long long v, int crank, int cl) {
+    if constexpr (CLU) {
+        const uint32_t a = smem_u32(p);
+        for (int j = 0; j < cl; ++j)
+            if (j != crank) st_cluster(cluster_addr(a, j), v);
+    }
+}
+template <bool CLU> __device__ __forceinline__ void push_peers(const float2 *p, float2 v, int crank, int cl) {
+    if constexpr (CLU)
+        push_peers<CLU>((const void *)p,
+                        ((unsigned long long)__float_as_uint(v.y) << 32) | (unsigned long long)__float_as_uint(v.x),
+                        crank, cl);
+}
+template <bool CLU> __device__ __forceinline__ void push_peers(const double2 *p, double2 v, int crank, int cl) {
+    if constexpr (CLU) {
+        push_peers<CLU>((const void *)p, (unsigned long long)__double_as_longlong(v.x), crank, cl);
+        push_peers<CLU>((const void *)(reinterpret_cast<const double *>(p) + 1),
+                        (unsigned long long)__double_as_longlong(v.y), crank, cl);
+    }
+}
+// Block reduction followed by a cluster-wide one (op 0 sum, 1 max, 2 min).
+// Partial results go to a double-buffered slot array in every CTA; all CTAs
+// combine them in rank order, so every CTA gets bit-identical results.
+template <bool CLU, int OP>
+__device__ double cluster_reduce(double v, double *red, double *cred, int &par, int crank, int cl) {
+    const double b = OP == 0 ? block_sum(v, red) : OP == 1 ? block_max(v, red) : block_min(v, red);
+    if constexpr (!CLU) {
+        return b;
+    } else {
+        double *slot = cred + par * kMaxCluster;
+        par ^= 1;
+        if ((int)threadIdx.x < cl) st_cluster(cluster_addr(smem_u32(slot + crank), (int)threadIdx.x), b);
+        csync<CLU>();
+        double r = slot[0];
+        for (int j = 1; j < cl; ++j) r = OP == 0 ? r + slot[j] : OP == 1 ? fmax(r, slot[j]) : fmin(r, slot[j]);
+        return r;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -292,13 +375,17 @@ struct DevRun {
     double *halfwidth;  // n_orient
     int *kused;         // n_orient
     int *mused;         // n_orient: time steps per chunk used
+    int cl;                 // CTAs per cluster (1: no cluster)
+    int cl_slices[kMaxCluster + 1];   // slice boundaries of the CTAs' row blocks (cluster launches)
+    int nsl_loc;            // largest slice count of one CTA (shared-memory sizing)
+    int ell_loc;            // largest ELL entry count of one CTA
 };
 
 // ---------------------------------------------------------------------------
 // Wigner D (Brink & Satchler convention, rows/cols from +l to -l), FP64.
 // Written from the closed forms d^1 and d^2 of the small-d matrices.
 // ---------------------------------------------------------------------------
-__device__ void wigner_element(int rank, int k, int m, double a, double b, double g,
+static __device__ void wigner_element(int rank, int k, int m, double a, double b, double g,
                                double &re, double &im) {
     // projections: row k -> p = rank - k, column m -> q = rank - m
     const int p = rank - k, q = rank - m;
@@ -329,7 +416,7 @@ __device__ void wigner_element(int rank, int k, int m, double a, double b, doubl
 }
 
 // Extreme eigenvalues of a symmetric tridiagonal matrix by Sturm bisection.
-__device__ int sturm_count(const double *al, const double *be, int m, double x) {
+static __device__ int sturm_count(const double *al, const double *be, int m, double x) {
     int cnt = 0;
     double q = al[0] - x;
     if (q < 0) ++cnt;
@@ -340,7 +427,7 @@ __device__ int sturm_count(const double *al, const double *be, int m, double x) 
     }
     return cnt;
 }
-__device__ void tridiag_extremes(const double *al, const double *be, int m, double &lo, double &hi) {
+static __device__ void tridiag_extremes(const double *al, const double *be, int m, double &lo, double &hi) {
     double glo = CUDART_INF, ghi = -CUDART_INF;
     for (int i = 0; i < m; ++i) {
         double r = 0.0;
@@ -365,7 +452,7 @@ __device__ void tridiag_extremes(const double *al, const double *be, int m, doub
 
 // |last component| of the normalised eigenvector of the tridiagonal matrix for
 // eigenvalue theta, by three steps of inverse iteration (Thomas algorithm).
-__device__ double ritz_last_component(const double *al, const double *be, int m, double theta) {
+static __device__ double ritz_last_component(const double *al, const double *be, int m, double theta) {
     if (m <= 1) return 1.0;
     double y[kMaxLanczos], c[kMaxLanczos], d[kMaxLanczos];
     const double shift = theta + 1e-10 * (fabs(theta) + 1e-300);
@@ -399,21 +486,24 @@ __device__ double ritz_last_component(const double *al, const double *be, int m,
 template <bool F64, bool CPLX>
 struct SmemLayout {
     using P = Prec<F64, CPLX>;
-    size_t coef, red, alpha, beta, slice_off, ell_col, ell_val, diag, xa, xb, part, atau, mu, phase, rec, total;
+    size_t coef, red, cred, alpha, beta, slice_off, ell_col, ell_val, diag, xa, xb, part, atau, mu, phase, rec, total;
     __host__ __device__ static size_t align(size_t x) { return (x + 15) & ~size_t(15); }
+    // n_pad: replicated vector length; nslices / ell_len: the slices and ELL
+    // entries one CTA owns (all of them without a cluster)
     __host__ __device__ SmemLayout(int n_pad, int nslices, int ell_len, int Kmax, int M, int nthreads) {
         size_t o = 0;
         coef = o; o = align(o + sizeof(double) * kMaxCoef);
         red = o; o = align(o + sizeof(double) * kRedSlots);
+        cred = o; o = align(o + sizeof(double) * 2 * kMaxCluster);
         alpha = o; o = align(o + sizeof(double) * kMaxLanczos);
         beta = o; o = align(o + sizeof(double) * kMaxLanczos);
         slice_off = o; o = align(o + sizeof(int) * (nslices + 1));
         ell_col = o; o = align(o + sizeof(uint16_t) * ell_len);
         ell_val = o; o = align(o + sizeof(typename P::Val) * ell_len);
-        diag = o; o = align(o + sizeof(typename P::Dg) * n_pad);
+        diag = o; o = align(o + sizeof(typename P::Dg) * 32 * (size_t)nslices);
         xa = o; o = align(o + sizeof(typename P::Vec) * n_pad);
         xb = o; o = align(o + sizeof(typename P::Vec) * n_pad);
-        part = o; o = align(o + sizeof(typename P::Vec) * (size_t)Kmax * (nthreads / 32));
+        part = o; o = align(o + sizeof(typename P::Vec) * 2 * (nthreads / 32));   // two terms in flight
         atau = o; o = align(o + sizeof(typename P::Af) * Kmax);
         mu = o; o = align(o + sizeof(typename P::Vec) * Kmax);
         phase = o; o = align(o + sizeof(typename P::Vec) * (M + 1));
@@ -423,11 +513,11 @@ struct SmemLayout {
 };
 
 // acc += a * t (FP64 propagation loop)
-__device__ __forceinline__ void acc_add64(double2 &acc, const double2 &a, const double2 t) { mac(acc, a, t); }
+static __device__ __forceinline__ void acc_add64(double2 &acc, const double2 &a, const double2 t) { mac(acc, a, t); }
 
 // Number of Chebyshev/Bessel terms after which |J_k(x)| * e^{k*lg} < tol
 // (Debye-type bound (e x / 2k)^k / sqrt(2 pi k), conservative for k > x).
-__device__ int series_terms(double x, double lg, double tol, int kcap) {
+static __device__ int series_terms(double x, double lg, double tol, int kcap) {
     if (!(x > 0.0)) return 1;
     const double ltol = log(tol);
     int k = max(1, (int)ceil(x) + 1);
@@ -443,7 +533,7 @@ __device__ int series_terms(double x, double lg, double tol, int kcap) {
 // by Miller's backward recurrence J_{k-1} = (2k/x) J_k - J_{k+1}, normalised
 // with J_0 + 2 sum J_2k = 1.  Rescaling is only needed above the stored range;
 // tiny arguments use the leading terms of the power series.
-__device__ void bessel_column(double *table, int M, int j, int K, double half, double dt) {
+static __device__ void bessel_column(double *table, int M, int j, int K, double half, double dt) {
     double *col = table + j;
     const size_t ld = (size_t)(M + 1);
     const double x = half * j * dt;
@@ -478,10 +568,21 @@ __device__ void bessel_column(double *table, int M, int j, int K, double half, d
     for (int k = kneed; k < K; ++k) col[k * ld] = 0.0;
 }
 
+// Moment of one term from the per-warp partials in slot `part` (nwarps
+// entries), by one warp: lane w takes warp w's partial, then a fixed
+// butterfly sum.
+template <class Vec>
+__device__ __forceinline__ void reduce_term(const Vec *part, int nwarps, int lane, Vec *mu) {
+    Vec q = vzero<Vec>();
+    if (lane < nwarps) q = part[lane];
+    q = warp_sum(q);
+    if (lane == 0) *mu = q;
+}
+
 // ---------------------------------------------------------------------------
 // The propagation kernel
 // ---------------------------------------------------------------------------
-template <bool F64, bool CPLX, int RMAX>
+template <bool F64, bool CPLX, int RMAX, bool CLU>
 __global__ void __launch_bounds__(512)
 powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     using P = Prec<F64, CPLX>;
@@ -493,9 +594,11 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     using Af = typename P::Af;
 
     extern __shared__ __align__(16) unsigned char smem[];
-    const SmemLayout<F64, CPLX> L(sys.n_pad, sys.nslices, sys.ell_len, run.Kmax, run.M, blockDim.x);
+    const SmemLayout<F64, CPLX> L(sys.n_pad, CLU ? run.nsl_loc : sys.nslices, CLU ? run.ell_loc : sys.ell_len,
+                                  run.Kmax, run.M, blockDim.x);
     double *s_coef = reinterpret_cast<double *>(smem + L.coef);
     double *s_red = reinterpret_cast<double *>(smem + L.red);
+    double *s_cred = reinterpret_cast<double *>(smem + L.cred);
     double *s_al = reinterpret_cast<double *>(smem + L.alpha);
     double *s_be = reinterpret_cast<double *>(smem + L.beta);
     int *s_soff = reinterpret_cast<int *>(smem + L.slice_off);
@@ -517,20 +620,30 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     const int M = run.M;
     const int nsteps = run.nsteps;
     double *table = run.table + (size_t)blockIdx.x * run.Kmax * (M + 1);
-    // Static pattern: copy once per CTA.
-    for (int i = tid; i <= sys.nslices; i += blockDim.x) s_soff[i] = sys.slice_off[i];
-    for (int e = tid; e < sys.ell_len; e += blockDim.x) s_col[e] = sys.ell_col[e];
+    // This CTA's block of slices [sb, se): global rows row0 .. row0 + 32*nsl.
+    const int CL = CLU ? run.cl : 1;
+    const int crank = CLU ? cluster_rank() : 0;
+    const int sb = CLU ? run.cl_slices[crank] : 0;
+    const int se = CLU ? run.cl_slices[crank + 1] : sys.nslices;
+    const int nsl = se - sb;
+    const int row0 = sb * 32, nrow_loc = nsl * 32;
+    const int eb = sys.slice_off[sb];
+    const int ell_loc = sys.slice_off[se] - eb;
+    int par = 0;              // cluster reduction buffer parity
+    // Static pattern: copy once per CTA (offsets local, columns global).
+    for (int i = tid; i <= nsl; i += blockDim.x) s_soff[i] = sys.slice_off[sb + i] - eb;
+    for (int e = tid; e < ell_loc; e += blockDim.x) s_col[e] = sys.ell_col[eb + e];
     // Slices to warps, longest-processing-time first: slices are stored in
     // non-increasing width, each goes to the least-loaded warp with room, so a
     // warp's slices also come in non-increasing width.  Cost ~ width + 5.
     __shared__ short s_wsl[32 * 8];
     __shared__ int s_wcnt[32];
     __shared__ int s_wload[32];
-    __syncthreads();
+    csync<CLU>();             // every CTA of the cluster has started before any remote access
     if (tid == 0) {
         for (int w = 0; w < nwarps; ++w) { s_wcnt[w] = 0; s_wload[w] = 0; }
         bool fits = true;
-        for (int sl = 0; sl < sys.nslices; ++sl) {
+        for (int sl = 0; sl < nsl; ++sl) {
             const int cost = ((s_soff[sl + 1] - s_soff[sl]) >> 5) + 5;
             int best = -1;
             for (int w = 0; w < nwarps; ++w)
@@ -543,12 +656,12 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         s_wload[0] = fits ? 1 : 0;          // reused as the "assignment fits" flag
     }
     __syncthreads();
-    const bool assignment_ok = s_wload[0] != 0;
+    const bool assignment_ok = cluster_reduce<CLU, 2>(s_wload[0] != 0 ? 1.0 : 0.0, s_red, s_cred, par, crank, CL) > 0.5;
     const int rows_per_lane = s_wcnt[warp];
 
-    for (int o = blockIdx.x; o < run.n_orient; o += gridDim.x) {
+    for (int o = blockIdx.x / CL; o < run.n_orient; o += gridDim.x / CL) {
         if (!assignment_ok) {                        // launch configuration error
-            if (tid == 0) run.status[o] = kDevTooManyRows;
+            if (tid == 0 && crank == 0) run.status[o] = kDevTooManyRows;
             continue;
         }
         // ---- 1. rotational coefficients (FP64) --------------------------------
@@ -565,20 +678,20 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 
         // ---- 2. assemble L(Omega) in FP64, store in working precision ---------
         double gmax = -CUDART_INF, gmin = CUDART_INF;
-        for (int e = tid; e < sys.ell_len; e += blockDim.x) {
+        for (int e = tid; e < ell_loc; e += blockDim.x) {
             double re = 0.0, im = 0.0;
             for (int s = 0; s < sys.nstreams; ++s) {
                 const double c = s_coef[sys.stream_coef[s]];
-                re = fma(c, sys.ell_re[(size_t)s * sys.ell_len + e], re);
-                if (CPLX) im = fma(c, sys.ell_im[(size_t)s * sys.ell_len + e], im);
+                re = fma(c, sys.ell_re[(size_t)s * sys.ell_len + eb + e], re);
+                if (CPLX) im = fma(c, sys.ell_im[(size_t)s * sys.ell_len + eb + e], im);
             }
             pack(s_val[e], re, im);
         }
-        for (int i = tid; i < sys.n_pad; i += blockDim.x) {
+        for (int i = tid; i < nrow_loc; i += blockDim.x) {
             double re = 0.0, im = 0.0;
             for (int s = 0; s < sys.nstreams; ++s) {
                 const double c = s_coef[sys.stream_coef[s]];
-                const double2 d = sys.diag[(size_t)s * sys.n_pad + i];
+                const double2 d = sys.diag[(size_t)s * sys.n_pad + row0 + i];
                 re = fma(c, d.x, re);
                 im = fma(c, d.y, im);
             }
@@ -588,37 +701,37 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         // Gershgorin interval of the Hermitian part (real diagonal + off-diagonal)
         for (int r = 0; r < rows_per_lane; ++r) {
             const int sl = s_wsl[warp * RMAX + r];
-            const int row = sl * 32 + lane;
-            if (row >= n) continue;
+            const int lrow = sl * 32 + lane;
+            if (row0 + lrow >= n) continue;
             const int off = s_soff[sl], w = (s_soff[sl + 1] - off) >> 5;
             double rad = 0.0;
             for (int c = 0; c < w; ++c) {
                 const double2 v = unpack(s_val[off + c * 32 + lane]);
                 rad += sqrt(v.x * v.x + v.y * v.y);
             }
-            const double dr = unpack(s_diag[row]).x;
+            const double dr = unpack(s_diag[lrow]).x;
             gmax = fmax(gmax, dr + rad);
             gmin = fmin(gmin, dr - rad);
         }
-        gmax = block_max(gmax, s_red);
-        gmin = block_min(gmin, s_red);
+        gmax = cluster_reduce<CLU, 1>(gmax, s_red, s_cred, par, crank, CL);
+        gmin = cluster_reduce<CLU, 2>(gmin, s_red, s_cred, par, crank, CL);
         double imax = 0.0;
-        for (int i = tid; i < n; i += blockDim.x) imax = fmax(imax, fabs(unpack(s_diag[i]).y));
-        imax = block_max(imax, s_red);
+        for (int i = tid; i < nrow_loc && row0 + i < n; i += blockDim.x) imax = fmax(imax, fabs(unpack(s_diag[i]).y));
+        imax = cluster_reduce<CLU, 1>(imax, s_red, s_cred, par, crank, CL);
 
         // ---- 3. Lanczos bounds on the Hermitian part ---------------------------
         Vec q_prev[RMAX], q_cur[RMAX];
         double nrm2 = 0.0;
 #pragma unroll
         for (int r = 0; r < RMAX; ++r) {
-            const int row = (r < rows_per_lane) ? s_wsl[warp * RMAX + r] * 32 + lane : n;
+            const int row = (r < rows_per_lane) ? row0 + s_wsl[warp * RMAX + r] * 32 + lane : n;
             const bool own = row < n;
             const double v = own ? 1.0 + 0.37 * sin(1.7 * row + 0.3) : 0.0;
             q_cur[r] = tovec(make_double2(v, 0.0), Vec());
             q_prev[r] = vzero<Vec>();
             nrm2 += v * v;
         }
-        nrm2 = block_sum(nrm2, s_red);
+        nrm2 = cluster_reduce<CLU, 0>(nrm2, s_red, s_cred, par, crank, CL);
         {
             const double inv = 1.0 / sqrt(nrm2);
 #pragma unroll
@@ -626,14 +739,15 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 if (r >= rows_per_lane) break;
                 const int sl = s_wsl[warp * RMAX + r];
                 q_cur[r].x *= inv; q_cur[r].y *= inv;
-                s_xa[sl * 32 + lane] = q_cur[r];
+                s_xa[row0 + sl * 32 + lane] = q_cur[r];
+                push_peers<CLU>(&s_xa[row0 + sl * 32 + lane], q_cur[r], crank, CL);
             }
         }
         int m_eff = 0;
         double beta_prev = 0.0;
         const int lits = min(run.lanczos_its, min(kMaxLanczos, n));
         for (int j = 0; j < lits; ++j) {
-            __syncthreads();
+            csync<CLU>();
             Vec wv[RMAX];
             double alpha_p = 0.0;
 #pragma unroll
@@ -641,15 +755,15 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 wv[r] = vzero<Vec>();
                 if (r >= rows_per_lane) continue;
                 const int sl = s_wsl[warp * RMAX + r];
-                const int row = sl * 32 + lane;
-                if (row >= n) continue;
+                const int lrow = sl * 32 + lane;
+                if (row0 + lrow >= n) continue;
                 const int off = s_soff[sl], w = (s_soff[sl + 1] - off) >> 5;
                 Vec y = vzero<Vec>();
                 for (int c = 0; c < w; ++c) {
                     const int e = off + c * 32 + lane;
                     mac(y, s_val[e], s_xa[s_col[e]]);
                 }
-                const double dr = unpack(s_diag[row]).x;
+                const double dr = unpack(s_diag[lrow]).x;
                 y.x += (Real)dr * q_cur[r].x;
                 y.y += (Real)dr * q_cur[r].y;
                 y.x -= (Real)beta_prev * q_prev[r].x;
@@ -657,7 +771,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 wv[r] = y;
                 alpha_p += (double)q_cur[r].x * y.x + (double)q_cur[r].y * y.y;
             }
-            const double alpha = block_sum(alpha_p, s_red);
+            const double alpha = cluster_reduce<CLU, 0>(alpha_p, s_red, s_cred, par, crank, CL);
             double b2 = 0.0;
 #pragma unroll
             for (int r = 0; r < RMAX; ++r) {
@@ -665,7 +779,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 wv[r].y -= (Real)alpha * q_cur[r].y;
                 b2 += (double)wv[r].x * wv[r].x + (double)wv[r].y * wv[r].y;
             }
-            const double beta = sqrt(block_sum(b2, s_red));
+            const double beta = sqrt(cluster_reduce<CLU, 0>(b2, s_red, s_cred, par, crank, CL));
             if (tid == 0) { s_al[j] = alpha; s_be[j] = beta; }
             m_eff = j + 1;
             if (!(beta > 1e-12 * (fabs(alpha) + 1e-300))) break;   // invariant subspace
@@ -675,7 +789,11 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 q_prev[r] = q_cur[r];
                 q_cur[r].x = wv[r].x * (Real)inv;
                 q_cur[r].y = wv[r].y * (Real)inv;
-                if (r < rows_per_lane) s_xb[s_wsl[warp * RMAX + r] * 32 + lane] = q_cur[r];
+                if (r < rows_per_lane) {
+                    Vec *dstp = &s_xb[row0 + s_wsl[warp * RMAX + r] * 32 + lane];
+                    *dstp = q_cur[r];
+                    push_peers<CLU>(dstp, q_cur[r], crank, CL);
+                }
             }
             Vec *t = s_xa; s_xa = s_xb; s_xb = t;
             beta_prev = beta;
@@ -732,30 +850,38 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             s_int[0] = K;
             s_int[1] = (K > run.Kmax) ? 1 : 0;
         }
-        __syncthreads();
-        const double cen = s_scalar[0], half = s_scalar[1];
-        const int K = s_int[0];
-        const int Mo = s_int[2];
-        if (s_int[1]) {
-            if (tid == 0) { run.status[o] = kDevTableTooSmall; run.kused[o] = K; run.halfwidth[o] = half; }
+        csync<CLU>();
+        // every CTA of a cluster takes rank 0's decisions, so their control flow
+        // (and their cluster barriers) cannot diverge
+        double cen = s_scalar[0], half = s_scalar[1];
+        int K = s_int[0], Mo = s_int[2], too_small = s_int[1];
+        if constexpr (CLU) {
+            cen = ld_cluster_f64(cluster_addr(smem_u32(&s_scalar[0]), 0));
+            half = ld_cluster_f64(cluster_addr(smem_u32(&s_scalar[1]), 0));
+            K = ld_cluster_s32(cluster_addr(smem_u32(&s_int[0]), 0));
+            too_small = ld_cluster_s32(cluster_addr(smem_u32(&s_int[1]), 0));
+            Mo = ld_cluster_s32(cluster_addr(smem_u32(&s_int[2]), 0));
+        }
+        if (too_small) {
+            if (tid == 0 && crank == 0) { run.status[o] = kDevTableTooSmall; run.kused[o] = K; run.halfwidth[o] = half; }
             continue;
         }
 
         // ---- 4. rescale to L~ = (L - c)/s -------------------------------------
         {
             const double inv = 1.0 / half;
-            for (int e = tid; e < sys.ell_len; e += blockDim.x) {
+            for (int e = tid; e < ell_loc; e += blockDim.x) {
                 const double2 v = unpack(s_val[e]);
                 pack(s_val[e], v.x * inv, v.y * inv);
             }
-            for (int i = tid; i < sys.n_pad; i += blockDim.x) {
+            for (int i = tid; i < nrow_loc; i += blockDim.x) {
                 const double2 d = unpack(s_diag[i]);
                 pack(s_diag[i], (d.x - cen) * inv, d.y * inv);
             }
         }
 
         // ---- 5. Bessel table J_k(s j dt), j = 0..M --------------------------
-        for (int j = tid; j < Mo; j += blockDim.x) bessel_column(table, Mo, j, K, half, run.dt);
+        for (int j = tid; j < (CLU ? Mo + 1 : Mo); j += blockDim.x) bessel_column(table, Mo, j, K, half, run.dt);
         __syncthreads();
         // series coefficients of one chunk (tau = M dt), centre phase folded in
         {
@@ -794,7 +920,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             if (r < rows_per_lane) {
                 const int sl = s_wsl[warp * RMAX + r];
                 nr = r + 1;
-                r_row[r] = sl * 32 + lane;
+                r_row[r] = row0 + sl * 32 + lane;
                 r_off[r] = s_soff[sl] + lane;
                 r_w[r] = (s_soff[sl + 1] - s_soff[sl]) >> 5;
             }
@@ -830,6 +956,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 for (int r = 0; r < RMAX; ++r) {
                     if (r < nr) {
                         s_xa[r_row[r]] = t_cur[r];
+                        push_peers<CLU>(&s_xa[r_row[r]], t_cur[r], crank, CL);
                         cdot_acc(mom, cc[r], t_cur[r]);
                         acc[r] = vzero<Vec>();
                         acc_add64(acc[r], s_atau[0], t_cur[r]);
@@ -839,17 +966,20 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 }
                 mom = warp_sum(mom);
                 if (lane == 0) s_part[warp] = mom;
-                __syncthreads();
+                csync<CLU>();
                 // k = 1 .. K-1: t_k = (k==1 ? 1 : 2) L~ t_{k-1} - t_{k-2}
                 for (int k = 1; k < K; ++k) {
                     const Vec *src = (k & 1) ? s_xa : s_xb;
                     Vec *dst = (k & 1) ? s_xb : s_xa;
                     const Real two = (k == 1) ? (Real)1 : (Real)2;
+                    // the last warp folds term k-1's partials while the others start term k;
+                    // slot (k-1)&1 is rewritten only in term k+1, after the next barrier
+                    if (warp == nwarps - 1) reduce_term(s_part + ((k - 1) & 1) * nwarps, nwarps, lane, &s_mu[k - 1]);
                     Acc y[RMAX];
 #pragma unroll
                     for (int r = 0; r < RMAX; ++r) {
                         y[r] = vzero<Vec>();
-                        if (r < nr) cmac(y[r], s_diag[r_row[r]], t_cur[r]);
+                        if (r < nr) cmac(y[r], s_diag[r_row[r] - row0], t_cur[r]);
                     }
                     int c = 0;
 #pragma unroll
@@ -873,13 +1003,14 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                             t_prev[r] = t_cur[r];
                             t_cur[r] = tn;
                             dst[r_row[r]] = tn;
+                            push_peers<CLU>(&dst[r_row[r]], tn, crank, CL);
                             cdot_acc(mom, cc[r], tn);
                             if (advance) acc_add64(acc[r], s_atau[k], tn);
                         }
                     }
                     mom = warp_sum(mom);
-                    if (lane == 0) s_part[k * nwarps + warp] = mom;
-                    __syncthreads();
+                    if (lane == 0) s_part[(k & 1) * nwarps + warp] = mom;
+                    csync<CLU>();
                 }
 #pragma unroll
                 for (int r = 0; r < RMAX; ++r) {
@@ -897,6 +1028,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     if (r < nr) {
                         const f2x T = tc[r];
                         reinterpret_cast<f2x *>(s_xa)[r_row[r]] = T;
+                        push_peers<CLU>(reinterpret_cast<f2x *>(s_xa) + r_row[r], T, crank, CL);
                         MOM = fma2(crr[r], T, MOM);
                         MOM = fma2(cim[r], swap2(T), MOM);
                         ac[r] = cmul_pk(s_atau[0], T);
@@ -910,18 +1042,19 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     float2 m = warp_sum(f2up(MOM));
                     if (lane == 0) s_part[warp] = m;
                 }
-                __syncthreads();
+                csync<CLU>();
                 for (int k = 1; k < K; ++k) {
                     const f2x *src = reinterpret_cast<const f2x *>((k & 1) ? s_xa : s_xb);
                     f2x *dst = reinterpret_cast<f2x *>((k & 1) ? s_xb : s_xa);
                     const f2x TW = (k == 1) ? ONE : TWO;
+                    if (warp == nwarps - 1) reduce_term(s_part + ((k - 1) & 1) * nwarps, nwarps, lane, &s_mu[k - 1]);
                     f2x Y[RMAX], Z[RMAX];
 #pragma unroll
                     for (int r = 0; r < RMAX; ++r) {
                         Y[r] = 0ull;
                         Z[r] = 0ull;
                         if (r < nr) {
-                            const PackD d = s_diag[r_row[r]];
+                            const PackD d = s_diag[r_row[r] - row0];
                             const f2x X = tc[r];
                             two_sum2(Y[r], Z[r], mul2(lo2(d.h), X));
                             two_sum2(Y[r], Z[r], mul2(hi2(d.h), swap2(X)));
@@ -963,6 +1096,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                             tp[r] = tc[r];
                             tc[r] = T;
                             dst[r_row[r]] = T;
+                            push_peers<CLU>(dst + r_row[r], T, crank, CL);
                             MOM = fma2(crr[r], T, MOM);
                             MOM = fma2(cim[r], swap2(T), MOM);
                             if (advance) {
@@ -976,9 +1110,9 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     }
                     {
                         float2 m = warp_sum(f2up(MOM));
-                        if (lane == 0) s_part[k * nwarps + warp] = m;
+                        if (lane == 0) s_part[(k & 1) * nwarps + warp] = m;
                     }
-                    __syncthreads();
+                    csync<CLU>();
                 }
 #pragma unroll
                 for (int r = 0; r < RMAX; ++r) {
@@ -989,18 +1123,35 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     }
                 }
             }
-            // moments: sum the per-warp partials of every term
-            for (int k = tid; k < K; k += blockDim.x) {
-                Vec v = vzero<Vec>();
-                for (int w2 = 0; w2 < nwarps; ++w2) {
-                    const Vec q = s_part[k * nwarps + w2];
-                    v.x += q.x; v.y += q.y;
+            // moment of the last term (the others were folded inside the loop)
+            if (warp == nwarps - 1) reduce_term(s_part + ((K - 1) & 1) * nwarps, nwarps, lane, &s_mu[K - 1]);
+            if constexpr (CLU) {
+                // rank 0 adds the peers' partial moments in rank order; the peers
+                // rewrite theirs only after the next cluster barrier, which rank 0
+                // reaches after this read
+                csync<CLU>();
+                if (crank == 0) {
+                    for (int k = tid; k < K; k += blockDim.x) {
+                        Vec v = s_mu[k];
+                        for (int j = 1; j < CL; ++j) {
+                            const uint32_t a = cluster_addr(smem_u32(&s_mu[k]), j);
+                            if constexpr (F64) {
+                                v.x += ld_cluster_f64(a);
+                                v.y += ld_cluster_f64(a + 8);
+                            } else {
+                                float fx, fy;
+                                asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(fx), "=f"(fy) : "r"(a) : "memory");
+                                v.x += fx;
+                                v.y += fy;
+                            }
+                        }
+                        s_mu[k] = v;
+                    }
                 }
-                s_mu[k] = v;
             }
             __syncthreads();
             // FID points of this chunk: f_j = ph_j * sum_k J_k(s j dt) (-i)^k mu_k
-            {
+            if (!CLU || crank == 0) {
                 const int parts = max(1, (int)blockDim.x / Mo);
                 const int kper = (K + parts - 1) / parts;
                 for (int jj = tid; jj < Mo * parts; jj += blockDim.x) {
@@ -1039,20 +1190,21 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             }
             // guard against a violated spectral bound (the series would then
             // grow; a dissipative L can only shrink the state)
-            end_n2 = block_sum(end_n2, s_red);
-            start_n2 = block_sum(start_n2, s_red);
+            end_n2 = cluster_reduce<CLU, 0>(end_n2, s_red, s_cred, par, crank, CL);
+            start_n2 = cluster_reduce<CLU, 0>(start_n2, s_red, s_cred, par, crank, CL);
             if (!isfinite(end_n2)) status = kDevNonFinite;
             else if (end_n2 > 16.0 * start_n2 + 1e-300) status = kDevDiverged;
         }
-        if (tid == 0) {
+        if (tid == 0 && crank == 0) {
             run.status[o] = status;
             run.kused[o] = K;
             run.mused[o] = Mo;
             run.halfwidth[o] = half;
             run.matvecs[o] = (long long)nchunks * (K - 1);
         }
-        __syncthreads();
+        csync<CLU>();
     }
+    csync<CLU>();             // no CTA leaves while a peer may still read its shared memory
 }
 
 // ---------------------------------------------------------------------------
@@ -1076,7 +1228,7 @@ __global__ void powder_partial_kernel(const Vec *__restrict__ fids, const double
     part[(size_t)g * npts + t] = s;
 }
 
-__global__ void powder_combine_kernel(const double2 *__restrict__ part, int ngroups, int npts,
+static __global__ void powder_combine_kernel(const double2 *__restrict__ part, int ngroups, int npts,
                                       double2 *__restrict__ out) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= npts) return;

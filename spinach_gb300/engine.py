@@ -25,7 +25,7 @@ class SpxCsc(C.Structure):
 
 class SpxOptions(C.Structure):
     _fields_ = [('precision', C.c_int32), ('chunk_steps', C.c_int32), ('threads', C.c_int32),
-                ('reserved0', C.c_int32), ('series_tol', C.c_double), ('reserved1', C.c_double)]
+                ('cluster', C.c_int32), ('series_tol', C.c_double), ('reserved1', C.c_double)]
 
 
 class SpxStats(C.Structure):
@@ -35,7 +35,8 @@ class SpxStats(C.Structure):
                 ('kernel_ms', C.c_double), ('reduce_ms', C.c_double),
                 ('min_half_width', C.c_double), ('max_half_width', C.c_double),
                 ('dim', C.c_int64), ('nnz', C.c_int64), ('ell_entries', C.c_int64),
-                ('value_streams', C.c_int32), ('real_offdiag', C.c_int32)]
+                ('value_streams', C.c_int32), ('real_offdiag', C.c_int32),
+                ('cluster', C.c_int32), ('smem_bytes', C.c_int32)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -174,7 +175,7 @@ class Engine:
 
     def run(self, alphas, betas, gammas, weights, dt: float, nsteps: int, precision: int = FP32,
             per_orientation: bool = False, chunk_steps: int = 0, threads: int = 0,
-            series_tol: float = 0.0) -> PowderResult:
+            series_tol: float = 0.0, cluster: int = 0) -> PowderResult:
         al = np.ascontiguousarray(alphas, np.float64)
         be = np.ascontiguousarray(betas, np.float64)
         ga = np.ascontiguousarray(gammas, np.float64)
@@ -182,7 +183,7 @@ class Engine:
         no = al.size
         fid = np.zeros(2 * (nsteps + 1))
         fids = np.zeros(2 * (nsteps + 1) * no) if per_orientation else None
-        opt = SpxOptions(precision, chunk_steps, threads, 0, series_tol, 0.0)
+        opt = SpxOptions(precision, chunk_steps, threads, cluster, series_tol, 0.0)
         self._check(self.lib.spx_run_powder(self.h, no, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
                                             float(dt), int(nsteps), C.byref(opt), _dptr(fid),
                                             _dptr(fids) if fids is not None else None), self.h)
@@ -191,9 +192,9 @@ class Engine:
 
     def run_device(self, d_alphas: int, d_betas: int, d_gammas: int, d_weights: int, n_orient: int,
                    dt: float, nsteps: int, d_fid: int, precision: int = FP32, chunk_steps: int = 0,
-                   threads: int = 0, series_tol: float = 0.0):
+                   threads: int = 0, series_tol: float = 0.0, cluster: int = 0):
         """Enqueue a run on device-resident buffers (raw device pointers); no sync."""
-        opt = SpxOptions(precision, chunk_steps, threads, 0, series_tol, 0.0)
+        opt = SpxOptions(precision, chunk_steps, threads, cluster, series_tol, 0.0)
         self._check(self.lib.spx_run_powder_device(self.h, n_orient, d_alphas, d_betas, d_gammas,
                                                    d_weights, float(dt), int(nsteps), C.byref(opt),
                                                    d_fid), self.h)

@@ -1,7 +1,8 @@
 """Generate the FP64 oracle fixtures used by the GPU parity tests.
 
 Run from the repository root:  python tests/golden/make_golden.py
-Writes tests/golden/*.npz.  Inputs are the seeded workloads of
+(and ``python tests/golden/make_golden.py large`` for the cluster-sized
+systems).  Writes tests/golden/*.npz.  Inputs are the seeded workloads of
 spinach_gb300.workloads; FIDs come from the oracle (oracle/spinach_ref.py).
 """
 import os
@@ -24,7 +25,30 @@ def save(name, **kw):
     print('wrote', name, {k: getattr(v, 'shape', v) for k, v in kw.items()})
 
 
+def large_systems():
+    """Systems whose share of L needs a cluster of CTAs on the GPU."""
+    # c4 EPR radical, IK-1(3) basis dim 2736, Krylov branch, 3 orientations x 4096 steps
+    w = W.c4()
+    al, be, ga, wt = W.zcwn_grid(w.n_orient)
+    sel = np.array([0, 1234, 3210])
+    sub = (al[sel], be[sel], ga[sel], np.full(sel.size, 1.0 / sel.size))
+    fk = oracle_powder(w, sub, krylov=True, sum_up=False)
+    save('c4_orient_krylov_fp64.npz', sel=sel, fids=np.array(fk), seed=w.seed, nsteps=w.nsteps)
+    # the first dim-4096 system of the batched workload (6 spins, full basis), 2 orientations x 1024 steps
+    ws = W.c2()
+    idx = next(i for i, x in enumerate(ws) if len(x.isotopes) == 6)
+    w = ws[idx]
+    al, be, ga, wt = W.zcwn_grid(w.n_orient)
+    sel = np.array([7, 211])
+    sub = (al[sel], be[sel], ga[sel], np.full(sel.size, 1.0 / sel.size))
+    fk = oracle_powder(w, sub, krylov=True, sum_up=False)
+    save('c2_dim4096_orient_krylov_fp64.npz', system=idx, sel=sel, fids=np.array(fk), seed=w.seed,
+         nsteps=w.nsteps)
+
+
 def main():
+    if 'large' in sys.argv[1:]:
+        return large_systems()
     t = time.time()
     # c0: full 200-point grid, 1024 steps, default tolerances (expm branch, dim < 200)
     w = W.c0()
@@ -40,6 +64,7 @@ def main():
     save('c1_orient_krylov_fp64.npz', sel=sel, fids=np.array(fk), seed=w.seed, nsteps=w.nsteps)
     fp = oracle_powder(w, (sub[0][:1], sub[1][:1], sub[2][:1], np.ones(1)), krylov=False, sum_up=False)
     save('c1_orient_propagator_fp64.npz', sel=sel[:1], fids=np.array(fp), seed=w.seed, nsteps=w.nsteps)
+    large_systems()
     print('done in', round(time.time() - t, 1), 's')
 
 
