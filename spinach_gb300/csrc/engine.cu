@@ -87,7 +87,9 @@ struct spx_handle {
     std::vector<int> slice_off_host;
     DevBuf<uint16_t> d_ell_col;
     DevBuf<double> d_ell_re, d_ell_im;
-    DevBuf<double2> d_diag, d_rho0, d_coil;
+    DevBuf<double2> d_diag, d_rho0, d_coil, d_coil_vals;
+    DevBuf<int> d_coil_rows;
+    int ncoil = -1;                 // non-zero coil rows if at most 32, else -1
 
     // run buffers
     DevBuf<double> d_grid;       // alpha | beta | gamma | weight
@@ -323,6 +325,16 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
     h->d_term_rkm.upload(term_rkm, h->stream);
     h->d_rho0.upload(r0, h->stream);
     h->d_coil.upload(cl, h->stream);
+    // sparse coil: at most 32 non-zero rows -> moments read straight from the state
+    std::vector<int> crow;
+    std::vector<double2> cval;
+    for (int i = 0; i < n_pad; ++i)
+        if (cl[i].x != 0.0 || cl[i].y != 0.0) { crow.push_back(i); cval.push_back(cl[i]); }
+    h->ncoil = (crow.size() <= 32) ? (int)crow.size() : -1;
+    if (h->ncoil > 0) {
+        h->d_coil_rows.upload(crow, h->stream);
+        h->d_coil_vals.upload(cval, h->stream);
+    }
     SPX_CUDA(cudaStreamSynchronize(h->stream));
     h->n = (int)n;
     h->n_pad = n_pad;
@@ -545,6 +557,7 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     sys.diag = h->d_diag.p; sys.stream_coef = h->d_stream_coef.p; sys.nstreams = h->nstreams;
     sys.ncoef = 1 + 2 * h->nterms; sys.nterms = h->nterms; sys.term_rkm = h->d_term_rkm.p;
     sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag;
+    sys.ncoil = h->ncoil; sys.coil_rows = h->d_coil_rows.p; sys.coil_vals = h->d_coil_vals.p;
     spx::DevRun run{};
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
@@ -745,6 +758,7 @@ void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, con
     sys.diag = h->d_diag.p; sys.stream_coef = h->d_stream_coef.p; sys.nstreams = h->nstreams;
     sys.ncoef = 1 + 2 * h->nterms; sys.nterms = h->nterms; sys.term_rkm = h->d_term_rkm.p;
     sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag;
+    sys.ncoil = h->ncoil; sys.coil_rows = h->d_coil_rows.p; sys.coil_vals = h->d_coil_vals.p;
     spx::DevRun run{};
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;

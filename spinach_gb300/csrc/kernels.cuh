@@ -202,6 +202,13 @@ static __device__ __forceinline__ void two_sum2(f2x &Y, f2x &Z, f2x P) {
     Y = S;
     Z = add2(Z, E);
 }
+// Kahan step: Y + (-C) += P, C the negated low part lost so far
+__device__ __forceinline__ void kahan_add2(f2x &Y, f2x &C, f2x P) {
+    const f2x y = sub2(P, C);
+    const f2x t = add2(Y, y);
+    C = sub2(sub2(t, Y), y);
+    Y = t;
+}
 // a * t for a packed complex coefficient (PackC/PackA layout), hi and lo parts
 static __device__ __forceinline__ f2x cmul_pk(const PackC &a, f2x T) {
     const f2x TS = swap2(T);
@@ -353,6 +360,9 @@ struct DevSystem {
     const int *term_rkm;        // 3 * nterms: rank, k, m (0-based k, m)
     const double2 *rho0;        // n_pad (sliced order)
     const double2 *coil;        // n_pad (sliced order)
+    int ncoil;                  // 1..32: non-zero coil rows listed below; 0 or -1: use the dense coil
+    const int *coil_rows;       // ncoil rows (sliced order)
+    const double2 *coil_vals;   // ncoil values
     double max_im_diag;         // largest |Im L_ii| (relaxation), rad/s
 };
 
@@ -579,6 +589,15 @@ __device__ __forceinline__ void reduce_term(const Vec *part, int nwarps, int lan
     if (lane == 0) *mu = q;
 }
 
+// Moment coil' x from the few non-zero coil rows (lane i takes row i), one warp.
+template <class Vec>
+__device__ __forceinline__ void coil_moment(const Vec *x, int ncoil, const int *rows, const Vec *cv, int lane, Vec *mu) {
+    Vec q = vzero<Vec>();
+    if (lane < ncoil) cdot_acc(q, cv[lane], x[rows[lane]]);
+    q = warp_sum(q);
+    if (lane == 0) *mu = q;
+}
+
 // ---------------------------------------------------------------------------
 // The propagation kernel
 // ---------------------------------------------------------------------------
@@ -614,6 +633,9 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     Vec *s_rec = reinterpret_cast<Vec *>(smem + L.rec);
     __shared__ double s_scalar[8];
     __shared__ int s_int[4];
+    __shared__ int s_crow[32];
+    __shared__ Vec s_cval[32];
+    const bool scoil = sys.ncoil > 0;       // moments from the coil rows, no per-row projection
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const int n = sys.n;
@@ -632,6 +654,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     int par = 0;              // cluster reduction buffer parity
     // Static pattern: copy once per CTA (offsets local, columns global).
     for (int i = tid; i <= nsl; i += blockDim.x) s_soff[i] = sys.slice_off[sb + i] - eb;
+    if (scoil && tid < sys.ncoil) {
+        s_crow[tid] = sys.coil_rows[tid];
+        s_cval[tid] = tovec(sys.coil_vals[tid], Vec());
+    }
     for (int e = tid; e < ell_loc; e += blockDim.x) s_col[e] = sys.ell_col[eb + e];
     // Slices to warps, longest-processing-time first: slices are stored in
     // non-increasing width, each goes to the least-loaded warp with room, so a
@@ -957,15 +983,17 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     if (r < nr) {
                         s_xa[r_row[r]] = t_cur[r];
                         push_peers<CLU>(&s_xa[r_row[r]], t_cur[r], crank, CL);
-                        cdot_acc(mom, cc[r], t_cur[r]);
+                        if (!scoil) cdot_acc(mom, cc[r], t_cur[r]);
                         acc[r] = vzero<Vec>();
                         acc_add64(acc[r], s_atau[0], t_cur[r]);
                         start_n2 += t_cur[r].x * t_cur[r].x + t_cur[r].y * t_cur[r].y;
                         t_prev[r] = vzero<Vec>();
                     }
                 }
-                mom = warp_sum(mom);
-                if (lane == 0) s_part[warp] = mom;
+                if (!scoil) {
+                    mom = warp_sum(mom);
+                    if (lane == 0) s_part[warp] = mom;
+                }
                 csync<CLU>();
                 // k = 1 .. K-1: t_k = (k==1 ? 1 : 2) L~ t_{k-1} - t_{k-2}
                 for (int k = 1; k < K; ++k) {
@@ -974,7 +1002,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     const Real two = (k == 1) ? (Real)1 : (Real)2;
                     // the last warp folds term k-1's partials while the others start term k;
                     // slot (k-1)&1 is rewritten only in term k+1, after the next barrier
-                    if (warp == nwarps - 1) reduce_term(s_part + ((k - 1) & 1) * nwarps, nwarps, lane, &s_mu[k - 1]);
+                    if (warp == nwarps - 1) {
+                        if (scoil) coil_moment(src, sys.ncoil, s_crow, s_cval, lane, &s_mu[k - 1]);
+                        else reduce_term(s_part + ((k - 1) & 1) * nwarps, nwarps, lane, &s_mu[k - 1]);
+                    }
                     Acc y[RMAX];
 #pragma unroll
                     for (int r = 0; r < RMAX; ++r) {
@@ -1004,12 +1035,14 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                             t_cur[r] = tn;
                             dst[r_row[r]] = tn;
                             push_peers<CLU>(&dst[r_row[r]], tn, crank, CL);
-                            cdot_acc(mom, cc[r], tn);
+                            if (!scoil) cdot_acc(mom, cc[r], tn);
                             if (advance) acc_add64(acc[r], s_atau[k], tn);
                         }
                     }
-                    mom = warp_sum(mom);
-                    if (lane == 0) s_part[(k & 1) * nwarps + warp] = mom;
+                    if (!scoil) {
+                        mom = warp_sum(mom);
+                        if (lane == 0) s_part[(k & 1) * nwarps + warp] = mom;
+                    }
                     csync<CLU>();
                 }
 #pragma unroll
@@ -1021,6 +1054,9 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 }
             } else {
                 // ---- FP32: packed (re, im) pairs, compensated row sums ----
+                // Row sums are Kahan-compensated: Y running sum, C its negated lost
+                // low part, L the products of the values' low parts; the row value
+                // Y + (L - C) is rounded once.
                 const f2x TWO = f2pk(2.f, 2.f), ONE = f2pk(1.f, 1.f);
                 f2x MOM = 0ull;
 #pragma unroll
@@ -1029,8 +1065,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                         const f2x T = tc[r];
                         reinterpret_cast<f2x *>(s_xa)[r_row[r]] = T;
                         push_peers<CLU>(reinterpret_cast<f2x *>(s_xa) + r_row[r], T, crank, CL);
-                        MOM = fma2(crr[r], T, MOM);
-                        MOM = fma2(cim[r], swap2(T), MOM);
+                        if (!scoil) {
+                            MOM = fma2(crr[r], T, MOM);
+                            MOM = fma2(cim[r], swap2(T), MOM);
+                        }
                         ac[r] = cmul_pk(s_atau[0], T);
                         cp[r] = 0ull;
                         tp[r] = 0ull;
@@ -1038,7 +1076,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                         start_n2 += (double)t.x * t.x + (double)t.y * t.y;
                     }
                 }
-                {
+                if (!scoil) {
                     float2 m = warp_sum(f2up(MOM));
                     if (lane == 0) s_part[warp] = m;
                 }
@@ -1047,18 +1085,23 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     const f2x *src = reinterpret_cast<const f2x *>((k & 1) ? s_xa : s_xb);
                     f2x *dst = reinterpret_cast<f2x *>((k & 1) ? s_xb : s_xa);
                     const f2x TW = (k == 1) ? ONE : TWO;
-                    if (warp == nwarps - 1) reduce_term(s_part + ((k - 1) & 1) * nwarps, nwarps, lane, &s_mu[k - 1]);
-                    f2x Y[RMAX], Z[RMAX];
+                    if (warp == nwarps - 1) {
+                        // moment of term k-1, whose vector is this term's source
+                        if (scoil) coil_moment(reinterpret_cast<const Vec *>(src), sys.ncoil, s_crow, s_cval, lane, &s_mu[k - 1]);
+                        else reduce_term(s_part + ((k - 1) & 1) * nwarps, nwarps, lane, &s_mu[k - 1]);
+                    }
+                    f2x Y[RMAX], C[RMAX], Lo[RMAX];
 #pragma unroll
                     for (int r = 0; r < RMAX; ++r) {
                         Y[r] = 0ull;
-                        Z[r] = 0ull;
+                        C[r] = 0ull;
+                        Lo[r] = 0ull;
                         if (r < nr) {
                             const PackD d = s_diag[r_row[r] - row0];
                             const f2x X = tc[r];
-                            two_sum2(Y[r], Z[r], mul2(lo2(d.h), X));
-                            two_sum2(Y[r], Z[r], mul2(hi2(d.h), swap2(X)));
-                            Z[r] = fma2(lo2(d.l), X, Z[r]);
+                            Y[r] = mul2(lo2(d.h), X);
+                            kahan_add2(Y[r], C[r], mul2(hi2(d.h), swap2(X)));
+                            Lo[r] = mul2(lo2(d.l), X);
                         }
                     }
                     int c = 0;
@@ -1074,14 +1117,14 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                                     if constexpr (CPLX) {
                                         const PackC v = s_val[e];
                                         const f2x XS = swap2(X);
-                                        two_sum2(Y[r], Z[r], mul2(lo2(v.h), X));
-                                        two_sum2(Y[r], Z[r], mul2(hi2(v.h), XS));
-                                        Z[r] = fma2(lo2(v.l), X, Z[r]);
-                                        Z[r] = fma2(hi2(v.l), XS, Z[r]);
+                                        kahan_add2(Y[r], C[r], mul2(lo2(v.h), X));
+                                        kahan_add2(Y[r], C[r], mul2(hi2(v.h), XS));
+                                        Lo[r] = fma2(lo2(v.l), X, Lo[r]);
+                                        Lo[r] = fma2(hi2(v.l), XS, Lo[r]);
                                     } else {
                                         const PackR v = s_val[e];
-                                        two_sum2(Y[r], Z[r], mul2(lo2(v.v), X));
-                                        Z[r] = fma2(hi2(v.v), X, Z[r]);
+                                        kahan_add2(Y[r], C[r], mul2(lo2(v.v), X));
+                                        Lo[r] = fma2(hi2(v.v), X, Lo[r]);
                                     }
                                 }
                             }
@@ -1091,14 +1134,16 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 #pragma unroll
                     for (int r = 0; r < RMAX; ++r) {
                         if (r < nr) {
-                            // t_k = TW * (Y + Z) - t_{k-2}, rounded once from the compensated sum
-                            const f2x T = sub2(fma2(TW, Y[r], mul2(TW, Z[r])), tp[r]);
+                            // t_k = TW * (Y + (Lo - C)) - t_{k-2}
+                            const f2x T = sub2(fma2(TW, Y[r], mul2(TW, sub2(Lo[r], C[r]))), tp[r]);
                             tp[r] = tc[r];
                             tc[r] = T;
                             dst[r_row[r]] = T;
                             push_peers<CLU>(dst + r_row[r], T, crank, CL);
-                            MOM = fma2(crr[r], T, MOM);
-                            MOM = fma2(cim[r], swap2(T), MOM);
+                            if (!scoil) {
+                                MOM = fma2(crr[r], T, MOM);
+                                MOM = fma2(cim[r], swap2(T), MOM);
+                            }
                             if (advance) {
                                 // Kahan-compensated chunk-end sum acc += a_k t_k
                                 const f2x Yk = sub2(cmul_pk(s_atau[k], T), cp[r]);
@@ -1108,7 +1153,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                             }
                         }
                     }
-                    {
+                    if (!scoil) {
                         float2 m = warp_sum(f2up(MOM));
                         if (lane == 0) s_part[(k & 1) * nwarps + warp] = m;
                     }
@@ -1124,8 +1169,11 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 }
             }
             // moment of the last term (the others were folded inside the loop)
-            if (warp == nwarps - 1) reduce_term(s_part + ((K - 1) & 1) * nwarps, nwarps, lane, &s_mu[K - 1]);
-            if constexpr (CLU) {
+            if (warp == nwarps - 1) {
+                if (scoil) coil_moment(((K - 1) & 1) ? s_xb : s_xa, sys.ncoil, s_crow, s_cval, lane, &s_mu[K - 1]);
+                else reduce_term(s_part + ((K - 1) & 1) * nwarps, nwarps, lane, &s_mu[K - 1]);
+            }
+            if (CLU && !scoil) {
                 // rank 0 adds the peers' partial moments in rank order; the peers
                 // rewrite theirs only after the next cluster barrier, which rank 0
                 // reaches after this read
