@@ -302,9 +302,12 @@ def run_gpu(args):
             cpu = {'value': nn / t, 'unit': UNIT, 'cores': cores, 'kind': 'port',
                    'sample': f'{nn} orientations of c1 (one per core, all 2048 steps), '
                              'oracle restatement of propagator.m + P*rho in FP64'}
-        sur = None
+        sur = c2 = c4 = None
         if not args.no_surrogate and world == 1 and args.workload == 'c1':
             sur = surrogate_leg(eng, w, local)
+        if not args.no_extra and world == 1 and args.workload == 'c1':
+            c4 = c4_leg(local)
+            c2 = c2_leg(local)
         line = {
             'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': statistics.mean(step_ms), 'higher_is_better': True,
@@ -327,6 +330,8 @@ def run_gpu(args):
                                  'below the algorithmic per-matvec bytes; see profiles/'},
             'cpu_baseline': cpu,
             'surrogate': sur,
+            'c4': c4,
+            'c2': c2,
             'clocks': clk,
             'gpu_launches': 3 * args.steps,
         }
@@ -335,6 +340,72 @@ def run_gpu(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def c4_leg(device):
+    """X-band EPR radical, IK-1(3) basis dim 2736 (complex values), 4000 orientations x 4096 steps of 1 ns,
+    FP32 and FP64 on the same GPU (host buffers in, powder FID out)."""
+    from spinach_gb300 import engine as E, workloads as W
+    w = W.c4()
+    L = W.build(w)
+    eng = E.Engine(device)
+    eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
+    g = W.zcwn_grid(w.n_orient)
+    eng.run(*[a[:64] for a in g], w.dt, w.nsteps, precision=E.FP32)          # warm-up
+    t0 = time.perf_counter()
+    r32 = eng.run(*g, w.dt, w.nsteps, precision=E.FP32)
+    t32 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    r64 = eng.run(*g, w.dt, w.nsteps, precision=E.FP64)
+    t64 = time.perf_counter() - t0
+    out = {'workload': 'c4: e + 14N + 10 1H at 0.34 T, IK-1(3) dim 2736, T2e, 4000-orientation zcwn grid, '
+                       '4096 steps of 1 ns', 'value': w.n_orient / t32, 'unit': UNIT,
+           'rel_err_vs_fp64_gpu': _rel(r32.fid, r64.fid), 'fp64_gpu': {'value': w.n_orient / t64},
+           'kernel_ms': r32.stats['kernel_ms'], 'cluster': r32.stats['cluster'], 'threads': r32.stats['threads'],
+           'matvecs': r32.stats['matvecs']}
+    eng.close()
+    return out
+
+
+def c2_leg(device):
+    """64 systems of 3-8 spins (dims 64-4096), 400 orientations x 1024 steps each, autotuned, one CUDA
+    graph per precision; value = all systems' orientation FIDs / graph time."""
+    from spinach_gb300 import batched as B, engine as E, workloads as W
+    ws = W.c2()
+    bp = B.prepare(ws, tune=True, precision=E.FP32)
+    try:
+        b = B.capture(bp, E.FP32)
+        b.launch()
+        b.synchronize()
+        ms = []
+        for _ in range(3):
+            b.launch()
+            ms.append(b.synchronize())
+        f32 = B.powder_fids(bp)
+        B.capture(bp, E.FP64)
+        bp.batch.launch()
+        ms64 = bp.batch.synchronize()
+        f64 = B.powder_fids(bp)
+        n_fids = sum(g.shape[1] for g in bp.grids)
+        dims = {}
+        for d in bp.dims:
+            dims[str(d)] = dims.get(str(d), 0) + 1
+        shapes = {}
+        for d, t in zip(bp.dims, bp.tuned):
+            shapes[str(d)] = t
+        return {'workload': 'c2: 64 seeded systems of 3-8 spins (full basis up to dim 4096, IK-0(3) above), '
+                            '400-orientation zcwn grid and 1024 steps of 10 us each, one graph launch',
+                'value': n_fids / (statistics.median(ms) / 1e3), 'unit': UNIT, 'graph_ms': statistics.median(ms),
+                'rel_err_vs_fp64_gpu_max': max(_rel(a, b_) for a, b_ in zip(f32, f64)),
+                'fp64_gpu': {'value': n_fids / (ms64 / 1e3), 'graph_ms': ms64},
+                'systems_by_dim': dims, 'tuned_shape_by_dim': shapes,
+                'setup_s': bp.setup_s, 'autotune_s': bp.tune_s}
+    finally:
+        bp.close()
 
 
 def surrogate_leg(eng, w, device):
@@ -383,6 +454,7 @@ def main():
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-surrogate', action='store_true', help='skip the learned-surrogate leg')
+    ap.add_argument('--no-extra', action='store_true', help='skip the c2 and c4 legs')
     ap.add_argument('--profile-only', action='store_true',
                     help='warm-up and timed powder runs only (for ncu captures); no FP64/e2e/CPU legs')
     args = ap.parse_args()

@@ -61,7 +61,8 @@ typedef struct {
     int32_t cluster;           /* CTAs sharing one orientation (1, 2, 4, 8), 0 = auto:
                                   the smallest whose per-CTA share of L fits shared memory */
     double series_tol;         /* truncation tolerance of the series, 0 = auto */
-    double reserved1;
+    double chunk_target;       /* series argument s*M*dt one expansion covers, 0 = auto
+                                  (the autotuned value, else the largest that fits) */
 } spx_options;
 
 /* Statistics of the last spx_run_powder* call on a handle. */
@@ -193,6 +194,44 @@ spx_status spx_surrogate_gradients(spx_surrogate *s, int64_t n, const double *d_
 spx_status spx_surrogate_get_params(spx_surrogate *s, float *h_params);
 spx_status spx_surrogate_set_params(spx_surrogate *s, const float *h_params);
 const char *spx_surrogate_last_error(const spx_surrogate *s);
+
+/*
+ * Autotuner (no counterpart in the reference, whose step.m/propagator.m pick
+ * their branch from fixed tolerances).  Times candidate launch shapes -- CTAs
+ * per orientation (1, 2, 4, 8), warps per CTA, series length per chunk -- on
+ * one wave of the given device-resident orientations over at most 128 steps,
+ * and keeps the fastest in the handle: later runs whose options leave
+ * threads, cluster and chunk_target at 0 use it.  Results are cached per
+ * system shape (dimension, ELL size, value streams, precision, spectral
+ * scale) for the life of the process.  best (may be NULL) receives the chosen
+ * options.  The dense-propagator alternative is costed, not run: best->
+ * reserved fields stay zero; see spx_stats for what a run used.
+ */
+spx_status spx_autotune(spx_handle *handle, int64_t n_orient, const double *d_alphas, const double *d_betas,
+                        const double *d_gammas, double dt, int64_t nsteps, int32_t precision,
+                        spx_options *best);
+
+/*
+ * Batched powders (no counterpart in the reference, which runs systems one
+ * powder() call at a time).  Captures one powder run of each of n handles --
+ * each with its own uploaded system, device-resident grid and output (the
+ * arguments of spx_run_powder_device, one entry per handle) -- into one CUDA
+ * graph whose per-system launches sit on parallel branches.  The handles'
+ * buffers are sized at creation; the handles must not run anything else
+ * while the batch exists.
+ */
+typedef struct spx_batch spx_batch;
+spx_status spx_batch_create(spx_batch **batch, int32_t n, spx_handle *const *handles, const int64_t *n_orient,
+                            const double *const *d_alphas, const double *const *d_betas,
+                            const double *const *d_gammas, const double *const *d_weights, const double *dt,
+                            const int64_t *nsteps, const spx_options *opts, double *const *d_fids);
+/* One launch of the whole graph on stream (a cudaStream_t; NULL = the batch's own stream). */
+spx_status spx_batch_launch(spx_batch *batch, void *stream);
+/* Wait for the last launch and check every system's status; ms = graph time (may be NULL). */
+spx_status spx_batch_synchronize(spx_batch *batch, double *ms);
+spx_status spx_batch_destroy(spx_batch *batch);
+/* Detail of the batch's last error; with batch NULL, why this thread's last spx_batch_create failed. */
+const char *spx_batch_last_error(const spx_batch *batch);
 
 /* Wait for all work on the handle's stream; returns the device status. */
 spx_status spx_synchronize(spx_handle *handle);

@@ -11,7 +11,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -103,7 +105,12 @@ struct spx_handle {
     // last run
     spx_stats stats{};
     bool stats_pending = false;
+    bool stats_timed = true;        // kernel events recorded (not inside a captured graph)
     int64_t last_norient = 0;
+
+    // autotuned launch shape per precision (threads, cluster, chunk_target)
+    bool has_tuned[2] = {false, false};
+    spx_options tuned[2] = {};
 };
 
 namespace {
@@ -352,6 +359,8 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
 // ---------------------------------------------------------------------------
 // Launch configuration
 // ---------------------------------------------------------------------------
+constexpr int kPowderGroup = 64;    // orientations per partial sum of the powder reduction
+
 struct Config {
     int threads, rmax, M, Kmax, grid;
     bool fixed;
@@ -446,7 +455,8 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     // sharing an orientation (rows split between them).
     c.fixed = opt.chunk_steps > 0;
     const double lg = (h->g_upper > 0) ? 2.0 * h->max_im_diag / (h->g_upper / 4.0) : 0.0;
-    const double targets[] = {300.0, 200.0, 150.0, 100.0, 60.0, 30.0};
+    std::vector<double> targets = {300.0, 200.0, 150.0, 100.0, 60.0, 30.0};
+    if (opt.chunk_target > 0) targets = {opt.chunk_target};
     bool placed = false;
     const int cls[] = {1, 2, 4, 8};
     for (int cl : cls) {
@@ -483,7 +493,14 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
         throw SpxError(SPX_ERR_UNSUPPORTED, "system does not fit the shared memory of a cluster of 8 SMs (" +
                                                 std::to_string(c.smem) + " bytes per SM)");
     const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1);
-    SPX_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem));
+    {
+        // allow the whole budget: several configurations of one kernel may be
+        // prepared before any of them launches (batched graphs)
+        cudaFuncAttributes fa{};
+        SPX_CUDA(cudaFuncGetAttributes(&fa, kfn));
+        SPX_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(h->smem_optin - fa.sharedSizeBytes)));
+    }
     if (c.cl == 1) {
         int per_sm = 0;
         SPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, c.threads, c.smem));
@@ -536,10 +553,8 @@ void launch_chebyshev(spx_handle *h, bool f64, const Config &c, spx::DevSystem &
     SPX_CUDA(cudaLaunchKernelExC(&lc, kfn, args));
 }
 
-void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be,
-                   const double *d_ga, const double *d_w, double dt, int64_t nsteps,
-                   const spx_options &opt, double2 *d_out, const Config &c, int safe_bounds = 0) {
-    const bool f64 = opt.precision == SPX_FP64;
+// Device buffers of one run (idempotent; called before graph capture too).
+void reserve_run(spx_handle *h, int64_t n_orient, int64_t nsteps, bool f64, const Config &c) {
     const size_t npts = (size_t)nsteps + 1;
     const size_t vec_bytes = f64 ? sizeof(double2) : sizeof(float2);
     h->d_fids.reserve(npts * n_orient * vec_bytes);
@@ -549,6 +564,16 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     h->d_mused.reserve(n_orient);
     h->d_matvecs.reserve(n_orient);
     h->d_halfwidth.reserve(n_orient);
+    const int ngroups = (int)((n_orient + kPowderGroup - 1) / kPowderGroup);
+    h->d_part.reserve((size_t)ngroups * npts);
+}
+
+void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be,
+                   const double *d_ga, const double *d_w, double dt, int64_t nsteps,
+                   const spx_options &opt, double2 *d_out, const Config &c, int safe_bounds = 0, bool timed = true) {
+    const bool f64 = opt.precision == SPX_FP64;
+    const size_t npts = (size_t)nsteps + 1;
+    reserve_run(h, n_orient, nsteps, f64, c);
 
     spx::DevSystem sys{};
     sys.n = h->n; sys.n_pad = h->n_pad; sys.nslices = h->nslices; sys.ell_len = h->ell_len;
@@ -567,13 +592,12 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     run.kused = h->d_kused.p;
     run.mused = h->d_mused.p;
 
-    SPX_CUDA(cudaEventRecord(h->ev[0], h->stream));
+    if (timed) SPX_CUDA(cudaEventRecord(h->ev[0], h->stream));
     launch_chebyshev(h, f64, c, sys, run);
-    SPX_CUDA(cudaEventRecord(h->ev[1], h->stream));
+    if (timed) SPX_CUDA(cudaEventRecord(h->ev[1], h->stream));
     // deterministic FP64 powder sum: fixed groups of orientations, fixed order
-    const int group = 64;
+    const int group = kPowderGroup;
     const int ngroups = (int)((n_orient + group - 1) / group);
-    h->d_part.reserve((size_t)ngroups * npts);
     const dim3 pb(256), pg((unsigned)((npts + 255) / 256), (unsigned)ngroups);
     if (f64)
         spx::powder_partial_kernel<double2><<<pg, pb, 0, h->stream>>>(
@@ -585,7 +609,8 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     spx::powder_combine_kernel<<<dim3((unsigned)((npts + 255) / 256)), dim3(256), 0, h->stream>>>(
         h->d_part.p, ngroups, (int)npts, d_out);
     SPX_CUDA(cudaGetLastError());
-    SPX_CUDA(cudaEventRecord(h->ev[2], h->stream));
+    if (timed) SPX_CUDA(cudaEventRecord(h->ev[2], h->stream));
+    h->stats_timed = timed;
 
     h->stats = spx_stats{};
     h->stats.n_orientations = n_orient;
@@ -619,8 +644,10 @@ spx_status finish_run(spx_handle *h) {
     SPX_CUDA(cudaMemcpy(mv.data(), h->d_matvecs.p, no * sizeof(long long), cudaMemcpyDeviceToHost));
     SPX_CUDA(cudaMemcpy(hw.data(), h->d_halfwidth.p, no * sizeof(double), cudaMemcpyDeviceToHost));
     float ms0 = 0, ms1 = 0;
-    SPX_CUDA(cudaEventElapsedTime(&ms0, h->ev[0], h->ev[1]));
-    SPX_CUDA(cudaEventElapsedTime(&ms1, h->ev[1], h->ev[2]));
+    if (h->stats_timed) {
+        SPX_CUDA(cudaEventElapsedTime(&ms0, h->ev[0], h->ev[1]));
+        SPX_CUDA(cudaEventElapsedTime(&ms1, h->ev[1], h->ev[2]));
+    }
     h->stats.kernel_ms = ms0;
     h->stats.reduce_ms = ms1;
     int64_t failed = 0, matvecs = 0;
@@ -682,6 +709,117 @@ spx_status guarded(spx_handle *h, F f) {
         if (h) h->err = "unknown failure";
         return SPX_ERR_INTERNAL;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner
+// ---------------------------------------------------------------------------
+// Options left at zero take the handle's tuned launch shape for that precision.
+spx_options apply_tuned(const spx_handle *h, spx_options o) {
+    const int p = o.precision == SPX_FP64 ? 1 : 0;
+    if (h->has_tuned[p] && o.threads == 0 && o.cluster == 0 && o.chunk_target == 0.0) {
+        o.threads = h->tuned[p].threads;
+        o.cluster = h->tuned[p].cluster;
+        o.chunk_target = h->tuned[p].chunk_target;
+    }
+    return o;
+}
+
+// shape of a tuning problem: systems with the same key get the same answer
+using TuneKey = std::tuple<int, int, int, int, int, int, int, int>;
+std::mutex g_tune_mutex;
+std::map<TuneKey, spx_options> g_tune_cache;
+
+TuneKey tune_key(const spx_handle *h, double dt, int64_t nsteps, int precision) {
+    const int scale = (int)std::lround(4.0 * std::log2(std::max(h->g_upper * dt, 1e-30)));
+    return TuneKey{h->n, h->ell_len, h->nslices, h->nstreams, h->cplx ? 1 : 0, precision, scale,
+                   (int)std::min<int64_t>(nsteps, 128)};
+}
+
+// Kernel time of one candidate over the sample, or +inf if it cannot run.
+double time_candidate(spx_handle *h, int64_t n, const double *d_al, const double *d_be, const double *d_ga,
+                      const double *d_w, double dt, int64_t nsteps, spx_options o, double2 *d_out) {
+    double best = INFINITY;
+    try {
+        const Config c = choose_config(h, n, dt, nsteps, o, 0);
+        for (int rep = 0; rep < 2; ++rep) {           // first launch also loads the kernel
+            launch_powder(h, n, d_al, d_be, d_ga, d_w, dt, nsteps, o, d_out, c);
+            finish_run(h);
+            best = std::min(best, h->stats.kernel_ms);
+        }
+    } catch (const SpxError &) {
+        SPX_CUDA(cudaStreamSynchronize(h->stream));
+        h->stats_pending = false;
+        return INFINITY;
+    }
+    return best;
+}
+
+spx_options autotune(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be, const double *d_ga,
+                     double dt, int64_t nsteps, int precision) {
+    const TuneKey key = tune_key(h, dt, nsteps, precision);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) return it->second;
+    }
+    spx_options base{};
+    base.precision = precision;
+    // sample: one wave of single-CTA orientations (at most 1024), at most 128 steps
+    const int64_t ns = std::min<int64_t>(nsteps, 128);
+    int64_t n = std::min<int64_t>(n_orient, 1024);
+    {
+        spx_options o1 = base;
+        try {
+            const Config c1 = choose_config(h, n, dt, ns, o1, 0);
+            n = std::min<int64_t>(n, c1.grid);
+        } catch (const SpxError &) {
+            n = std::min<int64_t>(n, h->sm_count);
+        }
+    }
+    DevBuf<double> w;
+    w.reserve((size_t)n);
+    std::vector<double> hw((size_t)n, 1.0 / (double)n);
+    SPX_CUDA(cudaMemcpyAsync(w.p, hw.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    DevBuf<double2> out;
+    out.reserve((size_t)ns + 1);
+    spx_options best = base;
+    double best_t = INFINITY;
+    const int cls[] = {1, 2, 4, 8};
+    for (int cl : cls) {
+        // warps: the default for this cluster size, half, one and a half, and 16
+        spx_options o = base;
+        o.cluster = cl;
+        Config c0{};
+        try {
+            c0 = choose_config(h, n, dt, ns, o, 0);
+        } catch (const SpxError &) {
+            continue;
+        }
+        const int nw0 = c0.threads / 32;
+        std::vector<int> nws = {nw0, std::max(1, nw0 / 2), std::min(16, nw0 + nw0 / 2), 16};
+        std::sort(nws.begin(), nws.end());
+        nws.erase(std::unique(nws.begin(), nws.end()), nws.end());
+        for (int nw : nws) {
+            o.threads = nw * 32;
+            const double t = time_candidate(h, n, d_al, d_be, d_ga, w.p, dt, ns, o, out.p);
+            if (t < best_t) { best_t = t; best = o; }
+        }
+    }
+    if (!std::isfinite(best_t)) throw SpxError(SPX_ERR_UNSUPPORTED, "no launch shape could run this system");
+    // series length per chunk for the best shape
+    const double targets[] = {300.0, 200.0, 100.0, 60.0};
+    spx_options bc = best;
+    for (double tx : targets) {
+        spx_options o = best;
+        o.chunk_target = tx;
+        const double t = time_candidate(h, n, d_al, d_be, d_ga, w.p, dt, ns, o, out.p);
+        if (t < best_t) { best_t = t; bc = o; }
+    }
+    best = bc;
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    g_tune_cache[key] = best;
+    return best;
 }
 
 // ---------------------------------------------------------------------------
@@ -870,6 +1008,7 @@ spx_status spx_run_powder(spx_handle *h, int64_t n_orient, const double *alphas,
         if (opt) o = *opt;
         if (o.precision != SPX_FP32 && o.precision != SPX_FP64)
             throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
+        o = apply_tuned(h, o);
         SPX_CUDA(cudaSetDevice(h->device));
         h->d_grid.reserve(4 * (size_t)n_orient);
         double *g = h->d_grid.p;
@@ -932,6 +1071,7 @@ spx_status spx_run_powder_device(spx_handle *h, int64_t n_orient, const double *
         if (opt) o = *opt;
         if (o.precision != SPX_FP32 && o.precision != SPX_FP64)
             throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
+        o = apply_tuned(h, o);
         SPX_CUDA(cudaSetDevice(h->device));
         const Config c = choose_config(h, n_orient, dt, nsteps, o, 0);
         launch_powder(h, n_orient, d_alphas, d_betas, d_gammas, d_weights, dt, nsteps, o,
@@ -977,5 +1117,208 @@ const char *spx_status_string(spx_status s) {
 const char *spx_last_error(const spx_handle *h) { return h ? h->err.c_str() : "NULL handle"; }
 
 const char *spx_version(void) { return "spinach-gb300 0.1 (sm_103a)"; }
+
+spx_status spx_autotune(spx_handle *h, int64_t n_orient, const double *d_alphas, const double *d_betas,
+                        const double *d_gammas, double dt, int64_t nsteps, int32_t precision, spx_options *best) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        validate_run(h, n_orient, dt, nsteps);
+        if (!d_alphas || !d_betas || !d_gammas) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL device pointer");
+        if (precision != SPX_FP32 && precision != SPX_FP64) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
+        SPX_CUDA(cudaSetDevice(h->device));
+        finish_run(h);
+        const spx_options o = autotune(h, n_orient, d_alphas, d_betas, d_gammas, dt, nsteps, precision);
+        const int p = precision == SPX_FP64 ? 1 : 0;
+        h->tuned[p] = o;
+        h->has_tuned[p] = true;
+        if (best) *best = o;
+    });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched powders: one CUDA graph, one branch per system
+// ---------------------------------------------------------------------------
+struct spx_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> marks;      // fork / join events used while capturing
+    std::vector<spx_handle *> hs;
+    std::vector<int64_t> n_orient;
+    std::string err;
+    bool launched = false;
+};
+
+namespace {
+
+thread_local std::string g_batch_create_error;     // why the last spx_batch_create on this thread failed
+
+template <class F>
+spx_status batch_guarded(spx_batch *b, F f) {
+    try {
+        f();
+        if (b) b->err.clear();
+        return SPX_OK;
+    } catch (const SpxError &e) {
+        if (b) b->err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        if (b) b->err = "host allocation failed";
+        return SPX_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception &e) {
+        if (b) b->err = e.what();
+        return SPX_ERR_INTERNAL;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+spx_status spx_batch_destroy(spx_batch *b) {
+    if (!b) return SPX_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    for (auto e : b->marks) cudaEventDestroy(e);
+    for (auto e : b->ev)
+        if (e) cudaEventDestroy(e);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return SPX_OK;
+}
+
+spx_status spx_batch_create(spx_batch **out, int32_t n, spx_handle *const *handles, const int64_t *n_orient,
+                            const double *const *d_alphas, const double *const *d_betas,
+                            const double *const *d_gammas, const double *const *d_weights, const double *dt,
+                            const int64_t *nsteps, const spx_options *opts, double *const *d_fids) {
+    if (!out || n < 1 || !handles || !n_orient || !d_alphas || !d_betas || !d_gammas || !d_weights || !dt ||
+        !nsteps || !d_fids)
+        return SPX_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    spx_batch *b = new (std::nothrow) spx_batch();
+    if (!b) return SPX_ERR_OUT_OF_MEMORY;
+    const spx_status st = batch_guarded(b, [&] {
+        for (int i = 0; i < n; ++i) {
+            spx_handle *h = handles[i];
+            if (!h) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL handle #" + std::to_string(i));
+            if (h->device != handles[0]->device) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "handles on different devices");
+            if (!d_alphas[i] || !d_betas[i] || !d_gammas[i] || !d_weights[i] || !d_fids[i])
+                throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL device pointer for system #" + std::to_string(i));
+            validate_run(h, n_orient[i], dt[i], nsteps[i]);
+            for (int j = 0; j < i; ++j)
+                if (handles[j] == h) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "a handle appears twice");
+        }
+        b->device = handles[0]->device;
+        SPX_CUDA(cudaSetDevice(b->device));
+        SPX_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+        for (auto &e : b->ev) SPX_CUDA(cudaEventCreate(&e));
+        // launch shapes and buffers first: nothing may allocate while capturing
+        std::vector<Config> cfg(n);
+        std::vector<spx_options> os(n);
+        for (int i = 0; i < n; ++i) {
+            spx_handle *h = handles[i];
+            finish_run(h);
+            spx_options o{};
+            if (opts) o = opts[i];
+            if (o.precision != SPX_FP32 && o.precision != SPX_FP64)
+                throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
+            os[i] = apply_tuned(h, o);
+            cfg[i] = choose_config(h, n_orient[i], dt[i], nsteps[i], os[i], 0);
+            reserve_run(h, n_orient[i], nsteps[i], os[i].precision == SPX_FP64, cfg[i]);
+            SPX_CUDA(cudaStreamSynchronize(h->stream));
+        }
+        // load every kernel the graph will hold before capturing (lazy module loading
+        // would otherwise happen inside the capture)
+        {
+            cudaFuncAttributes fa{};
+            SPX_CUDA(cudaFuncGetAttributes(&fa, reinterpret_cast<const void *>(&spx::powder_partial_kernel<float2>)));
+            SPX_CUDA(cudaFuncGetAttributes(&fa, reinterpret_cast<const void *>(&spx::powder_partial_kernel<double2>)));
+            SPX_CUDA(cudaFuncGetAttributes(&fa, reinterpret_cast<const void *>(&spx::powder_combine_kernel)));
+            for (int i = 0; i < n; ++i)
+                SPX_CUDA(cudaFuncGetAttributes(&fa, select_kernel(os[i].precision == SPX_FP64, handles[i]->cplx,
+                                                                  cfg[i].rmax, cfg[i].cl > 1)));
+        }
+        b->marks.resize(n + 1, nullptr);
+        for (auto &e : b->marks) SPX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        cudaGraph_t graph = nullptr;
+        SPX_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            SPX_CUDA(cudaEventRecord(b->marks[n], b->stream));             // fork
+            for (int i = 0; i < n; ++i) {
+                spx_handle *h = handles[i];
+                SPX_CUDA(cudaStreamWaitEvent(h->stream, b->marks[n], 0));
+                launch_powder(h, n_orient[i], d_alphas[i], d_betas[i], d_gammas[i], d_weights[i], dt[i], nsteps[i],
+                              os[i], reinterpret_cast<double2 *>(d_fids[i]), cfg[i], 0, false);
+                SPX_CUDA(cudaEventRecord(b->marks[i], h->stream));          // join
+                SPX_CUDA(cudaStreamWaitEvent(b->stream, b->marks[i], 0));
+            }
+        } catch (...) {
+            cudaStreamEndCapture(b->stream, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        SPX_CUDA(cudaStreamEndCapture(b->stream, &graph));
+        const cudaError_t ie = cudaGraphInstantiate(&b->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        SPX_CUDA(ie);
+        for (int i = 0; i < n; ++i) {
+            handles[i]->stats_pending = false;
+            b->hs.push_back(handles[i]);
+            b->n_orient.push_back(n_orient[i]);
+        }
+    });
+    if (st != SPX_OK) {
+        g_batch_create_error = b->err;
+        for (int i = 0; i < n && handles; ++i)
+            if (handles[i]) handles[i]->stats_pending = false;
+        spx_batch_destroy(b);
+        return st;
+    }
+    g_batch_create_error.clear();
+    *out = b;
+    return SPX_OK;
+}
+
+spx_status spx_batch_launch(spx_batch *b, void *stream) {
+    if (!b) return SPX_ERR_INVALID_ARGUMENT;
+    return batch_guarded(b, [&] {
+        SPX_CUDA(cudaSetDevice(b->device));
+        cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+        SPX_CUDA(cudaEventRecord(b->ev[0], s));
+        SPX_CUDA(cudaGraphLaunch(b->exec, s));
+        SPX_CUDA(cudaEventRecord(b->ev[1], s));
+        for (size_t i = 0; i < b->hs.size(); ++i) {
+            b->hs[i]->stats_pending = true;
+            b->hs[i]->stats_timed = false;
+            b->hs[i]->last_norient = b->n_orient[i];
+        }
+        b->launched = true;
+    });
+}
+
+spx_status spx_batch_synchronize(spx_batch *b, double *ms) {
+    if (!b) return SPX_ERR_INVALID_ARGUMENT;
+    return batch_guarded(b, [&] {
+        SPX_CUDA(cudaSetDevice(b->device));
+        if (!b->launched) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "batch not launched");
+        SPX_CUDA(cudaEventSynchronize(b->ev[1]));
+        float t = 0.f;
+        SPX_CUDA(cudaEventElapsedTime(&t, b->ev[0], b->ev[1]));
+        if (ms) *ms = t;
+        for (size_t i = 0; i < b->hs.size(); ++i) {
+            try {
+                finish_run(b->hs[i]);
+            } catch (const SpxError &e) {
+                throw SpxError(e.code, "system #" + std::to_string(i) + ": " + e.what());
+            }
+        }
+    });
+}
+
+const char *spx_batch_last_error(const spx_batch *b) { return b ? b->err.c_str() : g_batch_create_error.c_str(); }
 
 }  // extern "C"

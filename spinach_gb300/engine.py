@@ -25,7 +25,7 @@ class SpxCsc(C.Structure):
 
 class SpxOptions(C.Structure):
     _fields_ = [('precision', C.c_int32), ('chunk_steps', C.c_int32), ('threads', C.c_int32),
-                ('cluster', C.c_int32), ('series_tol', C.c_double), ('reserved1', C.c_double)]
+                ('cluster', C.c_int32), ('series_tol', C.c_double), ('chunk_target', C.c_double)]
 
 
 class SpxStats(C.Structure):
@@ -57,6 +57,16 @@ SIGNATURES = {
                                         C.POINTER(SpxOptions), _P]),
     'spx_run_powder_noalloc': (C.c_int, [_P, C.c_int64, _P, _P, _P, _P, C.c_double, C.c_int64,
                                          C.c_int32, _P]),
+    'spx_autotune': (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_double, C.c_int64, C.c_int32,
+                               C.POINTER(SpxOptions)]),
+    'spx_batch_create': (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(_P), C.POINTER(C.c_int64),
+                                   C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_P),
+                                   C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(SpxOptions),
+                                   C.POINTER(_P)]),
+    'spx_batch_launch': (C.c_int, [_P, _P]),
+    'spx_batch_synchronize': (C.c_int, [_P, C.POINTER(C.c_double)]),
+    'spx_batch_destroy': (C.c_int, [_P]),
+    'spx_batch_last_error': (C.c_char_p, [_P]),
     'spx_surrogate_create': (C.c_int, [C.POINTER(_P), C.c_int, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                        C.c_uint64]),
     'spx_surrogate_destroy': (C.c_int, [_P]),
@@ -207,6 +217,15 @@ class Engine:
                                                      d_weights, float(dt), int(nsteps), int(precision),
                                                      d_fid), self.h)
 
+    def autotune(self, d_alphas: int, d_betas: int, d_gammas: int, n_orient: int, dt: float, nsteps: int,
+                 precision: int = FP32) -> dict:
+        """Time candidate launch shapes on device-resident orientations; later
+        runs with default options use the fastest.  Returns the chosen options."""
+        best = SpxOptions()
+        self._check(self.lib.spx_autotune(self.h, n_orient, d_alphas, d_betas, d_gammas, float(dt), int(nsteps),
+                                          precision, C.byref(best)), self.h)
+        return {'threads': best.threads, 'cluster': best.cluster, 'chunk_target': best.chunk_target}
+
     def synchronize(self):
         self._check(self.lib.spx_synchronize(self.h), self.h)
 
@@ -281,3 +300,53 @@ class Surrogate:
     def set_params(self, p: np.ndarray):
         p = np.ascontiguousarray(p, np.float32)
         self._check(self.lib.spx_surrogate_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
+
+
+class Batch:
+    """One CUDA graph running a powder of every engine (spx_batch_*).
+
+    ``runs`` holds, per engine, (engine, n_orient, d_alphas, d_betas, d_gammas,
+    d_weights, dt, nsteps, d_fid, precision) with raw device pointers."""
+
+    def __init__(self, runs):
+        self.lib = load_library()
+        n = len(runs)
+        P = _P * n
+        self.engines = [r[0] for r in runs]
+        hs = P(*[r[0].h for r in runs])
+        no = (C.c_int64 * n)(*[r[1] for r in runs])
+        al, be, ga, wt = (P(*[r[i] for r in runs]) for i in (2, 3, 4, 5))
+        dts = (C.c_double * n)(*[r[6] for r in runs])
+        ns = (C.c_int64 * n)(*[r[7] for r in runs])
+        out = P(*[r[8] for r in runs])
+        opts = (SpxOptions * n)(*[SpxOptions(r[9], 0, 0, 0, 0.0, 0.0) for r in runs])
+        h = C.c_void_p()
+        st = self.lib.spx_batch_create(C.byref(h), n, hs, no, al, be, ga, wt, dts, ns, opts, out)
+        if st != 0:
+            raise SpxError(st, f'{self.lib.spx_status_string(st).decode()}: '
+                               f'{self.lib.spx_batch_last_error(None).decode()}')
+        self.h = h
+
+    def _check(self, st):
+        if st != 0:
+            raise SpxError(st, f'{self.lib.spx_status_string(st).decode()}: '
+                               f'{self.lib.spx_batch_last_error(self.h).decode()}')
+
+    def launch(self, stream: int = 0):
+        self._check(self.lib.spx_batch_launch(self.h, stream or None))
+
+    def synchronize(self) -> float:
+        ms = C.c_double()
+        self._check(self.lib.spx_batch_synchronize(self.h, C.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if getattr(self, 'h', None):
+            self.lib.spx_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
