@@ -208,6 +208,8 @@ def run_gpu(args):
     w = getattr(W, args.workload)()
     L = W.build(w)
     # weak scaling: the grid grows with the ranks and each rank owns one block of it
+    if args.orientations:
+        w.n_orient = args.orientations
     grid = shard_grid(W.zcwn_grid(w.n_orient * world), rank, world)
     eng = E.Engine(local)
     eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
@@ -455,6 +457,8 @@ def main():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-surrogate', action='store_true', help='skip the learned-surrogate leg')
     ap.add_argument('--no-extra', action='store_true', help='skip the c2 and c4 legs')
+    ap.add_argument('--orientations', type=int, default=0,
+                    help='grid size per rank (default: the workload\'s own; smaller for profiling)')
     ap.add_argument('--profile-only', action='store_true',
                     help='warm-up and timed powder runs only (for ncu captures); no FP64/e2e/CPU legs')
     args = ap.parse_args()

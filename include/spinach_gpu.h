@@ -199,13 +199,12 @@ const char *spx_surrogate_last_error(const spx_surrogate *s);
  * Autotuner (no counterpart in the reference, whose step.m/propagator.m pick
  * their branch from fixed tolerances).  Times candidate launch shapes -- CTAs
  * per orientation (1, 2, 4, 8), warps per CTA, series length per chunk -- on
- * one wave of the given device-resident orientations over at most 128 steps,
+ * one wave of the given device-resident orientations over at most 512 steps,
  * and keeps the fastest in the handle: later runs whose options leave
  * threads, cluster and chunk_target at 0 use it.  Results are cached per
  * system shape (dimension, ELL size, value streams, precision, spectral
  * scale) for the life of the process.  best (may be NULL) receives the chosen
- * options.  The dense-propagator alternative is costed, not run: best->
- * reserved fields stay zero; see spx_stats for what a run used.
+ * options; spx_stats reports what a run used.
  */
 spx_status spx_autotune(spx_handle *handle, int64_t n_orient, const double *d_alphas, const double *d_betas,
                         const double *d_gammas, double dt, int64_t nsteps, int32_t precision,

@@ -225,36 +225,23 @@ static __device__ __forceinline__ double2 recur(const double2 &y, double two, co
     return make_double2(two * y.x - tp.x, two * y.y - tp.y);
 }
 
-// Block-wide reductions through a shared scratch of kRedSlots doubles.
-// Every thread of the block must call them (they contain __syncthreads).
-static __device__ double block_sum(double v, double *red) {
+// Block reduction in the value's own type (op 0 sum, 1 max, 2 min); red holds
+// one value per warp.  Every thread of the block must call it.
+template <class T> __device__ __forceinline__ T rmax(T a, T b) { return a > b ? a : b; }
+template <class T> __device__ __forceinline__ T rmin(T a, T b) { return a < b ? a : b; }
+template <int OP, class T>
+static __device__ T block_reduce(T v, T *red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    v = warp_sum_d(v);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const T u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = OP == 0 ? v + u : OP == 1 ? rmax(v, u) : rmin(v, u);
+    }
     __syncthreads();
     if (lane == 0) red[warp] = v;
     __syncthreads();
-    double r = 0.0;
-    for (int w = 0; w < nw; ++w) r += red[w];
-    return r;
-}
-static __device__ double block_max(double v, double *red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    v = warp_max_d(v);
-    __syncthreads();
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    double r = -CUDART_INF;
-    for (int w = 0; w < nw; ++w) r = fmax(r, red[w]);
-    return r;
-}
-static __device__ double block_min(double v, double *red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    v = warp_min_d(v);
-    __syncthreads();
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    double r = CUDART_INF;
-    for (int w = 0; w < nw; ++w) r = fmin(r, red[w]);
+    T r = red[0];
+    for (int w = 1; w < nw; ++w) r = OP == 0 ? r + red[w] : OP == 1 ? rmax(r, red[w]) : rmin(r, red[w]);
     return r;
 }
 
@@ -324,18 +311,21 @@ template <bool CLU> __device__ __forceinline__ void push_peers(const double2 *p,
 // Block reduction followed by a cluster-wide one (op 0 sum, 1 max, 2 min).
 // Partial results go to a double-buffered slot array in every CTA; all CTAs
 // combine them in rank order, so every CTA gets bit-identical results.
-template <bool CLU, int OP>
-__device__ double cluster_reduce(double v, double *red, double *cred, int &par, int crank, int cl) {
-    const double b = OP == 0 ? block_sum(v, red) : OP == 1 ? block_max(v, red) : block_min(v, red);
+template <bool CLU, int OP, class T = double>
+__device__ T cluster_reduce(T v, double *red, double *cred, int &par, int crank, int cl) {
+    const T b = block_reduce<OP>(v, reinterpret_cast<T *>(red));
     if constexpr (!CLU) {
         return b;
     } else {
         double *slot = cred + par * kMaxCluster;
         par ^= 1;
-        if ((int)threadIdx.x < cl) st_cluster(cluster_addr(smem_u32(slot + crank), (int)threadIdx.x), b);
+        if ((int)threadIdx.x < cl) st_cluster(cluster_addr(smem_u32(slot + crank), (int)threadIdx.x), (double)b);
         csync<CLU>();
-        double r = slot[0];
-        for (int j = 1; j < cl; ++j) r = OP == 0 ? r + slot[j] : OP == 1 ? fmax(r, slot[j]) : fmin(r, slot[j]);
+        T r = (T)slot[0];
+        for (int j = 1; j < cl; ++j) {
+            const T u = (T)slot[j];
+            r = OP == 0 ? r + u : OP == 1 ? rmax(r, u) : rmin(r, u);
+        }
         return r;
     }
 }
@@ -425,69 +415,89 @@ static __device__ void wigner_element(int rank, int k, int m, double a, double b
     im = d * sin(ph);
 }
 
-// Extreme eigenvalues of a symmetric tridiagonal matrix by Sturm bisection.
-static __device__ int sturm_count(const double *al, const double *be, int m, double x) {
+// Spectral-bound helpers in FP32: the interval they feed is widened by Ritz
+// residuals and 2% of its width, so FP32 digits suffice, and GB300's FP64
+// division and transcendentals are two orders of magnitude slower.
+
+// Sturm count: eigenvalues of the symmetric tridiagonal matrix below x.
+static __device__ int sturm_count(const float *al, const float *be2, int m, float x) {
     int cnt = 0;
-    double q = al[0] - x;
-    if (q < 0) ++cnt;
+    float q = al[0] - x;
+    if (q < 0.f) ++cnt;
     for (int i = 1; i < m; ++i) {
-        const double den = (q == 0.0) ? 1e-300 : q;
-        q = al[i] - x - be[i - 1] * be[i - 1] / den;
-        if (q < 0) ++cnt;
+        const float den = (q == 0.f) ? 1e-30f : q;
+        q = al[i] - x - be2[i - 1] / den;
+        if (q < 0.f) ++cnt;
     }
     return cnt;
 }
-static __device__ void tridiag_extremes(const double *al, const double *be, int m, double &lo, double &hi) {
-    double glo = CUDART_INF, ghi = -CUDART_INF;
+
+// Extreme eigenvalues of the tridiagonal matrix by one warp: each round
+// evaluates the Sturm count at 32 interior points of the bracket
+// (multisection), shrinking it 33-fold, until it is 1e-6 relative.  All lanes
+// must call; all get the result.
+static __device__ void tridiag_extremes_warp(const double *al_d, const double *be_d, int m, double &lo, double &hi,
+                                             int lane) {
+    float al[kMaxLanczos], be2[kMaxLanczos];
+    float glo = CUDART_INF_F, ghi = -CUDART_INF_F;
     for (int i = 0; i < m; ++i) {
-        double r = 0.0;
-        if (i > 0) r += fabs(be[i - 1]);
-        if (i < m - 1) r += fabs(be[i]);
-        glo = fmin(glo, al[i] - r);
-        ghi = fmax(ghi, al[i] + r);
+        al[i] = (float)al_d[i];
+        be2[i] = (float)(be_d[i] * be_d[i]);
+        float r = 0.f;
+        if (i > 0) r += fabsf((float)be_d[i - 1]);
+        if (i < m - 1) r += fabsf((float)be_d[i]);
+        glo = fminf(glo, al[i] - r);
+        ghi = fmaxf(ghi, al[i] + r);
     }
-    double a = glo, b = ghi;
-    for (int it = 0; it < 100 && b - a > 1e-13 * fmax(fabs(a), fabs(b)) + 1e-300; ++it) {
-        const double x = 0.5 * (a + b);
-        if (sturm_count(al, be, m, x) >= 1) b = x; else a = x;
+    for (int which = 0; which < 2; ++which) {
+        const int target = which == 0 ? 1 : m;      // count >= target: right of the wanted eigenvalue
+        float a = glo, b = ghi;
+        for (int it = 0; it < 12 && b - a > 1e-6f * fmaxf(fabsf(a), fabsf(b)) + 1e-30f; ++it) {
+            const float step = (b - a) * (1.f / 33.f);
+            const bool right = sturm_count(al, be2, m, a + (lane + 1) * step) >= target;
+            const unsigned mask = __ballot_sync(0xffffffffu, right);
+            if (mask == 0u) {
+                a = a + 32.f * step;
+            } else {
+                const int j = __ffs(mask) - 1;
+                b = a + (j + 1) * step;
+                a = a + j * step;
+            }
+        }
+        if (which == 0) lo = b; else hi = a;
     }
-    lo = b;
-    a = glo; b = ghi;
-    for (int it = 0; it < 100 && b - a > 1e-13 * fmax(fabs(a), fabs(b)) + 1e-300; ++it) {
-        const double x = 0.5 * (a + b);
-        if (sturm_count(al, be, m, x) >= m) b = x; else a = x;
-    }
-    hi = a;
 }
 
 // |last component| of the normalised eigenvector of the tridiagonal matrix for
 // eigenvalue theta, by three steps of inverse iteration (Thomas algorithm).
-static __device__ double ritz_last_component(const double *al, const double *be, int m, double theta) {
+static __device__ double ritz_last_component(const double *al_d, const double *be_d, int m, double theta_d) {
     if (m <= 1) return 1.0;
-    double y[kMaxLanczos], c[kMaxLanczos], d[kMaxLanczos];
-    const double shift = theta + 1e-10 * (fabs(theta) + 1e-300);
-    for (int i = 0; i < m; ++i) y[i] = 1.0;
+    float y[kMaxLanczos], c[kMaxLanczos], d[kMaxLanczos];
+    const float theta = (float)theta_d;
+    const float shift = theta + 1e-5f * (fabsf(theta) + 1e-30f);
+    for (int i = 0; i < m; ++i) y[i] = 1.f;
     for (int it = 0; it < 3; ++it) {
         // solve (T - shift) x = y
-        double den = al[0] - shift;
-        if (den == 0.0) den = 1e-300;
-        c[0] = be[0] / den;
+        float den = (float)al_d[0] - shift;
+        if (den == 0.f) den = 1e-30f;
+        c[0] = (float)be_d[0] / den;
         d[0] = y[0] / den;
         for (int i = 1; i < m; ++i) {
-            den = (al[i] - shift) - be[i - 1] * c[i - 1];
-            if (den == 0.0) den = 1e-300;
-            c[i] = (i < m - 1) ? be[i] / den : 0.0;
-            d[i] = (y[i] - be[i - 1] * d[i - 1]) / den;
+            den = ((float)al_d[i] - shift) - (float)be_d[i - 1] * c[i - 1];
+            if (den == 0.f) den = 1e-30f;
+            c[i] = (i < m - 1) ? (float)be_d[i] / den : 0.f;
+            d[i] = (y[i] - (float)be_d[i - 1] * d[i - 1]) / den;
         }
         y[m - 1] = d[m - 1];
         for (int i = m - 2; i >= 0; --i) y[i] = d[i] - c[i] * y[i + 1];
-        double nrm = 0.0;
+        float nrm = 0.f;
         for (int i = 0; i < m; ++i) nrm += y[i] * y[i];
-        nrm = sqrt(nrm);
-        if (!(nrm > 0.0) || !isfinite(nrm)) return 1.0;
-        for (int i = 0; i < m; ++i) y[i] /= nrm;
+        nrm = sqrtf(nrm);
+        if (!(nrm > 0.f) || !isfinite(nrm)) return 1.0;
+        const float inv = 1.f / nrm;
+        for (int i = 0; i < m; ++i) y[i] *= inv;
     }
-    return fabs(y[m - 1]);
+    return fabsf(y[m - 1]);
 }
 
 // ---------------------------------------------------------------------------
@@ -527,12 +537,15 @@ static __device__ __forceinline__ void acc_add64(double2 &acc, const double2 &a,
 
 // Number of Chebyshev/Bessel terms after which |J_k(x)| * e^{k*lg} < tol
 // (Debye-type bound (e x / 2k)^k / sqrt(2 pi k), conservative for k > x).
+// Evaluated in FP32 (it only sizes the series; the exact tail is checked
+// against the Bessel column itself).
 static __device__ int series_terms(double x, double lg, double tol, int kcap) {
     if (!(x > 0.0)) return 1;
-    const double ltol = log(tol);
+    const float ltol = (float)log(tol), xf = (float)x, lgf = (float)lg;
     int k = max(1, (int)ceil(x) + 1);
     while (k < kcap) {
-        const double lt = -0.5 * log(2.0 * CUDART_PI * k) + k * log(2.718281828459045 * x / (2.0 * k)) + k * lg;
+        const float kf = (float)k;
+        const float lt = -0.5f * __logf(6.2831853f * kf) + kf * __logf(2.7182818f * xf / (2.f * kf)) + kf * lgf;
         if (lt < ltol) break;
         ++k;
     }
@@ -559,8 +572,9 @@ static __device__ void bessel_column(double *table, int M, int j, int K, double 
     int kst = base + 20 + (int)sqrt(160.0 * base);
     kst += kst & 1;
     double jp1 = 0.0, jk = 1e-30, norm = 0.0;
+    const double two_over_x = 2.0 / x;                // one division per column
     for (int k = kst; k >= 1; --k) {
-        const double jm1 = (2.0 * k / x) * jk - jp1;
+        const double jm1 = (k * two_over_x) * jk - jp1;
         jp1 = jk;
         jk = jm1;                                   // J_{k-1}, unnormalised
         const int km1 = k - 1;
@@ -577,6 +591,10 @@ static __device__ void bessel_column(double *table, int M, int j, int K, double 
     for (int k = 1; k < kneed; ++k) col[k * ld] = 2.0 * col[k * ld] * inv;
     for (int k = kneed; k < K; ++k) col[k * ld] = 0.0;
 }
+
+// Real part of a diagonal entry in the working precision
+__device__ __forceinline__ float diag_re(const PackD &d) { return d.h.x + d.l.x; }
+__device__ __forceinline__ double diag_re(const double2 &d) { return d.x; }
 
 // Moment of one term from the per-warp partials in slot `part` (nwarps
 // entries), by one warp: lane w takes warp w's partial, then a fixed
@@ -733,7 +751,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             double rad = 0.0;
             for (int c = 0; c < w; ++c) {
                 const double2 v = unpack(s_val[off + c * 32 + lane]);
-                rad += sqrt(v.x * v.x + v.y * v.y);
+                rad += CPLX ? sqrt(v.x * v.x + v.y * v.y) : fabs(v.x);
             }
             const double dr = unpack(s_diag[lrow]).x;
             gmax = fmax(gmax, dr + rad);
@@ -746,20 +764,23 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         imax = cluster_reduce<CLU, 1>(imax, s_red, s_cred, par, crank, CL);
 
         // ---- 3. Lanczos bounds on the Hermitian part ---------------------------
+        // (in the working precision: the bounds are widened afterwards)
         Vec q_prev[RMAX], q_cur[RMAX];
-        double nrm2 = 0.0;
+        Real nrm2 = 0;
 #pragma unroll
         for (int r = 0; r < RMAX; ++r) {
             const int row = (r < rows_per_lane) ? row0 + s_wsl[warp * RMAX + r] * 32 + lane : n;
             const bool own = row < n;
-            const double v = own ? 1.0 + 0.37 * sin(1.7 * row + 0.3) : 0.0;
-            q_cur[r] = tovec(make_double2(v, 0.0), Vec());
+            // deterministic pseudo-random start vector in [0.63, 1.37]
+            const Real v = own ? (Real)(1.0f + 0.37f * __sinf(1.7f * (float)(row % 4096) + 0.3f)) : (Real)0;
+            q_cur[r].x = v;
+            q_cur[r].y = 0;
             q_prev[r] = vzero<Vec>();
             nrm2 += v * v;
         }
-        nrm2 = cluster_reduce<CLU, 0>(nrm2, s_red, s_cred, par, crank, CL);
+        nrm2 = cluster_reduce<CLU, 0, Real>(nrm2, s_red, s_cred, par, crank, CL);
         {
-            const double inv = 1.0 / sqrt(nrm2);
+            const Real inv = (Real)1 / sqrt(nrm2);
 #pragma unroll
             for (int r = 0; r < RMAX; ++r) {
                 if (r >= rows_per_lane) break;
@@ -770,12 +791,12 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             }
         }
         int m_eff = 0;
-        double beta_prev = 0.0;
+        Real beta_prev = 0;
         const int lits = min(run.lanczos_its, min(kMaxLanczos, n));
         for (int j = 0; j < lits; ++j) {
             csync<CLU>();
             Vec wv[RMAX];
-            double alpha_p = 0.0;
+            Real alpha_p = 0;
 #pragma unroll
             for (int r = 0; r < RMAX; ++r) {
                 wv[r] = vzero<Vec>();
@@ -789,32 +810,32 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     const int e = off + c * 32 + lane;
                     mac(y, s_val[e], s_xa[s_col[e]]);
                 }
-                const double dr = unpack(s_diag[lrow]).x;
-                y.x += (Real)dr * q_cur[r].x;
-                y.y += (Real)dr * q_cur[r].y;
-                y.x -= (Real)beta_prev * q_prev[r].x;
-                y.y -= (Real)beta_prev * q_prev[r].y;
+                const Real dr = diag_re(s_diag[lrow]);
+                y.x += dr * q_cur[r].x;
+                y.y += dr * q_cur[r].y;
+                y.x -= beta_prev * q_prev[r].x;
+                y.y -= beta_prev * q_prev[r].y;
                 wv[r] = y;
-                alpha_p += (double)q_cur[r].x * y.x + (double)q_cur[r].y * y.y;
+                alpha_p += q_cur[r].x * y.x + q_cur[r].y * y.y;
             }
-            const double alpha = cluster_reduce<CLU, 0>(alpha_p, s_red, s_cred, par, crank, CL);
-            double b2 = 0.0;
+            const Real alpha = cluster_reduce<CLU, 0, Real>(alpha_p, s_red, s_cred, par, crank, CL);
+            Real b2 = 0;
 #pragma unroll
             for (int r = 0; r < RMAX; ++r) {
-                wv[r].x -= (Real)alpha * q_cur[r].x;
-                wv[r].y -= (Real)alpha * q_cur[r].y;
-                b2 += (double)wv[r].x * wv[r].x + (double)wv[r].y * wv[r].y;
+                wv[r].x -= alpha * q_cur[r].x;
+                wv[r].y -= alpha * q_cur[r].y;
+                b2 += wv[r].x * wv[r].x + wv[r].y * wv[r].y;
             }
-            const double beta = sqrt(cluster_reduce<CLU, 0>(b2, s_red, s_cred, par, crank, CL));
-            if (tid == 0) { s_al[j] = alpha; s_be[j] = beta; }
+            const Real beta = sqrt(cluster_reduce<CLU, 0, Real>(b2, s_red, s_cred, par, crank, CL));
+            if (tid == 0) { s_al[j] = (double)alpha; s_be[j] = (double)beta; }
             m_eff = j + 1;
-            if (!(beta > 1e-12 * (fabs(alpha) + 1e-300))) break;   // invariant subspace
-            const double inv = 1.0 / beta;
+            if (!(beta > (Real)1e-12 * (fabs(alpha) + (Real)1e-30))) break;   // invariant subspace
+            const Real inv = (Real)1 / beta;
 #pragma unroll
             for (int r = 0; r < RMAX; ++r) {
                 q_prev[r] = q_cur[r];
-                q_cur[r].x = wv[r].x * (Real)inv;
-                q_cur[r].y = wv[r].y * (Real)inv;
+                q_cur[r].x = wv[r].x * inv;
+                q_cur[r].y = wv[r].y * inv;
                 if (r < rows_per_lane) {
                     Vec *dstp = &s_xb[row0 + s_wsl[warp * RMAX + r] * 32 + lane];
                     *dstp = q_cur[r];
@@ -825,10 +846,15 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             beta_prev = beta;
         }
         __syncthreads();
-        if (tid == 0) {
+        if (warp == 0) {
             double tlo, thi;
-            tridiag_extremes(s_al, s_be, m_eff, tlo, thi);
+            tridiag_extremes_warp(s_al, s_be, m_eff, tlo, thi, lane);
             const double bl = fabs(s_be[m_eff - 1]);
+            // Ritz vectors' last components: lane 0 for the top, lane 1 for the bottom
+            double rr = 0.0;
+            if (!run.safe_bounds && lane < 2) rr = bl * ritz_last_component(s_al, s_be, m_eff, lane == 0 ? thi : tlo);
+            const double rhi = __shfl_sync(0xffffffffu, rr, 0), rlo = __shfl_sync(0xffffffffu, rr, 1);
+          if (lane == 0) {
             double hi, lo;
             if (run.safe_bounds) {
                 // theta +- beta_m (Zhou-Saad upper bound), clamped by Gershgorin
@@ -838,8 +864,6 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 // Ritz value plus its residual |beta_m * y_m| and 2% of the width;
                 // the propagation checks the norm and the host retries with the
                 // safe bound if this was too tight
-                const double rhi = bl * ritz_last_component(s_al, s_be, m_eff, thi);
-                const double rlo = bl * ritz_last_component(s_al, s_be, m_eff, tlo);
                 const double wid = thi - tlo;
                 hi = fmin(thi + rhi + 0.02 * wid, gmax);
                 lo = fmax(tlo - rlo - 0.02 * wid, gmin);
@@ -868,13 +892,19 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             const int Kb = min(run.Kmax, max(2, series_terms(x, lg, run.tol, run.Kmax + 1)) + 2);
             bessel_column(table, Mo, Mo, Kb, half, run.dt);
             int K = 2;
-            for (int k = Kb - 1; k >= 2; --k) {
-                if (fabs(table[(size_t)k * (Mo + 1) + Mo]) * exp(k * lg) > run.tol) { K = k + 1; break; }
+            {
+                // growth e^{k lg} of term k, stepped down from k = Kb-1 (one exp)
+                double grow = exp((Kb - 1) * lg);
+                const double shrink = exp(-lg);
+                for (int k = Kb - 1; k >= 2; --k, grow *= shrink) {
+                    if (fabs(table[(size_t)k * (Mo + 1) + Mo]) * grow > run.tol) { K = k + 1; break; }
+                }
             }
             K = min(K + 2, Kb);
             if (Kb >= run.Kmax && series_terms(x, lg, run.tol, run.Kmax + 1) + 2 > run.Kmax && K >= Kb - 2) K = run.Kmax + 1;
             s_int[0] = K;
             s_int[1] = (K > run.Kmax) ? 1 : 0;
+          }
         }
         csync<CLU>();
         // every CTA of a cluster takes rank 0's decisions, so their control flow

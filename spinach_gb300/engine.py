@@ -185,7 +185,7 @@ class Engine:
 
     def run(self, alphas, betas, gammas, weights, dt: float, nsteps: int, precision: int = FP32,
             per_orientation: bool = False, chunk_steps: int = 0, threads: int = 0,
-            series_tol: float = 0.0, cluster: int = 0) -> PowderResult:
+            series_tol: float = 0.0, cluster: int = 0, chunk_target: float = 0.0) -> PowderResult:
         al = np.ascontiguousarray(alphas, np.float64)
         be = np.ascontiguousarray(betas, np.float64)
         ga = np.ascontiguousarray(gammas, np.float64)
@@ -193,7 +193,7 @@ class Engine:
         no = al.size
         fid = np.zeros(2 * (nsteps + 1))
         fids = np.zeros(2 * (nsteps + 1) * no) if per_orientation else None
-        opt = SpxOptions(precision, chunk_steps, threads, cluster, series_tol, 0.0)
+        opt = SpxOptions(precision, chunk_steps, threads, cluster, series_tol, chunk_target)
         self._check(self.lib.spx_run_powder(self.h, no, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
                                             float(dt), int(nsteps), C.byref(opt), _dptr(fid),
                                             _dptr(fids) if fids is not None else None), self.h)
