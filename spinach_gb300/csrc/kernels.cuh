@@ -48,22 +48,25 @@ enum DeviceStatus : int {
     kDevTooManyRows = 4,
 };
 
-// FP32 shared-memory value layouts, pre-packed for f32x2 arithmetic:
-//   PackR  real off-diagonal value v = hi + lo as (hi, hi, lo, lo)
-//   PackC  complex value: h = (re_hi, re_hi, -im_hi, im_hi), l = same for lo parts
-//   PackD  diagonal d: h = (re_hi, re_hi, -im, im), l = (re_lo, re_lo, 0, 0)
-//   PackA  complex series coefficient, laid out as PackC
-struct __align__(16) PackR { float4 v; };
+// FP32 shared-memory layouts.  Liouvillian values are stored compactly (hi
+// + lo float pairs) and expanded into f32x2 operand pairs in registers:
+//   ValR  real off-diagonal value (hi, lo)                          8 B
+//   ValC  complex value (re_hi, im_hi, re_lo, im_lo)               16 B
+//   DgS   diagonal (re_hi, re_lo, im, 0)                           16 B
+// Series coefficients are few and read by every row, so they stay pre-packed:
+//   PackA  h = (re_hi, re_hi, -im_hi, im_hi), l = same for the lo parts
+struct __align__(8) ValR { float hi, lo; };
+struct __align__(16) ValC { float rh, ih, rl, il; };
+struct __align__(16) DgS { float rh, rl, im, pad; };
 struct __align__(16) PackC { float4 h, l; };
-struct __align__(16) PackD { float4 h, l; };
 typedef PackC PackA;
 
 // ---------------------------------------------------------------------------
 // Precision policies
 // ---------------------------------------------------------------------------
 template <bool F64, bool CPLX> struct Prec;
-template <> struct Prec<false, false> { using Vec = float2;  using Val = PackR;  using Dg = PackD;   using Af = PackA;   using Real = float;  using Acc = float2; };
-template <> struct Prec<false, true>  { using Vec = float2;  using Val = PackC;  using Dg = PackD;   using Af = PackA;   using Real = float;  using Acc = float2; };
+template <> struct Prec<false, false> { using Vec = float2;  using Val = ValR;   using Dg = DgS;     using Af = PackA;   using Real = float;  using Acc = float2; };
+template <> struct Prec<false, true>  { using Vec = float2;  using Val = ValC;   using Dg = DgS;     using Af = PackA;   using Real = float;  using Acc = float2; };
 template <> struct Prec<true, false>  { using Vec = double2; using Val = double;  using Dg = double2; using Af = double2; using Real = double; using Acc = double2; };
 template <> struct Prec<true, true>   { using Vec = double2; using Val = double2; using Dg = double2; using Af = double2; using Real = double; using Acc = double2; };
 
@@ -71,10 +74,15 @@ static __device__ __forceinline__ void split(double v, float &hi, float &lo) {
     hi = (float)v;
     lo = (float)(v - (double)hi);
 }
-static __device__ __forceinline__ void pack(PackR &o, double re, double) {
-    float h, l;
-    split(re, h, l);
-    o.v = make_float4(h, h, l, l);
+static __device__ __forceinline__ void pack(ValR &o, double re, double) { split(re, o.hi, o.lo); }
+static __device__ __forceinline__ void pack(ValC &o, double re, double im) {
+    split(re, o.rh, o.rl);
+    split(im, o.ih, o.il);
+}
+static __device__ __forceinline__ void pack(DgS &o, double re, double im) {
+    split(re, o.rh, o.rl);
+    o.im = (float)im;
+    o.pad = 0.f;
 }
 static __device__ __forceinline__ void pack(PackC &o, double re, double im) {
     float rh, rl, ih, il;
@@ -83,18 +91,11 @@ static __device__ __forceinline__ void pack(PackC &o, double re, double im) {
     o.h = make_float4(rh, rh, -ih, ih);
     o.l = make_float4(rl, rl, -il, il);
 }
-static __device__ __forceinline__ void pack(PackD &o, double re, double im) {
-    float rh, rl;
-    split(re, rh, rl);
-    const float fi = (float)im;
-    o.h = make_float4(rh, rh, -fi, fi);
-    o.l = make_float4(rl, rl, 0.f, 0.f);
+static __device__ __forceinline__ double2 unpack(const ValR &v) { return make_double2((double)v.hi + (double)v.lo, 0.0); }
+static __device__ __forceinline__ double2 unpack(const ValC &v) {
+    return make_double2((double)v.rh + (double)v.rl, (double)v.ih + (double)v.il);
 }
-static __device__ __forceinline__ double2 unpack(const PackR &v) { return make_double2((double)v.v.x + (double)v.v.z, 0.0); }
-static __device__ __forceinline__ double2 unpack(const PackC &v) {
-    return make_double2((double)v.h.x + (double)v.l.x, (double)v.h.w + (double)v.l.w);
-}
-static __device__ __forceinline__ double2 unpack(const PackD &v) { return make_double2((double)v.h.x + (double)v.l.x, (double)v.h.w); }
+static __device__ __forceinline__ double2 unpack(const DgS &v) { return make_double2((double)v.rh + (double)v.rl, (double)v.im); }
 static __device__ __forceinline__ void pack(double &o, double re, double) { o = re; }
 static __device__ __forceinline__ void pack(double2 &o, double re, double im) { o = make_double2(re, im); }
 
@@ -103,16 +104,16 @@ static __device__ __forceinline__ double2 unpack(const double2 &v) { return v; }
 
 // y += v * x  (value times complex state; plain arithmetic, used outside the
 // propagation loop and in the FP64 path)
-static __device__ __forceinline__ void mac(float2 &y, const PackR &v, const float2 x) {
-    y.x = fmaf(v.v.x, x.x, y.x); y.y = fmaf(v.v.x, x.y, y.y);
-    y.x = fmaf(v.v.z, x.x, y.x); y.y = fmaf(v.v.z, x.y, y.y);
+static __device__ __forceinline__ void mac(float2 &y, const ValR &v, const float2 x) {
+    y.x = fmaf(v.hi, x.x, y.x); y.y = fmaf(v.hi, x.y, y.y);
+    y.x = fmaf(v.lo, x.x, y.x); y.y = fmaf(v.lo, x.y, y.y);
 }
-static __device__ __forceinline__ void mac(float2 &y, const PackC &v, const float2 x) {
-    // h = (re, re, -im, im): re*x + (-im*x.y, im*x.x)
-    y.x = fmaf(v.h.x, x.x, y.x); y.y = fmaf(v.h.y, x.y, y.y);
-    y.x = fmaf(v.h.z, x.y, y.x); y.y = fmaf(v.h.w, x.x, y.y);
-    y.x = fmaf(v.l.x, x.x, y.x); y.y = fmaf(v.l.y, x.y, y.y);
-    y.x = fmaf(v.l.z, x.y, y.x); y.y = fmaf(v.l.w, x.x, y.y);
+static __device__ __forceinline__ void mac(float2 &y, const ValC &v, const float2 x) {
+    // (re + i im) x = re*x + (-im*x.y, im*x.x)
+    y.x = fmaf(v.rh, x.x, y.x); y.y = fmaf(v.rh, x.y, y.y);
+    y.x = fmaf(-v.ih, x.y, y.x); y.y = fmaf(v.ih, x.x, y.y);
+    y.x = fmaf(v.rl, x.x, y.x); y.y = fmaf(v.rl, x.y, y.y);
+    y.x = fmaf(-v.il, x.y, y.x); y.y = fmaf(v.il, x.x, y.y);
 }
 static __device__ __forceinline__ void mac(double2 &y, const double &v, const double2 x) {
     y.x = fma(v, x.x, y.x); y.y = fma(v, x.y, y.y);
@@ -593,7 +594,7 @@ static __device__ void bessel_column(double *table, int M, int j, int K, double 
 }
 
 // Real part of a diagonal entry in the working precision
-__device__ __forceinline__ float diag_re(const PackD &d) { return d.h.x + d.l.x; }
+__device__ __forceinline__ float diag_re(const DgS &d) { return d.rh + d.rl; }
 __device__ __forceinline__ double diag_re(const double2 &d) { return d.x; }
 
 // Moment of one term from the per-warp partials in slot `part` (nwarps
@@ -1127,11 +1128,11 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                         C[r] = 0ull;
                         Lo[r] = 0ull;
                         if (r < nr) {
-                            const PackD d = s_diag[r_row[r] - row0];
+                            const DgS d = s_diag[r_row[r] - row0];
                             const f2x X = tc[r];
-                            Y[r] = mul2(lo2(d.h), X);
-                            kahan_add2(Y[r], C[r], mul2(hi2(d.h), swap2(X)));
-                            Lo[r] = mul2(lo2(d.l), X);
+                            Y[r] = mul2(f2pk(d.rh, d.rh), X);
+                            kahan_add2(Y[r], C[r], mul2(f2pk(-d.im, d.im), swap2(X)));
+                            Lo[r] = mul2(f2pk(d.rl, d.rl), X);
                         }
                     }
                     int c = 0;
@@ -1145,16 +1146,16 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                                     const int e = r_off[r] + c * 32;
                                     const f2x X = src[s_col[e]];
                                     if constexpr (CPLX) {
-                                        const PackC v = s_val[e];
+                                        const ValC v = s_val[e];
                                         const f2x XS = swap2(X);
-                                        kahan_add2(Y[r], C[r], mul2(lo2(v.h), X));
-                                        kahan_add2(Y[r], C[r], mul2(hi2(v.h), XS));
-                                        Lo[r] = fma2(lo2(v.l), X, Lo[r]);
-                                        Lo[r] = fma2(hi2(v.l), XS, Lo[r]);
+                                        kahan_add2(Y[r], C[r], mul2(f2pk(v.rh, v.rh), X));
+                                        kahan_add2(Y[r], C[r], mul2(f2pk(-v.ih, v.ih), XS));
+                                        Lo[r] = fma2(f2pk(v.rl, v.rl), X, Lo[r]);
+                                        Lo[r] = fma2(f2pk(-v.il, v.il), XS, Lo[r]);
                                     } else {
-                                        const PackR v = s_val[e];
-                                        kahan_add2(Y[r], C[r], mul2(lo2(v.v), X));
-                                        Lo[r] = fma2(hi2(v.v), X, Lo[r]);
+                                        const ValR v = s_val[e];
+                                        kahan_add2(Y[r], C[r], mul2(f2pk(v.hi, v.hi), X));
+                                        Lo[r] = fma2(f2pk(v.lo, v.lo), X, Lo[r]);
                                     }
                                 }
                             }

@@ -54,7 +54,7 @@ def test_cluster_matches_single_cta(engine_lib):
 
 def test_c4_full_basis_dim2736(engine_lib):
     """EPR radical (e + 14N + 10 1H, IK-1(3), dim 2736, complex off-diagonal
-    values): too large for one SM, runs on a cluster."""
+    values): FP32 fits one SM, FP64 needs a cluster; both shapes checked."""
     from spinach_gb300 import engine as E, workloads as W
     w = W.c4()
     gold = np.load(os.path.join(GOLD, 'c4_orient_krylov_fp64.npz'))
@@ -62,11 +62,14 @@ def test_c4_full_basis_dim2736(engine_lib):
     sel = gold['sel']
     wt = np.full(sel.size, 1.0 / sel.size)
     eng = _engine(w)
-    for prec, tol in ((E.FP64, 1e-10), (E.FP32, 1e-5)):
-        res = eng.run(al[sel], be[sel], ga[sel], wt, w.dt, w.nsteps, precision=prec, per_orientation=True)
-        assert res.stats['cluster'] > 1 and res.stats['real_offdiag'] == 0
+    for prec, tol, cluster in ((E.FP64, 1e-10, 0), (E.FP32, 1e-5, 0), (E.FP32, 1e-5, 2)):
+        res = eng.run(al[sel], be[sel], ga[sel], wt, w.dt, w.nsteps, precision=prec, per_orientation=True,
+                      cluster=cluster)
+        assert res.stats['real_offdiag'] == 0
+        if cluster:
+            assert res.stats['cluster'] == cluster
         for i in range(sel.size):
-            assert rel_err(res.fids[i], gold['fids'][i]) <= tol, (prec, i)
+            assert rel_err(res.fids[i], gold['fids'][i]) <= tol, (prec, cluster, i)
         assert rel_err(res.fid, gold['fids'].mean(axis=0)) <= tol
 
 
