@@ -455,19 +455,28 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     // sharing an orientation (rows split between them).
     c.fixed = opt.chunk_steps > 0;
     const double lg = (h->g_upper > 0) ? 2.0 * h->max_im_diag / (h->g_upper / 4.0) : 0.0;
+    // c1 (chunks of any length): x_c = 300 -> 76.8 ms, 450 -> 81.0 ms, 600 -> 84.3 ms
     std::vector<double> targets = {300.0, 200.0, 150.0, 100.0, 60.0, 30.0};
     if (opt.chunk_target > 0) targets = {opt.chunk_target};
     bool placed = false;
     const int cls[] = {1, 2, 4, 8};
+    // first pass: at most 4 rows per lane (8 spill registers); second pass: 8 on one CTA
+    for (int pass = 0; pass < 2 && !placed; ++pass)
     for (int cl : cls) {
         if (opt.cluster > 0 && cl != opt.cluster) continue;       // cluster size set by the caller
+        if (pass == 1 && cl > 1) continue;
         if (!partition_slices(h, cl, c)) continue;
-        // warps: about two and a half 32-row slices per warp, at most 16 warps
-        // (c1: 16 warps 118.9 ms, 13 warps 121.3 ms per 1000-orientation powder)
-        int nwarps = std::min(16, std::max(1, (2 * c.nsl_loc + 4) / 5));
-        if (opt.threads > 0) nwarps = std::max(1, std::min(16, opt.threads / 32));
+        // warps: one per 32-row slice, at most 16 (c1: 16 warps 118.9 ms,
+        // 13 warps 121.3 ms per 1000-orientation powder; c2 dim 4096 on 8-CTA
+        // clusters: 16 warps 536 ms, 9 warps 584 ms)
+        // a smaller CTA is tried before a larger cluster (its reconstruction
+        // scratch is smaller), if the rows per lane stay within the limit
+        std::vector<int> nws = {std::min(16, std::max(1, c.nsl_loc))};
+        if (opt.threads > 0) nws = {std::max(1, std::min(16, opt.threads / 32))};
+        else if (nws[0] > 4) nws.push_back((nws[0] + 1) / 2);
+        for (int nwarps : nws) {
         const int rows = (c.nsl_loc + nwarps - 1) / nwarps;
-        if (rows > (cl > 1 ? 4 : 8)) continue;
+        if (rows > (pass == 0 ? 4 : 8)) continue;
         c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 8;
         c.threads = nwarps * 32;
         // dynamic shared memory may use what the kernel's static arrays leave
@@ -487,6 +496,8 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
             c.smem = smem_for(h, f64, c.nsl_loc, c.ell_loc, c.Kmax, c.M, c.threads);
             if (c.smem <= budget) { placed = true; break; }
             if (c.fixed) break;
+        }
+        if (placed) break;
         }
         if (placed) break;
     }
@@ -810,7 +821,7 @@ spx_options autotune(spx_handle *h, int64_t n_orient, const double *d_al, const 
     }
     if (!std::isfinite(best_t)) throw SpxError(SPX_ERR_UNSUPPORTED, "no launch shape could run this system");
     // series length per chunk for the best shape
-    const double targets[] = {300.0, 150.0, 60.0};
+    const double targets[] = {450.0, 300.0, 150.0, 60.0};
     spx_options bc = best;
     for (double tx : targets) {
         spx_options o = best;

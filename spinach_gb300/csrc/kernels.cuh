@@ -880,8 +880,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             int Mo = M;
             if (!run.fixed_chunk) {
                 const double target = run.chunk_x / (half * run.dt);
-                Mo = 1;
-                while (Mo * 2 <= target && Mo * 2 <= M) Mo *= 2;
+                Mo = (int)fmax(1.0, fmin((double)M, floor(target)));
             }
             Mo = min(Mo, nsteps + 1);
             s_int[2] = Mo;
@@ -940,6 +939,19 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         // ---- 5. Bessel table J_k(s j dt), j = 0..M --------------------------
         for (int j = tid; j < (CLU ? Mo + 1 : Mo); j += blockDim.x) bessel_column(table, Mo, j, K, half, run.dt);
         __syncthreads();
+        // the last chunk only reaches j_last steps: its series can stop where the
+        // Bessel column of j_last (times the growth from Im L) drops below tol
+        const int nchunks = (nsteps + Mo) / Mo;      // ceil((nsteps+1)/Mo)
+        if (tid == 0) {
+            const int j_last = nsteps - (nchunks - 1) * Mo;
+            const double lg = 2.0 * imax / half;
+            int kl = 2;
+            double grow = exp((K - 1) * lg);
+            const double shrink = exp(-lg);
+            for (int k = K - 1; k >= 2; --k, grow *= shrink)
+                if (fabs(table[(size_t)k * (Mo + 1) + j_last]) * grow > run.tol) { kl = k + 1; break; }
+            s_int[3] = min(K, kl + 2);
+        }
         // series coefficients of one chunk (tau = M dt), centre phase folded in
         {
             const double tau = Mo * run.dt;
@@ -961,7 +973,9 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 s_phase[j] = tovec(make_double2(cos(ph), sin(ph)), Vec());
             }
         }
-        __syncthreads();          // coefficients and phases visible before the first term
+        csync<CLU>();             // coefficients and phases visible before the first term
+        int K_last = s_int[3];
+        if constexpr (CLU) K_last = ld_cluster_s32(cluster_addr(smem_u32(&s_int[3]), 0));
 
         // ---- 6. chunked Chebyshev propagation with fused coil projection -------
         // Each lane owns up to RMAX rows (one per 32-row slice of its warp); the
@@ -982,7 +996,6 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 r_w[r] = (s_soff[sl + 1] - s_soff[sl]) >> 5;
             }
         }
-        const int nchunks = (nsteps + Mo) / Mo;      // ceil((nsteps+1)/Mo)
         Vec *fid_out = reinterpret_cast<Vec *>(run.fids) + (size_t)o * (nsteps + 1);
         int status = kDevOk;
         [[maybe_unused]] Vec t_prev[RMAX], t_cur[RMAX], acc[RMAX], cc[RMAX];
@@ -1003,8 +1016,11 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 cim[r] = f2pk((float)c0.y, -(float)c0.y);
             }
         }
+        long long mv = 0;
         for (int a = 0; a < nchunks && status == kDevOk; ++a) {
             const bool advance = (a + 1 < nchunks);
+            const int Kc = advance ? K : K_last;          // terms of this chunk
+            mv += Kc - 1;
             double start_n2 = 0.0, end_n2 = 0.0;
             if constexpr (F64) {
                 // k = 0: t0 = rho
@@ -1027,7 +1043,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 }
                 csync<CLU>();
                 // k = 1 .. K-1: t_k = (k==1 ? 1 : 2) L~ t_{k-1} - t_{k-2}
-                for (int k = 1; k < K; ++k) {
+                for (int k = 1; k < Kc; ++k) {
                     const Vec *src = (k & 1) ? s_xa : s_xb;
                     Vec *dst = (k & 1) ? s_xb : s_xa;
                     const Real two = (k == 1) ? (Real)1 : (Real)2;
@@ -1112,7 +1128,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     if (lane == 0) s_part[warp] = m;
                 }
                 csync<CLU>();
-                for (int k = 1; k < K; ++k) {
+                for (int k = 1; k < Kc; ++k) {
                     const f2x *src = reinterpret_cast<const f2x *>((k & 1) ? s_xa : s_xb);
                     f2x *dst = reinterpret_cast<f2x *>((k & 1) ? s_xb : s_xa);
                     const f2x TW = (k == 1) ? ONE : TWO;
@@ -1201,8 +1217,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             }
             // moment of the last term (the others were folded inside the loop)
             if (warp == nwarps - 1) {
-                if (scoil) coil_moment(((K - 1) & 1) ? s_xb : s_xa, sys.ncoil, s_crow, s_cval, lane, &s_mu[K - 1]);
-                else reduce_term(s_part + ((K - 1) & 1) * nwarps, nwarps, lane, &s_mu[K - 1]);
+                if (scoil) coil_moment(((Kc - 1) & 1) ? s_xb : s_xa, sys.ncoil, s_crow, s_cval, lane, &s_mu[Kc - 1]);
+                else reduce_term(s_part + ((Kc - 1) & 1) * nwarps, nwarps, lane, &s_mu[Kc - 1]);
             }
             if (CLU && !scoil) {
                 // rank 0 adds the peers' partial moments in rank order; the peers
@@ -1210,7 +1226,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 // reaches after this read
                 csync<CLU>();
                 if (crank == 0) {
-                    for (int k = tid; k < K; k += blockDim.x) {
+                    for (int k = tid; k < Kc; k += blockDim.x) {
                         Vec v = s_mu[k];
                         for (int j = 1; j < CL; ++j) {
                             const uint32_t a = cluster_addr(smem_u32(&s_mu[k]), j);
@@ -1232,10 +1248,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             // FID points of this chunk: f_j = ph_j * sum_k J_k(s j dt) (-i)^k mu_k
             if (!CLU || crank == 0) {
                 const int parts = max(1, (int)blockDim.x / Mo);
-                const int kper = (K + parts - 1) / parts;
+                const int kper = (Kc + parts - 1) / parts;
                 for (int jj = tid; jj < Mo * parts; jj += blockDim.x) {
                     const int j = jj % Mo, pidx = jj / Mo;
-                    const int k0 = pidx * kper, k1 = min(K, k0 + kper);
+                    const int k0 = pidx * kper, k1 = min(Kc, k0 + kper);
                     Vec f = vzero<Vec>();
                     for (int k = k0; k < k1; ++k) {
                         const Real jv = (Real)table[(size_t)k * (Mo + 1) + j];
@@ -1279,7 +1295,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             run.kused[o] = K;
             run.mused[o] = Mo;
             run.halfwidth[o] = half;
-            run.matvecs[o] = (long long)nchunks * (K - 1);
+            run.matvecs[o] = mv;
         }
         csync<CLU>();
     }
