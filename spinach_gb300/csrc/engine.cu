@@ -101,6 +101,7 @@ struct spx_handle {
     DevBuf<int> d_status, d_kused, d_mused;
     DevBuf<long long> d_matvecs;
     DevBuf<double> d_halfwidth;
+    DevBuf<int> d_counter;           // orientation work counter of the propagation kernel
 
     // last run
     spx_stats stats{};
@@ -540,6 +541,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
 
 // Launch the propagation kernel (plain or cluster launch) on the handle's stream.
 void launch_chebyshev(spx_handle *h, bool f64, const Config &c, spx::DevSystem &sys, spx::DevRun &run) {
+    SPX_CUDA(cudaMemsetAsync(run.next_orient, 0, sizeof(int), h->stream));
     run.cl = c.cl;
     run.nsl_loc = c.nsl_loc;
     run.ell_loc = c.ell_loc;
@@ -576,6 +578,7 @@ void reserve_run(spx_handle *h, int64_t n_orient, int64_t nsteps, bool f64, cons
     h->d_mused.reserve(n_orient);
     h->d_matvecs.reserve(n_orient);
     h->d_halfwidth.reserve(n_orient);
+    h->d_counter.reserve(1);
     const int ngroups = (int)((n_orient + kPowderGroup - 1) / kPowderGroup);
     h->d_part.reserve((size_t)ngroups * npts);
 }
@@ -603,6 +606,7 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     run.status = h->d_status.p; run.matvecs = h->d_matvecs.p; run.halfwidth = h->d_halfwidth.p;
     run.kused = h->d_kused.p;
     run.mused = h->d_mused.p;
+    run.next_orient = h->d_counter.p;
 
     if (timed) SPX_CUDA(cudaEventRecord(h->ev[0], h->stream));
     launch_chebyshev(h, f64, c, sys, run);
@@ -883,15 +887,15 @@ void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, con
     const int group = 64;
     const int ngroups = (int)((n_orient + group - 1) / group);
     // carve the scratch: sizes first, then check, then addresses
-    const size_t sizes[8] = {
+    const size_t sizes[9] = {
         (size_t)c.grid * c.Kmax * (c.M + 1) * sizeof(double),        // Bessel tables
         npts * (size_t)n_orient * (f64 ? sizeof(double2) : sizeof(float2)),   // per-orientation FIDs
         (size_t)ngroups * npts * sizeof(double2),                     // FP64 partial sums
         (size_t)n_orient * sizeof(int), (size_t)n_orient * sizeof(int), (size_t)n_orient * sizeof(int),
         (size_t)n_orient * sizeof(long long) + (size_t)n_orient * sizeof(double),
-        sizeof(int)};
-    size_t offs[8], total = 0;
-    for (int i = 0; i < 8; ++i) {
+        sizeof(int), sizeof(int)};
+    size_t offs[9], total = 0;
+    for (int i = 0; i < 9; ++i) {
         offs[i] = total;
         total += (sizes[i] + 255) & ~(size_t)255;
     }
@@ -922,6 +926,7 @@ void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, con
     run.mused = reinterpret_cast<int *>(base + offs[5]);
     run.matvecs = reinterpret_cast<long long *>(base + offs[6]);
     run.halfwidth = reinterpret_cast<double *>(base + offs[6] + (size_t)n_orient * sizeof(long long));
+    run.next_orient = reinterpret_cast<int *>(base + offs[8]);
     double2 *part = reinterpret_cast<double2 *>(base + offs[2]);
     // the only value that must start at zero is the failure flag
     SPX_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), h->stream));

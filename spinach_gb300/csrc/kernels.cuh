@@ -377,6 +377,8 @@ struct DevRun {
     int *kused;         // n_orient
     int *mused;         // n_orient: time steps per chunk used
     int cl;                 // CTAs per cluster (1: no cluster)
+    int *next_orient;       // work counter (zeroed before the launch): single CTAs take
+                            // orientations gridDim.x, gridDim.x + 1, ... as they finish
     int cl_slices[kMaxCluster + 1];   // slice boundaries of the CTAs' row blocks (cluster launches)
     int nsl_loc;            // largest slice count of one CTA (shared-memory sizing)
     int ell_loc;            // largest ELL entry count of one CTA
@@ -608,6 +610,18 @@ __device__ __forceinline__ void reduce_term(const Vec *part, int nwarps, int lan
     if (lane == 0) *mu = q;
 }
 
+// Next orientation of a CTA or cluster: orientations below `first` (one per
+// CTA or cluster) were handed out at launch, the counter numbers the rest.  In
+// a cluster rank 0 draws and every CTA reads its choice.  All threads call.
+template <bool CLU>
+static __device__ int next_orientation(int *counter, int *slot, int first, int crank) {
+    csync<CLU>();
+    if (threadIdx.x == 0 && crank == 0) *slot = first + atomicAdd(counter, 1);
+    csync<CLU>();
+    if constexpr (CLU) return ld_cluster_s32(cluster_addr(smem_u32(slot), 0));
+    return *slot;
+}
+
 // Moment coil' x from the few non-zero coil rows (lane i takes row i), one warp.
 template <class Vec>
 __device__ __forceinline__ void coil_moment(const Vec *x, int ncoil, const int *rows, const Vec *cv, int lane, Vec *mu) {
@@ -704,7 +718,11 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     const bool assignment_ok = cluster_reduce<CLU, 2>(s_wload[0] != 0 ? 1.0 : 0.0, s_red, s_cred, par, crank, CL) > 0.5;
     const int rows_per_lane = s_wcnt[warp];
 
-    for (int o = blockIdx.x / CL; o < run.n_orient; o += gridDim.x / CL) {
+    // Each CTA (cluster) starts at its own index and then takes the next free
+    // orientation from a global counter, since orientations differ in cost.
+    __shared__ int s_next;
+    for (int o = blockIdx.x / CL; o < run.n_orient;
+         o = next_orientation<CLU>(run.next_orient, &s_next, (int)(gridDim.x / CL), crank)) {
         if (!assignment_ok) {                        // launch configuration error
             if (tid == 0 && crank == 0) run.status[o] = kDevTooManyRows;
             continue;
