@@ -306,6 +306,15 @@ class OperatorFactory:
     def __init__(self, ss: SpinSystem, basis: Basis):
         self.ss, self.basis = ss, basis
         self.tables = {int(m): _product_tables(int(m)) for m in np.unique(ss.mults)}
+        self.op_cache = {}          # operator products as summed COO matrices
+
+    def comm_coo(self, ops) -> sp.coo_matrix:
+        """Commutation superoperator of a product of single-spin operators,
+        cached (it depends only on the basis and the spins' multiplicities)."""
+        key = tuple(ops)
+        if key not in self.op_cache:
+            self.op_cache[key] = self.operator(ops, 'comm').tocoo()
+        return self.op_cache[key]
 
     def product(self, codes: dict, side: str) -> sp.csr_matrix:
         """Left or right multiplication by prod_s T(codes[s]) (normalised basis).
@@ -313,10 +322,17 @@ class OperatorFactory:
         For the 'leftofcomm'/'rightofcomm' halves, terms whose input or output
         is the unit state on all active spins are dropped (they cancel exactly
         in the commutator, superop.m:139-145)."""
+        r, c, v = self.product_coo(codes, side)
+        dim = self.basis.dim
+        return sp.csr_matrix((v, (r, c)), shape=(dim, dim))
+
+    def product_coo(self, codes: dict, side: str):
+        """The same product as (rows, cols, values) triplets."""
         b = self.basis
         dim = b.dim
         if not codes:
-            return sp.identity(dim, format='csr', dtype=complex)
+            ar = np.arange(dim)
+            return ar, ar.copy(), np.ones(dim, complex)
         comm_half = side.endswith('ofcomm')
         which = 0 if side.startswith('left') else 1
         cols = np.arange(dim)
@@ -345,10 +361,17 @@ class OperatorFactory:
             cols, vals, keys = cols[keep], vals[keep], keys[keep]
         r = b.find(keys)
         ok = r >= 0
-        return sp.csr_matrix((vals[ok].astype(complex), (r[ok], cols[ok])), shape=(dim, dim))
+        return r[ok], cols[ok], vals[ok].astype(complex)
 
     def commutator(self, codes: dict) -> sp.csr_matrix:
-        return self.product(codes, 'leftofcomm') - self.product(codes, 'rightofcomm')
+        r, c, v = self.commutator_coo(codes)
+        dim = self.basis.dim
+        return sp.csr_matrix((v, (r, c)), shape=(dim, dim))
+
+    def commutator_coo(self, codes: dict):
+        rl, cl, vl = self.product_coo(codes, 'leftofcomm')
+        rr, cr, vr = self.product_coo(codes, 'rightofcomm')
+        return np.concatenate([rl, rr]), np.concatenate([cl, cr]), np.concatenate([vl, -vr])
 
     # Human-readable product operators: lists of (op, spin) with op in
     # E, Lz, L+, L-, Lx, Ly (kernel/utilities/human2opspec.m conventions).
@@ -358,6 +381,15 @@ class OperatorFactory:
              'Ly': ((1, -math.sqrt(2) / 2j), (3, -math.sqrt(2) / 2j))}
 
     def operator(self, ops, kind: str = 'comm') -> sp.csr_matrix:
+        r, c, v = self.operator_coo(ops, kind)
+        dim = self.basis.dim
+        M = sp.csr_matrix((v, (r, c)), shape=(dim, dim))
+        M.sum_duplicates()
+        return M
+
+    def operator_coo(self, ops, kind: str = 'comm'):
+        """Superoperator of a product of single-spin operators as (rows, cols,
+        values) triplets; duplicates are summed when a matrix is formed."""
         terms = [({}, 1.0 + 0j)]
         for op, s in ops:
             new = []
@@ -368,11 +400,13 @@ class OperatorFactory:
                         cc[s] = code
                     new.append((cc, c * f))
             terms = new
-        acc = None
+        rs, cs, vs = [], [], []
         for codes, c in terms:
-            M = self.commutator(codes) if kind == 'comm' else self.product(codes, kind)
-            acc = c * M if acc is None else acc + c * M
-        return acc.tocsr()
+            r, col, v = self.commutator_coo(codes) if kind == 'comm' else self.product_coo(codes, kind)
+            rs.append(r)
+            cs.append(col)
+            vs.append(c * v)
+        return np.concatenate(rs), np.concatenate(cs), np.concatenate(vs)
 
     def state(self, op: str, isotope: str) -> np.ndarray:
         """Liouville-space vector of sum_s op(s) over spins of an isotope
@@ -438,6 +472,24 @@ def interaction_strengths(ss: SpinSystem, assumptions: str):
     return zs, cs
 
 
+_FACTORIES: dict = {}
+_FACTORY_LIMIT = 8
+
+
+def factory_for(ss: SpinSystem, basis: Basis) -> OperatorFactory:
+    """An operator factory shared by systems with the same isotopes and
+    basis (operator matrices and states depend on nothing else), least
+    recently used first out after a few bases."""
+    key = (tuple(ss.isotopes), tuple(int(m) for m in ss.mults), basis.dim, basis.keys.tobytes())
+    f = _FACTORIES.pop(key, None)
+    if f is None:
+        f = OperatorFactory(ss, basis)
+        if len(_FACTORIES) >= _FACTORY_LIMIT:
+            _FACTORIES.pop(next(iter(_FACTORIES)))
+    _FACTORIES[key] = f
+    return f
+
+
 @dataclass
 class RotationalHamiltonian:
     """``H(Omega) = I + sum_{r,k,m} D^r_{km}(Omega) Q[(r,k,m)]`` before Hermitisation."""
@@ -483,35 +535,39 @@ def rotational_hamiltonian(ss: SpinSystem, basis: Basis, assumptions: str,
             for name in _STRENGTH_TERMS[strength]:
                 opL, opS, w1, w2 = _BILINEAR[name]
                 ani_terms.append((np.array(w1 + w2, float), irr, [(opL, a), (opS, b)]))
-    cache = {}
-
-    def op(ops):
-        key = tuple(ops)
-        if key not in cache:
-            cache[key] = f.operator(ops, 'comm')
-        return cache[key]
+    op = f.comm_coo        # one superoperator per distinct operator product
 
     dim = basis.dim
-    I = sp.csr_matrix((dim, dim), dtype=complex)
-    for c, ops in iso_terms:
-        I = I + c * op(ops)
+
+    def assemble(weighted):
+        # sum_i c_i M_i in one pass: concatenate the scaled triplets, then
+        # sum duplicates once
+        if not weighted:
+            return None
+        rows = np.concatenate([op(ops).row for _, ops in weighted])
+        cols = np.concatenate([op(ops).col for _, ops in weighted])
+        vals = np.concatenate([c * op(ops).data for c, ops in weighted])
+        M = sp.csr_matrix((vals, (rows, cols)), shape=(dim, dim))
+        M.sum_duplicates()
+        M.eliminate_zeros()
+        return M
+
+    I = assemble(iso_terms)
+    if I is None:
+        I = sp.csr_matrix((dim, dim), dtype=complex)
     aniso = {}
     for r in (1, 2):
         off = r * r - 1
         for k in range(2 * r + 1):
             for m in range(2 * r + 1):
-                acc = None
+                weighted = []
                 for ist, irr, ops in ani_terms:
                     c = ist[off + k] * irr[off + m]
                     if abs(c) > tz:
-                        acc = c * op(ops) if acc is None else acc + c * op(ops)
-                if acc is not None:
-                    acc = acc.tocsr()
-                    acc.eliminate_zeros()
-                    if acc.nnz:
-                        aniso[(r, k, m)] = acc
-    I = I.tocsr()
-    I.eliminate_zeros()
+                        weighted.append((c, ops))
+                acc = assemble(weighted)
+                if acc is not None and acc.nnz:
+                    aniso[(r, k, m)] = acc
     return RotationalHamiltonian(dim, I, aniso)
 
 

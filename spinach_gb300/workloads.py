@@ -181,7 +181,7 @@ def build(w: Workload) -> Liouvillian:
     """Host setup of a workload: I, Q{r}{k,m}, R, rho0, coil."""
     ss = spin_system_of(w)
     basis = ssm.build_basis(ss, w.approximation, w.level)
-    fac = ssm.OperatorFactory(ss, basis)
+    fac = ssm.factory_for(ss, basis)
     H = ssm.rotational_hamiltonian(ss, basis, w.assumptions, fac)
     R = sp.diags(ssm.relaxation_diagonal(ss, basis)).tocsr().astype(complex)
     return Liouvillian(H.iso, H.aniso, R, fac.state(*w.rho0), fac.state(*w.coil), basis.dim)
