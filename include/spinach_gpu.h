@@ -86,6 +86,8 @@ typedef struct {
     int32_t real_offdiag;      /* 1 if off-diagonal Liouvillian values are real */
     int32_t cluster;           /* CTAs that shared one orientation (thread-block cluster size) */
     int32_t smem_bytes;        /* dynamic shared memory of each CTA */
+    int32_t channels;          /* detection channels of the run */
+    int32_t reserved;
 } spx_stats;
 
 typedef struct spx_handle spx_handle;
@@ -194,6 +196,18 @@ spx_status spx_surrogate_gradients(spx_surrogate *s, int64_t n, const double *d_
 spx_status spx_surrogate_get_params(spx_surrogate *s, float *h_params);
 spx_status spx_surrogate_set_params(spx_surrogate *s, const float *h_params);
 const char *spx_surrogate_last_error(const spx_surrogate *s);
+
+/*
+ * Several detection states at once (kernel/evolution.m 'multichannel',
+ * evolution.m:589-673: one FID row per coil column).  coils holds nchan
+ * (1..8) columns of the Liouville dimension, column-major, interleaved
+ * complex; it replaces the coil of spx_upload_system.  With nchan > 1 the
+ * columns may hold at most 32 non-zeros together (SPX_ERR_UNSUPPORTED
+ * otherwise).  Runs then return nchan FIDs: fid holds nchan*(nsteps+1)
+ * complex values, channel by channel, and fids_per_orient / d_fid scale the
+ * same way.
+ */
+spx_status spx_upload_coils(spx_handle *handle, int32_t nchan, const double *coils);
 
 /*
  * Autotuner (no counterpart in the reference, whose step.m/propagator.m pick

@@ -90,8 +90,10 @@ struct spx_handle {
     DevBuf<uint16_t> d_ell_col;
     DevBuf<double> d_ell_re, d_ell_im;
     DevBuf<double2> d_diag, d_rho0, d_coil, d_coil_vals;
-    DevBuf<int> d_coil_rows;
-    int ncoil = -1;                 // non-zero coil rows if at most 32, else -1
+    DevBuf<int> d_coil_rows, d_coil_chan;
+    int ncoil = -1;                 // non-zero coil entries if at most 32, else -1
+    int nchan = 1;                  // detection channels
+    std::vector<int> row_of;        // sliced-ELL row of every basis state
 
     // run buffers
     DevBuf<double> d_grid;       // alpha | beta | gamma | weight
@@ -342,7 +344,10 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
     if (h->ncoil > 0) {
         h->d_coil_rows.upload(crow, h->stream);
         h->d_coil_vals.upload(cval, h->stream);
+        h->d_coil_chan.upload(std::vector<int>(crow.size(), 0), h->stream);
     }
+    h->nchan = 1;
+    h->row_of = inv;
     SPX_CUDA(cudaStreamSynchronize(h->stream));
     h->n = (int)n;
     h->n_pad = n_pad;
@@ -359,6 +364,44 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
 
 // ---------------------------------------------------------------------------
 // Launch configuration
+// Several detection states (evolution.m 'multichannel'): column c of the
+// n x nchan column-major complex array is channel c.
+void upload_coils(spx_handle *h, int32_t nchan, const double *coils) {
+    if (!h->have_system) throw SpxError(SPX_ERR_NO_SYSTEM, "no spin system uploaded");
+    if (!coils) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "coils is NULL");
+    if (nchan < 1 || nchan > 8) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "channels must be 1..8");
+    const int n = h->n;
+    for (int64_t i = 0; i < 2 * (int64_t)n * nchan; ++i)
+        if (!std::isfinite(coils[i])) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite coil");
+    std::vector<int> crow, cchan;
+    std::vector<double2> cval;
+    for (int c = 0; c < nchan; ++c)
+        for (int i = 0; i < n; ++i) {
+            const double re = coils[2 * ((size_t)c * n + i)], im = coils[2 * ((size_t)c * n + i) + 1];
+            if (re != 0.0 || im != 0.0) {
+                crow.push_back(h->row_of[i]);
+                cval.push_back(make_double2(re, im));
+                cchan.push_back(c);
+            }
+        }
+    if (nchan > 1 && crow.size() > 32)
+        throw SpxError(SPX_ERR_UNSUPPORTED, "several channels need at most 32 non-zero coil entries in total");
+    SPX_CUDA(cudaSetDevice(h->device));
+    if (nchan == 1) {                               // dense copy for the per-row projection path
+        std::vector<double2> cl(h->n_pad, make_double2(0, 0));
+        for (size_t e = 0; e < crow.size(); ++e) cl[crow[e]] = cval[e];
+        h->d_coil.upload(cl, h->stream);
+    }
+    h->ncoil = crow.size() <= 32 ? (int)crow.size() : -1;
+    if (h->ncoil > 0) {
+        h->d_coil_rows.upload(crow, h->stream);
+        h->d_coil_vals.upload(cval, h->stream);
+        h->d_coil_chan.upload(cchan, h->stream);
+    }
+    h->nchan = nchan;
+    SPX_CUDA(cudaStreamSynchronize(h->stream));
+}
+
 // ---------------------------------------------------------------------------
 constexpr int kPowderGroup = 64;    // orientations per partial sum of the powder reduction
 
@@ -387,7 +430,7 @@ double host_series_terms(double x, double lg, double tol) {
 
 template <bool F64, bool CPLX>
 size_t smem_bytes(const spx_handle *h, int nsl_loc, int ell_loc, int Kmax, int M, int threads) {
-    spx::SmemLayout<F64, CPLX> L(h->n_pad, nsl_loc, ell_loc, Kmax, M, threads);
+    spx::SmemLayout<F64, CPLX> L(h->n_pad, nsl_loc, ell_loc, Kmax, M, threads, h->nchan);
     return L.total;
 }
 
@@ -569,7 +612,7 @@ void launch_chebyshev(spx_handle *h, bool f64, const Config &c, spx::DevSystem &
 
 // Device buffers of one run (idempotent; called before graph capture too).
 void reserve_run(spx_handle *h, int64_t n_orient, int64_t nsteps, bool f64, const Config &c) {
-    const size_t npts = (size_t)nsteps + 1;
+    const size_t npts = ((size_t)nsteps + 1) * h->nchan;       // every channel's points
     const size_t vec_bytes = f64 ? sizeof(double2) : sizeof(float2);
     h->d_fids.reserve(npts * n_orient * vec_bytes);
     h->d_table.reserve((size_t)c.grid * c.Kmax * (c.M + 1));
@@ -587,7 +630,7 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
                    const double *d_ga, const double *d_w, double dt, int64_t nsteps,
                    const spx_options &opt, double2 *d_out, const Config &c, int safe_bounds = 0, bool timed = true) {
     const bool f64 = opt.precision == SPX_FP64;
-    const size_t npts = (size_t)nsteps + 1;
+    const size_t npts = ((size_t)nsteps + 1) * h->nchan;   // the powder sum treats channels as more points
     reserve_run(h, n_orient, nsteps, f64, c);
 
     spx::DevSystem sys{};
@@ -598,6 +641,7 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     sys.ncoef = 1 + 2 * h->nterms; sys.nterms = h->nterms; sys.term_rkm = h->d_term_rkm.p;
     sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag;
     sys.ncoil = h->ncoil; sys.coil_rows = h->d_coil_rows.p; sys.coil_vals = h->d_coil_vals.p;
+    sys.coil_chan = h->d_coil_chan.p; sys.nchan = h->nchan;
     spx::DevRun run{};
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
@@ -640,6 +684,7 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     h->stats.value_streams = h->nstreams;
     h->stats.real_offdiag = h->cplx ? 0 : 1;
     h->stats.cluster = c.cl;
+    h->stats.channels = h->nchan;
     h->stats.smem_bytes = (int32_t)c.smem;
     h->stats_pending = true;
     h->last_norient = n_orient;
@@ -883,7 +928,7 @@ void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, con
     opt.precision = precision;
     const Config c = choose_config(h, n_orient, dt, nsteps, opt, 0, kNoallocChunkCap);
     const bool f64 = precision == SPX_FP64;
-    const size_t npts = (size_t)nsteps + 1;
+    const size_t npts = ((size_t)nsteps + 1) * h->nchan;   // all channels' points
     const int group = 64;
     const int ngroups = (int)((n_orient + group - 1) / group);
     // carve the scratch: sizes first, then check, then addresses
@@ -914,6 +959,7 @@ void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, con
     sys.ncoef = 1 + 2 * h->nterms; sys.nterms = h->nterms; sys.term_rkm = h->d_term_rkm.p;
     sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag;
     sys.ncoil = h->ncoil; sys.coil_rows = h->d_coil_rows.p; sys.coil_vals = h->d_coil_vals.p;
+    sys.coil_chan = h->d_coil_chan.p; sys.nchan = h->nchan;
     spx::DevRun run{};
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
@@ -1035,7 +1081,7 @@ spx_status spx_run_powder(spx_handle *h, int64_t n_orient, const double *alphas,
         SPX_CUDA(cudaMemcpyAsync(g + n_orient, betas, b, cudaMemcpyHostToDevice, h->stream));
         SPX_CUDA(cudaMemcpyAsync(g + 2 * n_orient, gammas, b, cudaMemcpyHostToDevice, h->stream));
         SPX_CUDA(cudaMemcpyAsync(g + 3 * n_orient, weights, b, cudaMemcpyHostToDevice, h->stream));
-        h->d_fid.reserve((size_t)nsteps + 1);
+        h->d_fid.reserve(((size_t)nsteps + 1) * h->nchan);
         Config c = choose_config(h, n_orient, dt, nsteps, o, 0);
         launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o, h->d_fid.p, c);
         spx_status st = SPX_OK;
@@ -1060,9 +1106,10 @@ spx_status spx_run_powder(spx_handle *h, int64_t n_orient, const double *alphas,
             st = finish_run(h);
         }
         (void)st;
-        SPX_CUDA(cudaMemcpy(fid, h->d_fid.p, ((size_t)nsteps + 1) * sizeof(double2), cudaMemcpyDeviceToHost));
+        SPX_CUDA(cudaMemcpy(fid, h->d_fid.p, ((size_t)nsteps + 1) * h->nchan * sizeof(double2),
+                            cudaMemcpyDeviceToHost));
         if (fids_per_orient) {
-            const size_t cnt = ((size_t)nsteps + 1) * n_orient;
+            const size_t cnt = ((size_t)nsteps + 1) * h->nchan * n_orient;
             if (o.precision == SPX_FP64) {
                 SPX_CUDA(cudaMemcpy(fids_per_orient, h->d_fids.p, cnt * sizeof(double2), cudaMemcpyDeviceToHost));
             } else {
@@ -1135,6 +1182,11 @@ const char *spx_status_string(spx_status s) {
 const char *spx_last_error(const spx_handle *h) { return h ? h->err.c_str() : "NULL handle"; }
 
 const char *spx_version(void) { return "spinach-gb300 0.1 (sm_103a)"; }
+
+spx_status spx_upload_coils(spx_handle *h, int32_t nchan, const double *coils) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] { upload_coils(h, nchan, coils); });
+}
 
 spx_status spx_autotune(spx_handle *h, int64_t n_orient, const double *d_alphas, const double *d_betas,
                         const double *d_gammas, double dt, int64_t nsteps, int32_t precision, spx_options *best) {

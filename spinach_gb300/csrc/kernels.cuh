@@ -351,9 +351,11 @@ struct DevSystem {
     const int *term_rkm;        // 3 * nterms: rank, k, m (0-based k, m)
     const double2 *rho0;        // n_pad (sliced order)
     const double2 *coil;        // n_pad (sliced order)
-    int ncoil;                  // 1..32: non-zero coil rows listed below; 0 or -1: use the dense coil
+    int ncoil;                  // 1..32: non-zero coil entries listed below; 0 or -1: use the dense coil
     const int *coil_rows;       // ncoil rows (sliced order)
     const double2 *coil_vals;   // ncoil values
+    const int *coil_chan;       // ncoil detection channels (0 .. nchan-1)
+    int nchan;                  // detection channels (evolution.m 'multichannel'); > 1 needs the listed coil
     double max_im_diag;         // largest |Im L_ii| (relaxation), rad/s
 };
 
@@ -513,7 +515,7 @@ struct SmemLayout {
     __host__ __device__ static size_t align(size_t x) { return (x + 15) & ~size_t(15); }
     // n_pad: replicated vector length; nslices / ell_len: the slices and ELL
     // entries one CTA owns (all of them without a cluster)
-    __host__ __device__ SmemLayout(int n_pad, int nslices, int ell_len, int Kmax, int M, int nthreads) {
+    __host__ __device__ SmemLayout(int n_pad, int nslices, int ell_len, int Kmax, int M, int nthreads, int nchan = 1) {
         size_t o = 0;
         coef = o; o = align(o + sizeof(double) * kMaxCoef);
         red = o; o = align(o + sizeof(double) * kRedSlots);
@@ -528,7 +530,7 @@ struct SmemLayout {
         xb = o; o = align(o + sizeof(typename P::Vec) * n_pad);
         part = o; o = align(o + sizeof(typename P::Vec) * 2 * (nthreads / 32));   // two terms in flight
         atau = o; o = align(o + sizeof(typename P::Af) * Kmax);
-        mu = o; o = align(o + sizeof(typename P::Vec) * Kmax);
+        mu = o; o = align(o + sizeof(typename P::Vec) * Kmax * nchan);
         phase = o; o = align(o + sizeof(typename P::Vec) * (M + 1));
         rec = o; o = align(o + sizeof(typename P::Vec) * (nthreads > M ? nthreads : M));
         total = o;
@@ -631,6 +633,22 @@ __device__ __forceinline__ void coil_moment(const Vec *x, int ncoil, const int *
     if (lane == 0) *mu = q;
 }
 
+// Several channels (evolution.m 'multichannel'): each channel's entries are
+// summed separately; channel c's moment goes to mu[c * stride].  Kept out of
+// line so the term loop's code stays the size of the one-channel case.
+template <class Vec>
+static __device__ __noinline__ void coil_moments(const Vec *x, int ncoil, const int *rows, const Vec *cv,
+                                                 const int *chan, int nchan, int stride, int lane, Vec *mu) {
+    Vec q = vzero<Vec>();
+    if (lane < ncoil) cdot_acc(q, cv[lane], x[rows[lane]]);
+    const int my = lane < ncoil ? chan[lane] : -1;
+    for (int c = 0; c < nchan; ++c) {
+        Vec qc = (my == c) ? q : vzero<Vec>();
+        qc = warp_sum(qc);
+        if (lane == 0) mu[c * stride] = qc;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // The propagation kernel
 // ---------------------------------------------------------------------------
@@ -647,7 +665,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 
     extern __shared__ __align__(16) unsigned char smem[];
     const SmemLayout<F64, CPLX> L(sys.n_pad, CLU ? run.nsl_loc : sys.nslices, CLU ? run.ell_loc : sys.ell_len,
-                                  run.Kmax, run.M, blockDim.x);
+                                  run.Kmax, run.M, blockDim.x, sys.nchan);
     double *s_coef = reinterpret_cast<double *>(smem + L.coef);
     double *s_red = reinterpret_cast<double *>(smem + L.red);
     double *s_cred = reinterpret_cast<double *>(smem + L.cred);
@@ -668,6 +686,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     __shared__ int s_int[4];
     __shared__ int s_crow[32];
     __shared__ Vec s_cval[32];
+    __shared__ int s_cchan[32];
     const bool scoil = sys.ncoil > 0;       // moments from the coil rows, no per-row projection
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
@@ -690,6 +709,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     if (scoil && tid < sys.ncoil) {
         s_crow[tid] = sys.coil_rows[tid];
         s_cval[tid] = tovec(sys.coil_vals[tid], Vec());
+        s_cchan[tid] = sys.coil_chan ? sys.coil_chan[tid] : 0;
     }
     for (int e = tid; e < ell_loc; e += blockDim.x) s_col[e] = sys.ell_col[eb + e];
     // Slices to warps, longest-processing-time first: slices are stored in
@@ -1014,7 +1034,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 r_w[r] = (s_soff[sl + 1] - s_soff[sl]) >> 5;
             }
         }
-        Vec *fid_out = reinterpret_cast<Vec *>(run.fids) + (size_t)o * (nsteps + 1);
+        Vec *fid_out = reinterpret_cast<Vec *>(run.fids) + (size_t)o * sys.nchan * (nsteps + 1);
         int status = kDevOk;
         [[maybe_unused]] Vec t_prev[RMAX], t_cur[RMAX], acc[RMAX], cc[RMAX];
         [[maybe_unused]] f2x tp[RMAX], tc[RMAX], ac[RMAX], cp[RMAX], crr[RMAX], cim[RMAX];
@@ -1068,7 +1088,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     // the last warp folds term k-1's partials while the others start term k;
                     // slot (k-1)&1 is rewritten only in term k+1, after the next barrier
                     if (warp == nwarps - 1) {
-                        if (scoil) coil_moment(src, sys.ncoil, s_crow, s_cval, lane, &s_mu[k - 1]);
+                        if (sys.nchan > 1) coil_moments(src, sys.ncoil, s_crow, s_cval, s_cchan, sys.nchan, run.Kmax, lane, &s_mu[k - 1]);
+                        else if (scoil) coil_moment(src, sys.ncoil, s_crow, s_cval, lane, &s_mu[k - 1]);
                         else reduce_term(s_part + ((k - 1) & 1) * nwarps, nwarps, lane, &s_mu[k - 1]);
                     }
                     Acc y[RMAX];
@@ -1152,7 +1173,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     const f2x TW = (k == 1) ? ONE : TWO;
                     if (warp == nwarps - 1) {
                         // moment of term k-1, whose vector is this term's source
-                        if (scoil) coil_moment(reinterpret_cast<const Vec *>(src), sys.ncoil, s_crow, s_cval, lane, &s_mu[k - 1]);
+                        if (sys.nchan > 1)
+                            coil_moments(reinterpret_cast<const Vec *>(src), sys.ncoil, s_crow, s_cval, s_cchan, sys.nchan,
+                                         run.Kmax, lane, &s_mu[k - 1]);
+                        else if (scoil) coil_moment(reinterpret_cast<const Vec *>(src), sys.ncoil, s_crow, s_cval, lane, &s_mu[k - 1]);
                         else reduce_term(s_part + ((k - 1) & 1) * nwarps, nwarps, lane, &s_mu[k - 1]);
                     }
                     f2x Y[RMAX], C[RMAX], Lo[RMAX];
@@ -1235,7 +1259,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             }
             // moment of the last term (the others were folded inside the loop)
             if (warp == nwarps - 1) {
-                if (scoil) coil_moment(((Kc - 1) & 1) ? s_xb : s_xa, sys.ncoil, s_crow, s_cval, lane, &s_mu[Kc - 1]);
+                if (sys.nchan > 1)
+                    coil_moments(((Kc - 1) & 1) ? s_xb : s_xa, sys.ncoil, s_crow, s_cval, s_cchan, sys.nchan, run.Kmax, lane,
+                                 &s_mu[Kc - 1]);
+                else if (scoil) coil_moment(((Kc - 1) & 1) ? s_xb : s_xa, sys.ncoil, s_crow, s_cval, lane, &s_mu[Kc - 1]);
                 else reduce_term(s_part + ((Kc - 1) & 1) * nwarps, nwarps, lane, &s_mu[Kc - 1]);
             }
             if (CLU && !scoil) {
@@ -1265,6 +1292,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             __syncthreads();
             // FID points of this chunk: f_j = ph_j * sum_k J_k(s j dt) (-i)^k mu_k
             if (!CLU || crank == 0) {
+              for (int ch = 0; ch < sys.nchan; ++ch) {
+                const Vec *mu_c = s_mu + ch * run.Kmax;
+                Vec *out_c = fid_out + (size_t)ch * (nsteps + 1);
+                if (ch > 0) __syncthreads();         // s_rec reused per channel
                 const int parts = max(1, (int)blockDim.x / Mo);
                 const int kper = (Kc + parts - 1) / parts;
                 for (int jj = tid; jj < Mo * parts; jj += blockDim.x) {
@@ -1273,7 +1304,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     Vec f = vzero<Vec>();
                     for (int k = k0; k < k1; ++k) {
                         const Real jv = (Real)table[(size_t)k * (Mo + 1) + j];
-                        const Vec mu = s_mu[k];
+                        const Vec mu = mu_c[k];
                         Real re, im;
                         switch (k & 3) {
                             case 0: re = mu.x; im = mu.y; break;
@@ -1298,8 +1329,9 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     out.x = ph.x * f.x - ph.y * f.y;
                     out.y = ph.x * f.y + ph.y * f.x;
                     const int nidx = a * Mo + j;
-                    if (nidx <= nsteps) fid_out[nidx] = out;
+                    if (nidx <= nsteps) out_c[nidx] = out;
                 }
+              }
             }
             // guard against a violated spectral bound (the series would then
             // grow; a dissipative L can only shrink the state)

@@ -36,7 +36,8 @@ class SpxStats(C.Structure):
                 ('min_half_width', C.c_double), ('max_half_width', C.c_double),
                 ('dim', C.c_int64), ('nnz', C.c_int64), ('ell_entries', C.c_int64),
                 ('value_streams', C.c_int32), ('real_offdiag', C.c_int32),
-                ('cluster', C.c_int32), ('smem_bytes', C.c_int32)]
+                ('cluster', C.c_int32), ('smem_bytes', C.c_int32), ('channels', C.c_int32),
+                ('reserved', C.c_int32)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -57,6 +58,7 @@ SIGNATURES = {
                                         C.POINTER(SpxOptions), _P]),
     'spx_run_powder_noalloc': (C.c_int, [_P, C.c_int64, _P, _P, _P, _P, C.c_double, C.c_int64,
                                          C.c_int32, _P]),
+    'spx_upload_coils': (C.c_int, [_P, C.c_int32, _D]),
     'spx_autotune': (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_double, C.c_int64, C.c_int32,
                                C.POINTER(SpxOptions)]),
     'spx_batch_create': (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(_P), C.POINTER(C.c_int64),
@@ -182,6 +184,16 @@ class Engine:
             self.h, C.byref(self._holders[0].struct), len(keys), ip(rank), ip(kk), ip(mm), Qarr,
             C.byref(Rh.struct) if Rh else None, _dptr(rho0), _dptr(coil)), self.h)
         self.dim = n
+        self.nchan = 1
+
+    def upload_coils(self, coils):
+        """Several detection states (evolution.m 'multichannel'): ``coils`` is
+        a list of Liouville vectors or an (nchan, dim) array.  Runs then return
+        one FID per channel (``fid`` of shape (nchan, nsteps+1))."""
+        cs = np.atleast_2d(np.asarray(coils, np.complex128))
+        arr = np.ascontiguousarray(cs.view(np.float64).ravel())      # column c = row c of cs
+        self._check(self.lib.spx_upload_coils(self.h, cs.shape[0], _dptr(arr)), self.h)
+        self.nchan = cs.shape[0]
 
     def run(self, alphas, betas, gammas, weights, dt: float, nsteps: int, precision: int = FP32,
             per_orientation: bool = False, chunk_steps: int = 0, threads: int = 0,
@@ -191,14 +203,20 @@ class Engine:
         ga = np.ascontiguousarray(gammas, np.float64)
         w = np.ascontiguousarray(weights, np.float64)
         no = al.size
-        fid = np.zeros(2 * (nsteps + 1))
-        fids = np.zeros(2 * (nsteps + 1) * no) if per_orientation else None
+        nch = getattr(self, 'nchan', 1)
+        fid = np.zeros(2 * (nsteps + 1) * nch)
+        fids = np.zeros(2 * (nsteps + 1) * nch * no) if per_orientation else None
         opt = SpxOptions(precision, chunk_steps, threads, cluster, series_tol, chunk_target)
         self._check(self.lib.spx_run_powder(self.h, no, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
                                             float(dt), int(nsteps), C.byref(opt), _dptr(fid),
                                             _dptr(fids) if fids is not None else None), self.h)
-        return PowderResult(fid.view(np.complex128), None if fids is None else
-                            fids.view(np.complex128).reshape(no, nsteps + 1), self.stats())
+        f = fid.view(np.complex128)
+        fs = None if fids is None else fids.view(np.complex128).reshape(no, nch, nsteps + 1)
+        if nch == 1:
+            fs = None if fs is None else fs[:, 0, :]
+        else:
+            f = f.reshape(nch, nsteps + 1)
+        return PowderResult(f, fs, self.stats())
 
     def run_device(self, d_alphas: int, d_betas: int, d_gammas: int, d_weights: int, n_orient: int,
                    dt: float, nsteps: int, d_fid: int, precision: int = FP32, chunk_steps: int = 0,

@@ -1,6 +1,8 @@
 // MATLAB MEX gateway to the GB300 powder-FID engine.
 //
 //   fid          = spinach_powder_gpu(I, Q, R, rho0, coil, grid, dt, nsteps)
+//                  (coil with several columns: one FID row per column, as
+//                  evolution(...,'multichannel') returns)
 //   [fid, fids]  = spinach_powder_gpu(I, Q, R, rho0, coil, grid, dt, nsteps, opts)
 //
 // I, Q     the outputs of [I,Q]=hamiltonian(spin_system) (kernel/hamiltonian.m:44):
@@ -75,28 +77,38 @@ void fill_csc(const mxArray *A, int64_t n, const char *name, CscCopy &out) {
     out.view.values = out.values.data();
 }
 
-std::vector<double> column(const mxArray *A, int64_t n, const char *name) {
-    if (!mxIsDouble(A) || (int64_t)mxGetNumberOfElements(A) != n)
-        throw GatewayError{"Spinach:spinach_powder_gpu:input", std::string(name) + " must be a double vector of length dim."};
-    std::vector<double> out(2 * (size_t)n, 0.0);
+// Columns of a dim x ncol double array (dense or sparse, real or complex) as
+// interleaved complex, column after column.
+std::vector<double> columns(const mxArray *A, int64_t n, int64_t ncol, const char *name) {
+    if (!mxIsDouble(A) || (int64_t)mxGetM(A) != n || (int64_t)mxGetN(A) != ncol)
+        throw GatewayError{"Spinach:spinach_powder_gpu:input", std::string(name) + " must be a double array with dim rows."};
+    std::vector<double> out(2 * (size_t)n * (size_t)ncol, 0.0);
     if (mxIsSparse(A)) {
         const mwIndex *jc = mxGetJc(A), *ir = mxGetIr(A);
-        const int64_t nnz = (int64_t)jc[1];
-        if (mxIsComplex(A)) {
-            const mxComplexDouble *v = mxGetComplexDoubles(A);
-            for (int64_t p = 0; p < nnz; ++p) { out[2 * ir[p]] = v[p].real; out[2 * ir[p] + 1] = v[p].imag; }
-        } else {
-            const mxDouble *v = mxGetDoubles(A);
-            for (int64_t p = 0; p < nnz; ++p) out[2 * ir[p]] = v[p];
+        for (int64_t c = 0; c < ncol; ++c) {
+            double *col = out.data() + 2 * (size_t)n * (size_t)c;
+            if (mxIsComplex(A)) {
+                const mxComplexDouble *v = mxGetComplexDoubles(A);
+                for (mwIndex p = jc[c]; p < jc[c + 1]; ++p) { col[2 * ir[p]] = v[p].real; col[2 * ir[p] + 1] = v[p].imag; }
+            } else {
+                const mxDouble *v = mxGetDoubles(A);
+                for (mwIndex p = jc[c]; p < jc[c + 1]; ++p) col[2 * ir[p]] = v[p];
+            }
         }
     } else if (mxIsComplex(A)) {
         const mxComplexDouble *v = mxGetComplexDoubles(A);
-        for (int64_t i = 0; i < n; ++i) { out[2 * i] = v[i].real; out[2 * i + 1] = v[i].imag; }
+        for (size_t i = 0; i < (size_t)n * (size_t)ncol; ++i) { out[2 * i] = v[i].real; out[2 * i + 1] = v[i].imag; }
     } else {
         const mxDouble *v = mxGetDoubles(A);
-        for (int64_t i = 0; i < n; ++i) out[2 * i] = v[i];
+        for (size_t i = 0; i < (size_t)n * (size_t)ncol; ++i) out[2 * i] = v[i];
     }
     return out;
+}
+
+std::vector<double> column(const mxArray *A, int64_t n, const char *name) {
+    if (!mxIsDouble(A) || (int64_t)mxGetNumberOfElements(A) != n)
+        throw GatewayError{"Spinach:spinach_powder_gpu:input", std::string(name) + " must be a double vector of length dim."};
+    return columns(A, n, 1, name);
 }
 
 std::vector<double> grid_field(const mxArray *g, const char *name, int64_t &count) {
@@ -159,7 +171,14 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     const bool have_R = !mxIsEmpty(prhs[2]);
     if (have_R) fill_csc(prhs[2], n, "R", R);
     const std::vector<double> rho0 = column(prhs[3], n, "rho0");
-    const std::vector<double> coil = column(prhs[4], n, "coil");
+    // several coil columns = several detection channels (evolution.m 'multichannel')
+    const int64_t nchan = (int64_t)mxGetN(prhs[4]);
+    if (nchan < 1 || nchan > 8)
+        throw GatewayError{"Spinach:spinach_powder_gpu:coil", "coil must have 1 to 8 columns."};
+    if (nchan > 1 && nlhs > 1)
+        throw GatewayError{"Spinach:spinach_powder_gpu:nlhs", "per-orientation FIDs need a single coil column."};
+    const std::vector<double> coils = columns(prhs[4], n, nchan, "coil");
+    const std::vector<double> coil(coils.begin(), coils.begin() + 2 * n);
     int64_t no = -1;
     const std::vector<double> al = grid_field(prhs[5], "alphas", no);
     const std::vector<double> be = grid_field(prhs[5], "betas", no);
@@ -191,21 +210,29 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     }
     spx_status st = spx_upload_system(g_handle, &I.view, (int32_t)rank.size(), rank.data(), kk.data(), mm.data(),
                                       qv.data(), have_R ? &R.view : nullptr, rho0.data(), coil.data());
+    if (st == SPX_OK && nchan > 1) st = spx_upload_coils(g_handle, (int32_t)nchan, coils.data());
     if (st != SPX_OK)
         throw GatewayError{"Spinach:spinach_powder_gpu:upload", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
-    plhs[0] = mxCreateDoubleMatrix((mwSize)(nsteps + 1), 1, mxCOMPLEX);
+    // one channel: (nsteps+1) x 1 like powder(); several: one row per channel
+    plhs[0] = nchan == 1 ? mxCreateDoubleMatrix((mwSize)(nsteps + 1), 1, mxCOMPLEX)
+                         : mxCreateDoubleMatrix((mwSize)nchan, (mwSize)(nsteps + 1), mxCOMPLEX);
     double *per = nullptr;
     std::vector<double> per_buf;
     if (nlhs > 1) {
         per_buf.assign(2 * (size_t)(nsteps + 1) * (size_t)no, 0.0);
         per = per_buf.data();
     }
-    std::vector<double> fid(2 * (size_t)(nsteps + 1));
+    std::vector<double> fid(2 * (size_t)(nsteps + 1) * (size_t)nchan);
     st = spx_run_powder(g_handle, no, al.data(), be.data(), ga.data(), wt.data(), dt, nsteps, &opt, fid.data(), per);
     if (st != SPX_OK)
         throw GatewayError{"Spinach:spinach_powder_gpu:run", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
     mxComplexDouble *out = mxGetComplexDoubles(plhs[0]);
-    for (int64_t i = 0; i <= nsteps; ++i) { out[i].real = fid[2 * i]; out[i].imag = fid[2 * i + 1]; }
+    for (int64_t c = 0; c < nchan; ++c)             // engine: channel-major; MATLAB: column-major
+        for (int64_t i = 0; i <= nsteps; ++i) {
+            const size_t src = (size_t)c * (nsteps + 1) + i, dst = (size_t)c + (size_t)i * nchan;
+            out[dst].real = fid[2 * src];
+            out[dst].imag = fid[2 * src + 1];
+        }
     if (nlhs > 1) {
         plhs[1] = mxCreateDoubleMatrix((mwSize)(nsteps + 1), (mwSize)no, mxCOMPLEX);
         mxComplexDouble *o2 = mxGetComplexDoubles(plhs[1]);

@@ -16,7 +16,8 @@ struct Recorded {
     std::vector<int> rank, k, m;
     std::vector<std::vector<double>> Q_values;
     bool have_R = false;
-    std::vector<double> R_values, rho0, coil, grid;
+    std::vector<double> R_values, rho0, coil, coils, grid;
+    int nchan = 1;
     double dt = 0;
     int64_t nsteps = 0, n_orient = 0;
     int precision = -1;
@@ -46,6 +47,13 @@ spx_status spx_upload_system(spx_handle *, const spx_csc *I, int32_t nt, const i
     if (R) g_rec.R_values.assign(R->values, R->values + 2 * R->colptr[n]);
     g_rec.rho0.assign(rho0, rho0 + 2 * n);
     g_rec.coil.assign(coil, coil + 2 * n);
+    g_rec.nchan = 1;
+    g_rec.coils.clear();
+    return SPX_OK;
+}
+spx_status spx_upload_coils(spx_handle *, int32_t nchan, const double *coils) {
+    g_rec.nchan = nchan;
+    g_rec.coils.assign(coils, coils + 2 * g_rec.n * nchan);
     return SPX_OK;
 }
 spx_status spx_run_powder(spx_handle *, int64_t no, const double *a, const double *b, const double *g,
@@ -60,7 +68,11 @@ spx_status spx_run_powder(spx_handle *, int64_t no, const double *a, const doubl
     g_rec.nsteps = nsteps;
     g_rec.precision = opt ? opt->precision : -1;
     g_rec.want_per = per != nullptr;
-    for (int64_t i = 0; i <= nsteps; ++i) { fid[2 * i] = (double)i; fid[2 * i + 1] = -0.5 * i; }
+    for (int c = 0; c < g_rec.nchan; ++c)
+        for (int64_t i = 0; i <= nsteps; ++i) {
+            fid[2 * (c * (nsteps + 1) + i)] = (double)i + 1000.0 * c;
+            fid[2 * (c * (nsteps + 1) + i) + 1] = -0.5 * i;
+        }
     if (per)
         for (int64_t o = 0; o < no; ++o)
             for (int64_t i = 0; i <= nsteps; ++i) {

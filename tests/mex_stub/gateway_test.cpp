@@ -15,7 +15,8 @@ struct Recorded {
     std::vector<int> rank, k, m;
     std::vector<std::vector<double>> Q_values;
     bool have_R;
-    std::vector<double> R_values, rho0, coil, grid;
+    std::vector<double> R_values, rho0, coil, coils, grid;
+    int nchan;
     double dt;
     int64_t nsteps, n_orient;
     int precision;
@@ -104,6 +105,16 @@ int main() {
     mxArray *o1[1] = {nullptr};
     mexFunction(1, o1, 8, p8);
     CHECK(g_rec.precision == 1 && !g_rec.have_R && !g_rec.want_per && o1[0]->m == 1);
+    // two coil columns: spx_upload_coils gets both, the FIDs come back as rows
+    mxArray *coil2 = new mxArray; coil2->m = n; coil2->n = 2; coil2->complex = true;
+    coil2->cx = {{0, 0}, {1, 2}, {0, 0}, {3, -4}, {5, 0}, {0, 0}, {0, 0}, {0, 1}};
+    const mxArray *pc[8] = {I, Q, R, rho0, coil2, grid, scalar(1e-5), scalar(5)};
+    mxArray *oc[1] = {nullptr};
+    mexFunction(1, oc, 8, pc);
+    CHECK(g_rec.nchan == 2 && g_rec.coils.size() == 16 && g_rec.coils[8] == 5.0 && g_rec.coils[15] == 1.0);
+    CHECK((g_rec.coil == std::vector<double>{0, 0, 1, 2, 0, 0, 3, -4}));
+    CHECK(oc[0] && oc[0]->m == 2 && oc[0]->n == 6);
+    CHECK(oc[0]->cx[2 * 3 + 1].real == 1003.0 && oc[0]->cx[2 * 3].real == 3.0);
     // error identifiers
     auto expect = [&](int nl, int nr, const mxArray **pr, const char *id) {
         mxArray *o[2] = {nullptr, nullptr};
@@ -120,6 +131,9 @@ int main() {
     expect(1, 8, badq, "Spinach:spinach_powder_gpu:Q");
     const mxArray *badn[8] = {I, Q, R, rho0, coil, grid, scalar(1e-5), scalar(2.5)};
     expect(1, 8, badn, "Spinach:spinach_powder_gpu:nsteps");
+    mxArray *o2[2] = {nullptr, nullptr};
+    expect(2, 8, pc, "Spinach:spinach_powder_gpu:nlhs");
+    (void)o2;
     g_rec.fail_run = 1;
     expect(1, 8, p8, "Spinach:spinach_powder_gpu:run");
     stub_run_atexit();
