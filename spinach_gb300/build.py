@@ -7,7 +7,8 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 SOURCES = [os.path.join(HERE, 'csrc', f) for f in
-           ('engine.cu', 'surrogate.cu', 'kern_f32r.cu', 'kern_f32c.cu', 'kern_f64r.cu', 'kern_f64c.cu')]
+           ['engine.cu', 'surrogate.cu'] + [f'kern_{p}_{c}.cu' for p in ('f32r', 'f32c', 'f64r', 'f64c')
+                                            for c in ('sc', 'dc')]]
 DEPS = SOURCES + [os.path.join(HERE, 'csrc', 'kernels.cuh'), os.path.join(HERE, 'csrc', 'kern_inst.inc'),
                   os.path.join(ROOT, 'include', 'spinach_gpu.h')]
 LIB = os.path.join(HERE, 'lib', 'libspinach_gpu.so')

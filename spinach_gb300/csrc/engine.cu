@@ -444,17 +444,26 @@ size_t smem_for(const spx_handle *h, bool f64, int nsl_loc, int ell_loc, int Kma
 
 }  // namespace
 // Kernel addresses from the translation units that instantiate them
-// (kern_f32r.cu, kern_f32c.cu, kern_f64r.cu, kern_f64c.cu).
-const void *spx_kernel_f32r(int rmax, bool cluster);
-const void *spx_kernel_f32c(int rmax, bool cluster);
-const void *spx_kernel_f64r(int rmax, bool cluster);
-const void *spx_kernel_f64c(int rmax, bool cluster);
+// (kern_<precision><value type>_<sc: listed coil | dc: dense coil>.cu).
+const void *spx_kernel_f32r_sc(int rmax, bool cluster);
+const void *spx_kernel_f32c_sc(int rmax, bool cluster);
+const void *spx_kernel_f64r_sc(int rmax, bool cluster);
+const void *spx_kernel_f64c_sc(int rmax, bool cluster);
+const void *spx_kernel_f32r_dc(int rmax, bool cluster);
+const void *spx_kernel_f32c_dc(int rmax, bool cluster);
+const void *spx_kernel_f64r_dc(int rmax, bool cluster);
+const void *spx_kernel_f64c_dc(int rmax, bool cluster);
 namespace {
 
-// Single-CTA kernels for RMAX 1, 2, 4, 8; cluster kernels for RMAX 1, 2, 4.
-const void *select_kernel(bool f64, bool cplx, int rmax, bool clu) {
-    if (f64) return cplx ? spx_kernel_f64c(rmax, clu) : spx_kernel_f64r(rmax, clu);
-    return cplx ? spx_kernel_f32c(rmax, clu) : spx_kernel_f32r(rmax, clu);
+// Single-CTA kernels for RMAX 1, 2, 4, 8; cluster kernels for RMAX 1, 2, 4;
+// sc: the coil is listed (at most 32 non-zeros), else the dense projection.
+const void *select_kernel(bool f64, bool cplx, int rmax, bool clu, bool sc) {
+    if (sc) {
+        if (f64) return cplx ? spx_kernel_f64c_sc(rmax, clu) : spx_kernel_f64r_sc(rmax, clu);
+        return cplx ? spx_kernel_f32c_sc(rmax, clu) : spx_kernel_f32r_sc(rmax, clu);
+    }
+    if (f64) return cplx ? spx_kernel_f64c_dc(rmax, clu) : spx_kernel_f64r_dc(rmax, clu);
+    return cplx ? spx_kernel_f32c_dc(rmax, clu) : spx_kernel_f32r_dc(rmax, clu);
 }
 
 // Split the slices into cl contiguous blocks of about equal cost (ELL entries
@@ -525,7 +534,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
         c.threads = nwarps * 32;
         // dynamic shared memory may use what the kernel's static arrays leave
         cudaFuncAttributes fa{};
-        SPX_CUDA(cudaFuncGetAttributes(&fa, select_kernel(f64, h->cplx, c.rmax, cl > 1)));
+        SPX_CUDA(cudaFuncGetAttributes(&fa, select_kernel(f64, h->cplx, c.rmax, cl > 1, h->ncoil > 0)));
         const size_t budget = h->smem_optin > fa.sharedSizeBytes ? h->smem_optin - fa.sharedSizeBytes : 0;
         for (double tx : targets) {
             c.chunk_x = tx;
@@ -548,7 +557,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     if (!placed)
         throw SpxError(SPX_ERR_UNSUPPORTED, "system does not fit the shared memory of a cluster of 8 SMs (" +
                                                 std::to_string(c.smem) + " bytes per SM)");
-    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1);
+    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1, h->ncoil > 0);
     {
         // allow the whole budget: several configurations of one kernel may be
         // prepared before any of them launches (batched graphs)
@@ -589,7 +598,7 @@ void launch_chebyshev(spx_handle *h, bool f64, const Config &c, spx::DevSystem &
     run.nsl_loc = c.nsl_loc;
     run.ell_loc = c.ell_loc;
     for (int j = 0; j <= spx::kMaxCluster; ++j) run.cl_slices[j] = j <= c.cl ? c.slices[j] : 0;
-    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1);
+    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1, h->ncoil > 0);
     void *args[] = {&sys, &run};
     if (c.cl == 1) {
         SPX_CUDA(cudaLaunchKernel(kfn, dim3(c.grid), dim3(c.threads), args, c.smem, h->stream));
@@ -1310,7 +1319,7 @@ spx_status spx_batch_create(spx_batch **out, int32_t n, spx_handle *const *handl
             SPX_CUDA(cudaFuncGetAttributes(&fa, reinterpret_cast<const void *>(&spx::powder_combine_kernel)));
             for (int i = 0; i < n; ++i)
                 SPX_CUDA(cudaFuncGetAttributes(&fa, select_kernel(os[i].precision == SPX_FP64, handles[i]->cplx,
-                                                                  cfg[i].rmax, cfg[i].cl > 1)));
+                                                                  cfg[i].rmax, cfg[i].cl > 1, handles[i]->ncoil > 0)));
         }
         b->marks.resize(n + 1, nullptr);
         for (auto &e : b->marks) SPX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));

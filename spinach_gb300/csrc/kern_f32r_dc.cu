@@ -1,0 +1,7 @@
+// Instantiations of the propagation kernel for one precision, value type and
+// coil layout (separate translation units so the build compiles them in parallel).
+#define SPX_INST_F64 false
+#define SPX_INST_CPLX false
+#define SPX_INST_SC false
+#define SPX_INST_FN spx_kernel_f32r_dc
+#include "kern_inst.inc"

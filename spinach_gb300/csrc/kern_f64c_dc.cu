@@ -1,0 +1,7 @@
+// Instantiations of the propagation kernel for one precision, value type and
+// coil layout (separate translation units so the build compiles them in parallel).
+#define SPX_INST_F64 true
+#define SPX_INST_CPLX true
+#define SPX_INST_SC false
+#define SPX_INST_FN spx_kernel_f64c_dc
+#include "kern_inst.inc"

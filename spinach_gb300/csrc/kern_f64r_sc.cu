@@ -1,0 +1,7 @@
+// Instantiations of the propagation kernel for one precision, value type and
+// coil layout (separate translation units so the build compiles them in parallel).
+#define SPX_INST_F64 true
+#define SPX_INST_CPLX false
+#define SPX_INST_SC true
+#define SPX_INST_FN spx_kernel_f64r_sc
+#include "kern_inst.inc"

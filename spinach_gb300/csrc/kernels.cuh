@@ -652,7 +652,10 @@ static __device__ __noinline__ void coil_moments(const Vec *x, int ncoil, const 
 // ---------------------------------------------------------------------------
 // The propagation kernel
 // ---------------------------------------------------------------------------
-template <bool F64, bool CPLX, int RMAX, bool CLU>
+// SC: the coil has at most 32 non-zeros (sys.ncoil > 0), read by one warp per
+// term; the dense-coil projection is compiled out, which keeps the term loop
+// small (6 % on c1).
+template <bool F64, bool CPLX, int RMAX, bool CLU, bool SC>
 __global__ void __launch_bounds__(512)
 powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     using P = Prec<F64, CPLX>;
@@ -687,7 +690,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     __shared__ int s_crow[32];
     __shared__ Vec s_cval[32];
     __shared__ int s_cchan[32];
-    const bool scoil = sys.ncoil > 0;       // moments from the coil rows, no per-row projection
+    constexpr bool scoil = SC;              // moments from the coil rows, no per-row projection
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const int n = sys.n;
