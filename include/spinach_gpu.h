@@ -63,6 +63,9 @@ typedef struct {
     double series_tol;         /* truncation tolerance of the series, 0 = auto */
     double chunk_target;       /* series argument s*M*dt one expansion covers, 0 = auto
                                   (the autotuned value, else the largest that fits) */
+    int32_t lanczos_its;       /* Lanczos steps of the per-orientation spectral bound,
+                                  0 = 32, else 2..48 (fewer: looser, cheaper bounds) */
+    int32_t reserved;
 } spx_options;
 
 /* Statistics of the last spx_run_powder* call on a handle. */
@@ -87,7 +90,8 @@ typedef struct {
     int32_t cluster;           /* CTAs that shared one orientation (thread-block cluster size) */
     int32_t smem_bytes;        /* dynamic shared memory of each CTA */
     int32_t channels;          /* detection channels of the run */
-    int32_t reserved;
+    int32_t retries;           /* 1 if spx_run_powder re-ran after a device status
+                                  (wider series table and the safe spectral bound) */
 } spx_stats;
 
 typedef struct spx_handle spx_handle;

@@ -500,6 +500,8 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     const bool f64 = opt.precision == SPX_FP64;
     if (opt.cluster != 0 && opt.cluster != 1 && opt.cluster != 2 && opt.cluster != 4 && opt.cluster != 8)
         throw SpxError(SPX_ERR_INVALID_ARGUMENT, "cluster must be 0 (auto), 1, 2, 4 or 8");
+    if (opt.lanczos_its != 0 && (opt.lanczos_its < 2 || opt.lanczos_its > spx::kMaxLanczos))
+        throw SpxError(SPX_ERR_INVALID_ARGUMENT, "lanczos_its must be 0 or 2..48");
     c.tol = opt.series_tol > 0 ? opt.series_tol : (f64 ? 1e-16 : 1e-11);
     // chunk: each orientation picks a power-of-two step count whose series
     // argument s*M*dt is about chunk_x (kernel side); M here is the cap.  The
@@ -655,7 +657,8 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
     run.fixed_chunk = c.fixed ? 1 : 0; run.chunk_x = c.chunk_x;
-    run.lanczos_its = 32; run.safe_bounds = safe_bounds; run.fids = h->d_fids.p; run.table = h->d_table.p;
+    run.lanczos_its = opt.lanczos_its > 0 ? opt.lanczos_its : 32;
+    run.safe_bounds = safe_bounds; run.fids = h->d_fids.p; run.table = h->d_table.p;
     run.status = h->d_status.p; run.matvecs = h->d_matvecs.p; run.halfwidth = h->d_halfwidth.p;
     run.kused = h->d_kused.p;
     run.mused = h->d_mused.p;
@@ -973,7 +976,7 @@ void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, con
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
     run.fixed_chunk = c.fixed ? 1 : 0; run.chunk_x = c.chunk_x;
-    run.lanczos_its = 32; run.safe_bounds = 0;
+    run.lanczos_its = opt.lanczos_its > 0 ? opt.lanczos_its : 32; run.safe_bounds = 0;
     run.table = reinterpret_cast<double *>(base + offs[0]);
     run.fids = base + offs[1];
     run.status = reinterpret_cast<int *>(base + offs[3]);
@@ -1094,6 +1097,7 @@ spx_status spx_run_powder(spx_handle *h, int64_t n_orient, const double *alphas,
         Config c = choose_config(h, n_orient, dt, nsteps, o, 0);
         launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o, h->d_fid.p, c);
         spx_status st = SPX_OK;
+        bool retried = false;
         try {
             finish_run(h);
         } catch (const SpxError &e) {
@@ -1110,11 +1114,13 @@ spx_status spx_run_powder(spx_handle *h, int64_t n_orient, const double *alphas,
             }
             if (!retriable) throw;
             c = choose_config(h, n_orient, dt, nsteps, o, 2 * kneed + 16);
+            retried = true;
             launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o,
                           h->d_fid.p, c, 1);
             st = finish_run(h);
         }
         (void)st;
+        h->stats.retries = retried ? 1 : 0;
         SPX_CUDA(cudaMemcpy(fid, h->d_fid.p, ((size_t)nsteps + 1) * h->nchan * sizeof(double2),
                             cudaMemcpyDeviceToHost));
         if (fids_per_orient) {

@@ -899,9 +899,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
           if (lane == 0) {
             double hi, lo;
             if (run.safe_bounds) {
-                // theta +- beta_m (Zhou-Saad upper bound), clamped by Gershgorin
-                hi = fmin(thi + bl, gmax);
-                lo = fmax(tlo - bl, gmin);
+                // the retry after a violated bound: Gershgorin discs (FP64), which
+                // enclose the spectrum of the Hermitian part whatever Lanczos found
+                hi = gmax;
+                lo = gmin;
             } else {
                 // Ritz value plus its residual |beta_m * y_m| and 2% of the width;
                 // the propagation checks the norm and the host retries with the

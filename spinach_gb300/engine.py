@@ -25,7 +25,8 @@ class SpxCsc(C.Structure):
 
 class SpxOptions(C.Structure):
     _fields_ = [('precision', C.c_int32), ('chunk_steps', C.c_int32), ('threads', C.c_int32),
-                ('cluster', C.c_int32), ('series_tol', C.c_double), ('chunk_target', C.c_double)]
+                ('cluster', C.c_int32), ('series_tol', C.c_double), ('chunk_target', C.c_double),
+                ('lanczos_its', C.c_int32), ('reserved', C.c_int32)]
 
 
 class SpxStats(C.Structure):
@@ -37,7 +38,7 @@ class SpxStats(C.Structure):
                 ('dim', C.c_int64), ('nnz', C.c_int64), ('ell_entries', C.c_int64),
                 ('value_streams', C.c_int32), ('real_offdiag', C.c_int32),
                 ('cluster', C.c_int32), ('smem_bytes', C.c_int32), ('channels', C.c_int32),
-                ('reserved', C.c_int32)]
+                ('retries', C.c_int32)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -197,7 +198,8 @@ class Engine:
 
     def run(self, alphas, betas, gammas, weights, dt: float, nsteps: int, precision: int = FP32,
             per_orientation: bool = False, chunk_steps: int = 0, threads: int = 0,
-            series_tol: float = 0.0, cluster: int = 0, chunk_target: float = 0.0) -> PowderResult:
+            series_tol: float = 0.0, cluster: int = 0, chunk_target: float = 0.0,
+            lanczos_its: int = 0) -> PowderResult:
         al = np.ascontiguousarray(alphas, np.float64)
         be = np.ascontiguousarray(betas, np.float64)
         ga = np.ascontiguousarray(gammas, np.float64)
@@ -206,7 +208,7 @@ class Engine:
         nch = getattr(self, 'nchan', 1)
         fid = np.zeros(2 * (nsteps + 1) * nch)
         fids = np.zeros(2 * (nsteps + 1) * nch * no) if per_orientation else None
-        opt = SpxOptions(precision, chunk_steps, threads, cluster, series_tol, chunk_target)
+        opt = SpxOptions(precision, chunk_steps, threads, cluster, series_tol, chunk_target, lanczos_its, 0)
         self._check(self.lib.spx_run_powder(self.h, no, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
                                             float(dt), int(nsteps), C.byref(opt), _dptr(fid),
                                             _dptr(fids) if fids is not None else None), self.h)

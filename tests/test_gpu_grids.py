@@ -73,3 +73,24 @@ def test_option_checks(gpu_engine):
         gpu_engine.run(*g, w.dt, 16, precision=7)
     with pytest.raises(E.SpxError):
         gpu_engine.run(*g, w.dt, 16, cluster=16)
+
+
+@pytest.mark.parametrize('its', [2, 48])
+def test_loose_spectral_bounds_are_caught_and_retried(gpu_engine, its):
+    """Few Lanczos steps give loose Ritz bounds; a chunk whose state norm grows
+    is reported by the kernel and spx_run_powder reruns with Gershgorin bounds,
+    so the FID still matches the oracle (failure detection without a GPU fault)."""
+    import os
+    w = W.c1()
+    L = W.build(w)
+    gpu_engine.upload(L.I, L.terms, L.R, L.rho0, L.coil)
+    gold = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'c1_orient_krylov_fp64.npz'))
+    al, be, ga, _ = W.zcwn_grid(w.n_orient)
+    sel = gold['sel']
+    res = gpu_engine.run(al[sel], be[sel], ga[sel], np.full(sel.size, 1 / sel.size), w.dt, w.nsteps,
+                         precision=E.FP64, per_orientation=True, lanczos_its=its)
+    assert res.stats['retries'] in (0, 1)
+    for i in range(sel.size):
+        assert rel_err(res.fids[i], gold['fids'][i]) <= 1e-10
+    with pytest.raises(E.SpxError):
+        gpu_engine.run(al[:2], be[:2], ga[:2], [0.5, 0.5], w.dt, 8, lanczos_its=1)
