@@ -4,7 +4,9 @@
 // kernel/hamiltonian.m returns) into Hermitised value streams on one union
 // sparsity pattern, reorders the basis by row length into a 32-row sliced
 // ELL layout, uploads it once, and launches the propagation and powder-sum
-// kernels of kernels.cuh for every orientation grid.
+// kernels of kernels.cuh for every orientation grid.  Also here: the launch
+// configuration (one CTA or a cluster per orientation), the autotuner, the
+// no-allocation entry point and batched CUDA graphs over many handles.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -362,8 +364,6 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
     h->have_system = true;
 }
 
-// ---------------------------------------------------------------------------
-// Launch configuration
 // Several detection states (evolution.m 'multichannel'): column c of the
 // n x nchan column-major complex array is channel c.
 void upload_coils(spx_handle *h, int32_t nchan, const double *coils) {
@@ -402,6 +402,8 @@ void upload_coils(spx_handle *h, int32_t nchan, const double *coils) {
     SPX_CUDA(cudaStreamSynchronize(h->stream));
 }
 
+// ---------------------------------------------------------------------------
+// Launch configuration
 // ---------------------------------------------------------------------------
 constexpr int kPowderGroup = 64;    // orientations per partial sum of the powder reduction
 
@@ -503,11 +505,11 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     if (opt.lanczos_its != 0 && (opt.lanczos_its < 2 || opt.lanczos_its > spx::kMaxLanczos))
         throw SpxError(SPX_ERR_INVALID_ARGUMENT, "lanczos_its must be 0 or 2..48");
     c.tol = opt.series_tol > 0 ? opt.series_tol : (f64 ? 1e-16 : 1e-11);
-    // chunk: each orientation picks a power-of-two step count whose series
-    // argument s*M*dt is about chunk_x (kernel side); M here is the cap.  The
-    // first layout that fits one SM's shared memory is used: one CTA per
-    // orientation with the longest chunk target, else clusters of 2, 4, 8 CTAs
-    // sharing an orientation (rows split between them).
+    // chunk: each orientation picks the step count whose series argument
+    // s*M*dt is about chunk_x (kernel side); M here is the cap.  The first
+    // layout that fits one SM's shared memory is used: one CTA per orientation
+    // with the longest chunk target, else clusters of 2, 4, 8 CTAs sharing an
+    // orientation (rows split between them).
     c.fixed = opt.chunk_steps > 0;
     const double lg = (h->g_upper > 0) ? 2.0 * h->max_im_diag / (h->g_upper / 4.0) : 0.0;
     // c1 (chunks of any length): x_c = 300 -> 76.8 ms, 450 -> 81.0 ms, 600 -> 84.3 ms

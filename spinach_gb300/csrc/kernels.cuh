@@ -1,7 +1,8 @@
 // Device code of the GB300 powder-FID engine.
 //
-// One CTA owns one orientation at a time (persistent grid, orientations
-// strided over CTAs).  For each orientation it
+// One CTA -- or a thread-block cluster of 2-8 CTAs for systems whose share of
+// L does not fit one SM -- owns one orientation at a time (persistent grid,
+// orientations handed out by a work counter).  For each orientation it
 //   1. forms the Wigner-D coefficients of its Euler angles in FP64
 //      (kernel/utilities/wigner.m:45-77) and assembles the Hermitised
 //      Liouvillian L = Ih + sum_t Re(D_t) S_t + Im(D_t) A_t + 1i R on the
@@ -23,8 +24,8 @@
 //
 // FP32 mode stores Liouvillian values and series coefficients as hi+lo float
 // pairs (about 48 significant bits), keeps state vectors in complex float, and
-// sums every matvec row with a compensated (TwoSum) accumulator in packed
-// f32x2 (re, im) arithmetic: rounding each term at most once is what keeps the
+// sums every matvec row with a Kahan-compensated accumulator in packed f32x2
+// (re, im) arithmetic, rounding the row value once: that is what keeps the
 // phase from drifting over thousands of steps.  FP64 mode stores everything in
 // double.
 #pragma once
@@ -150,26 +151,11 @@ template <class V> __device__ __forceinline__ V warp_sum(V v) {
     }
     return v;
 }
-static __device__ __forceinline__ double warp_sum_d(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-static __device__ __forceinline__ double warp_max_d(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-static __device__ __forceinline__ double warp_min_d(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
 
 // ---------------------------------------------------------------------------
 // Packed f32x2 arithmetic (sm_100+ PTX add/sub/mul/fma.rn.f32x2).  A complex
 // float is one 64-bit register pair (re, im).  Inline PTX is never contracted
-// or reassociated by the compiler, which the TwoSum bookkeeping relies on.
+// or reassociated by the compiler, which the Kahan bookkeeping relies on.
 // ---------------------------------------------------------------------------
 typedef unsigned long long f2x;
 
@@ -195,14 +181,6 @@ static __device__ __forceinline__ f2x swap2(f2x a) { const float2 f = f2up(a); r
 static __device__ __forceinline__ f2x lo2(const float4 &v) { return f2pk(v.x, v.y); }
 static __device__ __forceinline__ f2x hi2(const float4 &v) { return f2pk(v.z, v.w); }
 
-// Y + Z += P with Y the running sum and Z collecting its rounding errors (TwoSum)
-static __device__ __forceinline__ void two_sum2(f2x &Y, f2x &Z, f2x P) {
-    const f2x S = add2(Y, P);
-    const f2x B = sub2(S, Y);
-    const f2x E = add2(sub2(Y, sub2(S, B)), sub2(P, B));
-    Y = S;
-    Z = add2(Z, E);
-}
 // Kahan step: Y + (-C) += P, C the negated low part lost so far
 __device__ __forceinline__ void kahan_add2(f2x &Y, f2x &C, f2x P) {
     const f2x y = sub2(P, C);
@@ -918,7 +896,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             const double half = fmax(0.5 * width * 1.01 + 1e-9 * scale, imax) + 1e-30;
             s_scalar[0] = 0.5 * (hi + lo);   // centre c
             s_scalar[1] = half;              // half-width s
-            // chunk length: about chunk_x series argument per chunk, power of two
+            // chunk length: about chunk_x series argument per chunk
             int Mo = M;
             if (!run.fixed_chunk) {
                 const double target = run.chunk_x / (half * run.dt);
