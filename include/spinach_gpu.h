@@ -202,6 +202,16 @@ spx_status spx_surrogate_set_params(spx_surrogate *s, const float *h_params);
 const char *spx_surrogate_last_error(const spx_surrogate *s);
 
 /*
+ * Per-orientation initial states (kernel/contexts/powder.m:244-254: the
+ * 'aniso_eq' equilibrium or a function-handle rho0 evaluated at every grid
+ * point).  states holds n_states Liouville vectors, orientation after
+ * orientation, interleaved complex; later runs must use grids of exactly
+ * n_states orientations and start orientation n from state n.  n_states = 0
+ * returns to the single rho0 of spx_upload_system (which also clears them).
+ */
+spx_status spx_set_initial_states(spx_handle *handle, int64_t n_states, const double *states);
+
+/*
  * Several detection states at once (kernel/evolution.m 'multichannel',
  * evolution.m:589-673: one FID row per coil column).  coils holds nchan
  * (1..8) columns of the Liouville dimension, column-major, interleaved

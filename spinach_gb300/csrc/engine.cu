@@ -95,6 +95,8 @@ struct spx_handle {
     DevBuf<int> d_coil_rows, d_coil_chan;
     int ncoil = -1;                 // non-zero coil entries if at most 32, else -1
     int nchan = 1;                  // detection channels
+    DevBuf<double2> d_rho0s;        // per-orientation initial states (sliced order)
+    int64_t n_states = 0;           // their count (0: one initial state for all)
     std::vector<int> row_of;        // sliced-ELL row of every basis state
 
     // run buffers
@@ -349,6 +351,7 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
         h->d_coil_chan.upload(std::vector<int>(crow.size(), 0), h->stream);
     }
     h->nchan = 1;
+    h->n_states = 0;
     h->row_of = inv;
     SPX_CUDA(cudaStreamSynchronize(h->stream));
     h->n = (int)n;
@@ -400,6 +403,27 @@ void upload_coils(spx_handle *h, int32_t nchan, const double *coils) {
     }
     h->nchan = nchan;
     SPX_CUDA(cudaStreamSynchronize(h->stream));
+}
+
+// Per-orientation initial states (powder.m:244-254: 'aniso_eq' or a function
+// handle rho0 evaluated at every orientation): states holds n_states
+// Liouville vectors, orientation after orientation, interleaved complex.
+void set_initial_states(spx_handle *h, int64_t n_states, const double *states) {
+    if (!h->have_system) throw SpxError(SPX_ERR_NO_SYSTEM, "no spin system uploaded");
+    if (n_states == 0) { h->n_states = 0; return; }
+    if (n_states < 0 || !states) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "bad initial-state array");
+    const int n = h->n;
+    std::vector<double2> st((size_t)n_states * h->n_pad, make_double2(0, 0));
+    for (int64_t o = 0; o < n_states; ++o)
+        for (int i = 0; i < n; ++i) {
+            const double re = states[2 * ((size_t)o * n + i)], im = states[2 * ((size_t)o * n + i) + 1];
+            if (!std::isfinite(re) || !std::isfinite(im)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite initial state");
+            st[(size_t)o * h->n_pad + h->row_of[i]] = make_double2(re, im);
+        }
+    SPX_CUDA(cudaSetDevice(h->device));
+    h->d_rho0s.upload(st, h->stream);
+    SPX_CUDA(cudaStreamSynchronize(h->stream));
+    h->n_states = n_states;
 }
 
 // ---------------------------------------------------------------------------
@@ -655,6 +679,7 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag;
     sys.ncoil = h->ncoil; sys.coil_rows = h->d_coil_rows.p; sys.coil_vals = h->d_coil_vals.p;
     sys.coil_chan = h->d_coil_chan.p; sys.nchan = h->nchan;
+    sys.rho0s = h->n_states > 0 ? h->d_rho0s.p : nullptr;
     spx::DevRun run{};
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
@@ -758,6 +783,8 @@ spx_status finish_run(spx_handle *h) {
 
 void validate_run(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps) {
     if (!h->have_system) throw SpxError(SPX_ERR_NO_SYSTEM, "no spin system uploaded");
+    if (h->n_states > 0 && h->n_states != n_orient)
+        throw SpxError(SPX_ERR_INVALID_ARGUMENT, "the grid size differs from the number of per-orientation initial states");
     if (n_orient < 1 || n_orient > (1LL << 30)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "bad orientation count");
     if (!(dt > 0.0) || !std::isfinite(dt)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
     if (nsteps < 0 || nsteps > (1LL << 28)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "bad step count");
@@ -974,6 +1001,7 @@ void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, con
     sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag;
     sys.ncoil = h->ncoil; sys.coil_rows = h->d_coil_rows.p; sys.coil_vals = h->d_coil_vals.p;
     sys.coil_chan = h->d_coil_chan.p; sys.nchan = h->nchan;
+    sys.rho0s = h->n_states > 0 ? h->d_rho0s.p : nullptr;
     spx::DevRun run{};
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
@@ -1199,6 +1227,11 @@ const char *spx_status_string(spx_status s) {
 const char *spx_last_error(const spx_handle *h) { return h ? h->err.c_str() : "NULL handle"; }
 
 const char *spx_version(void) { return "spinach-gb300 0.1 (sm_103a)"; }
+
+spx_status spx_set_initial_states(spx_handle *h, int64_t n_states, const double *states) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] { set_initial_states(h, n_states, states); });
+}
 
 spx_status spx_upload_coils(spx_handle *h, int32_t nchan, const double *coils) {
     if (!h) return SPX_ERR_INVALID_ARGUMENT;

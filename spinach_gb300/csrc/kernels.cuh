@@ -328,6 +328,7 @@ struct DevSystem {
     int nterms;
     const int *term_rkm;        // 3 * nterms: rank, k, m (0-based k, m)
     const double2 *rho0;        // n_pad (sliced order)
+    const double2 *rho0s;       // per-orientation initial states (n_orient x n_pad, sliced order) or null
     const double2 *coil;        // n_pad (sliced order)
     int ncoil;                  // 1..32: non-zero coil entries listed below; 0 or -1: use the dense coil
     const int *coil_rows;       // ncoil rows (sliced order)
@@ -1022,7 +1023,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         [[maybe_unused]] f2x tp[RMAX], tc[RMAX], ac[RMAX], cp[RMAX], crr[RMAX], cim[RMAX];
 #pragma unroll
         for (int r = 0; r < RMAX; ++r) {
-            const double2 x0 = r < nr ? sys.rho0[r_row[r]] : make_double2(0.0, 0.0);
+            const double2 x0 = r >= nr ? make_double2(0.0, 0.0)
+                               : sys.rho0s ? sys.rho0s[(size_t)o * sys.n_pad + r_row[r]] : sys.rho0[r_row[r]];
             const double2 c0 = r < nr ? sys.coil[r_row[r]] : make_double2(0.0, 0.0);
             if constexpr (F64) {
                 t_prev[r] = vzero<Vec>(); acc[r] = vzero<Vec>();

@@ -60,6 +60,7 @@ SIGNATURES = {
     'spx_run_powder_noalloc': (C.c_int, [_P, C.c_int64, _P, _P, _P, _P, C.c_double, C.c_int64,
                                          C.c_int32, _P]),
     'spx_upload_coils': (C.c_int, [_P, C.c_int32, _D]),
+    'spx_set_initial_states': (C.c_int, [_P, C.c_int64, _D]),
     'spx_autotune': (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_double, C.c_int64, C.c_int32,
                                C.POINTER(SpxOptions)]),
     'spx_batch_create': (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(_P), C.POINTER(C.c_int64),
@@ -186,6 +187,16 @@ class Engine:
             C.byref(Rh.struct) if Rh else None, _dptr(rho0), _dptr(coil)), self.h)
         self.dim = n
         self.nchan = 1
+
+    def set_initial_states(self, states):
+        """One initial state per orientation (powder.m 'aniso_eq' or a function
+        handle rho0): an (n_orient, dim) array; None returns to the single rho0."""
+        if states is None:
+            self._check(self.lib.spx_set_initial_states(self.h, 0, None), self.h)
+            return
+        arr = np.ascontiguousarray(np.asarray(states, np.complex128))
+        flat = arr.view(np.float64).ravel()
+        self._check(self.lib.spx_set_initial_states(self.h, arr.shape[0], _dptr(flat)), self.h)
 
     def upload_coils(self, coils):
         """Several detection states (evolution.m 'multichannel'): ``coils`` is

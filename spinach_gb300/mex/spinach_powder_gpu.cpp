@@ -2,7 +2,8 @@
 //
 //   fid          = spinach_powder_gpu(I, Q, R, rho0, coil, grid, dt, nsteps)
 //                  (coil with several columns: one FID row per column, as
-//                  evolution(...,'multichannel') returns)
+//                  evolution(...,'multichannel') returns; rho0 with one
+//                  column per orientation: per-orientation initial states)
 //   [fid, fids]  = spinach_powder_gpu(I, Q, R, rho0, coil, grid, dt, nsteps, opts)
 //
 // I, Q     the outputs of [I,Q]=hamiltonian(spin_system) (kernel/hamiltonian.m:44):
@@ -105,12 +106,6 @@ std::vector<double> columns(const mxArray *A, int64_t n, int64_t ncol, const cha
     return out;
 }
 
-std::vector<double> column(const mxArray *A, int64_t n, const char *name) {
-    if (!mxIsDouble(A) || (int64_t)mxGetNumberOfElements(A) != n)
-        throw GatewayError{"Spinach:spinach_powder_gpu:input", std::string(name) + " must be a double vector of length dim."};
-    return columns(A, n, 1, name);
-}
-
 std::vector<double> grid_field(const mxArray *g, const char *name, int64_t &count) {
     const mxArray *f = mxGetField(g, 0, name);
     if (!f || !mxIsDouble(f) || mxIsComplex(f) || mxIsSparse(f))
@@ -170,7 +165,11 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     CscCopy R;
     const bool have_R = !mxIsEmpty(prhs[2]);
     if (have_R) fill_csc(prhs[2], n, "R", R);
-    const std::vector<double> rho0 = column(prhs[3], n, "rho0");
+    // rho0 with one column per orientation: the per-orientation initial states
+    // of powder.m:244-254 ('aniso_eq' or a function handle, evaluated by the caller)
+    const int64_t nrho = (int64_t)mxGetN(prhs[3]);
+    const std::vector<double> rho0s = columns(prhs[3], n, nrho, "rho0");
+    const std::vector<double> rho0(rho0s.begin(), rho0s.begin() + 2 * n);
     // several coil columns = several detection channels (evolution.m 'multichannel')
     const int64_t nchan = (int64_t)mxGetN(prhs[4]);
     if (nchan < 1 || nchan > 8)
@@ -211,6 +210,11 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     spx_status st = spx_upload_system(g_handle, &I.view, (int32_t)rank.size(), rank.data(), kk.data(), mm.data(),
                                       qv.data(), have_R ? &R.view : nullptr, rho0.data(), coil.data());
     if (st == SPX_OK && nchan > 1) st = spx_upload_coils(g_handle, (int32_t)nchan, coils.data());
+    if (st == SPX_OK && nrho > 1) {
+        if (nrho != no)
+            throw GatewayError{"Spinach:spinach_powder_gpu:rho0", "rho0 needs one column, or one per grid orientation."};
+        st = spx_set_initial_states(g_handle, nrho, rho0s.data());
+    }
     if (st != SPX_OK)
         throw GatewayError{"Spinach:spinach_powder_gpu:upload", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
     // one channel: (nsteps+1) x 1 like powder(); several: one row per channel

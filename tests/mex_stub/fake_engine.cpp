@@ -16,7 +16,7 @@ struct Recorded {
     std::vector<int> rank, k, m;
     std::vector<std::vector<double>> Q_values;
     bool have_R = false;
-    std::vector<double> R_values, rho0, coil, coils, grid;
+    std::vector<double> R_values, rho0, coil, coils, states, grid;
     int nchan = 1;
     double dt = 0;
     int64_t nsteps = 0, n_orient = 0;
@@ -49,6 +49,11 @@ spx_status spx_upload_system(spx_handle *, const spx_csc *I, int32_t nt, const i
     g_rec.coil.assign(coil, coil + 2 * n);
     g_rec.nchan = 1;
     g_rec.coils.clear();
+    g_rec.states.clear();
+    return SPX_OK;
+}
+spx_status spx_set_initial_states(spx_handle *, int64_t n_states, const double *states) {
+    g_rec.states.assign(states, states + 2 * g_rec.n * n_states);
     return SPX_OK;
 }
 spx_status spx_upload_coils(spx_handle *, int32_t nchan, const double *coils) {

@@ -15,7 +15,7 @@ struct Recorded {
     std::vector<int> rank, k, m;
     std::vector<std::vector<double>> Q_values;
     bool have_R;
-    std::vector<double> R_values, rho0, coil, coils, grid;
+    std::vector<double> R_values, rho0, coil, coils, states, grid;
     int nchan;
     double dt;
     int64_t nsteps, n_orient;
@@ -131,6 +131,17 @@ int main() {
     expect(1, 8, badq, "Spinach:spinach_powder_gpu:Q");
     const mxArray *badn[8] = {I, Q, R, rho0, coil, grid, scalar(1e-5), scalar(2.5)};
     expect(1, 8, badn, "Spinach:spinach_powder_gpu:nsteps");
+    // one rho0 column per orientation: spx_set_initial_states gets all three
+    mxArray *rho3 = new mxArray; rho3->m = n; rho3->n = 3;
+    rho3->re = {1, 0, 0, 0, 0, 2, 0, 0, 0, 0, 3, 0};
+    const mxArray *pr3[8] = {I, Q, R, rho3, coil, grid, scalar(1e-5), scalar(5)};
+    mxArray *or3[1] = {nullptr};
+    mexFunction(1, or3, 8, pr3);
+    CHECK(g_rec.states.size() == 24 && g_rec.states[0] == 1.0 && g_rec.states[2 * 5] == 2.0 && g_rec.states[2 * 10] == 3.0);
+    CHECK((g_rec.rho0 == std::vector<double>{1, 0, 0, 0, 0, 0, 0, 0}));
+    mxArray *rho2 = new mxArray; rho2->m = n; rho2->n = 2; rho2->re = {1, 0, 0, 0, 0, 2, 0, 0};
+    const mxArray *pr2[8] = {I, Q, R, rho2, coil, grid, scalar(1e-5), scalar(5)};
+    expect(1, 8, pr2, "Spinach:spinach_powder_gpu:rho0");
     mxArray *o2[2] = {nullptr, nullptr};
     expect(2, 8, pc, "Spinach:spinach_powder_gpu:nlhs");
     (void)o2;
