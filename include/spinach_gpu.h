@@ -202,6 +202,19 @@ spx_status spx_surrogate_set_params(spx_surrogate *s, const float *h_params);
 const char *spx_surrogate_last_error(const spx_surrogate *s);
 
 /*
+ * CPMG echo train on the same evolution core (experiments/cpmg.m): a hard
+ * 90-degree pulse exp(-1i*(pi/2)*pulse_op) on rho0, npoints-1 steps of
+ * acquisition, then nloops times a 180-degree pulse and 2*npoints-1 steps;
+ * fid receives the concatenated powder FIDs, npoints*(1 + 2*nloops) complex
+ * values.  pulse_op is the pulse's commutation superoperator in the basis of
+ * the uploaded system (operator(spin_system,'Lx',...) in Spinach).  Needs one
+ * coil and the single rho0.
+ */
+spx_status spx_run_cpmg(spx_handle *handle, int64_t n_orient, const double *alphas, const double *betas,
+                        const double *gammas, const double *weights, double dt, int64_t npoints, int32_t nloops,
+                        const spx_csc *pulse_op, const spx_options *opt, double *fid);
+
+/*
  * Per-orientation initial states (kernel/contexts/powder.m:244-254: the
  * 'aniso_eq' equilibrium or a function-handle rho0 evaluated at every grid
  * point).  states holds n_states Liouville vectors, orientation after

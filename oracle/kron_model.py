@@ -118,6 +118,33 @@ class KronModel:
             r = P @ r
         return out
 
+    def cpmg(self, angles, rho0, coil, pulse_op, dt, npoints, nloops):
+        """CPMG echo train with hard pulses U rho U^dagger, U = exp(-1i theta
+        pulse_op) (Hilbert space), theta = pi/2 first and pi in every loop;
+        segments of npoints-1 and 2*npoints-1 steps, each starting from the
+        pulsed last state of the one before."""
+        H = self.hamiltonian(angles)
+        I = np.eye(self.dim)
+        L = np.kron(H, I) - np.kron(I, H.T) + 1j * self.relaxation()
+        P = sla.expm(-1j * dt * L)
+        c = coil.reshape(-1)
+
+        def pulse(r, theta):
+            U = sla.expm(-1j * theta * pulse_op)
+            return (U @ r.reshape(self.dim, self.dim) @ U.conj().T).reshape(-1)
+
+        r = pulse(rho0.reshape(-1).astype(complex), np.pi / 2)
+        out = []
+        for seg in range(nloops + 1):
+            n = npoints - 1 if seg == 0 else 2 * npoints - 1
+            if seg:
+                r = pulse(r, np.pi)
+            for k in range(n + 1):
+                out.append(np.vdot(c, r))
+                if k < n:
+                    r = P @ r
+        return np.array(out)
+
 
 def gamma_of(isotope):
     return ISOTOPES[isotope][1]

@@ -817,6 +817,47 @@ def acquire(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
                                 1.0 / parameters['sweep'], parameters['npoints'] - 1)
 
 
+def evolution_trajectory(ss: SpinSystem, L, rho, dt: float, nsteps: int) -> np.ndarray:
+    """kernel/evolution.m:310-381 ('trajectory', one subspace): the states at
+    steps 0..nsteps as columns; propagator below krylov_tol, else repeated
+    step() (kernel/krylov.m 'trajectory')."""
+    L = clean_up(ss, sp.csc_matrix(L), ss.tols['liouv_zero'])
+    rho = clean_up(ss, np.asarray(rho, complex), ss.tols['zte_tol'])
+    dim = L.shape[0]
+    ans = np.zeros((dim, nsteps + 1), complex)
+    if dim < ss.tols['krylov_tol'] and 'krylov' not in ss.enable:
+        P = propagator(ss, L, dt)
+        for n in range(nsteps + 1):
+            ans[:, n] = rho
+            rho = P @ rho
+    else:
+        L = sp.csr_matrix(L)
+        ans[:, 0] = rho
+        for n in range(1, nsteps + 1):
+            rho = step(ss, L, rho, dt)
+            ans[:, n] = rho
+    return clean_up(ss, ans, ss.tols['zte_tol'])
+
+
+def cpmg(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
+    """experiments/cpmg.m:29-63 (K = 0, one spatial point): a 90-degree pulse
+    step(pulse_op, rho0, pi/2), a half-echo of npoints-1 steps, then nloops
+    times a 180-degree pulse on the last state and an echo of 2*npoints-1
+    steps; the detected trajectories concatenated."""
+    L = H + 1j * R
+    coil = np.asarray(parameters['coil'], complex)
+    P = parameters['pulse_op']
+    dt = parameters['timestep']
+    rho = step(ss, P, parameters['rho0'], np.pi / 2)
+    traj = evolution_trajectory(ss, L, rho, dt, parameters['npoints'] - 1)
+    fid = [coil.conj() @ traj]
+    for _ in range(parameters['nloops']):
+        last = step(ss, P, traj[:, -1], np.pi)
+        traj = evolution_trajectory(ss, L, last, dt, 2 * parameters['npoints'] - 1)
+        fid.append(coil.conj() @ traj)
+    return np.concatenate(fid)
+
+
 # --------------------------------------------------------------------------
 # Grids and the powder context
 # --------------------------------------------------------------------------
@@ -854,6 +895,14 @@ def powder_orientation_fid(ss, I, Q, parameters, angles) -> np.ndarray:
     H = (H + H.conj().T) / 2
     R = relaxation(ss)
     return acquire(ss, parameters, H, R)
+
+
+def powder_orientation_cpmg(ss, I, Q, parameters, angles) -> np.ndarray:
+    """One iteration of kernel/contexts/powder.m:226-274 with @cpmg."""
+    A = orientation(Q, angles)
+    H = I if A is None else I + A
+    H = (H + H.conj().T) / 2
+    return cpmg(ss, parameters, H, relaxation(ss))
 
 
 def powder(ss: SpinSystem, parameters: dict, assumptions: str, grid, setup=None,

@@ -96,6 +96,10 @@ struct spx_handle {
     int ncoil = -1;                 // non-zero coil entries if at most 32, else -1
     int nchan = 1;                  // detection channels
     DevBuf<double2> d_rho0s;        // per-orientation initial states (sliced order)
+    DevBuf<double2> d_seq[2], d_seq_rho;   // pulse sequences: states between segments
+    DevBuf<int> d_pulse_ptr, d_pulse_col;  // pulse superoperator, CSR in sliced order
+    DevBuf<double2> d_pulse_val;
+    double pulse_norm1 = 0.0;
     int64_t n_states = 0;           // their count (0: one initial state for all)
     std::vector<int> row_of;        // sliced-ELL row of every basis state
 
@@ -663,9 +667,18 @@ void reserve_run(spx_handle *h, int64_t n_orient, int64_t nsteps, bool f64, cons
     h->d_part.reserve((size_t)ngroups * npts);
 }
 
+// Initial and final states of one run when they are not the handle's own
+// (pulse sequences hand the state of one segment to the next).
+struct RunIO {
+    const double2 *rho0 = nullptr;     // one initial state for every orientation (sliced order)
+    const double2 *rho0s = nullptr;    // one per orientation, n_orient x n_pad
+    double2 *state_out = nullptr;      // the state after the last step, n_orient x n_pad
+};
+
 void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be,
                    const double *d_ga, const double *d_w, double dt, int64_t nsteps,
-                   const spx_options &opt, double2 *d_out, const Config &c, int safe_bounds = 0, bool timed = true) {
+                   const spx_options &opt, double2 *d_out, const Config &c, int safe_bounds = 0, bool timed = true,
+                   const RunIO &io = RunIO{}) {
     const bool f64 = opt.precision == SPX_FP64;
     const size_t npts = ((size_t)nsteps + 1) * h->nchan;   // the powder sum treats channels as more points
     reserve_run(h, n_orient, nsteps, f64, c);
@@ -680,7 +693,10 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     sys.ncoil = h->ncoil; sys.coil_rows = h->d_coil_rows.p; sys.coil_vals = h->d_coil_vals.p;
     sys.coil_chan = h->d_coil_chan.p; sys.nchan = h->nchan;
     sys.rho0s = h->n_states > 0 ? h->d_rho0s.p : nullptr;
+    if (io.rho0) sys.rho0 = io.rho0;
+    if (io.rho0s) sys.rho0s = io.rho0s;
     spx::DevRun run{};
+    run.state_out = io.state_out;
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
     run.fixed_chunk = c.fixed ? 1 : 0; run.chunk_x = c.chunk_x;
@@ -810,6 +826,142 @@ spx_status guarded(spx_handle *h, F f) {
     } catch (...) {
         if (h) h->err = "unknown failure";
         return SPX_ERR_INTERNAL;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pulse sequences
+// ---------------------------------------------------------------------------
+// exp(-1i * theta * P) applied to many states (kernel/step.m: a hard pulse
+// step(spin_system, pulse_op, rho, angle)), FP64: nsub substeps of a Taylor
+// series with nterms terms, each substep's argument at most 1 in the 1-norm.
+// One CTA per state at a time; x (the sum), t (the term) and u in shared memory.
+__global__ void pulse_kernel(int n_states, int n_pad, const int *__restrict__ ptr, const int *__restrict__ col,
+                             const double2 *__restrict__ val, double theta_sub, int nsub, int nterms,
+                             double2 *states) {
+    extern __shared__ double2 ps[];
+    double2 *x = ps, *t = ps + n_pad, *u = ps + 2 * n_pad;
+    for (int st = blockIdx.x; st < n_states; st += gridDim.x) {
+        double2 *sv = states + (size_t)st * n_pad;
+        for (int i = threadIdx.x; i < n_pad; i += blockDim.x) x[i] = sv[i];
+        __syncthreads();
+        for (int sub = 0; sub < nsub; ++sub) {
+            for (int i = threadIdx.x; i < n_pad; i += blockDim.x) t[i] = x[i];
+            __syncthreads();
+            for (int k = 1; k <= nterms; ++k) {
+                // u = (-1i theta / k) P t
+                const double f = theta_sub / k;
+                for (int i = threadIdx.x; i < n_pad; i += blockDim.x) {
+                    double re = 0.0, im = 0.0;
+                    for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+                        const double2 a = val[e], b = t[col[e]];
+                        re = fma(a.x, b.x, fma(-a.y, b.y, re));
+                        im = fma(a.x, b.y, fma(a.y, b.x, im));
+                    }
+                    u[i] = make_double2(f * im, -f * re);       // -1i * f * (re + 1i im)
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < n_pad; i += blockDim.x) {
+                    t[i] = u[i];
+                    x[i].x += u[i].x;
+                    x[i].y += u[i].y;
+                }
+                __syncthreads();
+            }
+        }
+        for (int i = threadIdx.x; i < n_pad; i += blockDim.x) sv[i] = x[i];
+        __syncthreads();
+    }
+}
+
+// Upload a pulse superoperator (CSC, the caller's basis order) as CSR rows in
+// the sliced order of the uploaded system.
+void upload_pulse(spx_handle *h, const spx_csc *P) {
+    check_csc(P, h->n, "pulse_op");
+    const int n_pad = h->n_pad;
+    std::vector<std::vector<std::pair<int, double2>>> rows(n_pad);
+    std::vector<double> colsum(h->n, 0.0);
+    for_each_entry(P, [&](int64_t r, int64_t c, Cplx v) {
+        if (v.re == 0.0 && v.im == 0.0) return;
+        rows[h->row_of[r]].push_back({h->row_of[c], make_double2(v.re, v.im)});
+        colsum[c] += std::hypot(v.re, v.im);
+    });
+    std::vector<int> ptr(n_pad + 1, 0), col;
+    std::vector<double2> val;
+    for (int i = 0; i < n_pad; ++i) {
+        for (auto &e : rows[i]) { col.push_back(e.first); val.push_back(e.second); }
+        ptr[i + 1] = (int)col.size();
+    }
+    if (col.empty()) { col.push_back(0); val.push_back(make_double2(0, 0)); }
+    SPX_CUDA(cudaSetDevice(h->device));
+    h->d_pulse_ptr.upload(ptr, h->stream);
+    h->d_pulse_col.upload(col, h->stream);
+    h->d_pulse_val.upload(val, h->stream);
+    h->pulse_norm1 = colsum.empty() ? 0.0 : *std::max_element(colsum.begin(), colsum.end());
+}
+
+void apply_pulse(spx_handle *h, double theta, int64_t n_states, double2 *states) {
+    const double x = h->pulse_norm1 * std::fabs(theta);
+    const int nsub = std::max(1, (int)std::ceil(x));
+    const int nterms = 25;                     // 1 / 25! < 1e-25 per substep
+    const size_t smem = 3 * (size_t)h->n_pad * sizeof(double2);
+    if (smem > h->smem_optin) throw SpxError(SPX_ERR_UNSUPPORTED, "pulse states do not fit shared memory");
+    SPX_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void *>(&pulse_kernel),
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = (int)std::min<int64_t>(n_states, (int64_t)h->sm_count * 2);
+    pulse_kernel<<<grid, 256, smem, h->stream>>>((int)n_states, h->n_pad, h->d_pulse_ptr.p, h->d_pulse_col.p,
+                                                 h->d_pulse_val.p, theta / nsub, nsub, nterms, states);
+    SPX_CUDA(cudaGetLastError());
+}
+
+// experiments/cpmg.m: a 90-degree pulse, npoints-1 steps of acquisition, then
+// nloops times (180-degree pulse, 2*npoints-1 steps), the FIDs concatenated
+// (npoints + 2*npoints*nloops points).  Each segment is one powder run that
+// starts from the previous segment's final states.
+void run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
+              const double *weights, double dt, int64_t npoints, int32_t nloops, const spx_csc *pulse_op,
+              const spx_options &o, double *fid) {
+    if (h->nchan != 1 || h->n_states != 0)
+        throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil and one initial state");
+    // experiments/cpmg.m:77-90: both positive integers
+    if (npoints < 1 || nloops < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "npoints and nloops must be positive");
+    validate_run(h, n_orient, dt, 2 * npoints);
+    upload_pulse(h, pulse_op);
+    h->d_grid.reserve(4 * (size_t)n_orient);
+    double *g = h->d_grid.p;
+    const size_t b = (size_t)n_orient * sizeof(double);
+    SPX_CUDA(cudaMemcpyAsync(g, alphas, b, cudaMemcpyHostToDevice, h->stream));
+    SPX_CUDA(cudaMemcpyAsync(g + n_orient, betas, b, cudaMemcpyHostToDevice, h->stream));
+    SPX_CUDA(cudaMemcpyAsync(g + 2 * n_orient, gammas, b, cudaMemcpyHostToDevice, h->stream));
+    SPX_CUDA(cudaMemcpyAsync(g + 3 * n_orient, weights, b, cudaMemcpyHostToDevice, h->stream));
+    const size_t ns = (size_t)n_orient * h->n_pad;
+    h->d_seq[0].reserve(ns);
+    h->d_seq[1].reserve(ns);
+    h->d_seq_rho.reserve(h->n_pad);
+    h->d_fid.reserve(2 * (size_t)npoints);
+    // the first pulse acts on the orientation-independent rho0
+    SPX_CUDA(cudaMemcpyAsync(h->d_seq_rho.p, h->d_rho0.p, h->n_pad * sizeof(double2), cudaMemcpyDeviceToDevice,
+                             h->stream));
+    apply_pulse(h, M_PI / 2, 1, h->d_seq_rho.p);
+    size_t at = 0;
+    int cur = 0;
+    for (int seg = 0; seg <= nloops; ++seg) {
+        const int64_t nsteps = seg == 0 ? npoints - 1 : 2 * npoints - 1;
+        RunIO io;
+        if (seg == 0) {
+            io.rho0 = h->d_seq_rho.p;
+        } else {
+            apply_pulse(h, M_PI, n_orient, h->d_seq[cur].p);
+            io.rho0s = h->d_seq[cur].p;
+        }
+        io.state_out = h->d_seq[cur ^ 1].p;
+        const Config c = choose_config(h, n_orient, dt, nsteps, o, 0);
+        launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o, h->d_fid.p, c,
+                      0, true, io);
+        finish_run(h);
+        SPX_CUDA(cudaMemcpy(fid + 2 * at, h->d_fid.p, ((size_t)nsteps + 1) * sizeof(double2), cudaMemcpyDeviceToHost));
+        at += (size_t)nsteps + 1;
+        cur ^= 1;
     }
 }
 
@@ -1227,6 +1379,27 @@ const char *spx_status_string(spx_status s) {
 const char *spx_last_error(const spx_handle *h) { return h ? h->err.c_str() : "NULL handle"; }
 
 const char *spx_version(void) { return "spinach-gb300 0.1 (sm_103a)"; }
+
+spx_status spx_run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
+                        const double *gammas, const double *weights, double dt, int64_t npoints, int32_t nloops,
+                        const spx_csc *pulse_op, const spx_options *opt, double *fid) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (!alphas || !betas || !gammas || !weights || !fid || !pulse_op)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL argument");
+        for (int64_t o = 0; o < n_orient; ++o)
+            if (!std::isfinite(alphas[o]) || !std::isfinite(betas[o]) || !std::isfinite(gammas[o]) ||
+                !std::isfinite(weights[o]))
+                throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite grid entry");
+        spx_options o{};
+        if (opt) o = *opt;
+        if (o.precision != SPX_FP32 && o.precision != SPX_FP64)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
+        o = apply_tuned(h, o);
+        SPX_CUDA(cudaSetDevice(h->device));
+        run_cpmg(h, n_orient, alphas, betas, gammas, weights, dt, npoints, nloops, pulse_op, o, fid);
+    });
+}
 
 spx_status spx_set_initial_states(spx_handle *h, int64_t n_states, const double *states) {
     if (!h) return SPX_ERR_INVALID_ARGUMENT;

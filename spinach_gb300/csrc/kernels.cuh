@@ -358,6 +358,7 @@ struct DevRun {
     int *kused;         // n_orient
     int *mused;         // n_orient: time steps per chunk used
     int cl;                 // CTAs per cluster (1: no cluster)
+    double2 *state_out;     // or null: the state after the last step, n_orient x n_pad (sliced order)
     int *next_orient;       // work counter (zeroed before the launch): single CTAs take
                             // orientations gridDim.x, gridDim.x + 1, ... as they finish
     int cl_slices[kMaxCluster + 1];   // slice boundaries of the CTAs' row blocks (cluster launches)
@@ -1040,9 +1041,31 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         }
         long long mv = 0;
         for (int a = 0; a < nchunks && status == kDevOk; ++a) {
-            const bool advance = (a + 1 < nchunks);
-            const int Kc = advance ? K : K_last;          // terms of this chunk
+            const bool last = (a + 1 == nchunks);
+            // the last chunk also propagates the state when the caller wants it
+            // (pulse sequences continue from it): its coefficients are those of
+            // its own length j_last, from the same Bessel table
+            const bool advance = !last || run.state_out != nullptr;
+            const int Kc = last ? K_last : K;              // terms of this chunk
             mv += Kc - 1;
+            if (last && run.state_out && nchunks > 0) {
+                const int j_last = nsteps - (nchunks - 1) * Mo;
+                const double tau = j_last * run.dt;
+                const double pr = cos(-cen * tau), pi_ = sin(-cen * tau);
+                csync<CLU>();                              // the previous chunk's reads of the coefficients are done
+                for (int k = tid; k < Kc; k += blockDim.x) {
+                    const double jv = table[(size_t)k * (Mo + 1) + j_last];
+                    double re, im;
+                    switch (k & 3) {
+                        case 0: re = pr; im = pi_; break;
+                        case 1: re = pi_; im = -pr; break;
+                        case 2: re = -pr; im = -pi_; break;
+                        default: re = -pi_; im = pr; break;
+                    }
+                    pack(s_atau[k], re * jv, im * jv);
+                }
+                csync<CLU>();
+            }
             double start_n2 = 0.0, end_n2 = 0.0;
             if constexpr (F64) {
                 // k = 0: t0 = rho
@@ -1323,6 +1346,18 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             start_n2 = cluster_reduce<CLU, 0>(start_n2, s_red, s_cred, par, crank, CL);
             if (!isfinite(end_n2)) status = kDevNonFinite;
             else if (end_n2 > 16.0 * start_n2 + 1e-300) status = kDevDiverged;
+        }
+        if (run.state_out) {
+            // the state at the last step, each CTA its own rows
+#pragma unroll
+            for (int r = 0; r < RMAX; ++r) {
+                if (r < nr) {
+                    double2 v;
+                    if constexpr (F64) v = tod(t_cur[r]);
+                    else v = tod(f2up(tc[r]));
+                    run.state_out[(size_t)o * sys.n_pad + r_row[r]] = v;
+                }
+            }
         }
         if (tid == 0 && crank == 0) {
             run.status[o] = status;

@@ -59,6 +59,8 @@ SIGNATURES = {
                                         C.POINTER(SpxOptions), _P]),
     'spx_run_powder_noalloc': (C.c_int, [_P, C.c_int64, _P, _P, _P, _P, C.c_double, C.c_int64,
                                          C.c_int32, _P]),
+    'spx_run_cpmg': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.c_int32,
+                               C.POINTER(SpxCsc), C.POINTER(SpxOptions), _D]),
     'spx_upload_coils': (C.c_int, [_P, C.c_int32, _D]),
     'spx_set_initial_states': (C.c_int, [_P, C.c_int64, _D]),
     'spx_autotune': (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_double, C.c_int64, C.c_int32,
@@ -230,6 +232,24 @@ class Engine:
         else:
             f = f.reshape(nch, nsteps + 1)
         return PowderResult(f, fs, self.stats())
+
+    def run_cpmg(self, alphas, betas, gammas, weights, dt: float, npoints: int, nloops: int, pulse_op,
+                 precision: int = FP32, threads: int = 0, cluster: int = 0) -> PowderResult:
+        """CPMG echo train (experiments/cpmg.m): 90-degree pulse about ``pulse_op``
+        (a commutation superoperator), npoints-1 steps, then ``nloops`` times a
+        180-degree pulse and 2*npoints-1 steps.  ``fid`` holds the concatenated
+        powder FIDs, npoints*(1 + 2*nloops) points."""
+        al = np.ascontiguousarray(alphas, np.float64)
+        be = np.ascontiguousarray(betas, np.float64)
+        ga = np.ascontiguousarray(gammas, np.float64)
+        w = np.ascontiguousarray(weights, np.float64)
+        fid = np.zeros(2 * npoints * (1 + 2 * nloops))
+        P = _CscHolder(pulse_op, self.dim)
+        opt = SpxOptions(precision, 0, threads, cluster, 0.0, 0.0, 0, 0)
+        self._check(self.lib.spx_run_cpmg(self.h, al.size, _dptr(al), _dptr(be), _dptr(ga), _dptr(w), float(dt),
+                                          int(npoints), int(nloops), C.byref(P.struct), C.byref(opt), _dptr(fid)),
+                    self.h)
+        return PowderResult(fid.view(np.complex128), None, self.stats())
 
     def run_device(self, d_alphas: int, d_betas: int, d_gammas: int, d_weights: int, n_orient: int,
                    dt: float, nsteps: int, d_fid: int, precision: int = FP32, chunk_steps: int = 0,

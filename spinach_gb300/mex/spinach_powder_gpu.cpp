@@ -13,7 +13,10 @@
 // rho0     initial state, coil detection state (dense or sparse columns).
 // grid     struct with alphas, betas, gammas, weights (a kernel/grids/*.mat file).
 // dt       1/parameters.sweep,  nsteps  parameters.npoints-1  (acquire.m:70-71).
-// opts     optional struct: precision ('double' default, or 'single').
+// opts     optional struct: precision ('double' default, or 'single');
+//          pulse_op (sparse dim x dim) and nloops run experiments/cpmg.m
+//          instead of acquire.m: npoints = nsteps+1 per half-echo, fid
+//          npoints*(1+2*nloops) x 1.
 // fid      (nsteps+1) x 1 complex: sum_n weights(n) fid_n (powder.m:280-287).
 // fids     (nsteps+1) x n_orient complex, the sum_up=false output (powder.m:291-297).
 //
@@ -190,7 +193,22 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     const int64_t nsteps = (int64_t)ns;
     spx_options opt{};
     opt.precision = SPX_FP64;
+    CscCopy pulse;
+    int32_t nloops = 0;                 // > 0: a CPMG echo train (experiments/cpmg.m)
     if (nrhs == 9) {
+        const mxArray *po = mxGetField(prhs[8], 0, "pulse_op");
+        const mxArray *nl = mxGetField(prhs[8], 0, "nloops");
+        if ((po == nullptr) != (nl == nullptr))
+            throw GatewayError{"Spinach:spinach_powder_gpu:cpmg", "opts.pulse_op and opts.nloops go together."};
+        if (po) {
+            fill_csc(po, n, "opts.pulse_op", pulse);
+            const double v = scalar(nl, "opts.nloops");
+            if (v < 1 || v != (double)(int32_t)v)
+                throw GatewayError{"Spinach:spinach_powder_gpu:cpmg", "opts.nloops must be a positive integer."};
+            nloops = (int32_t)v;
+            if (nlhs > 1)
+                throw GatewayError{"Spinach:spinach_powder_gpu:nlhs", "a CPMG train returns the powder FID only."};
+        }
         const mxArray *p = mxGetField(prhs[8], 0, "precision");
         if (p) {
             char buf[16] = {0};
@@ -217,6 +235,18 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     }
     if (st != SPX_OK)
         throw GatewayError{"Spinach:spinach_powder_gpu:upload", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
+    if (nloops > 0) {
+        const int64_t npts = (nsteps + 1) * (1 + 2 * (int64_t)nloops);
+        std::vector<double> fid(2 * (size_t)npts);
+        st = spx_run_cpmg(g_handle, no, al.data(), be.data(), ga.data(), wt.data(), dt, nsteps + 1, nloops,
+                          &pulse.view, &opt, fid.data());
+        if (st != SPX_OK)
+            throw GatewayError{"Spinach:spinach_powder_gpu:run", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
+        plhs[0] = mxCreateDoubleMatrix((mwSize)npts, 1, mxCOMPLEX);
+        mxComplexDouble *out = mxGetComplexDoubles(plhs[0]);
+        for (int64_t i = 0; i < npts; ++i) { out[i].real = fid[2 * i]; out[i].imag = fid[2 * i + 1]; }
+        return;
+    }
     // one channel: (nsteps+1) x 1 like powder(); several: one row per channel
     plhs[0] = nchan == 1 ? mxCreateDoubleMatrix((mwSize)(nsteps + 1), 1, mxCOMPLEX)
                          : mxCreateDoubleMatrix((mwSize)nchan, (mwSize)(nsteps + 1), mxCOMPLEX);

@@ -23,6 +23,9 @@ struct Recorded {
     int precision = -1;
     bool want_per = false;
     int fail_run = 0;
+    std::vector<double> pulse;
+    int64_t npoints = 0;
+    int nloops = 0;
 } g_rec;
 
 static spx_handle g_h;
@@ -84,6 +87,18 @@ spx_status spx_run_powder(spx_handle *, int64_t no, const double *a, const doubl
                 per[2 * (o * (nsteps + 1) + i)] = 100.0 * o + i;
                 per[2 * (o * (nsteps + 1) + i) + 1] = 1.0;
             }
+    return SPX_OK;
+}
+spx_status spx_run_cpmg(spx_handle *, int64_t no, const double *, const double *, const double *, const double *,
+                        double dt, int64_t npoints, int32_t nloops, const spx_csc *P, const spx_options *opt,
+                        double *fid) {
+    g_rec.n_orient = no;
+    g_rec.dt = dt;
+    g_rec.npoints = npoints;
+    g_rec.nloops = nloops;
+    g_rec.precision = opt ? opt->precision : -1;
+    g_rec.pulse.assign(P->values, P->values + 2 * P->colptr[P->n]);
+    for (int64_t i = 0; i < npoints * (1 + 2 * nloops); ++i) { fid[2 * i] = 2.0 * i; fid[2 * i + 1] = 1.0; }
     return SPX_OK;
 }
 spx_status spx_run_powder_device(spx_handle *, int64_t, const double *, const double *, const double *,

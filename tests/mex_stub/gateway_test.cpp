@@ -22,6 +22,9 @@ struct Recorded {
     int precision;
     bool want_per;
     int fail_run;
+    std::vector<double> pulse;
+    int64_t npoints;
+    int nloops;
 };
 extern Recorded g_rec;
 void stub_run_atexit();
@@ -142,6 +145,26 @@ int main() {
     mxArray *rho2 = new mxArray; rho2->m = n; rho2->n = 2; rho2->re = {1, 0, 0, 0, 0, 2, 0, 0};
     const mxArray *pr2[8] = {I, Q, R, rho2, coil, grid, scalar(1e-5), scalar(5)};
     expect(1, 8, pr2, "Spinach:spinach_powder_gpu:rho0");
+    // opts.pulse_op + opts.nloops: the CPMG train (experiments/cpmg.m)
+    mxArray *copt = strct();
+    copt->fields["pulse_op"] = sparse(n, {0, 1}, {1, 0}, {0.5, 0.5}, {0.0, -0.25});
+    copt->fields["nloops"] = scalar(2);
+    const mxArray *pcp[9] = {I, Q, R, rho0, coil, grid, scalar(1e-5), scalar(5), copt};
+    mxArray *ocp[1] = {nullptr};
+    mexFunction(1, ocp, 9, pcp);
+    CHECK(g_rec.npoints == 6 && g_rec.nloops == 2 && g_rec.precision == 1 && g_rec.dt == 1e-5);
+    CHECK((g_rec.pulse == std::vector<double>{0.5, -0.25, 0.5, 0.0}));
+    CHECK(ocp[0] && ocp[0]->m == 30 && ocp[0]->n == 1 && ocp[0]->cx[7].real == 14.0 && ocp[0]->cx[7].imag == 1.0);
+    expect(2, 9, pcp, "Spinach:spinach_powder_gpu:nlhs");
+    mxArray *copt2 = strct();
+    copt2->fields["pulse_op"] = copt->fields["pulse_op"];
+    copt2->fields["nloops"] = scalar(0);
+    const mxArray *pcp2[9] = {I, Q, R, rho0, coil, grid, scalar(1e-5), scalar(5), copt2};
+    expect(1, 9, pcp2, "Spinach:spinach_powder_gpu:cpmg");
+    mxArray *copt3 = strct();
+    copt3->fields["nloops"] = scalar(1);
+    const mxArray *pcp3[9] = {I, Q, R, rho0, coil, grid, scalar(1e-5), scalar(5), copt3};
+    expect(1, 9, pcp3, "Spinach:spinach_powder_gpu:cpmg");
     mxArray *o2[2] = {nullptr, nullptr};
     expect(2, 8, pc, "Spinach:spinach_powder_gpu:nlhs");
     (void)o2;

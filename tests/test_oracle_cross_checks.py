@@ -87,3 +87,38 @@ def test_ik1_basis_dimension_of_epr_radical():
                          coupling=dict(eigs=w.coupling_eigs, euler=w.coupling_euler)))
     ss_o = R.basis(ss_o, dict(approximation='IK-1', level=3, space_level=1))
     assert np.array_equal(ss_o.basis, b.codes)
+
+
+@pytest.mark.parametrize('relax', [False, True])
+def test_cpmg_matches_kron_model(relax):
+    """experiments/cpmg.m restated on the spherical-tensor basis vs the same
+    pulse sequence with Hilbert-space pulses U rho U^dagger."""
+    w = _c0_like(relax)
+    ss, I, Q = oracle_system(w)
+    km = KronModel(ss)
+    rho_h = km.spin_op('Lz', '13C') / np.sqrt(km.dim)
+    coil_h = km.spin_op(*w.coil) / np.sqrt(km.dim)
+    par = dict(rho0=R.state(ss, 'Lz', '13C'), coil=R.state(ss, *w.coil), pulse_op=R.operator(ss, 'Ly', '13C'),
+               timestep=w.dt, npoints=20, nloops=3)
+    for ang in [(0.0, 0.7, 1.3), (0.4, 1.0, -0.3)]:
+        f_st = R.powder_orientation_cpmg(ss, I, Q, par, ang)
+        f_kr = km.cpmg(ang, rho_h, coil_h, km.spin_op('Ly', '13C'), w.dt, 20, 3)
+        assert f_st.shape == (20 * 7,)
+        assert np.abs(f_kr).max() > 0.1
+        assert rel_err(f_st, f_kr) < 1e-8, ang
+
+
+def test_cpmg_with_a_zero_pulse_is_one_continuous_acquisition():
+    """Each echo starts from the last state of the previous segment: with no
+    pulse the segments tile one acquisition, the joints counted twice."""
+    w = W.c0()
+    ss, I, Q = oracle_system(w)
+    zero = 0 * R.operator(ss, 'Ly', '13C')
+    par = dict(rho0=R.state(ss, *w.rho0), coil=R.state(ss, *w.coil), pulse_op=zero, timestep=w.dt,
+               npoints=10, nloops=2)
+    ang = (0.0, 1.1, 0.5)
+    f = R.powder_orientation_cpmg(ss, I, Q, par, ang)
+    acq = R.powder_orientation_fid(ss, I, Q, dict(rho0=par['rho0'], coil=par['coil'], sweep=1 / w.dt,
+                                                  npoints=10 + 2 * 19), ang)
+    idx = list(range(10)) + list(range(9, 29)) + list(range(28, 48))
+    assert rel_err(f, acq[idx]) < 1e-12
