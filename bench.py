@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = 'powder FIDs/sec at <=1e-5 rel err vs FP64: FP32 exact, surrogate vs plain FP64'
 UNIT = 'FIDs/s'
-FID_NOTE = 'one FID = one orientation over all time steps; a powder FID of c1 is 1000 of them'
+FID_NOTE = 'one FID = one orientation over all time steps; a powder FID is one per grid orientation'
 WORKLOAD_TEXT = {
     'c0': 'c0: 13C+2x1H, full basis dim 64, 200-orientation zcwn grid, 1024 steps of 10 us',
     'c1': 'c1: 13C+6x1H, IK-0(3) dim 1156, T1/T2, 1000-orientation zcwn grid, 2048 steps of 5 us',

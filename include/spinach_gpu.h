@@ -103,6 +103,32 @@ spx_status spx_create(spx_handle **handle, int device);
 spx_status spx_destroy(spx_handle *handle);
 
 /*
+ * Builds I and Q{r}{k,m} on the GPU from the interaction content and uploads
+ * the system (replaces [I,Q]=hamiltonian(assume(spin_system,...)) of
+ * kernel/hamiltonian.m:59-790 with kernel/operators/superop.m:36-185, followed
+ * by spx_upload_system).
+ *   mults[n_spins]       spin multiplicities (2..8)
+ *   basis_keys[dim]      basis states as mixed-radix keys sum_s code_s*radix[s],
+ *                        code_s = l*l+l-m of spin s (kernel/indexing/lm2lin.m),
+ *                        strictly ascending; radix[s] = prod_{s'>s} mults[s']^2
+ *   rank/k/m[n_terms]    the anisotropic terms (as spx_upload_system)
+ *   mono_*[n_mono]       monomials coef * [T(code_a)@spin_a T(code_b)@spin_b, .]:
+ *                        mono_term 0 = isotropic part, t = anisotropic term t-1;
+ *                        mono_spins/mono_codes two per monomial (spin -1: none);
+ *                        mono_coefs interleaved complex
+ *   r_diag[dim]          diagonal relaxation superoperator (real) or NULL
+ *   rho0, coil           as spx_upload_system
+ *   build_ms             device time of the construction (may be NULL)
+ * Coefficients equal in every monomial of a term may be summed by the caller;
+ * entries whose contributions cancel (to 1e-14 of their magnitudes) are dropped.
+ */
+spx_status spx_build_system(spx_handle *handle, int32_t n_spins, const int32_t *mults, int64_t dim,
+                            const int64_t *basis_keys, const int64_t *radix, int32_t n_terms, const int32_t *rank,
+                            const int32_t *k, const int32_t *m, int64_t n_mono, const int32_t *mono_term,
+                            const int32_t *mono_spins, const int32_t *mono_codes, const double *mono_coefs,
+                            const double *r_diag, const double *rho0, const double *coil, double *build_ms);
+
+/*
  * Upload one spin system: the isotropic part I, n_terms rotational-basis
  * terms Q{rank}{k,m} (rank 1 or 2, 0-based k, m in 0..2*rank), the
  * relaxation superoperator R (diagonal; may be NULL for no relaxation), and

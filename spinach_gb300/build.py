@@ -7,9 +7,9 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 SOURCES = [os.path.join(HERE, 'csrc', f) for f in
-           ['engine.cu', 'surrogate.cu'] + [f'kern_{p}_{c}.cu' for p in ('f32r', 'f32c', 'f64r', 'f64c')
+           ['engine.cu', 'builder.cu', 'surrogate.cu'] + [f'kern_{p}_{c}.cu' for p in ('f32r', 'f32c', 'f64r', 'f64c')
                                             for c in ('sc', 'dc')]]
-DEPS = SOURCES + [os.path.join(HERE, 'csrc', 'kernels.cuh'), os.path.join(HERE, 'csrc', 'kern_inst.inc'),
+DEPS = SOURCES + [os.path.join(HERE, 'csrc', 'kernels.cuh'), os.path.join(HERE, 'csrc', 'builder.h'), os.path.join(HERE, 'csrc', 'kern_inst.inc'),
                   os.path.join(ROOT, 'include', 'spinach_gpu.h')]
 LIB = os.path.join(HERE, 'lib', 'libspinach_gpu.so')
 NVCC_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a', '-O3', '-lineinfo', '-std=c++17',

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "spinach_gpu.h"
+#include "builder.h"
 #include "kernels.cuh"
 
 namespace {
@@ -177,12 +178,26 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
         if (!std::isfinite(rho0[i]) || !std::isfinite(coil[i]))
             throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite rho0/coil");
 
+    // off-diagonal entries at or below 1e-14 of the largest input value are
+    // rounding residues of cancelled commutators (a host builder that sums
+    // operator products in another order leaves them): they are dropped, so
+    // that they neither widen the pattern nor cost matvec work
+    double vin = 0.0;
+    auto scan = [&](const spx_csc *A) {
+        for_each_entry(A, [&](int64_t, int64_t, Cplx v) { vin = std::max(vin, std::hypot(v.re, v.im)); });
+    };
+    scan(I);
+    for (int t = 0; t < n_terms; ++t) scan(&Q[t]);
+    const double residue = 1e-14 * vin;
+    auto kept = [&](int64_t r, int64_t c, Cplx v) { return r == c || std::hypot(v.re, v.im) > residue; };
+
     // union pattern (structurally symmetric, full diagonal)
     std::vector<int64_t> keys;
     keys.reserve((size_t)n * 4);
     for (int64_t i = 0; i < n; ++i) keys.push_back(i * n + i);
     auto add_pattern = [&](const spx_csc *A) {
-        for_each_entry(A, [&](int64_t r, int64_t c, Cplx) {
+        for_each_entry(A, [&](int64_t r, int64_t c, Cplx v) {
+            if (!kept(r, c, v)) return;
             keys.push_back(r * n + c);
             keys.push_back(c * n + r);
         });
@@ -200,6 +215,7 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
     const int nst_all = 1 + 2 * n_terms;
     std::vector<std::vector<Cplx>> st(nst_all, std::vector<Cplx>(nk));
     for_each_entry(I, [&](int64_t r, int64_t c, Cplx v) {
+        if (!kept(r, c, v)) return;
         Cplx &a = st[0][pos(r, c)];
         a.re += 0.5 * v.re; a.im += 0.5 * v.im;
         Cplx &b = st[0][pos(c, r)];
@@ -209,6 +225,7 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
         auto &S = st[1 + 2 * t];
         auto &A = st[2 + 2 * t];
         for_each_entry(&Q[t], [&](int64_t r, int64_t c, Cplx v) {
+            if (!kept(r, c, v)) return;
             const size_t p = pos(r, c), q = pos(c, r);
             // S = (Q + Q^H)/2,  A = 1i (Q - Q^H)/2
             S[p].re += 0.5 * v.re; S[p].im += 0.5 * v.im;
@@ -241,11 +258,13 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
             const int64_t r = keys[p] / n, c = keys[p] % n;
             if (r != c && std::fabs(s[p].im) > im_tol) cplx = true;
         }
-    // drop all-zero streams
+    // drop streams that are zero up to rounding (1e-14 of the largest value:
+    // e.g. the anti-Hermitian part of a term whose commutators cancel only to
+    // the last bits in the caller's summation order)
     std::vector<int> keep;
     for (int s = 0; s < nst_all; ++s) {
         bool nz = (s == 0);
-        for (size_t p = 0; p < nk && !nz; ++p) nz = (st[s][p].re != 0.0 || st[s][p].im != 0.0);
+        for (size_t p = 0; p < nk && !nz; ++p) nz = std::fabs(st[s][p].re) > im_tol || std::fabs(st[s][p].im) > im_tol;
         if (nz) keep.push_back(s);
     }
     const int nst = (int)keep.size();
@@ -1404,6 +1423,80 @@ spx_status spx_run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, c
 spx_status spx_set_initial_states(spx_handle *h, int64_t n_states, const double *states) {
     if (!h) return SPX_ERR_INVALID_ARGUMENT;
     return guarded(h, [&] { set_initial_states(h, n_states, states); });
+}
+
+spx_status spx_build_system(spx_handle *h, int32_t n_spins, const int32_t *mults, int64_t dim,
+                            const int64_t *basis_keys, const int64_t *radix, int32_t n_terms, const int32_t *rank,
+                            const int32_t *k, const int32_t *m, int64_t n_mono, const int32_t *mono_term,
+                            const int32_t *mono_spins, const int32_t *mono_codes, const double *mono_coefs,
+                            const double *r_diag, const double *rho0, const double *coil, double *build_ms) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (n_terms < 0 || n_terms > (spx::kMaxCoef - 1) / 2)
+            throw SpxError(SPX_ERR_UNSUPPORTED, "too many rotational-basis terms");
+        if (n_terms > 0 && (!rank || !k || !m)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL term arrays");
+        if (!rho0 || !coil) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "rho0/coil is NULL");
+        SPX_CUDA(cudaSetDevice(h->device));
+        spx::BuildSpec spec;
+        spec.n_spins = n_spins;
+        spec.mults = mults;
+        spec.dim = dim;
+        spec.keys = basis_keys;
+        spec.radix = radix;
+        spec.n_terms = n_terms;
+        spec.n_mono = n_mono;
+        spec.mono_term = mono_term;
+        spec.mono_spins = mono_spins;
+        spec.mono_codes = mono_codes;
+        spec.mono_coefs = mono_coefs;
+        spx::BuildInfo info;
+        std::vector<spx::HostCsc> mats;
+        try {
+            mats = spx::build_operators(spec, h->stream, &info);
+        } catch (const std::invalid_argument &e) {
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, e.what());
+        } catch (const std::runtime_error &e) {
+            throw SpxError(SPX_ERR_CUDA, e.what());
+        }
+        auto view = [&](spx::HostCsc &A) {
+            spx_csc v{};
+            v.n = dim;
+            v.colptr = A.colptr.data();
+            v.rowidx = A.rowidx.data();
+            v.values = A.values.data();
+            return v;
+        };
+        // terms whose matrix came out empty are dropped (as hamiltonian.m keeps
+        // only the non-zero rotational components)
+        spx_csc I = view(mats[0]);
+        std::vector<spx_csc> Q;
+        std::vector<int32_t> rk, kk, mm;
+        for (int t = 0; t < n_terms; ++t) {
+            if (mats[1 + t].rowidx.empty()) continue;
+            Q.push_back(view(mats[1 + t]));
+            rk.push_back(rank[t]);
+            kk.push_back(k[t]);
+            mm.push_back(m[t]);
+        }
+        spx::HostCsc R;
+        if (r_diag) {
+            R.colptr.resize(dim + 1);
+            for (int64_t i = 0; i < dim; ++i) {
+                if (!std::isfinite(r_diag[i])) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite relaxation rate");
+                R.colptr[i] = (int64_t)R.rowidx.size();
+                if (r_diag[i] != 0.0) {
+                    R.rowidx.push_back(i);
+                    R.values.push_back(r_diag[i]);
+                    R.values.push_back(0.0);
+                }
+            }
+            R.colptr[dim] = (int64_t)R.rowidx.size();
+        }
+        spx_csc Rv = view(R);
+        upload_system(h, &I, (int32_t)Q.size(), rk.data(), kk.data(), mm.data(), Q.data(), r_diag ? &Rv : nullptr,
+                      rho0, coil);
+        if (build_ms) *build_ms = info.kernel_ms;
+    });
 }
 
 spx_status spx_upload_coils(spx_handle *h, int32_t nchan, const double *coils) {

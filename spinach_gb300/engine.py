@@ -61,6 +61,10 @@ SIGNATURES = {
                                          C.c_int32, _P]),
     'spx_run_cpmg': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.c_int32,
                                C.POINTER(SpxCsc), C.POINTER(SpxOptions), _D]),
+    'spx_build_system': (C.c_int, [_P, C.c_int32, C.POINTER(C.c_int32), C.c_int64, C.POINTER(C.c_int64),
+                                   C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_int32), C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_int32), _D, _D, _D, _D, _D]),
     'spx_upload_coils': (C.c_int, [_P, C.c_int32, _D]),
     'spx_set_initial_states': (C.c_int, [_P, C.c_int64, _D]),
     'spx_autotune': (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_double, C.c_int64, C.c_int32,
@@ -189,6 +193,33 @@ class Engine:
             C.byref(Rh.struct) if Rh else None, _dptr(rho0), _dptr(coil)), self.h)
         self.dim = n
         self.nchan = 1
+
+    def build_system(self, hm, r_diag=None, rho0=None, coil=None) -> float:
+        """Build I and Q on the GPU from ``hm`` (spin_system.HamiltonianMonomials)
+        and upload the system with the relaxation diagonal and the states.
+        Returns the device time of the construction (ms)."""
+        i32 = lambda a: np.ascontiguousarray(a, np.int32)
+        i64 = lambda a: np.ascontiguousarray(a, np.int64)
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+        lp = lambda a: a.ctypes.data_as(C.POINTER(C.c_int64))
+        mults, keys, radix = i32(hm.mults), i64(hm.keys), i64(hm.radix)
+        rank = i32([t[0] for t in hm.terms] or [0])
+        kk = i32([t[1] for t in hm.terms] or [0])
+        mm = i32([t[2] for t in hm.terms] or [0])
+        mt, ms, mc = i32(hm.mono_term), i32(hm.mono_spins), i32(hm.mono_codes)
+        mf = np.ascontiguousarray(np.asarray(hm.mono_coefs, np.complex128).view(np.float64))
+        n = keys.size
+        rd = None if r_diag is None else np.ascontiguousarray(r_diag, np.float64)
+        rho0 = np.ascontiguousarray(np.asarray(rho0, np.complex128).view(np.float64))
+        coil = np.ascontiguousarray(np.asarray(coil, np.complex128).view(np.float64))
+        ms_out = C.c_double(0.0)
+        self._check(self.lib.spx_build_system(
+            self.h, mults.size, ip(mults), n, lp(keys), lp(radix), len(hm.terms), ip(rank), ip(kk), ip(mm),
+            mt.size, ip(mt), ip(ms), ip(mc), _dptr(mf), _dptr(rd) if rd is not None else None, _dptr(rho0),
+            _dptr(coil), C.byref(ms_out)), self.h)
+        self.dim = n
+        self.nchan = 1
+        return ms_out.value
 
     def set_initial_states(self, states):
         """One initial state per orientation (powder.m 'aniso_eq' or a function

@@ -289,10 +289,9 @@ def build_basis(ss: SpinSystem, approximation: str = 'none', level: int = 0,
         codes = np.zeros((sub.shape[0], ss.nspins), np.int64)
         codes[:, cl] = sub
         blocks.append(codes)
-    codes = np.unique(np.vstack(blocks), axis=0)
-    keys = codes @ radix
-    order = np.argsort(keys)
-    return Basis(codes[order].astype(np.int16), radix, keys[order])
+    codes = np.vstack(blocks)
+    keys, first = np.unique(codes @ radix, return_index=True)     # one key per product state
+    return Basis(codes[first].astype(np.int16), radix, keys)
 
 
 # ---------------------------------------------------------------------------
@@ -498,10 +497,11 @@ class RotationalHamiltonian:
     aniso: dict                       # (r, k, m) with 0-based k, m -> csr
 
 
-def rotational_hamiltonian(ss: SpinSystem, basis: Basis, assumptions: str,
-                           factory: OperatorFactory | None = None) -> RotationalHamiltonian:
-    """Isotropic part and rotational basis (kernel/hamiltonian.m:59-790)."""
-    f = factory or OperatorFactory(ss, basis)
+def interaction_terms(ss: SpinSystem, assumptions: str):
+    """The operator content of the Hamiltonian (kernel/hamiltonian.m:59-790):
+    isotropic terms ``(coefficient, ops)`` and anisotropic terms ``(ist
+    weights (8,), irreducible components (8,), ops)``, ``ops`` a list of
+    ``(operator, spin)``."""
     tz = ss.tols['liouv_zero']
     zs, cs = interaction_strengths(ss, assumptions)
     iso_terms = []       # (coefficient, ops)
@@ -535,6 +535,76 @@ def rotational_hamiltonian(ss: SpinSystem, basis: Basis, assumptions: str,
             for name in _STRENGTH_TERMS[strength]:
                 opL, opS, w1, w2 = _BILINEAR[name]
                 ani_terms.append((np.array(w1 + w2, float), irr, [(opL, a), (opS, b)]))
+    return iso_terms, ani_terms
+
+
+def _term_groups(ss: SpinSystem, assumptions: str):
+    """[(key, [(coefficient, ops), ...])]: the isotropic part (key None) and
+    every rotational component (r, k, m) with at least one coefficient above
+    liouv_zero."""
+    tz = ss.tols['liouv_zero']
+    iso_terms, ani_terms = interaction_terms(ss, assumptions)
+    groups = [(None, iso_terms)]
+    for r in (1, 2):
+        off = r * r - 1
+        for k in range(2 * r + 1):
+            for m in range(2 * r + 1):
+                weighted = []
+                for ist, irr, ops in ani_terms:
+                    c = ist[off + k] * irr[off + m]
+                    if abs(c) > tz:
+                        weighted.append((c, ops))
+                if weighted:
+                    groups.append(((r, k, m), weighted))
+    return groups
+
+
+@dataclass
+class HamiltonianMonomials:
+    """Input of the on-GPU construction: the basis as mixed-radix keys and
+    the Hamiltonian as single-code monomials coef * [T(code_a) T(code_b), .]."""
+    mults: np.ndarray                 # (nspins,) int32
+    keys: np.ndarray                  # (dim,) int64, ascending
+    radix: np.ndarray                 # (nspins,) int64
+    terms: list                       # [(r, k, m)], term t+1 of the monomials
+    mono_term: np.ndarray             # (n,) int32, 0 = isotropic part
+    mono_spins: np.ndarray            # (n, 2) int32, -1 = none
+    mono_codes: np.ndarray            # (n, 2) int32
+    mono_coefs: np.ndarray            # (n,) complex128
+
+
+def hamiltonian_monomials(ss: SpinSystem, basis: Basis, assumptions: str) -> HamiltonianMonomials:
+    """The same Hamiltonian as ``rotational_hamiltonian`` as monomials: each
+    human-readable operator product is expanded into products of single
+    irreducible spherical tensor codes (``OperatorFactory._CODE``)."""
+    groups = _term_groups(ss, assumptions)
+    terms, mt, msp, mco, mcf = [], [], [], [], []
+    for t, (key, weighted) in enumerate(groups):
+        if key is not None:
+            terms.append(key)
+        for c, ops in weighted:
+            for combo in itertools.product(*[OperatorFactory._CODE[op] for op, _ in ops]):
+                f = 1.0 + 0j
+                sp_, co_ = [-1, -1], [0, 0]
+                for slot, ((op, spin), (code, fac)) in enumerate(zip(ops, combo)):
+                    f *= fac
+                    if code:
+                        sp_[slot], co_[slot] = spin, code
+                mt.append(t)
+                msp.append(sp_)
+                mco.append(co_)
+                mcf.append(c * f)
+    return HamiltonianMonomials(np.asarray(ss.mults, np.int32), np.ascontiguousarray(basis.keys, np.int64),
+                                np.ascontiguousarray(basis.radix, np.int64), terms,
+                                np.asarray(mt, np.int32), np.asarray(msp, np.int32).reshape(-1, 2),
+                                np.asarray(mco, np.int32).reshape(-1, 2), np.asarray(mcf, np.complex128))
+
+
+def rotational_hamiltonian(ss: SpinSystem, basis: Basis, assumptions: str,
+                           factory: OperatorFactory | None = None) -> RotationalHamiltonian:
+    """Isotropic part and rotational basis (kernel/hamiltonian.m:59-790)."""
+    f = factory or OperatorFactory(ss, basis)
+    groups = _term_groups(ss, assumptions)
     op = f.comm_coo        # one superoperator per distinct operator product
 
     dim = basis.dim
@@ -552,22 +622,14 @@ def rotational_hamiltonian(ss: SpinSystem, basis: Basis, assumptions: str,
         M.eliminate_zeros()
         return M
 
-    I = assemble(iso_terms)
+    I = assemble(groups[0][1])
     if I is None:
         I = sp.csr_matrix((dim, dim), dtype=complex)
     aniso = {}
-    for r in (1, 2):
-        off = r * r - 1
-        for k in range(2 * r + 1):
-            for m in range(2 * r + 1):
-                weighted = []
-                for ist, irr, ops in ani_terms:
-                    c = ist[off + k] * irr[off + m]
-                    if abs(c) > tz:
-                        weighted.append((c, ops))
-                acc = assemble(weighted)
-                if acc is not None and acc.nnz:
-                    aniso[(r, k, m)] = acc
+    for key, weighted in groups[1:]:
+        acc = assemble(weighted)
+        if acc is not None and acc.nnz:
+            aniso[key] = acc
     return RotationalHamiltonian(dim, I, aniso)
 
 

@@ -187,6 +187,25 @@ def build(w: Workload) -> Liouvillian:
     return Liouvillian(H.iso, H.aniso, R, fac.state(*w.rho0), fac.state(*w.coil), basis.dim)
 
 
+@dataclass
+class BuildSpec:
+    """Input of the on-GPU construction of a workload (Engine.build_system)."""
+    monomials: object                 # spin_system.HamiltonianMonomials
+    r_diag: np.ndarray
+    rho0: np.ndarray
+    coil: np.ndarray
+    dim: int
+
+
+def build_spec(w: Workload) -> BuildSpec:
+    """Host half of the on-GPU setup: basis, monomials, relaxation, states."""
+    ss = spin_system_of(w)
+    basis = ssm.build_basis(ss, w.approximation, w.level)
+    fac = ssm.factory_for(ss, basis)
+    hm = ssm.hamiltonian_monomials(ss, basis, w.assumptions)
+    return BuildSpec(hm, ssm.relaxation_diagonal(ss, basis), fac.state(*w.rho0), fac.state(*w.coil), basis.dim)
+
+
 def c4_small(seed: int = 4, n_protons: int = 2) -> Workload:
     """The c4 radical cut to ``n_protons`` protons in the full basis (parity-test size)."""
     w = c4(seed)
