@@ -40,16 +40,24 @@ class BatchedPowders:
 
 
 def prepare(workloads, n_orient=None, nsteps=None, device: int = 0, tune: bool = True,
-            precision: int = E.FP32) -> BatchedPowders:
-    """Build, upload and (optionally) autotune every system."""
+            precision: int = E.FP32, builder: str = 'gpu') -> BatchedPowders:
+    """Build, upload and (optionally) autotune every system.  ``builder``
+    'gpu' constructs I and Q on the device (Engine.build_system), 'host' with
+    the host builder (Engine.upload)."""
     import torch
+    if builder not in ('gpu', 'host'):
+        raise ValueError("builder must be 'gpu' or 'host'")
     dev = torch.device('cuda', device)
     t0 = time.perf_counter()
     engines, grids, fids, dts, nss, dims = [], [], [], [], [], []
     for w in workloads:
-        L = W.build(w)
         eng = E.Engine(device)
-        eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
+        if builder == 'gpu':
+            L = W.build_spec(w)
+            eng.build_system(L.monomials, L.r_diag, L.rho0, L.coil)
+        else:
+            L = W.build(w)
+            eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
         no = n_orient or w.n_orient
         ns = nsteps or w.nsteps
         g = torch.tensor(np.stack(W.zcwn_grid(no)), dtype=torch.float64, device=dev).contiguous()

@@ -182,33 +182,68 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
     // rounding residues of cancelled commutators (a host builder that sums
     // operator products in another order leaves them): they are dropped, so
     // that they neither widen the pattern nor cost matvec work
-    double vin = 0.0;
+    double vin2 = 0.0;                                  // squared magnitudes
     auto scan = [&](const spx_csc *A) {
-        for_each_entry(A, [&](int64_t, int64_t, Cplx v) { vin = std::max(vin, std::hypot(v.re, v.im)); });
+        for_each_entry(A, [&](int64_t, int64_t, Cplx v) { vin2 = std::max(vin2, v.re * v.re + v.im * v.im); });
     };
     scan(I);
     for (int t = 0; t < n_terms; ++t) scan(&Q[t]);
-    const double residue = 1e-14 * vin;
-    auto kept = [&](int64_t r, int64_t c, Cplx v) { return r == c || std::hypot(v.re, v.im) > residue; };
+    const double residue2 = 1e-28 * vin2;
+    auto kept = [&](int64_t r, int64_t c, Cplx v) { return r == c || v.re * v.re + v.im * v.im > residue2; };
 
-    // union pattern (structurally symmetric, full diagonal)
+    // union pattern (structurally symmetric, full diagonal) as sorted keys
+    // r*n + c: a bitmap of the n x n positions when it is small (a few MB),
+    // else a sort of every entry and its transpose
     std::vector<int64_t> keys;
-    keys.reserve((size_t)n * 4);
-    for (int64_t i = 0; i < n; ++i) keys.push_back(i * n + i);
-    auto add_pattern = [&](const spx_csc *A) {
-        for_each_entry(A, [&](int64_t r, int64_t c, Cplx v) {
-            if (!kept(r, c, v)) return;
-            keys.push_back(r * n + c);
-            keys.push_back(c * n + r);
-        });
-    };
-    add_pattern(I);
-    for (int t = 0; t < n_terms; ++t) add_pattern(&Q[t]);
-    std::sort(keys.begin(), keys.end());
-    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    if (n <= 8192) {
+        const int64_t wpr = (n + 63) / 64;                 // 64-bit words per row
+        std::vector<uint64_t> bits((size_t)(n * wpr), 0);
+        auto mark = [&](int64_t r, int64_t c) { bits[(size_t)(r * wpr + (c >> 6))] |= 1ull << (c & 63); };
+        for (int64_t i = 0; i < n; ++i) mark(i, i);
+        auto add = [&](const spx_csc *A) {
+            for_each_entry(A, [&](int64_t r, int64_t c, Cplx v) {
+                if (!kept(r, c, v)) return;
+                mark(r, c);
+                mark(c, r);
+            });
+        };
+        add(I);
+        for (int t = 0; t < n_terms; ++t) add(&Q[t]);
+        size_t cnt_bits = 0;
+        for (uint64_t w : bits) cnt_bits += (size_t)__builtin_popcountll(w);
+        keys.reserve(cnt_bits);
+        for (int64_t r = 0; r < n; ++r)
+            for (int64_t q = 0; q < wpr; ++q) {
+                uint64_t w = bits[(size_t)(r * wpr + q)];
+                while (w) {
+                    const int b = __builtin_ctzll(w);
+                    keys.push_back(r * n + q * 64 + b);
+                    w &= w - 1;
+                }
+            }
+    } else {
+        keys.reserve((size_t)n * 4);
+        for (int64_t i = 0; i < n; ++i) keys.push_back(i * n + i);
+        auto add = [&](const spx_csc *A) {
+            for_each_entry(A, [&](int64_t r, int64_t c, Cplx v) {
+                if (!kept(r, c, v)) return;
+                keys.push_back(r * n + c);
+                keys.push_back(c * n + r);
+            });
+        };
+        add(I);
+        for (int t = 0; t < n_terms; ++t) add(&Q[t]);
+        std::sort(keys.begin(), keys.end());
+        keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    }
     const size_t nk = keys.size();
+    // row start of each row in the key list; a position is found within its row
+    std::vector<size_t> rstart(n + 1, 0);
+    for (size_t p = 0; p < nk; ++p) rstart[keys[p] / n + 1]++;
+    for (int64_t i = 0; i < n; ++i) rstart[i + 1] += rstart[i];
     auto pos = [&](int64_t r, int64_t c) -> size_t {
-        return (size_t)(std::lower_bound(keys.begin(), keys.end(), r * n + c) - keys.begin());
+        return (size_t)(std::lower_bound(keys.begin() + rstart[r], keys.begin() + rstart[r + 1], r * n + c) -
+                        keys.begin());
     };
 
     // streams: 0 = Ih + iR (coefficient 1), then S_t, A_t per term
@@ -291,10 +326,6 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
         slice_off[s + 1] = slice_off[s] + 32 * w;
     }
     const int ell_len = slice_off[nslices];
-    // row start of each old row in the key list
-    std::vector<size_t> rstart(n + 1, 0);
-    for (size_t p = 0; p < nk; ++p) rstart[keys[p] / n + 1]++;
-    for (int64_t i = 0; i < n; ++i) rstart[i + 1] += rstart[i];
 
     std::vector<uint16_t> ell_col(std::max(ell_len, 1), 0);
     std::vector<double> ell_re((size_t)nst * std::max(ell_len, 1), 0.0), ell_im;
