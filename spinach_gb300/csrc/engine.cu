@@ -1035,7 +1035,8 @@ std::mutex g_tune_mutex;
 std::map<TuneKey, spx_options> g_tune_cache;
 
 TuneKey tune_key(const spx_handle *h, double dt, int64_t nsteps, int precision) {
-    const int scale = (int)std::lround(4.0 * std::log2(std::max(h->g_upper * dt, 1e-30)));
+    // spectral scale in octaves: the series length per step follows it
+    const int scale = (int)std::lround(std::log2(std::max(h->g_upper * dt, 1e-30)));
     return TuneKey{h->n, h->ell_len, h->nslices, h->nstreams, h->cplx ? 1 : 0, precision, scale,
                    (int)std::min<int64_t>(nsteps, 512)};
 }
@@ -1070,7 +1071,8 @@ spx_options autotune(spx_handle *h, int64_t n_orient, const double *d_al, const 
     spx_options base{};
     base.precision = precision;
     // sample: one wave of single-CTA orientations (at most 1024), at most 512
-    // steps (several chunks, so long chunks are not penalised)
+    // steps (several chunks, so long chunks are not penalised; a 256-step
+    // sample picked shorter chunks and made the c2 graph 2 % slower)
     const int64_t ns = std::min<int64_t>(nsteps, 512);
     int64_t n = std::min<int64_t>(n_orient, 1024);
     {
@@ -1091,8 +1093,10 @@ spx_options autotune(spx_handle *h, int64_t n_orient, const double *d_al, const 
     spx_options best = base;
     double best_t = INFINITY;
     const int cls[] = {1, 2, 4, 8};
+    int cl_min = 0;                 // smallest cluster that fits; it and twice it are tried
     for (int cl : cls) {
-        // warps: the default for this cluster size, half, one and a half, and 16
+        if (cl_min && cl > 2 * cl_min) break;
+        // warps: the default for this cluster size, half, and 16
         spx_options o = base;
         o.cluster = cl;
         Config c0{};
@@ -1101,6 +1105,7 @@ spx_options autotune(spx_handle *h, int64_t n_orient, const double *d_al, const 
         } catch (const SpxError &) {
             continue;
         }
+        if (!cl_min) cl_min = cl;
         const int nw0 = c0.threads / 32;
         std::vector<int> nws = {nw0, std::max(1, nw0 / 2), 16};
         std::sort(nws.begin(), nws.end());
