@@ -905,6 +905,59 @@ def powder_orientation_cpmg(ss, I, Q, parameters, angles) -> np.ndarray:
     return cpmg(ss, parameters, H, relaxation(ss))
 
 
+def fourdif1(N: int):
+    """kernel/derivatives/fourdif.m:44-77 with m = 1: rotor grid points and the
+    first-derivative Fourier collocation matrix (first column, then Toeplitz)."""
+    x = 2 * np.pi * np.arange(N) / N
+    h = 2 * np.pi / N
+    kk = np.arange(1, N)
+    n1 = (N - 1) // 2
+    n2 = -(-(N - 1) // 2)
+    if N % 2 == 0:
+        topc = 1 / np.tan(np.arange(1, n2 + 1) * h / 2)
+        col1 = np.concatenate([[0.0], 0.5 * ((-1.0) ** kk) * np.concatenate([topc, -topc[:n1][::-1]])])
+    else:
+        topc = 1 / np.sin(np.arange(1, n2 + 1) * h / 2)
+        col1 = np.concatenate([[0.0], 0.5 * ((-1.0) ** kk) * np.concatenate([topc, topc[:n1][::-1]])])
+    row1 = -col1
+    return x, sla.toeplitz(col1, row1)
+
+
+def singlerot_orientation_fid(ss, I, Q, parameters, angles) -> np.ndarray:
+    """One orientation of kernel/contexts/singlerot.m:134-307 with @acquire,
+    sphten-liouv, no rotating frames: H_n = I + sum D_comp(k,m) Q{r}{k,m} with
+    D_comp = D_lab2rot*D_rotor(phi_n)*D_mol2rot (:269-283, not Hermitised
+    without rframes), G = clean_up(blkdiag(H)+1i*M, liouv_zero) (:298),
+    M = 2*pi*rate*kron(d/dphi, I) (:190), R and states projected into rotor
+    space (:191-215)."""
+    N = 2 * parameters['max_rank'] + 1
+    dim = I.shape[0]
+    phases, Dfd = fourdif1(N)
+    x, y, z = parameters['axis']
+    rotor_phi = math.atan2(y, x)
+    rotor_theta = math.pi / 2 - math.atan2(z, math.hypot(x, y))
+    M = 2 * np.pi * parameters['rate'] * sp.kron(sp.csr_matrix(Dfd), sp.identity(dim))
+    H = []
+    for n in range(N):
+        Hn = sp.csc_matrix(I, dtype=complex)
+        for r in sorted(Q):
+            Dc = wigner(r, rotor_phi, rotor_theta, 0) @ wigner(r, 0, 0, phases[n]) @ wigner(r, *angles)
+            for k in range(2 * r + 1):
+                for m in range(2 * r + 1):
+                    if Q[r][k][m] is not None:
+                        Hn = Hn + Dc[k, m] * Q[r][k][m]
+        H.append(Hn)
+    G = clean_up(ss, sp.csc_matrix(sp.block_diag(H) + 1j * M), ss.tols['liouv_zero'])
+    R = sp.kron(sp.identity(N), relaxation(ss))
+    if parameters.get('single_crystal'):
+        space = np.zeros(N); space[0] = 1.0
+    else:
+        space = np.full(N, 1.0 / N)
+    par = dict(parameters, rho0=np.kron(space, parameters['rho0']),
+               coil=np.kron(np.ones(N), parameters['coil']))
+    return acquire(ss, par, G, R)
+
+
 def powder(ss: SpinSystem, parameters: dict, assumptions: str, grid, setup=None,
            sum_up: bool = True):
     """kernel/contexts/powder.m:99-309 with pulse_sequence=@acquire, serial order.

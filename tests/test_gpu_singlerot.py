@@ -1,0 +1,49 @@
+"""Magic-angle spinning (kernel/contexts/singlerot.m, Fokker-Planck) through the
+engine: the rotor-space Liouvillian in upload form runs on the same kernels."""
+import numpy as np
+import pytest
+
+from spinach_gb300 import engine as E, singlerot as SR, workloads as W
+from oracle_cases import oracle_system, rel_err
+from oracle import spinach_ref as R
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize('max_rank,rate', [(3, 12.5e3), (5, 5e3)])
+def test_mas_powder_matches_oracle(gpu_engine, max_rank, rate):
+    w = W.c0()
+    L = W.build(w)
+    axis = (1.0, 1.0, 1.0)
+    I_fp, terms, R_fp, rho0, coil = SR.fokker_planck(L.I, L.terms, L.R, L.rho0, L.coil, max_rank, rate, axis)
+    ss, I, Q = oracle_system(w, krylov=True)
+    al, be, ga, _ = W.zcwn_grid(w.n_orient)
+    sel = np.array([7, 66, 131])
+    g = (al[sel], be[sel], ga[sel], np.array([0.25, 0.35, 0.4]))
+    nsteps = 160
+    par = dict(rho0=R.state(ss, *w.rho0), coil=R.state(ss, *w.coil), sweep=1 / w.dt, npoints=nsteps + 1,
+               rate=rate, axis=axis, max_rank=max_rank)
+    ref = sum(g[3][i] * R.singlerot_orientation_fid(ss, I, Q, par, (g[0][i], g[1][i], g[2][i]))
+              for i in range(sel.size))
+    gpu_engine.upload(I_fp, terms, R_fp, rho0, coil)
+    for prec, tol in ((E.FP64, 1e-10), (E.FP32, 1e-5)):
+        res = gpu_engine.run(*g, w.dt, nsteps, precision=prec)
+        assert res.stats['dim'] == (2 * max_rank + 1) * L.dim
+        assert rel_err(res.fid, ref) <= tol, prec
+
+
+def test_reference_single_crystal_case(gpu_engine):
+    """tests/kernel/test_ctx_singlerot_acquire.m through the engine."""
+    from spinach_gb300 import spin_system as S
+    ss = S.make_spin_system(['1H'], 14.1, zeeman_eigs=[[-2.0, -2.0, 4.0]], zeeman_euler=[[0.0, 0.0, 0.0]])
+    basis = S.build_basis(ss, 'none', 0, projections=[1])
+    fac = S.factory_for(ss, basis)
+    H = S.rotational_hamiltonian(ss, basis, 'nmr', fac)
+    rho0 = fac.state('L+', '1H')
+    I_fp, terms, _, r0, cl = SR.fokker_planck(H.iso, H.aniso, None, rho0, rho0, 1, 1000.0, (1, 1, 1),
+                                             single_crystal=True)
+    gpu_engine.upload(I_fp, terms, None, r0, cl)
+    fid = gpu_engine.run(np.zeros(1), np.zeros(1), np.zeros(1), np.ones(1), 1 / 2000.0, 2, precision=E.FP64).fid
+    assert fid.shape == (3,)
+    assert abs(fid[0] - np.vdot(rho0, rho0)) <= 1e-12
+    assert np.all(np.isfinite(fid))
