@@ -331,12 +331,13 @@ def run_gpu(args):
             cpu = {'value': nn / t, 'unit': UNIT, 'cores': cores, 'kind': 'port',
                    'sample': f'{nn} orientations of {args.workload} (one per core, all time steps), '
                              f'oracle restatement in FP64: {BRANCH_TEXT[args.workload]}'}
-        sur = c2 = c4 = None
+        sur = c2 = c4 = mas = None
         if not args.no_surrogate and world == 1 and args.workload == 'c1':
             sur = surrogate_leg(eng, w, local)
         if not args.no_extra and world == 1 and args.workload == 'c1':
             c4 = c4_leg(local)
             c2 = c2_leg(local)
+            mas = mas_leg(local)
         line = {
             'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': statistics.mean(step_ms), 'higher_is_better': True,
@@ -366,6 +367,7 @@ def run_gpu(args):
             'surrogate': sur,
             'c4': c4,
             'c2': c2,
+            'mas': mas,
             'clocks': clk,
             'gpu_launches': 3 * args.steps,
         }
@@ -401,6 +403,37 @@ def c4_leg(device):
            'rel_err_vs_fp64_gpu': _rel(r32.fid, r64.fid), 'fp64_gpu': {'value': w.n_orient / t64},
            'kernel_ms': r32.stats['kernel_ms'], 'cluster': r32.stats['cluster'], 'threads': r32.stats['threads'],
            'matvecs': r32.stats['matvecs']}
+    eng.close()
+    return out
+
+
+def mas_leg(device):
+    """Magic-angle spinning (singlerot.m Fokker-Planck): the c0 system at 10 kHz about (1,1,1), rotor
+    rank 8 (17 rotor points, dim 1088), 200-orientation zcwn grid, 1024 steps of 10 us; upload and run
+    with host buffers, FP32 and FP64."""
+    from spinach_gb300 import engine as E, singlerot as SR, workloads as W
+    w = W.c0()
+    L = W.build(w)
+    t0 = time.perf_counter()
+    fp = SR.fokker_planck(L.I, L.terms, L.R, L.rho0, L.coil, 8, 10e3, (1.0, 1.0, 1.0))
+    t_fp = time.perf_counter() - t0
+    eng = E.Engine(device)
+    g = W.zcwn_grid(w.n_orient)
+    eng.upload(*fp)
+    eng.run(*[a[:16] for a in g], w.dt, w.nsteps, precision=E.FP32)           # warm-up
+    res = {}
+    for p in (E.FP32, E.FP64):
+        t0 = time.perf_counter()
+        eng.upload(*fp)
+        r = eng.run(*g, w.dt, w.nsteps, precision=p)
+        res[p] = (time.perf_counter() - t0, r)
+    out = {'workload': 'MAS (singlerot.m, Fokker-Planck): c0 system at 10 kHz about (1,1,1), rotor rank 8 '
+                       '(dim 17 x 64 = 1088), 200-orientation zcwn grid, 1024 steps of 10 us, upload + run',
+           'value': w.n_orient / res[E.FP32][0], 'unit': UNIT,
+           'rel_err_vs_fp64_gpu': _rel(res[E.FP32][1].fid, res[E.FP64][1].fid),
+           'fp64_gpu': {'value': w.n_orient / res[E.FP64][0]},
+           'kernel_ms': res[E.FP32][1].stats['kernel_ms'], 'cluster': res[E.FP32][1].stats['cluster'],
+           'nnz': res[E.FP32][1].stats['nnz'], 'rotor_space_setup_s': t_fp}
     eng.close()
     return out
 
