@@ -241,6 +241,18 @@ spx_status spx_run_cpmg(spx_handle *handle, int64_t n_orient, const double *alph
                         const spx_csc *pulse_op, const spx_options *opt, double *fid);
 
 /*
+ * Two-pulse echo (experiments/esr_dipolar/eseem.m): a 90-degree pulse
+ * exp(-1i*(pi/2)*pulse_op) on rho0, a trajectory of npoints-1 steps of
+ * timestep/2, a 180-degree pulse on every state of it and the refocusing of
+ * state n by n more steps; fid[n] = coil' * that state, powder-summed
+ * (npoints complex values).  Needs one coil and the single rho0; the
+ * dimension is limited to 8192.
+ */
+spx_status spx_run_eseem(spx_handle *handle, int64_t n_orient, const double *alphas, const double *betas,
+                         const double *gammas, const double *weights, double timestep, int64_t npoints,
+                         const spx_csc *pulse_op, const spx_options *opt, double *fid);
+
+/*
  * Per-orientation initial states (kernel/contexts/powder.m:244-254: the
  * 'aniso_eq' equilibrium or a function-handle rho0 evaluated at every grid
  * point).  states holds n_states Liouville vectors, orientation after

@@ -145,6 +145,29 @@ class KronModel:
                     r = P @ r
         return np.array(out)
 
+    def eseem(self, angles, rho0, coil, pulse_op, timestep, npoints):
+        """Two-pulse echo: U rho U^dagger pulses (90 then 180 degrees), point n
+        after n steps of timestep/2 on each side of the 180-degree pulse."""
+        H = self.hamiltonian(angles)
+        I = np.eye(self.dim)
+        L = np.kron(H, I) - np.kron(I, H.T) + 1j * self.relaxation()
+        P = sla.expm(-1j * (timestep / 2) * L)
+
+        def pulse(r, theta):
+            U = sla.expm(-1j * theta * pulse_op)
+            return (U @ r.reshape(self.dim, self.dim) @ U.conj().T).reshape(-1)
+
+        r = pulse(rho0.reshape(-1).astype(complex), np.pi / 2)
+        c = coil.reshape(-1)
+        out = []
+        for n in range(npoints):
+            x = pulse(r, np.pi)
+            for _ in range(n):
+                x = P @ x
+            out.append(np.vdot(c, x))
+            r = P @ r
+        return np.array(out)
+
 
 def gamma_of(isotope):
     return ISOTOPES[isotope][1]

@@ -858,6 +858,38 @@ def cpmg(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
     return np.concatenate(fid)
 
 
+def evolution_refocus(ss: SpinSystem, stack, L, dt: float) -> np.ndarray:
+    """kernel/evolution.m:402-470 ('refocus', one subspace): column n of the
+    stack is propagated n steps; propagator below krylov_tol, else the stack
+    stepping of kernel/krylov.m:116-137."""
+    L = clean_up(ss, sp.csc_matrix(L), ss.tols['liouv_zero'])
+    stack = clean_up(ss, np.array(stack, complex), ss.tols['zte_tol'])
+    dim, ncol = stack.shape
+    if dim < ss.tols['krylov_tol'] and 'krylov' not in ss.enable:
+        P = propagator(ss, L, dt)
+        for n in range(1, ncol):
+            stack[:, n:] = P @ stack[:, n:]
+    else:
+        L = sp.csr_matrix(L)
+        for n in range(1, ncol):
+            stack[:, n:] = step(ss, L, stack[:, n:], dt)
+    return clean_up(ss, stack, ss.tols['zte_tol'])
+
+
+def eseem(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
+    """experiments/esr_dipolar/eseem.m:40-64 (K = 0, no screening): 90-degree
+    pulse, trajectory of npoints-1 steps of timestep/2, 180-degree pulse on
+    every column, refocusing, detection."""
+    L = H + 1j * R
+    P = parameters['pulse_op']
+    tau = parameters['timestep'] / 2
+    rho = step(ss, P, parameters['rho0'], np.pi / 2)
+    stack = evolution_trajectory(ss, L, rho, tau, parameters['npoints'] - 1)
+    stack = step(ss, P, stack, np.pi)
+    stack = evolution_refocus(ss, stack, L, tau)
+    return np.asarray(parameters['coil'], complex).conj() @ stack
+
+
 # --------------------------------------------------------------------------
 # Grids and the powder context
 # --------------------------------------------------------------------------
@@ -956,6 +988,14 @@ def singlerot_orientation_fid(ss, I, Q, parameters, angles) -> np.ndarray:
     par = dict(parameters, rho0=np.kron(space, parameters['rho0']),
                coil=np.kron(np.ones(N), parameters['coil']))
     return acquire(ss, par, G, R)
+
+
+def powder_orientation_eseem(ss, I, Q, parameters, angles) -> np.ndarray:
+    """One iteration of kernel/contexts/powder.m:226-274 with @eseem."""
+    A = orientation(Q, angles)
+    H = I if A is None else I + A
+    H = (H + H.conj().T) / 2
+    return eseem(ss, parameters, H, relaxation(ss))
 
 
 def powder(ss: SpinSystem, parameters: dict, assumptions: str, grid, setup=None,

@@ -101,6 +101,11 @@ struct spx_handle {
     DevBuf<int> d_pulse_ptr, d_pulse_col;  // pulse superoperator, CSR in sliced order
     DevBuf<double2> d_pulse_val;
     double pulse_norm1 = 0.0;
+    DevBuf<double> d_neg_re, d_neg_im;     // echo detection: the adjoint generator's streams
+    DevBuf<double2> d_neg_diag;
+    DevBuf<double2> d_traj[2], d_echo_f;   // forward / adjoint trajectories, per-orientation echoes
+    DevBuf<int> d_echo_ptr, d_echo_col;    // exp(-1i pi P) as CSR (sliced order)
+    DevBuf<double2> d_echo_val;
     int64_t n_states = 0;           // their count (0: one initial state for all)
     std::vector<int> row_of;        // sliced-ELL row of every basis state
 
@@ -723,6 +728,8 @@ struct RunIO {
     const double2 *rho0 = nullptr;     // one initial state for every orientation (sliced order)
     const double2 *rho0s = nullptr;    // one per orientation, n_orient x n_pad
     double2 *state_out = nullptr;      // the state after the last step, n_orient x n_pad
+    double2 *traj_out = nullptr;       // the state entering every chunk, n_orient x (nsteps+1) x n_pad
+    bool adjoint = false;              // propagate under -H + 1i R (the adjoint of L, negated)
 };
 
 void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be,
@@ -745,8 +752,14 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     sys.rho0s = h->n_states > 0 ? h->d_rho0s.p : nullptr;
     if (io.rho0) sys.rho0 = io.rho0;
     if (io.rho0s) sys.rho0s = io.rho0s;
+    if (io.adjoint) {
+        sys.ell_re = h->d_neg_re.p;
+        sys.ell_im = h->cplx ? h->d_neg_im.p : nullptr;
+        sys.diag = h->d_neg_diag.p;
+    }
     spx::DevRun run{};
     run.state_out = io.state_out;
+    run.traj_out = io.traj_out;
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
     run.fixed_chunk = c.fixed ? 1 : 0; run.chunk_x = c.chunk_x;
@@ -1013,6 +1026,179 @@ void run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, const doubl
         at += (size_t)nsteps + 1;
         cur ^= 1;
     }
+}
+
+// Echo detection (experiments/esr_dipolar/eseem.m): the stack of half-echo
+// states is pulsed and refocused, point n being coil' U^n Pi U^n rho1 with
+// U = exp(-1i L tau), rho1 the 90-degree-pulsed rho0 and Pi = exp(-1i pi P).
+// With v_n = (U')^n coil = exp(1i L' n tau) coil, point n is v_n' * Pi * u_n,
+// u_n = U^n rho1: two trajectories (L, and -H + 1i R for the adjoint) and one
+// sparse bilinear form per orientation and step, instead of the reference's
+// n-step refocusing of every column.
+
+// The adjoint generator -(H) + 1i R from the uploaded streams: every value is
+// negated except the imaginary diagonal of stream 0 (the relaxation rates).
+__global__ void negate_streams_kernel(int64_t n_ell, const double *re, const double *im, double *nre, double *nim,
+                                      int64_t n_diag, int n_pad, const double2 *diag, double2 *ndiag) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_ell; i += stride) {
+        nre[i] = -re[i];
+        if (im) nim[i] = -im[i];
+    }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_diag; i += stride) {
+        const double2 d = diag[i];
+        ndiag[i] = make_double2(-d.x, i < n_pad ? d.y : -d.y);
+    }
+}
+
+__global__ void identity_kernel(int n_pad, double2 *a) {
+    const int64_t n2 = (int64_t)n_pad * n_pad;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = make_double2(i / n_pad == i % n_pad ? 1.0 : 0.0, 0.0);
+}
+
+// out[o][n] = sum_i conj(v[o][n][i]) * (Pi u[o][n])[i], one warp per (o, n).
+__global__ void echo_form_kernel(int n_orient, int npoints, int n_pad, const int *__restrict__ ptr,
+                                 const int *__restrict__ col, const double2 *__restrict__ val,
+                                 const double2 *__restrict__ u, const double2 *__restrict__ v, double2 *out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)n_orient * npoints;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw;
+         w += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const double2 *uu = u + w * n_pad, *vv = v + w * n_pad;
+        double re = 0.0, im = 0.0;
+        for (int i = lane; i < n_pad; i += 32) {
+            double wr = 0.0, wi = 0.0;
+            for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+                const double2 a = val[e], b = uu[col[e]];
+                wr = fma(a.x, b.x, fma(-a.y, b.y, wr));
+                wi = fma(a.x, b.y, fma(a.y, b.x, wi));
+            }
+            const double2 c = vv[i];                 // conj(c) * w
+            re = fma(c.x, wr, fma(c.y, wi, re));
+            im = fma(c.x, wi, fma(-c.y, wr, im));
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            re += __shfl_xor_sync(0xffffffffu, re, o);
+            im += __shfl_xor_sync(0xffffffffu, im, o);
+        }
+        if (lane == 0) out[w] = make_double2(re, im);
+    }
+}
+
+// fid[n] = sum_o w[o] f[o][n] in orientation order (powder.m:280-287).
+__global__ void echo_powder_kernel(int n_orient, int npoints, const double2 *f, const double *w, double2 *fid) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= npoints) return;
+    double re = 0.0, im = 0.0;
+    for (int o = 0; o < n_orient; ++o) {
+        const double2 v = f[(size_t)o * npoints + n];
+        re = fma(w[o], v.x, re);
+        im = fma(w[o], v.y, im);
+    }
+    fid[n] = make_double2(re, im);
+}
+
+void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
+               const double *weights, double timestep, int64_t npoints, const spx_csc *pulse_op,
+               const spx_options &o, double *fid) {
+    if (h->nchan != 1 || h->n_states != 0)
+        throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil and one initial state");
+    if (npoints < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "npoints must be positive");
+    const double tau = timestep / 2;                // eseem.m: steps of timestep/2
+    const int64_t nsteps = npoints - 1;
+    validate_run(h, n_orient, tau, nsteps);
+    const int n_pad = h->n_pad;
+    if (n_pad > 8192) throw SpxError(SPX_ERR_UNSUPPORTED, "echo detection is limited to dimension 8192");
+    upload_pulse(h, pulse_op);
+    h->d_grid.reserve(4 * (size_t)n_orient);
+    double *g = h->d_grid.p;
+    const size_t b = (size_t)n_orient * sizeof(double);
+    SPX_CUDA(cudaMemcpyAsync(g, alphas, b, cudaMemcpyHostToDevice, h->stream));
+    SPX_CUDA(cudaMemcpyAsync(g + n_orient, betas, b, cudaMemcpyHostToDevice, h->stream));
+    SPX_CUDA(cudaMemcpyAsync(g + 2 * n_orient, gammas, b, cudaMemcpyHostToDevice, h->stream));
+    SPX_CUDA(cudaMemcpyAsync(g + 3 * n_orient, weights, b, cudaMemcpyHostToDevice, h->stream));
+    // rho1 = exp(-1i pi/2 P) rho0
+    h->d_seq_rho.reserve(n_pad);
+    SPX_CUDA(cudaMemcpyAsync(h->d_seq_rho.p, h->d_rho0.p, n_pad * sizeof(double2), cudaMemcpyDeviceToDevice,
+                             h->stream));
+    apply_pulse(h, M_PI / 2, 1, h->d_seq_rho.p);
+    // Pi = exp(-1i pi P) column by column, kept as CSR (entries above 1e-15;
+    // Pi is unitary, so they are at most 1)
+    {
+        DevBuf<double2> dense;
+        dense.reserve((size_t)n_pad * n_pad);
+        identity_kernel<<<h->sm_count * 4, 256, 0, h->stream>>>(n_pad, dense.p);
+        SPX_CUDA(cudaGetLastError());
+        apply_pulse(h, M_PI, n_pad, dense.p);
+        std::vector<double2> hd((size_t)n_pad * n_pad);
+        SPX_CUDA(cudaMemcpyAsync(hd.data(), dense.p, hd.size() * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+        SPX_CUDA(cudaStreamSynchronize(h->stream));
+        std::vector<int> ptr(n_pad + 1, 0), col;
+        std::vector<double2> val;
+        for (int i = 0; i < n_pad; ++i) {
+            for (int j = 0; j < n_pad; ++j) {
+                const double2 v = hd[(size_t)j * n_pad + i];         // column j holds Pi e_j
+                if (std::fabs(v.x) > 1e-15 || std::fabs(v.y) > 1e-15) {
+                    col.push_back(j);
+                    val.push_back(v);
+                }
+            }
+            ptr[i + 1] = (int)col.size();
+        }
+        if (col.empty()) { col.push_back(0); val.push_back(make_double2(0, 0)); }
+        h->d_echo_ptr.upload(ptr, h->stream);
+        h->d_echo_col.upload(col, h->stream);
+        h->d_echo_val.upload(val, h->stream);
+    }
+    // adjoint generator
+    const int64_t n_ell = (int64_t)h->nstreams * h->ell_len, n_diag = (int64_t)h->nstreams * n_pad;
+    h->d_neg_re.reserve((size_t)std::max<int64_t>(n_ell, 1));
+    if (h->cplx) h->d_neg_im.reserve((size_t)std::max<int64_t>(n_ell, 1));
+    h->d_neg_diag.reserve((size_t)n_diag);
+    negate_streams_kernel<<<h->sm_count * 4, 256, 0, h->stream>>>(
+        n_ell, h->d_ell_re.p, h->cplx ? h->d_ell_im.p : nullptr, h->d_neg_re.p, h->cplx ? h->d_neg_im.p : nullptr,
+        n_diag, n_pad, h->d_diag.p, h->d_neg_diag.p);
+    SPX_CUDA(cudaGetLastError());
+    // one-step chunks give the state at every step; orientations in batches
+    // whose two trajectories take a quarter of the free device memory (at
+    // most 48 GB): few batches, so few partly filled waves
+    spx_options o1 = o;
+    o1.chunk_steps = 1;
+    size_t free_b = 0, total_b = 0;
+    SPX_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t budget = std::min<size_t>(free_b / 4, 48ull << 30);
+    const size_t per_orient = 2 * (size_t)npoints * n_pad * sizeof(double2);
+    const int64_t batch = std::max<int64_t>(1, std::min<int64_t>(n_orient, (int64_t)(budget / per_orient)));
+    h->d_traj[0].reserve((size_t)batch * npoints * n_pad);
+    h->d_traj[1].reserve((size_t)batch * npoints * n_pad);
+    h->d_echo_f.reserve((size_t)n_orient * npoints);
+    h->d_fid.reserve((size_t)npoints);
+    for (int64_t b0 = 0; b0 < n_orient; b0 += batch) {
+        const int64_t nb = std::min(batch, n_orient - b0);
+        const Config c = choose_config(h, nb, tau, nsteps, o1, 0);
+        for (int dir = 0; dir < 2; ++dir) {
+            RunIO io;
+            io.rho0 = dir == 0 ? h->d_seq_rho.p : h->d_coil.p;
+            io.traj_out = h->d_traj[dir].p;
+            io.adjoint = dir == 1;
+            launch_powder(h, nb, g + b0, g + n_orient + b0, g + 2 * n_orient + b0, g + 3 * n_orient + b0, tau, nsteps,
+                          o1, h->d_fid.p, c, 0, true, io);
+            finish_run(h);
+        }
+        const int64_t warps = nb * npoints;
+        const int blocks = (int)std::min<int64_t>((warps + 7) / 8, (int64_t)h->sm_count * 16);
+        echo_form_kernel<<<blocks, 256, 0, h->stream>>>((int)nb, (int)npoints, n_pad, h->d_echo_ptr.p, h->d_echo_col.p,
+                                                        h->d_echo_val.p, h->d_traj[0].p, h->d_traj[1].p,
+                                                        h->d_echo_f.p + b0 * npoints);
+        SPX_CUDA(cudaGetLastError());
+    }
+    echo_powder_kernel<<<(unsigned)((npoints + 127) / 128), 128, 0, h->stream>>>(
+        (int)n_orient, (int)npoints, h->d_echo_f.p, g + 3 * n_orient, h->d_fid.p);
+    SPX_CUDA(cudaGetLastError());
+    SPX_CUDA(cudaMemcpyAsync(fid, h->d_fid.p, (size_t)npoints * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    SPX_CUDA(cudaStreamSynchronize(h->stream));
 }
 
 // ---------------------------------------------------------------------------
@@ -1453,6 +1639,26 @@ spx_status spx_run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, c
         o = apply_tuned(h, o);
         SPX_CUDA(cudaSetDevice(h->device));
         run_cpmg(h, n_orient, alphas, betas, gammas, weights, dt, npoints, nloops, pulse_op, o, fid);
+    });
+}
+
+spx_status spx_run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
+                         const double *gammas, const double *weights, double timestep, int64_t npoints,
+                         const spx_csc *pulse_op, const spx_options *opt, double *fid) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (!alphas || !betas || !gammas || !weights || !fid || !pulse_op)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL argument");
+        for (int64_t o = 0; o < n_orient; ++o)
+            if (!std::isfinite(alphas[o]) || !std::isfinite(betas[o]) || !std::isfinite(gammas[o]) ||
+                !std::isfinite(weights[o]))
+                throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite grid entry");
+        spx_options o{};
+        if (opt) o = *opt;
+        if (o.precision != SPX_FP32 && o.precision != SPX_FP64)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
+        SPX_CUDA(cudaSetDevice(h->device));
+        run_eseem(h, n_orient, alphas, betas, gammas, weights, timestep, npoints, pulse_op, o, fid);
     });
 }
 

@@ -359,6 +359,8 @@ struct DevRun {
     int *mused;         // n_orient: time steps per chunk used
     int cl;                 // CTAs per cluster (1: no cluster)
     double2 *state_out;     // or null: the state after the last step, n_orient x n_pad (sliced order)
+    double2 *traj_out;      // or null: the state at the start of every chunk, n_orient x (nsteps+1) x n_pad
+                            // (sliced order; with one-step chunks the state at every time step)
     int *next_orient;       // work counter (zeroed before the launch): single CTAs take
                             // orientations gridDim.x, gridDim.x + 1, ... as they finish
     int cl_slices[kMaxCluster + 1];   // slice boundaries of the CTAs' row blocks (cluster launches)
@@ -1047,6 +1049,19 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             // its own length j_last, from the same Bessel table
             const bool advance = !last || run.state_out != nullptr;
             const int Kc = last ? K_last : K;              // terms of this chunk
+            if (run.traj_out) {
+                // trajectory output ('trajectory' of evolution.m): the state entering chunk a
+                double2 *tr = run.traj_out + ((size_t)o * (nsteps + 1) + (size_t)a * Mo) * sys.n_pad;
+#pragma unroll
+                for (int r = 0; r < RMAX; ++r) {
+                    if (r < nr) {
+                        double2 v;
+                        if constexpr (F64) v = tod(t_cur[r]);
+                        else v = tod(f2up(tc[r]));
+                        tr[r_row[r]] = v;
+                    }
+                }
+            }
             mv += Kc - 1;
             if (last && run.state_out && nchunks > 0) {
                 const int j_last = nsteps - (nchunks - 1) * Mo;

@@ -65,6 +65,8 @@ SIGNATURES = {
                                    C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_int32), C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_int32), _D, _D, _D, _D, _D]),
+    'spx_run_eseem': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.POINTER(SpxCsc),
+                                C.POINTER(SpxOptions), _D]),
     'spx_upload_coils': (C.c_int, [_P, C.c_int32, _D]),
     'spx_set_initial_states': (C.c_int, [_P, C.c_int64, _D]),
     'spx_autotune': (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_double, C.c_int64, C.c_int32,
@@ -280,6 +282,23 @@ class Engine:
         self._check(self.lib.spx_run_cpmg(self.h, al.size, _dptr(al), _dptr(be), _dptr(ga), _dptr(w), float(dt),
                                           int(npoints), int(nloops), C.byref(P.struct), C.byref(opt), _dptr(fid)),
                     self.h)
+        return PowderResult(fid.view(np.complex128), None, self.stats())
+
+    def run_eseem(self, alphas, betas, gammas, weights, timestep: float, npoints: int, pulse_op,
+                  precision: int = FP32, threads: int = 0, cluster: int = 0) -> PowderResult:
+        """Two-pulse echo (experiments/esr_dipolar/eseem.m): ``fid[n]`` is the powder
+        echo after a 90-degree pulse, n steps of timestep/2, a 180-degree pulse
+        and n more steps (npoints values)."""
+        al = np.ascontiguousarray(alphas, np.float64)
+        be = np.ascontiguousarray(betas, np.float64)
+        ga = np.ascontiguousarray(gammas, np.float64)
+        w = np.ascontiguousarray(weights, np.float64)
+        fid = np.zeros(2 * npoints)
+        P = _CscHolder(pulse_op, self.dim)
+        opt = SpxOptions(precision, 0, threads, cluster, 0.0, 0.0, 0, 0)
+        self._check(self.lib.spx_run_eseem(self.h, al.size, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
+                                           float(timestep), int(npoints), C.byref(P.struct), C.byref(opt),
+                                           _dptr(fid)), self.h)
         return PowderResult(fid.view(np.complex128), None, self.stats())
 
     def run_device(self, d_alphas: int, d_betas: int, d_gammas: int, d_weights: int, n_orient: int,

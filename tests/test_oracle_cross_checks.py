@@ -122,3 +122,22 @@ def test_cpmg_with_a_zero_pulse_is_one_continuous_acquisition():
                                                   npoints=10 + 2 * 19), ang)
     idx = list(range(10)) + list(range(9, 29)) + list(range(28, 48))
     assert rel_err(f, acq[idx]) < 1e-12
+
+
+@pytest.mark.parametrize('relax', [False, True])
+def test_eseem_matches_kron_model(relax):
+    """experiments/esr_dipolar/eseem.m restated on the spherical-tensor basis
+    (trajectory, stacked pulse, refocusing) vs Hilbert-space pulses."""
+    w = _c0_like(relax)
+    ss, I, Q = oracle_system(w)
+    km = KronModel(ss)
+    rho_h = km.spin_op('Lz', '13C') / np.sqrt(km.dim)
+    coil_h = km.spin_op(*w.coil) / np.sqrt(km.dim)
+    par = dict(rho0=R.state(ss, 'Lz', '13C'), coil=R.state(ss, *w.coil), pulse_op=R.operator(ss, 'Ly', '13C'),
+               timestep=2 * w.dt, npoints=24)
+    for ang in [(0.0, 0.7, 1.3), (0.4, 1.0, -0.3)]:
+        f_st = R.powder_orientation_eseem(ss, I, Q, par, ang)
+        f_kr = km.eseem(ang, rho_h, coil_h, km.spin_op('Ly', '13C'), 2 * w.dt, 24)
+        assert f_st.shape == (24,)
+        assert np.abs(f_kr).max() > 0.1
+        assert rel_err(f_st, f_kr) < 1e-8, ang
