@@ -16,7 +16,9 @@
 // opts     optional struct: precision ('double' default, or 'single');
 //          pulse_op (sparse dim x dim) and nloops run experiments/cpmg.m
 //          instead of acquire.m: npoints = nsteps+1 per half-echo, fid
-//          npoints*(1+2*nloops) x 1.
+//          npoints*(1+2*nloops) x 1; pulse_op and sequence = 'eseem' run
+//          experiments/esr_dipolar/eseem.m with timestep = dt and
+//          npoints = nsteps+1 (fid (nsteps+1) x 1).
 // fid      (nsteps+1) x 1 complex: sum_n weights(n) fid_n (powder.m:280-287).
 // fids     (nsteps+1) x n_orient complex, the sum_up=false output (powder.m:291-297).
 //
@@ -195,12 +197,28 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     opt.precision = SPX_FP64;
     CscCopy pulse;
     int32_t nloops = 0;                 // > 0: a CPMG echo train (experiments/cpmg.m)
+    bool eseem = false;                 // a two-pulse echo (experiments/esr_dipolar/eseem.m)
     if (nrhs == 9) {
         const mxArray *po = mxGetField(prhs[8], 0, "pulse_op");
         const mxArray *nl = mxGetField(prhs[8], 0, "nloops");
-        if ((po == nullptr) != (nl == nullptr))
+        const mxArray *sq = mxGetField(prhs[8], 0, "sequence");
+        if (sq) {
+            char buf[16] = {0};
+            if (!mxIsChar(sq) || mxGetString(sq, buf, sizeof buf) != 0 ||
+                (std::strcmp(buf, "eseem") != 0 && std::strcmp(buf, "cpmg") != 0))
+                throw GatewayError{"Spinach:spinach_powder_gpu:sequence", "opts.sequence must be 'cpmg' or 'eseem'."};
+            eseem = std::strcmp(buf, "eseem") == 0;
+        }
+        if (eseem) {
+            if (!po || nl)
+                throw GatewayError{"Spinach:spinach_powder_gpu:sequence", "an echo takes opts.pulse_op and no opts.nloops."};
+            fill_csc(po, n, "opts.pulse_op", pulse);
+            if (nlhs > 1)
+                throw GatewayError{"Spinach:spinach_powder_gpu:nlhs", "an echo returns the powder signal only."};
+        } else if ((po == nullptr) != (nl == nullptr)) {
             throw GatewayError{"Spinach:spinach_powder_gpu:cpmg", "opts.pulse_op and opts.nloops go together."};
-        if (po) {
+        }
+        if (po && !eseem) {
             fill_csc(po, n, "opts.pulse_op", pulse);
             const double v = scalar(nl, "opts.nloops");
             if (v < 1 || v != (double)(int32_t)v)
@@ -235,6 +253,17 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     }
     if (st != SPX_OK)
         throw GatewayError{"Spinach:spinach_powder_gpu:upload", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
+    if (eseem) {
+        std::vector<double> fid(2 * (size_t)(nsteps + 1));
+        st = spx_run_eseem(g_handle, no, al.data(), be.data(), ga.data(), wt.data(), dt, nsteps + 1, &pulse.view, &opt,
+                           fid.data());
+        if (st != SPX_OK)
+            throw GatewayError{"Spinach:spinach_powder_gpu:run", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
+        plhs[0] = mxCreateDoubleMatrix((mwSize)(nsteps + 1), 1, mxCOMPLEX);
+        mxComplexDouble *out = mxGetComplexDoubles(plhs[0]);
+        for (int64_t i = 0; i <= nsteps; ++i) { out[i].real = fid[2 * i]; out[i].imag = fid[2 * i + 1]; }
+        return;
+    }
     if (nloops > 0) {
         const int64_t npts = (nsteps + 1) * (1 + 2 * (int64_t)nloops);
         std::vector<double> fid(2 * (size_t)npts);

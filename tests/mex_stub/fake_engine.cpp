@@ -101,6 +101,17 @@ spx_status spx_run_cpmg(spx_handle *, int64_t no, const double *, const double *
     for (int64_t i = 0; i < npoints * (1 + 2 * nloops); ++i) { fid[2 * i] = 2.0 * i; fid[2 * i + 1] = 1.0; }
     return SPX_OK;
 }
+spx_status spx_run_eseem(spx_handle *, int64_t no, const double *, const double *, const double *, const double *,
+                         double dt, int64_t npoints, const spx_csc *P, const spx_options *opt, double *fid) {
+    g_rec.n_orient = no;
+    g_rec.dt = dt;
+    g_rec.npoints = npoints;
+    g_rec.nloops = -1;
+    g_rec.precision = opt ? opt->precision : -1;
+    g_rec.pulse.assign(P->values, P->values + 2 * P->colptr[P->n]);
+    for (int64_t i = 0; i < npoints; ++i) { fid[2 * i] = 3.0 * i; fid[2 * i + 1] = -1.0; }
+    return SPX_OK;
+}
 spx_status spx_run_powder_device(spx_handle *, int64_t, const double *, const double *, const double *,
                                  const double *, double, int64_t, const spx_options *, double *) {
     return SPX_ERR_UNSUPPORTED;

@@ -165,6 +165,26 @@ int main() {
     copt3->fields["nloops"] = scalar(1);
     const mxArray *pcp3[9] = {I, Q, R, rho0, coil, grid, scalar(1e-5), scalar(5), copt3};
     expect(1, 9, pcp3, "Spinach:spinach_powder_gpu:cpmg");
+    // opts.pulse_op + opts.sequence = 'eseem': the two-pulse echo
+    mxArray *eopt = strct();
+    eopt->fields["pulse_op"] = copt->fields["pulse_op"];
+    eopt->fields["sequence"] = str("eseem");
+    eopt->fields["precision"] = str("single");
+    const mxArray *pe[9] = {I, Q, R, rho0, coil, grid, scalar(2e-8), scalar(7), eopt};
+    mxArray *oe[1] = {nullptr};
+    mexFunction(1, oe, 9, pe);
+    CHECK(g_rec.npoints == 8 && g_rec.nloops == -1 && g_rec.precision == 0 && g_rec.dt == 2e-8);
+    CHECK(oe[0] && oe[0]->m == 8 && oe[0]->n == 1 && oe[0]->cx[5].real == 15.0 && oe[0]->cx[5].imag == -1.0);
+    expect(2, 9, pe, "Spinach:spinach_powder_gpu:nlhs");
+    mxArray *eopt2 = strct();
+    eopt2->fields["pulse_op"] = copt->fields["pulse_op"];
+    eopt2->fields["sequence"] = str("hahn");
+    const mxArray *pe2[9] = {I, Q, R, rho0, coil, grid, scalar(2e-8), scalar(7), eopt2};
+    expect(1, 9, pe2, "Spinach:spinach_powder_gpu:sequence");
+    mxArray *eopt3 = strct();
+    eopt3->fields["sequence"] = str("eseem");
+    const mxArray *pe3[9] = {I, Q, R, rho0, coil, grid, scalar(2e-8), scalar(7), eopt3};
+    expect(1, 9, pe3, "Spinach:spinach_powder_gpu:sequence");
     mxArray *o2[2] = {nullptr, nullptr};
     expect(2, 8, pc, "Spinach:spinach_powder_gpu:nlhs");
     (void)o2;
