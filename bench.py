@@ -331,13 +331,14 @@ def run_gpu(args):
             cpu = {'value': nn / t, 'unit': UNIT, 'cores': cores, 'kind': 'port',
                    'sample': f'{nn} orientations of {args.workload} (one per core, all time steps), '
                              f'oracle restatement in FP64: {BRANCH_TEXT[args.workload]}'}
-        sur = c2 = c4 = mas = None
+        sur = c2 = c4 = mas = echoes = None
         if not args.no_surrogate and world == 1 and args.workload == 'c1':
             sur = surrogate_leg(eng, w, local)
         if not args.no_extra and world == 1 and args.workload == 'c1':
             c4 = c4_leg(local)
             c2 = c2_leg(local)
             mas = mas_leg(local)
+            echoes = echo_legs(local)
         line = {
             'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': statistics.mean(step_ms), 'higher_is_better': True,
@@ -368,6 +369,7 @@ def run_gpu(args):
             'c4': c4,
             'c2': c2,
             'mas': mas,
+            'sequences': echoes,
             'clocks': clk,
             'gpu_launches': 3 * args.steps,
         }
@@ -435,6 +437,39 @@ def mas_leg(device):
            'kernel_ms': res[E.FP32][1].stats['kernel_ms'], 'cluster': res[E.FP32][1].stats['cluster'],
            'nnz': res[E.FP32][1].stats['nnz'], 'rotor_space_setup_s': t_fp}
     eng.close()
+    return out
+
+
+def echo_legs(device):
+    """Pulse sequences on the evolution core, FP32 with host buffers: CPMG on the c1 system (1000
+    orientations, 128-point half-echoes, 8 loops: 2176 points) and the two-pulse echo on the c4 radical
+    (4000 orientations, 256 points of 8 ns), each against the same run in FP64."""
+    from spinach_gb300 import engine as E, spin_system as S, workloads as W
+    out = {}
+    for name, w, spin in (('cpmg', W.c1(), '13C'), ('eseem', W.c4(), 'E')):
+        L = W.build(w)
+        ss = W.spin_system_of(w)
+        fac = S.factory_for(ss, S.build_basis(ss, w.approximation, w.level))
+        pulse = sum(fac.operator([('Ly', i)]) for i, iso in enumerate(w.isotopes) if iso == spin)
+        eng = E.Engine(device)
+        eng.upload(L.I, L.terms, L.R, fac.state('Lz', spin), L.coil)
+        g = W.zcwn_grid(w.n_orient)
+        if name == 'cpmg':
+            run = lambda p: eng.run_cpmg(*g, w.dt, 128, 8, pulse, precision=p)
+            text = ('CPMG (cpmg.m) on the c1 system: Lz(13C), Ly(13C) pulses, 1000 orientations, '
+                    '128-point half-echoes of 5 us, 8 loops (2176 points)')
+        else:
+            run = lambda p: eng.run_eseem(*g, 8e-9, 256, pulse, precision=p)
+            text = ('two-pulse echo (eseem.m) on the c4 radical: Lz(E), Ly(E) pulses, 4000 orientations, '
+                    '256 echo points, timestep 8 ns')
+        run(E.FP32)                                                           # warm-up
+        t0 = time.perf_counter()
+        r32 = run(E.FP32)
+        t32 = time.perf_counter() - t0
+        r64 = run(E.FP64)
+        out[name] = {'workload': text, 'value': w.n_orient / t32, 'unit': UNIT, 'seconds': t32,
+                     'rel_err_vs_fp64_gpu': _rel(r32.fid, r64.fid)}
+        eng.close()
     return out
 
 
