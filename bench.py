@@ -12,7 +12,15 @@ Reported:
   e2e    the same metric through the C ABI with host buffers
          (spx_upload_system + spx_run_powder: H2D of I/Q/R/states/grid,
          D2H of the powder FID inside the timed region);
-  roofline / cpu_baseline / clocks / gpu_launches as described in DESIGN.md.
+  roofline   algorithmic sparse-matvec bytes (12 per non-zero + 16 per row,
+             per matvec) / kernel time against the measured HBM copy peak,
+             the ncu DRAM traffic of one launch, and the same bytes against
+             shared-memory bandwidth and the MACs against the FP32 pipe;
+  cpu_baseline  the oracle's FP64 restatement on the host cores (bounded
+             sample, one process per core);
+  clocks     nvidia-smi samples during the timed steps;
+  gpu_launches  kernels of this library launched in the timed region;
+  c4 / c2 / mas / sequences / surrogate  the other workloads, once each.
 
 --impl reference times the reference algorithm (the oracle's restatement of
 Spinach's default CPU branch, propagator.m + P*rho) on the host cores.
