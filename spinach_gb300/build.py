@@ -7,8 +7,8 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 SOURCES = [os.path.join(HERE, 'csrc', f) for f in
-           ['engine.cu', 'builder.cu', 'surrogate.cu'] + [f'kern_{p}_{c}.cu' for p in ('f32r', 'f32c', 'f64r', 'f64c')
-                                            for c in ('sc', 'dc')]]
+           ['engine.cu', 'builder.cu', 'surrogate.cu'] +
+           [f'kern_{p}_{c}{t}.cu' for p in ('f32r', 'f32c', 'f64r', 'f64c') for c in ('sc', 'dc') for t in ('', '_t')]]
 DEPS = SOURCES + [os.path.join(HERE, 'csrc', 'kernels.cuh'), os.path.join(HERE, 'csrc', 'builder.h'), os.path.join(HERE, 'csrc', 'kern_inst.inc'),
                   os.path.join(ROOT, 'include', 'spinach_gpu.h')]
 LIB = os.path.join(HERE, 'lib', 'libspinach_gpu.so')

@@ -499,6 +499,8 @@ struct Config {
     int cl = 1;                                   // CTAs per cluster
     int slices[spx::kMaxCluster + 1] = {};        // row blocks of the cluster's CTAs
     int nsl_loc = 0, ell_loc = 0;                 // largest block (slices, ELL entries)
+    int traj_m = 1;                               // trajectory outputs: chunk length (1: none)
+    bool traj = false;                            // the kernels with trajectory outputs
 };
 
 double host_series_terms(double x, double lg, double tol) {
@@ -514,17 +516,18 @@ double host_series_terms(double x, double lg, double tol) {
 }
 
 template <bool F64, bool CPLX>
-size_t smem_bytes(const spx_handle *h, int nsl_loc, int ell_loc, int Kmax, int M, int threads) {
-    spx::SmemLayout<F64, CPLX> L(h->n_pad, nsl_loc, ell_loc, Kmax, M, threads, h->nchan);
+size_t smem_bytes(const spx_handle *h, int nsl_loc, int ell_loc, int Kmax, int M, int threads, int traj_m) {
+    spx::SmemLayout<F64, CPLX> L(h->n_pad, nsl_loc, ell_loc, Kmax, M, threads, h->nchan, traj_m);
     return L.total;
 }
 
-size_t smem_for(const spx_handle *h, bool f64, int nsl_loc, int ell_loc, int Kmax, int M, int threads) {
+size_t smem_for(const spx_handle *h, bool f64, int nsl_loc, int ell_loc, int Kmax, int M, int threads,
+                int traj_m = 1) {
     if (f64)
-        return h->cplx ? smem_bytes<true, true>(h, nsl_loc, ell_loc, Kmax, M, threads)
-                       : smem_bytes<true, false>(h, nsl_loc, ell_loc, Kmax, M, threads);
-    return h->cplx ? smem_bytes<false, true>(h, nsl_loc, ell_loc, Kmax, M, threads)
-                   : smem_bytes<false, false>(h, nsl_loc, ell_loc, Kmax, M, threads);
+        return h->cplx ? smem_bytes<true, true>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m)
+                       : smem_bytes<true, false>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m);
+    return h->cplx ? smem_bytes<false, true>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m)
+                   : smem_bytes<false, false>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m);
 }
 
 }  // namespace
@@ -538,11 +541,27 @@ const void *spx_kernel_f32r_dc(int rmax, bool cluster);
 const void *spx_kernel_f32c_dc(int rmax, bool cluster);
 const void *spx_kernel_f64r_dc(int rmax, bool cluster);
 const void *spx_kernel_f64c_dc(int rmax, bool cluster);
+const void *spx_kernel_f32r_sc_t(int rmax, bool cluster);     // with trajectory outputs
+const void *spx_kernel_f32c_sc_t(int rmax, bool cluster);
+const void *spx_kernel_f64r_sc_t(int rmax, bool cluster);
+const void *spx_kernel_f64c_sc_t(int rmax, bool cluster);
+const void *spx_kernel_f32r_dc_t(int rmax, bool cluster);
+const void *spx_kernel_f32c_dc_t(int rmax, bool cluster);
+const void *spx_kernel_f64r_dc_t(int rmax, bool cluster);
+const void *spx_kernel_f64c_dc_t(int rmax, bool cluster);
 namespace {
 
 // Single-CTA kernels for RMAX 1, 2, 4, 8; cluster kernels for RMAX 1, 2, 4;
 // sc: the coil is listed (at most 32 non-zeros), else the dense projection.
-const void *select_kernel(bool f64, bool cplx, int rmax, bool clu, bool sc) {
+const void *select_kernel(bool f64, bool cplx, int rmax, bool clu, bool sc, bool traj = false) {
+    if (traj) {
+        if (sc) {
+            if (f64) return cplx ? spx_kernel_f64c_sc_t(rmax, clu) : spx_kernel_f64r_sc_t(rmax, clu);
+            return cplx ? spx_kernel_f32c_sc_t(rmax, clu) : spx_kernel_f32r_sc_t(rmax, clu);
+        }
+        if (f64) return cplx ? spx_kernel_f64c_dc_t(rmax, clu) : spx_kernel_f64r_dc_t(rmax, clu);
+        return cplx ? spx_kernel_f32c_dc_t(rmax, clu) : spx_kernel_f32r_dc_t(rmax, clu);
+    }
     if (sc) {
         if (f64) return cplx ? spx_kernel_f64c_sc(rmax, clu) : spx_kernel_f64r_sc(rmax, clu);
         return cplx ? spx_kernel_f32c_sc(rmax, clu) : spx_kernel_f32r_sc(rmax, clu);
@@ -579,9 +598,12 @@ bool partition_slices(const spx_handle *h, int cl, Config &c) {
     return true;
 }
 
+// traj: the run writes the state at every step (chunks of opt.chunk_steps
+// steps, their intermediate states accumulated in shared memory).
 Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps, const spx_options &opt,
-                     int kmax_override, int m_cap = 256) {
+                     int kmax_override, int m_cap = 256, bool traj = false) {
     Config c{};
+    c.traj = traj;
     const bool f64 = opt.precision == SPX_FP64;
     if (opt.cluster != 0 && opt.cluster != 1 && opt.cluster != 2 && opt.cluster != 4 && opt.cluster != 8)
         throw SpxError(SPX_ERR_INVALID_ARGUMENT, "cluster must be 0 (auto), 1, 2, 4 or 8");
@@ -621,7 +643,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
         c.threads = nwarps * 32;
         // dynamic shared memory may use what the kernel's static arrays leave
         cudaFuncAttributes fa{};
-        SPX_CUDA(cudaFuncGetAttributes(&fa, select_kernel(f64, h->cplx, c.rmax, cl > 1, h->ncoil > 0)));
+        SPX_CUDA(cudaFuncGetAttributes(&fa, select_kernel(f64, h->cplx, c.rmax, cl > 1, h->ncoil > 0, traj)));
         const size_t budget = h->smem_optin > fa.sharedSizeBytes ? h->smem_optin - fa.sharedSizeBytes : 0;
         for (double tx : targets) {
             c.chunk_x = tx;
@@ -633,7 +655,8 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
             int K = (int)host_series_terms(xu, std::min(lg, 0.05), c.tol) + 16;
             if (kmax_override > 0) K = std::max(K, kmax_override);
             c.Kmax = std::min(K, 8192);
-            c.smem = smem_for(h, f64, c.nsl_loc, c.ell_loc, c.Kmax, c.M, c.threads);
+            c.traj_m = traj ? c.M : 1;
+            c.smem = smem_for(h, f64, c.nsl_loc, c.ell_loc, c.Kmax, c.M, c.threads, c.traj_m);
             if (c.smem <= budget) { placed = true; break; }
             if (c.fixed) break;
         }
@@ -644,7 +667,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     if (!placed)
         throw SpxError(SPX_ERR_UNSUPPORTED, "system does not fit the shared memory of a cluster of 8 SMs (" +
                                                 std::to_string(c.smem) + " bytes per SM)");
-    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1, h->ncoil > 0);
+    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1, h->ncoil > 0, c.traj);
     {
         // allow the whole budget: several configurations of one kernel may be
         // prepared before any of them launches (batched graphs)
@@ -685,7 +708,7 @@ void launch_chebyshev(spx_handle *h, bool f64, const Config &c, spx::DevSystem &
     run.nsl_loc = c.nsl_loc;
     run.ell_loc = c.ell_loc;
     for (int j = 0; j <= spx::kMaxCluster; ++j) run.cl_slices[j] = j <= c.cl ? c.slices[j] : 0;
-    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1, h->ncoil > 0);
+    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1, h->ncoil > 0, c.traj);
     void *args[] = {&sys, &run};
     if (c.cl == 1) {
         SPX_CUDA(cudaLaunchKernel(kfn, dim3(c.grid), dim3(c.threads), args, c.smem, h->stream));
@@ -728,7 +751,8 @@ struct RunIO {
     const double2 *rho0 = nullptr;     // one initial state for every orientation (sliced order)
     const double2 *rho0s = nullptr;    // one per orientation, n_orient x n_pad
     double2 *state_out = nullptr;      // the state after the last step, n_orient x n_pad
-    double2 *traj_out = nullptr;       // the state entering every chunk, n_orient x (nsteps+1) x n_pad
+    double2 *traj_out = nullptr;       // the state at every step, n_orient x (nsteps+1) x n_pad (needs a
+                                       // trajectory configuration: choose_config(..., traj = true))
     bool adjoint = false;              // propagate under -H + 1i R (the adjoint of L, negated)
 };
 
@@ -759,7 +783,9 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     }
     spx::DevRun run{};
     run.state_out = io.state_out;
+    if (io.traj_out && !c.traj) throw SpxError(SPX_ERR_INTERNAL, "trajectory output needs a trajectory configuration");
     run.traj_out = io.traj_out;
+    run.traj_m = c.traj_m;
     run.n_orient = (int)n_orient; run.alpha = d_al; run.beta = d_be; run.gamma = d_ga;
     run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
     run.fixed_chunk = c.fixed ? 1 : 0; run.chunk_x = c.chunk_x;
@@ -1100,6 +1126,8 @@ __global__ void echo_powder_kernel(int n_orient, int npoints, const double2 *f, 
     fid[n] = make_double2(re, im);
 }
 
+constexpr int kTrajChunk = 4;       // steps per chunk of trajectory outputs (falls back to 2, 1)
+
 void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
                const double *weights, double timestep, int64_t npoints, const spx_csc *pulse_op,
                const spx_options &o, double *fid) {
@@ -1161,11 +1189,12 @@ void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const doub
         n_ell, h->d_ell_re.p, h->cplx ? h->d_ell_im.p : nullptr, h->d_neg_re.p, h->cplx ? h->d_neg_im.p : nullptr,
         n_diag, n_pad, h->d_diag.p, h->d_neg_diag.p);
     SPX_CUDA(cudaGetLastError());
-    // one-step chunks give the state at every step; orientations in batches
+    // the states at every step come from chunks of a few steps (their
+    // intermediate states accumulated in shared memory: one-step chunks spend
+    // most of their series on the truncation tail); orientations in batches
     // whose two trajectories take a quarter of the free device memory (at
     // most 48 GB): few batches, so few partly filled waves
     spx_options o1 = o;
-    o1.chunk_steps = 1;
     size_t free_b = 0, total_b = 0;
     SPX_CUDA(cudaMemGetInfo(&free_b, &total_b));
     const size_t budget = std::min<size_t>(free_b / 4, 48ull << 30);
@@ -1177,7 +1206,16 @@ void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const doub
     h->d_fid.reserve((size_t)npoints);
     for (int64_t b0 = 0; b0 < n_orient; b0 += batch) {
         const int64_t nb = std::min(batch, n_orient - b0);
-        const Config c = choose_config(h, nb, tau, nsteps, o1, 0);
+        Config c{};
+        for (int m : {kTrajChunk, 2, 1}) {
+            o1.chunk_steps = m;
+            try {
+                c = choose_config(h, nb, tau, nsteps, o1, 0, 256, true);
+                break;
+            } catch (const SpxError &e) {
+                if (m == 1 || e.code != SPX_ERR_UNSUPPORTED) throw;
+            }
+        }
         for (int dir = 0; dir < 2; ++dir) {
             RunIO io;
             io.rho0 = dir == 0 ? h->d_seq_rho.p : h->d_coil.p;

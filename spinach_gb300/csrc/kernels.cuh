@@ -359,8 +359,8 @@ struct DevRun {
     int *mused;         // n_orient: time steps per chunk used
     int cl;                 // CTAs per cluster (1: no cluster)
     double2 *state_out;     // or null: the state after the last step, n_orient x n_pad (sliced order)
-    double2 *traj_out;      // or null: the state at the start of every chunk, n_orient x (nsteps+1) x n_pad
-                            // (sliced order; with one-step chunks the state at every time step)
+    double2 *traj_out;      // or null: the state at every time step, n_orient x (nsteps+1) x n_pad (sliced order)
+    int traj_m;             // trajectory outputs: steps per chunk (the fixed chunk length; 1 otherwise)
     int *next_orient;       // work counter (zeroed before the launch): single CTAs take
                             // orientations gridDim.x, gridDim.x + 1, ... as they finish
     int cl_slices[kMaxCluster + 1];   // slice boundaries of the CTAs' row blocks (cluster launches)
@@ -493,11 +493,15 @@ static __device__ double ritz_last_component(const double *al_d, const double *b
 template <bool F64, bool CPLX>
 struct SmemLayout {
     using P = Prec<F64, CPLX>;
-    size_t coef, red, cred, alpha, beta, slice_off, ell_col, ell_val, diag, xa, xb, part, atau, mu, phase, rec, total;
+    size_t coef, red, cred, alpha, beta, slice_off, ell_col, ell_val, diag, xa, xb, part, atau, mu, phase, rec, tco, tacc,
+        total;
     __host__ __device__ static size_t align(size_t x) { return (x + 15) & ~size_t(15); }
     // n_pad: replicated vector length; nslices / ell_len: the slices and ELL
     // entries one CTA owns (all of them without a cluster)
-    __host__ __device__ SmemLayout(int n_pad, int nslices, int ell_len, int Kmax, int M, int nthreads, int nchan = 1) {
+    // traj_m > 1: trajectory outputs with chunks of traj_m steps (coefficients
+    // and accumulators of the traj_m - 1 states inside a chunk)
+    __host__ __device__ SmemLayout(int n_pad, int nslices, int ell_len, int Kmax, int M, int nthreads, int nchan = 1,
+                                   int traj_m = 1) {
         size_t o = 0;
         coef = o; o = align(o + sizeof(double) * kMaxCoef);
         red = o; o = align(o + sizeof(double) * kRedSlots);
@@ -515,6 +519,9 @@ struct SmemLayout {
         mu = o; o = align(o + sizeof(typename P::Vec) * Kmax * nchan);
         phase = o; o = align(o + sizeof(typename P::Vec) * (M + 1));
         rec = o; o = align(o + sizeof(typename P::Vec) * (nthreads > M ? nthreads : M));
+        const size_t tm1 = traj_m > 1 ? (size_t)(traj_m - 1) : 0;
+        tco = o; o = align(o + sizeof(typename P::Vec) * tm1 * Kmax);
+        tacc = o; o = align(o + sizeof(typename P::Vec) * tm1 * 32 * (size_t)nslices);
         total = o;
     }
 };
@@ -631,13 +638,37 @@ static __device__ __noinline__ void coil_moments(const Vec *x, int ncoil, const 
     }
 }
 
+// Trajectory outputs with chunks of m steps (evolution.m 'trajectory'): the
+// state j steps into a chunk is sum_k c_k(j) t_k, accumulated for j = 1..m-1
+// as acc[(j-1) * stride] (+)= c[j-1] * t (c: term k's m-1 coefficients).  Out
+// of line, so the term loop of the other runs keeps its size.
+template <class Vec>
+static __device__ __noinline__ void traj_accumulate(Vec *acc, int stride, const Vec *c, int m1, Vec t, bool init) {
+    for (int j = 0; j < m1; ++j) {
+        const Vec cj = c[j];
+        Vec p;
+        p.x = cj.x * t.x - cj.y * t.y;
+        p.y = cj.x * t.y + cj.y * t.x;
+        Vec &a = acc[(size_t)j * stride];
+        if (init) {
+            a = p;
+        } else {
+            a.x += p.x;
+            a.y += p.y;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // The propagation kernel
 // ---------------------------------------------------------------------------
 // SC: the coil has at most 32 non-zeros (sys.ncoil > 0), read by one warp per
 // term; the dense-coil projection is compiled out, which keeps the term loop
 // small (6 % on c1).
-template <bool F64, bool CPLX, int RMAX, bool CLU, bool SC>
+// TRJ: trajectory outputs (the state at every step, run.traj_out); compiled
+// into separate instantiations so that the other runs' term loop keeps its
+// registers (the out-of-line accumulation calls cost c1 5 % when present).
+template <bool F64, bool CPLX, int RMAX, bool CLU, bool SC, bool TRJ>
 __global__ void __launch_bounds__(512)
 powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     using P = Prec<F64, CPLX>;
@@ -650,7 +681,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 
     extern __shared__ __align__(16) unsigned char smem[];
     const SmemLayout<F64, CPLX> L(sys.n_pad, CLU ? run.nsl_loc : sys.nslices, CLU ? run.ell_loc : sys.ell_len,
-                                  run.Kmax, run.M, blockDim.x, sys.nchan);
+                                  run.Kmax, run.M, blockDim.x, sys.nchan, TRJ ? run.traj_m : 1);
     double *s_coef = reinterpret_cast<double *>(smem + L.coef);
     double *s_red = reinterpret_cast<double *>(smem + L.red);
     double *s_cred = reinterpret_cast<double *>(smem + L.cred);
@@ -667,6 +698,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     Vec *s_mu = reinterpret_cast<Vec *>(smem + L.mu);
     Vec *s_phase = reinterpret_cast<Vec *>(smem + L.phase);
     Vec *s_rec = reinterpret_cast<Vec *>(smem + L.rec);
+    Vec *s_tco = reinterpret_cast<Vec *>(smem + L.tco);      // trajectory: [k][j-1] coefficients
+    Vec *s_tacc = reinterpret_cast<Vec *>(smem + L.tacc);    // trajectory: [j-1][local row] states
     __shared__ double s_scalar[8];
     __shared__ int s_int[4];
     __shared__ int s_crow[32];
@@ -997,6 +1030,22 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 s_phase[j] = tovec(make_double2(cos(ph), sin(ph)), Vec());
             }
         }
+        // trajectory outputs: coefficients of the states 1 .. Mo-1 steps into a chunk
+        const int TM1 = TRJ ? Mo - 1 : 0;
+        for (int q = tid; q < TM1 * K; q += blockDim.x) {
+            const int k = q / TM1, j = 1 + q % TM1;
+            const double tau = j * run.dt;
+            const double pr = cos(-cen * tau), pi_ = sin(-cen * tau);
+            const double jv = table[(size_t)k * (Mo + 1) + j];
+            double re, im;
+            switch (k & 3) {
+                case 0: re = pr; im = pi_; break;
+                case 1: re = pi_; im = -pr; break;
+                case 2: re = -pr; im = -pi_; break;
+                default: re = -pi_; im = pr; break;
+            }
+            s_tco[q] = tovec(make_double2(re * jv, im * jv), Vec());
+        }
         csync<CLU>();             // coefficients and phases visible before the first term
         int K_last = s_int[3];
         if constexpr (CLU) K_last = ld_cluster_s32(cluster_addr(smem_u32(&s_int[3]), 0));
@@ -1049,7 +1098,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             // its own length j_last, from the same Bessel table
             const bool advance = !last || run.state_out != nullptr;
             const int Kc = last ? K_last : K;              // terms of this chunk
-            if (run.traj_out) {
+            if (TRJ) {
                 // trajectory output ('trajectory' of evolution.m): the state entering chunk a
                 double2 *tr = run.traj_out + ((size_t)o * (nsteps + 1) + (size_t)a * Mo) * sys.n_pad;
 #pragma unroll
@@ -1093,6 +1142,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                         if (!scoil) cdot_acc(mom, cc[r], t_cur[r]);
                         acc[r] = vzero<Vec>();
                         acc_add64(acc[r], s_atau[0], t_cur[r]);
+                        if (TRJ && TM1 > 0) traj_accumulate(s_tacc + (r_row[r] - row0), nrow_loc, s_tco, TM1, t_cur[r], true);
                         start_n2 += t_cur[r].x * t_cur[r].x + t_cur[r].y * t_cur[r].y;
                         t_prev[r] = vzero<Vec>();
                     }
@@ -1145,6 +1195,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                             push_peers<CLU>(&dst[r_row[r]], tn, crank, CL);
                             if (!scoil) cdot_acc(mom, cc[r], tn);
                             if (advance) acc_add64(acc[r], s_atau[k], tn);
+                            if (TRJ && TM1 > 0) traj_accumulate(s_tacc + (r_row[r] - row0), nrow_loc, s_tco + k * TM1, TM1, tn, false);
                         }
                     }
                     if (!scoil) {
@@ -1178,6 +1229,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                             MOM = fma2(cim[r], swap2(T), MOM);
                         }
                         ac[r] = cmul_pk(s_atau[0], T);
+                        if (TRJ && TM1 > 0) traj_accumulate(s_tacc + (r_row[r] - row0), nrow_loc, s_tco, TM1, f2up(T), true);
                         cp[r] = 0ull;
                         tp[r] = 0ull;
                         const float2 t = f2up(T);
@@ -1262,6 +1314,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                                 cp[r] = sub2(sub2(S, ac[r]), Yk);
                                 ac[r] = S;
                             }
+                            if (TRJ && TM1 > 0)
+                                traj_accumulate(s_tacc + (r_row[r] - row0), nrow_loc, s_tco + k * TM1, TM1, f2up(T), false);
                         }
                     }
                     if (!scoil) {
@@ -1276,6 +1330,20 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                         if (advance) tc[r] = ac[r];
                         const float2 t = f2up(tc[r]);
                         end_n2 += (double)t.x * t.x + (double)t.y * t.y;
+                    }
+                }
+            }
+            if (TRJ && TM1 > 0) {
+                // the states 1 .. Mo-1 steps into this chunk (up to the last step)
+                const int jn = min(TM1, nsteps - a * Mo);
+#pragma unroll
+                for (int r = 0; r < RMAX; ++r) {
+                    if (r < nr) {
+                        for (int j = 1; j <= jn; ++j) {
+                            const Vec v = s_tacc[(size_t)(j - 1) * nrow_loc + (r_row[r] - row0)];
+                            run.traj_out[((size_t)o * (nsteps + 1) + (size_t)a * Mo + j) * sys.n_pad + r_row[r]] =
+                                make_double2((double)v.x, (double)v.y);
+                        }
                     }
                 }
             }
