@@ -228,6 +228,31 @@ spx_status spx_surrogate_set_params(spx_surrogate *s, const float *h_params);
 const char *spx_surrogate_last_error(const spx_surrogate *s);
 
 /*
+ * Pulse programs on the evolution core.  A program is a list of operations:
+ *   SPX_SEQ_PULSE   state <- exp(-1i*angle*pulse_ops[pulse]) state
+ *                   (kernel/step.m with a commutation superoperator)
+ *   SPX_SEQ_EVOLVE  nsteps steps of dt under the orientation's Liouvillian
+ *                   (kernel/evolution.m); record != 0 appends the powder FID
+ *                   coil'*rho at steps 0..nsteps to fid
+ * Every orientation starts from rho0; fid receives sum over recorded
+ * segments of (nsteps+1) complex values.  Needs one coil and the single rho0.
+ */
+enum { SPX_SEQ_PULSE = 0, SPX_SEQ_EVOLVE = 1 };
+typedef struct spx_seq_op {
+    int32_t kind;       /* SPX_SEQ_PULSE or SPX_SEQ_EVOLVE */
+    int32_t pulse;      /* PULSE: index into pulse_ops */
+    double angle;       /* PULSE: rotation angle (rad) */
+    int64_t nsteps;     /* EVOLVE: number of steps */
+    double dt;          /* EVOLVE: time step (s) */
+    int32_t record;     /* EVOLVE: append this segment's FID */
+    int32_t reserved;
+} spx_seq_op;
+
+spx_status spx_run_sequence(spx_handle *handle, int64_t n_orient, const double *alphas, const double *betas,
+                            const double *gammas, const double *weights, int32_t n_pulse, const spx_csc *pulse_ops,
+                            int32_t n_ops, const spx_seq_op *ops, const spx_options *opt, double *fid);
+
+/*
  * CPMG echo train on the same evolution core (experiments/cpmg.m): a hard
  * 90-degree pulse exp(-1i*(pi/2)*pulse_op) on rho0, npoints-1 steps of
  * acquisition, then nloops times a 180-degree pulse and 2*npoints-1 steps;

@@ -858,6 +858,21 @@ def cpmg(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
     return np.concatenate(fid)
 
 
+def hp_acquire(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
+    """experiments/hp_acquire.m (K = 0, no decoupling): pulse_op by
+    pulse_angle; if echo_time is given, echo_time of evolution ('final', one
+    step), echo_oper by echo_angle, echo_time again; then the observable of
+    npoints-1 steps of 1/sweep."""
+    L = H + 1j * R
+    rho = step(ss, parameters['pulse_op'], parameters['rho0'], parameters['pulse_angle'])
+    if 'echo_time' in parameters:
+        rho = evolution_trajectory(ss, L, rho, parameters['echo_time'], 1)[:, -1]
+        rho = step(ss, parameters['echo_oper'], rho, parameters['echo_angle'])
+        rho = evolution_trajectory(ss, L, rho, parameters['echo_time'], 1)[:, -1]
+    return evolution_observable(ss, L, parameters['coil'], rho, 1.0 / parameters['sweep'],
+                                parameters['npoints'] - 1)
+
+
 def evolution_refocus(ss: SpinSystem, stack, L, dt: float) -> np.ndarray:
     """kernel/evolution.m:402-470 ('refocus', one subspace): column n of the
     stack is propagated n steps; propagator below krylov_tol, else the stack
@@ -988,6 +1003,14 @@ def singlerot_orientation_fid(ss, I, Q, parameters, angles) -> np.ndarray:
     par = dict(parameters, rho0=np.kron(space, parameters['rho0']),
                coil=np.kron(np.ones(N), parameters['coil']))
     return acquire(ss, par, G, R)
+
+
+def powder_orientation_hp_acquire(ss, I, Q, parameters, angles) -> np.ndarray:
+    """One iteration of kernel/contexts/powder.m:226-274 with @hp_acquire."""
+    A = orientation(Q, angles)
+    H = I if A is None else I + A
+    H = (H + H.conj().T) / 2
+    return hp_acquire(ss, parameters, H, relaxation(ss))
 
 
 def powder_orientation_eseem(ss, I, Q, parameters, angles) -> np.ndarray:

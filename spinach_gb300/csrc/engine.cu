@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <tuple>
 #include <new>
@@ -71,6 +72,13 @@ struct Cplx {
     double re = 0.0, im = 0.0;
 };
 
+// A pulse superoperator as CSR rows in the sliced order, with its 1-norm.
+struct PulseOp {
+    DevBuf<int> ptr, col;
+    DevBuf<double2> val;
+    double norm1 = 0.0;
+};
+
 }  // namespace
 
 struct spx_handle {
@@ -98,9 +106,7 @@ struct spx_handle {
     int nchan = 1;                  // detection channels
     DevBuf<double2> d_rho0s;        // per-orientation initial states (sliced order)
     DevBuf<double2> d_seq[2], d_seq_rho;   // pulse sequences: states between segments
-    DevBuf<int> d_pulse_ptr, d_pulse_col;  // pulse superoperator, CSR in sliced order
-    DevBuf<double2> d_pulse_val;
-    double pulse_norm1 = 0.0;
+    std::vector<std::unique_ptr<PulseOp>> pulses;   // pulse superoperators of the last sequence
     DevBuf<double> d_neg_re, d_neg_im;     // echo detection: the adjoint generator's streams
     DevBuf<double2> d_neg_diag;
     DevBuf<double2> d_traj[2], d_echo_f;   // forward / adjoint trajectories, per-orientation echoes
@@ -965,7 +971,7 @@ __global__ void pulse_kernel(int n_states, int n_pad, const int *__restrict__ pt
 
 // Upload a pulse superoperator (CSC, the caller's basis order) as CSR rows in
 // the sliced order of the uploaded system.
-void upload_pulse(spx_handle *h, const spx_csc *P) {
+void upload_pulse(spx_handle *h, const spx_csc *P, PulseOp &op) {
     check_csc(P, h->n, "pulse_op");
     const int n_pad = h->n_pad;
     std::vector<std::vector<std::pair<int, double2>>> rows(n_pad);
@@ -983,14 +989,15 @@ void upload_pulse(spx_handle *h, const spx_csc *P) {
     }
     if (col.empty()) { col.push_back(0); val.push_back(make_double2(0, 0)); }
     SPX_CUDA(cudaSetDevice(h->device));
-    h->d_pulse_ptr.upload(ptr, h->stream);
-    h->d_pulse_col.upload(col, h->stream);
-    h->d_pulse_val.upload(val, h->stream);
-    h->pulse_norm1 = colsum.empty() ? 0.0 : *std::max_element(colsum.begin(), colsum.end());
+    op.ptr.upload(ptr, h->stream);
+    op.col.upload(col, h->stream);
+    op.val.upload(val, h->stream);
+    op.norm1 = colsum.empty() ? 0.0 : *std::max_element(colsum.begin(), colsum.end());
 }
 
-void apply_pulse(spx_handle *h, double theta, int64_t n_states, double2 *states) {
-    const double x = h->pulse_norm1 * std::fabs(theta);
+// exp(-1i * theta * P) on n_states states of n_pad entries (sliced order).
+void apply_pulse(spx_handle *h, const PulseOp &op, double theta, int64_t n_states, double2 *states) {
+    const double x = op.norm1 * std::fabs(theta);
     const int nsub = std::max(1, (int)std::ceil(x));
     const int nterms = 25;                     // 1 / 25! < 1e-25 per substep
     const size_t smem = 3 * (size_t)h->n_pad * sizeof(double2);
@@ -998,24 +1005,18 @@ void apply_pulse(spx_handle *h, double theta, int64_t n_states, double2 *states)
     SPX_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void *>(&pulse_kernel),
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = (int)std::min<int64_t>(n_states, (int64_t)h->sm_count * 2);
-    pulse_kernel<<<grid, 256, smem, h->stream>>>((int)n_states, h->n_pad, h->d_pulse_ptr.p, h->d_pulse_col.p,
-                                                 h->d_pulse_val.p, theta / nsub, nsub, nterms, states);
+    pulse_kernel<<<grid, 256, smem, h->stream>>>((int)n_states, h->n_pad, op.ptr.p, op.col.p, op.val.p, theta / nsub,
+                                                 nsub, nterms, states);
     SPX_CUDA(cudaGetLastError());
 }
 
-// experiments/cpmg.m: a 90-degree pulse, npoints-1 steps of acquisition, then
-// nloops times (180-degree pulse, 2*npoints-1 steps), the FIDs concatenated
-// (npoints + 2*npoints*nloops points).  Each segment is one powder run that
-// starts from the previous segment's final states.
-void run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
-              const double *weights, double dt, int64_t npoints, int32_t nloops, const spx_csc *pulse_op,
-              const spx_options &o, double *fid) {
-    if (h->nchan != 1 || h->n_states != 0)
-        throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil and one initial state");
-    // experiments/cpmg.m:77-90: both positive integers
-    if (npoints < 1 || nloops < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "npoints and nloops must be positive");
-    validate_run(h, n_orient, dt, 2 * npoints);
-    upload_pulse(h, pulse_op);
+// A pulse program on the evolution core: hard pulses exp(-1i*angle*P) and
+// evolution segments, each segment one powder run that starts from the
+// previous segment's final states (per orientation; before the first segment
+// the pulses act on the single rho0).  Recorded segments append their powder
+// FID (nsteps+1 points) to fid.
+void upload_grid(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
+                 const double *weights) {
     h->d_grid.reserve(4 * (size_t)n_orient);
     double *g = h->d_grid.p;
     const size_t b = (size_t)n_orient * sizeof(double);
@@ -1023,35 +1024,102 @@ void run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, const doubl
     SPX_CUDA(cudaMemcpyAsync(g + n_orient, betas, b, cudaMemcpyHostToDevice, h->stream));
     SPX_CUDA(cudaMemcpyAsync(g + 2 * n_orient, gammas, b, cudaMemcpyHostToDevice, h->stream));
     SPX_CUDA(cudaMemcpyAsync(g + 3 * n_orient, weights, b, cudaMemcpyHostToDevice, h->stream));
+}
+
+void run_sequence(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
+                  const double *weights, int32_t n_pulse, const spx_csc *pulse_ops, int32_t n_ops,
+                  const spx_seq_op *ops, const spx_options &o, double *fid) {
+    if (h->nchan != 1 || h->n_states != 0)
+        throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil and one initial state");
+    if (n_pulse < 0 || n_ops < 0 || (n_pulse > 0 && !pulse_ops) || (n_ops > 0 && !ops))
+        throw SpxError(SPX_ERR_INVALID_ARGUMENT, "bad pulse or operation arrays");
+    int64_t max_steps = 0;
+    for (int i = 0; i < n_ops; ++i) {
+        const spx_seq_op &q = ops[i];
+        if (q.kind == SPX_SEQ_PULSE) {
+            if (q.pulse < 0 || q.pulse >= n_pulse) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "pulse index out of range");
+            if (!std::isfinite(q.angle)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite pulse angle");
+        } else if (q.kind == SPX_SEQ_EVOLVE) {
+            validate_run(h, n_orient, q.dt, q.nsteps);
+            max_steps = std::max(max_steps, q.nsteps);
+        } else {
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown sequence operation");
+        }
+    }
+    if (n_orient < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "bad orientation count");
+    h->pulses.clear();
+    for (int k = 0; k < n_pulse; ++k) {
+        h->pulses.push_back(std::make_unique<PulseOp>());
+        upload_pulse(h, &pulse_ops[k], *h->pulses.back());
+    }
+    upload_grid(h, n_orient, alphas, betas, gammas, weights);
+    double *g = h->d_grid.p;
     const size_t ns = (size_t)n_orient * h->n_pad;
     h->d_seq[0].reserve(ns);
     h->d_seq[1].reserve(ns);
     h->d_seq_rho.reserve(h->n_pad);
-    h->d_fid.reserve(2 * (size_t)npoints);
-    // the first pulse acts on the orientation-independent rho0
+    h->d_fid.reserve((size_t)max_steps + 1);
     SPX_CUDA(cudaMemcpyAsync(h->d_seq_rho.p, h->d_rho0.p, h->n_pad * sizeof(double2), cudaMemcpyDeviceToDevice,
                              h->stream));
-    apply_pulse(h, M_PI / 2, 1, h->d_seq_rho.p);
-    size_t at = 0;
+    bool per_orient = false;        // states differ per orientation after the first segment
     int cur = 0;
-    for (int seg = 0; seg <= nloops; ++seg) {
-        const int64_t nsteps = seg == 0 ? npoints - 1 : 2 * npoints - 1;
-        RunIO io;
-        if (seg == 0) {
-            io.rho0 = h->d_seq_rho.p;
-        } else {
-            apply_pulse(h, M_PI, n_orient, h->d_seq[cur].p);
-            io.rho0s = h->d_seq[cur].p;
+    size_t at = 0;
+    for (int i = 0; i < n_ops; ++i) {
+        const spx_seq_op &q = ops[i];
+        if (q.kind == SPX_SEQ_PULSE) {
+            if (per_orient) apply_pulse(h, *h->pulses[q.pulse], q.angle, n_orient, h->d_seq[cur].p);
+            else apply_pulse(h, *h->pulses[q.pulse], q.angle, 1, h->d_seq_rho.p);
+            continue;
         }
+        RunIO io;
+        if (per_orient) io.rho0s = h->d_seq[cur].p;
+        else io.rho0 = h->d_seq_rho.p;
         io.state_out = h->d_seq[cur ^ 1].p;
-        const Config c = choose_config(h, n_orient, dt, nsteps, o, 0);
-        launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o, h->d_fid.p, c,
-                      0, true, io);
+        const Config c = choose_config(h, n_orient, q.dt, q.nsteps, o, 0);
+        launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, q.dt, q.nsteps, o, h->d_fid.p,
+                      c, 0, true, io);
         finish_run(h);
-        SPX_CUDA(cudaMemcpy(fid + 2 * at, h->d_fid.p, ((size_t)nsteps + 1) * sizeof(double2), cudaMemcpyDeviceToHost));
-        at += (size_t)nsteps + 1;
+        if (q.record) {
+            SPX_CUDA(cudaMemcpy(fid + 2 * at, h->d_fid.p, ((size_t)q.nsteps + 1) * sizeof(double2),
+                                cudaMemcpyDeviceToHost));
+            at += (size_t)q.nsteps + 1;
+        }
         cur ^= 1;
+        per_orient = true;
     }
+}
+
+// experiments/cpmg.m: a 90-degree pulse, npoints-1 steps of acquisition, then
+// nloops times (180-degree pulse, 2*npoints-1 steps), the FIDs concatenated
+// (npoints + 2*npoints*nloops points).
+void run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
+              const double *weights, double dt, int64_t npoints, int32_t nloops, const spx_csc *pulse_op,
+              const spx_options &o, double *fid) {
+    // experiments/cpmg.m:77-90: both positive integers
+    if (npoints < 1 || nloops < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "npoints and nloops must be positive");
+    std::vector<spx_seq_op> prog;
+    auto pulse = [&](double angle) {
+        spx_seq_op q{};
+        q.kind = SPX_SEQ_PULSE;
+        q.pulse = 0;
+        q.angle = angle;
+        prog.push_back(q);
+    };
+    auto evolve = [&](int64_t nsteps) {
+        spx_seq_op q{};
+        q.kind = SPX_SEQ_EVOLVE;
+        q.nsteps = nsteps;
+        q.dt = dt;
+        q.record = 1;
+        prog.push_back(q);
+    };
+    pulse(M_PI / 2);
+    evolve(npoints - 1);
+    for (int n = 0; n < nloops; ++n) {
+        pulse(M_PI);
+        evolve(2 * npoints - 1);
+    }
+    run_sequence(h, n_orient, alphas, betas, gammas, weights, 1, pulse_op, (int32_t)prog.size(), prog.data(), o, fid);
 }
 
 // Echo detection (experiments/esr_dipolar/eseem.m): the stack of half-echo
@@ -1139,19 +1207,17 @@ void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const doub
     validate_run(h, n_orient, tau, nsteps);
     const int n_pad = h->n_pad;
     if (n_pad > 8192) throw SpxError(SPX_ERR_UNSUPPORTED, "echo detection is limited to dimension 8192");
-    upload_pulse(h, pulse_op);
-    h->d_grid.reserve(4 * (size_t)n_orient);
+    h->pulses.clear();
+    h->pulses.push_back(std::make_unique<PulseOp>());
+    const PulseOp &P = *h->pulses.back();
+    upload_pulse(h, pulse_op, *h->pulses.back());
+    upload_grid(h, n_orient, alphas, betas, gammas, weights);
     double *g = h->d_grid.p;
-    const size_t b = (size_t)n_orient * sizeof(double);
-    SPX_CUDA(cudaMemcpyAsync(g, alphas, b, cudaMemcpyHostToDevice, h->stream));
-    SPX_CUDA(cudaMemcpyAsync(g + n_orient, betas, b, cudaMemcpyHostToDevice, h->stream));
-    SPX_CUDA(cudaMemcpyAsync(g + 2 * n_orient, gammas, b, cudaMemcpyHostToDevice, h->stream));
-    SPX_CUDA(cudaMemcpyAsync(g + 3 * n_orient, weights, b, cudaMemcpyHostToDevice, h->stream));
     // rho1 = exp(-1i pi/2 P) rho0
     h->d_seq_rho.reserve(n_pad);
     SPX_CUDA(cudaMemcpyAsync(h->d_seq_rho.p, h->d_rho0.p, n_pad * sizeof(double2), cudaMemcpyDeviceToDevice,
                              h->stream));
-    apply_pulse(h, M_PI / 2, 1, h->d_seq_rho.p);
+    apply_pulse(h, P, M_PI / 2, 1, h->d_seq_rho.p);
     // Pi = exp(-1i pi P) column by column, kept as CSR (entries above 1e-15;
     // Pi is unitary, so they are at most 1)
     {
@@ -1159,7 +1225,7 @@ void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const doub
         dense.reserve((size_t)n_pad * n_pad);
         identity_kernel<<<h->sm_count * 4, 256, 0, h->stream>>>(n_pad, dense.p);
         SPX_CUDA(cudaGetLastError());
-        apply_pulse(h, M_PI, n_pad, dense.p);
+        apply_pulse(h, P, M_PI, n_pad, dense.p);
         std::vector<double2> hd((size_t)n_pad * n_pad);
         SPX_CUDA(cudaMemcpyAsync(hd.data(), dense.p, hd.size() * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
         SPX_CUDA(cudaStreamSynchronize(h->stream));
@@ -1677,6 +1743,26 @@ spx_status spx_run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, c
         o = apply_tuned(h, o);
         SPX_CUDA(cudaSetDevice(h->device));
         run_cpmg(h, n_orient, alphas, betas, gammas, weights, dt, npoints, nloops, pulse_op, o, fid);
+    });
+}
+
+spx_status spx_run_sequence(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
+                            const double *gammas, const double *weights, int32_t n_pulse, const spx_csc *pulse_ops,
+                            int32_t n_ops, const spx_seq_op *ops, const spx_options *opt, double *fid) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (!alphas || !betas || !gammas || !weights || !fid) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL argument");
+        for (int64_t o = 0; o < n_orient; ++o)
+            if (!std::isfinite(alphas[o]) || !std::isfinite(betas[o]) || !std::isfinite(gammas[o]) ||
+                !std::isfinite(weights[o]))
+                throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite grid entry");
+        spx_options o{};
+        if (opt) o = *opt;
+        if (o.precision != SPX_FP32 && o.precision != SPX_FP64)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
+        o = apply_tuned(h, o);
+        SPX_CUDA(cudaSetDevice(h->device));
+        run_sequence(h, n_orient, alphas, betas, gammas, weights, n_pulse, pulse_ops, n_ops, ops, o, fid);
     });
 }
 

@@ -29,6 +29,14 @@ class SpxOptions(C.Structure):
                 ('lanczos_its', C.c_int32), ('reserved', C.c_int32)]
 
 
+SEQ_PULSE, SEQ_EVOLVE = 0, 1
+
+
+class SpxSeqOp(C.Structure):
+    _fields_ = [('kind', C.c_int32), ('pulse', C.c_int32), ('angle', C.c_double), ('nsteps', C.c_int64),
+                ('dt', C.c_double), ('record', C.c_int32), ('reserved', C.c_int32)]
+
+
 class SpxStats(C.Structure):
     _fields_ = [('n_orientations', C.c_int64), ('nsteps', C.c_int64), ('matvecs', C.c_int64),
                 ('orientations_failed', C.c_int64), ('chunk_steps', C.c_int32),
@@ -65,6 +73,8 @@ SIGNATURES = {
                                    C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_int32), C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_int32), _D, _D, _D, _D, _D]),
+    'spx_run_sequence': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_int32, C.POINTER(SpxCsc), C.c_int32,
+                                   C.POINTER(SpxSeqOp), C.POINTER(SpxOptions), _D]),
     'spx_run_eseem': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.POINTER(SpxCsc),
                                 C.POINTER(SpxOptions), _D]),
     'spx_upload_coils': (C.c_int, [_P, C.c_int32, _D]),
@@ -283,6 +293,36 @@ class Engine:
                                           int(npoints), int(nloops), C.byref(P.struct), C.byref(opt), _dptr(fid)),
                     self.h)
         return PowderResult(fid.view(np.complex128), None, self.stats())
+
+    def run_sequence(self, alphas, betas, gammas, weights, pulse_ops, program, precision: int = FP32,
+                     threads: int = 0, cluster: int = 0) -> PowderResult:
+        """A pulse program (spx_run_sequence): ``pulse_ops`` a list of
+        commutation superoperators, ``program`` a list of ``('pulse', index,
+        angle)`` and ``('evolve', nsteps, dt[, record])`` entries.  ``fid`` is
+        the concatenation of the recorded segments' powder FIDs."""
+        al = np.ascontiguousarray(alphas, np.float64)
+        be = np.ascontiguousarray(betas, np.float64)
+        ga = np.ascontiguousarray(gammas, np.float64)
+        w = np.ascontiguousarray(weights, np.float64)
+        holders = [_CscHolder(P, self.dim) for P in pulse_ops]
+        parr = (SpxCsc * max(1, len(holders)))(*[hd.struct for hd in holders])
+        ops = []
+        npts = 0
+        for op in program:
+            if op[0] == 'pulse':
+                ops.append(SpxSeqOp(SEQ_PULSE, int(op[1]), float(op[2]), 0, 0.0, 0, 0))
+            elif op[0] == 'evolve':
+                rec = 1 if (len(op) < 4 or op[3]) else 0
+                ops.append(SpxSeqOp(SEQ_EVOLVE, 0, 0.0, int(op[1]), float(op[2]), rec, 0))
+                npts += (int(op[1]) + 1) if rec else 0
+            else:
+                raise ValueError(f'unknown program entry {op[0]!r}')
+        oarr = (SpxSeqOp * max(1, len(ops)))(*ops)
+        fid = np.zeros(2 * max(npts, 1))
+        opt = SpxOptions(precision, 0, threads, cluster, 0.0, 0.0, 0, 0)
+        self._check(self.lib.spx_run_sequence(self.h, al.size, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
+                                              len(holders), parr, len(ops), oarr, C.byref(opt), _dptr(fid)), self.h)
+        return PowderResult(fid.view(np.complex128)[:npts], None, self.stats())
 
     def run_eseem(self, alphas, betas, gammas, weights, timestep: float, npoints: int, pulse_op,
                   precision: int = FP32, threads: int = 0, cluster: int = 0) -> PowderResult:

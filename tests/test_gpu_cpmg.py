@@ -85,3 +85,37 @@ def test_cpmg_argument_checks(gpu_engine):
     plain = gpu_engine.run(*g, w.dt, 46, precision=E.FP64)
     assert np.abs(plain.fid).max() > 0.05
     assert rel_err(pre.fid, plain.fid[list(range(16)) + list(range(15, 47))]) <= 1e-13
+
+
+@pytest.mark.parametrize('wname,spin', [('c0', '13C'), ('c4_small', 'E')])
+def test_hp_acquire_echo_program_matches_oracle(gpu_engine, wname, spin):
+    """experiments/hp_acquire.m with an echo (pulse, echo_time, echo pulse,
+    echo_time, acquisition) as a pulse program."""
+    from spinach_gb300 import spin_system as S
+    w = getattr(W, wname)()
+    L = W.build(w)
+    ss_b = W.spin_system_of(w)
+    fac = S.factory_for(ss_b, S.build_basis(ss_b, w.approximation, w.level))
+    ss, I, Q = oracle_system(w, krylov=(wname != 'c0'))
+    spins = [i for i, iso in enumerate(w.isotopes) if iso == spin]
+    Py = sum(fac.operator([('Ly', s)]) for s in spins)
+    Px = sum(fac.operator([('Lx', s)]) for s in spins)
+    echo = 37 * w.dt
+    npoints = 64
+    par = dict(rho0=R.state(ss, 'Lz', spin), coil=R.state(ss, 'L+', spin), pulse_op=R.operator(ss, 'Ly', spin),
+               pulse_angle=np.pi / 2, echo_time=echo, echo_oper=R.operator(ss, 'Lx', spin), echo_angle=np.pi,
+               sweep=1 / w.dt, npoints=npoints)
+    g = W.zcwn_grid(6)
+    g = (g[0], g[1], g[2], np.linspace(0.1, 0.3, 6))
+    ref = sum(g[3][i] * R.powder_orientation_hp_acquire(ss, I, Q, par, (g[0][i], g[1][i], g[2][i]))
+              for i in range(6))
+    assert np.abs(ref).max() > 0.05
+    gpu_engine.upload(L.I, L.terms, L.R, fac.state('Lz', spin), fac.state('L+', spin))
+    prog = [('pulse', 0, np.pi / 2), ('evolve', 1, echo, False), ('pulse', 1, np.pi), ('evolve', 1, echo, False),
+            ('evolve', npoints - 1, w.dt)]
+    for prec, tol in ((E.FP64, 1e-10), (E.FP32, 1e-5)):
+        res = gpu_engine.run_sequence(*g, [Py, Px], prog, precision=prec)
+        assert res.fid.shape == (npoints,)
+        assert rel_err(res.fid, ref) <= tol, prec
+    with pytest.raises(E.SpxError):                          # pulse index out of range
+        gpu_engine.run_sequence(*g, [Py], prog)
