@@ -18,7 +18,11 @@
 //          instead of acquire.m: npoints = nsteps+1 per half-echo, fid
 //          npoints*(1+2*nloops) x 1; pulse_op and sequence = 'eseem' run
 //          experiments/esr_dipolar/eseem.m with timestep = dt and
-//          npoints = nsteps+1 (fid (nsteps+1) x 1).
+//          npoints = nsteps+1 (fid (nsteps+1) x 1); pulse_ops (cell of
+//          sparse dim x dim) and program (n x 6: kind 0 = pulse / 1 =
+//          evolution, pulse index (1-based), angle, nsteps, dt, record) run a
+//          pulse program (dt and nsteps of the call are then unused; fid the
+//          recorded segments' FIDs, concatenated).
 // fid      (nsteps+1) x 1 complex: sum_n weights(n) fid_n (powder.m:280-287).
 // fids     (nsteps+1) x n_orient complex, the sum_up=false output (powder.m:291-297).
 //
@@ -198,7 +202,43 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     CscCopy pulse;
     int32_t nloops = 0;                 // > 0: a CPMG echo train (experiments/cpmg.m)
     bool eseem = false;                 // a two-pulse echo (experiments/esr_dipolar/eseem.m)
-    if (nrhs == 9) {
+    std::vector<CscCopy> prog_pulses;   // a pulse program: its operators and operations
+    std::vector<spx_seq_op> prog;
+    bool program = false;
+    if (nrhs == 9 && mxGetField(prhs[8], 0, "program")) {
+        program = true;
+        const mxArray *pg = mxGetField(prhs[8], 0, "program");
+        const mxArray *pc = mxGetField(prhs[8], 0, "pulse_ops");
+        if (!mxIsDouble(pg) || mxIsComplex(pg) || mxIsSparse(pg) || mxGetN(pg) != 6)
+            throw GatewayError{"Spinach:spinach_powder_gpu:program", "opts.program must be a real n x 6 matrix."};
+        const size_t np = pc ? mxGetNumberOfElements(pc) : 0;
+        if (pc && !mxIsCell(pc))
+            throw GatewayError{"Spinach:spinach_powder_gpu:program", "opts.pulse_ops must be a cell array."};
+        prog_pulses.resize(np);
+        for (size_t k = 0; k < np; ++k) fill_csc(mxGetCell(pc, (mwIndex)k), n, "opts.pulse_ops", prog_pulses[k]);
+        const size_t m = mxGetM(pg);
+        const mxDouble *v = mxGetDoubles(pg);
+        for (size_t i = 0; i < m; ++i) {
+            spx_seq_op q{};
+            const double kind = v[i], idx = v[i + m], steps = v[i + 3 * m];
+            if (kind != 0.0 && kind != 1.0)
+                throw GatewayError{"Spinach:spinach_powder_gpu:program", "program kinds are 0 (pulse) and 1 (evolution)."};
+            q.kind = kind == 0.0 ? SPX_SEQ_PULSE : SPX_SEQ_EVOLVE;
+            if (q.kind == SPX_SEQ_PULSE && (idx < 1 || idx > (double)np || idx != (double)(int32_t)idx))
+                throw GatewayError{"Spinach:spinach_powder_gpu:program", "pulse index out of range."};
+            if (q.kind == SPX_SEQ_EVOLVE && (steps < 0 || steps != (double)(int64_t)steps))
+                throw GatewayError{"Spinach:spinach_powder_gpu:program", "evolution steps must be non-negative integers."};
+            q.pulse = q.kind == SPX_SEQ_PULSE ? (int32_t)idx - 1 : 0;
+            q.angle = v[i + 2 * m];
+            q.nsteps = q.kind == SPX_SEQ_EVOLVE ? (int64_t)steps : 0;
+            q.dt = v[i + 4 * m];
+            q.record = v[i + 5 * m] != 0.0;
+            prog.push_back(q);
+        }
+        if (nlhs > 1)
+            throw GatewayError{"Spinach:spinach_powder_gpu:nlhs", "a pulse program returns the powder signal only."};
+    }
+    if (nrhs == 9 && !program) {
         const mxArray *po = mxGetField(prhs[8], 0, "pulse_op");
         const mxArray *nl = mxGetField(prhs[8], 0, "nloops");
         const mxArray *sq = mxGetField(prhs[8], 0, "sequence");
@@ -227,6 +267,8 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
             if (nlhs > 1)
                 throw GatewayError{"Spinach:spinach_powder_gpu:nlhs", "a CPMG train returns the powder FID only."};
         }
+    }
+    if (nrhs == 9) {
         const mxArray *p = mxGetField(prhs[8], 0, "precision");
         if (p) {
             char buf[16] = {0};
@@ -253,6 +295,22 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     }
     if (st != SPX_OK)
         throw GatewayError{"Spinach:spinach_powder_gpu:upload", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
+    if (program) {
+        int64_t npts = 0;
+        for (const auto &q : prog)
+            if (q.kind == SPX_SEQ_EVOLVE && q.record) npts += q.nsteps + 1;
+        std::vector<spx_csc> views;
+        for (auto &c : prog_pulses) views.push_back(c.view);
+        std::vector<double> fid(2 * (size_t)std::max<int64_t>(npts, 1));
+        st = spx_run_sequence(g_handle, no, al.data(), be.data(), ga.data(), wt.data(), (int32_t)views.size(),
+                              views.data(), (int32_t)prog.size(), prog.data(), &opt, fid.data());
+        if (st != SPX_OK)
+            throw GatewayError{"Spinach:spinach_powder_gpu:run", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
+        plhs[0] = mxCreateDoubleMatrix((mwSize)npts, 1, mxCOMPLEX);
+        mxComplexDouble *out = mxGetComplexDoubles(plhs[0]);
+        for (int64_t i = 0; i < npts; ++i) { out[i].real = fid[2 * i]; out[i].imag = fid[2 * i + 1]; }
+        return;
+    }
     if (eseem) {
         std::vector<double> fid(2 * (size_t)(nsteps + 1));
         st = spx_run_eseem(g_handle, no, al.data(), be.data(), ga.data(), wt.data(), dt, nsteps + 1, &pulse.view, &opt,

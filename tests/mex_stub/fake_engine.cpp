@@ -101,6 +101,29 @@ spx_status spx_run_cpmg(spx_handle *, int64_t no, const double *, const double *
     for (int64_t i = 0; i < npoints * (1 + 2 * nloops); ++i) { fid[2 * i] = 2.0 * i; fid[2 * i + 1] = 1.0; }
     return SPX_OK;
 }
+spx_status spx_run_sequence(spx_handle *, int64_t no, const double *, const double *, const double *,
+                            const double *, int32_t n_pulse, const spx_csc *P, int32_t n_ops, const spx_seq_op *ops,
+                            const spx_options *opt, double *fid) {
+    g_rec.n_orient = no;
+    g_rec.precision = opt ? opt->precision : -1;
+    g_rec.nloops = -2;
+    g_rec.npoints = n_ops;
+    g_rec.pulse.clear();
+    for (int k = 0; k < n_pulse; ++k) g_rec.pulse.insert(g_rec.pulse.end(), P[k].values, P[k].values + 2 * P[k].colptr[P[k].n]);
+    g_rec.grid.clear();
+    int64_t npts = 0;
+    for (int i = 0; i < n_ops; ++i) {
+        g_rec.grid.push_back(ops[i].kind);
+        g_rec.grid.push_back(ops[i].pulse);
+        g_rec.grid.push_back(ops[i].angle);
+        g_rec.grid.push_back((double)ops[i].nsteps);
+        g_rec.grid.push_back(ops[i].dt);
+        g_rec.grid.push_back(ops[i].record);
+        if (ops[i].kind == SPX_SEQ_EVOLVE && ops[i].record) npts += ops[i].nsteps + 1;
+    }
+    for (int64_t i = 0; i < npts; ++i) { fid[2 * i] = 5.0 * i; fid[2 * i + 1] = 2.0; }
+    return SPX_OK;
+}
 spx_status spx_run_eseem(spx_handle *, int64_t no, const double *, const double *, const double *, const double *,
                          double dt, int64_t npoints, const spx_csc *P, const spx_options *opt, double *fid) {
     g_rec.n_orient = no;

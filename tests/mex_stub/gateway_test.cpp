@@ -185,6 +185,29 @@ int main() {
     eopt3->fields["sequence"] = str("eseem");
     const mxArray *pe3[9] = {I, Q, R, rho0, coil, grid, scalar(2e-8), scalar(7), eopt3};
     expect(1, 9, pe3, "Spinach:spinach_powder_gpu:sequence");
+    // opts.pulse_ops + opts.program: a pulse program (hp_acquire with an echo)
+    mxArray *popt = strct();
+    mxArray *pops = cell(1, 2);
+    pops->cells[0] = copt->fields["pulse_op"];
+    pops->cells[1] = sparse(n, {2}, {3}, {0.75}, {});
+    popt->fields["pulse_ops"] = pops;
+    mxArray *pg = new mxArray; pg->m = 3; pg->n = 6;
+    pg->re = {0, 1, 1,   1, 0, 0,   1.5, 0, 0,   0, 1, 9,   0, 4e-5, 1e-5,   0, 0, 1};   // column-major
+    popt->fields["program"] = pg;
+    const mxArray *pp[9] = {I, Q, R, rho0, coil, grid, scalar(1e-5), scalar(5), popt};
+    mxArray *op_[1] = {nullptr};
+    mexFunction(1, op_, 9, pp);
+    CHECK(g_rec.nloops == -2 && g_rec.npoints == 3 && g_rec.precision == 1);
+    CHECK((g_rec.grid == std::vector<double>{0, 0, 1.5, 0, 0, 0,  1, 0, 0, 1, 4e-5, 0,  1, 0, 0, 9, 1e-5, 1}));
+    CHECK(g_rec.pulse.size() == 6 && g_rec.pulse[4] == 0.75);
+    CHECK(op_[0] && op_[0]->m == 10 && op_[0]->n == 1 && op_[0]->cx[3].real == 15.0 && op_[0]->cx[3].imag == 2.0);
+    mxArray *pg2 = new mxArray; pg2->m = 1; pg2->n = 6; pg2->re = {0, 3, 1.0, 0, 0, 0};         // pulse 3 of 2
+    mxArray *popt2 = strct();
+    popt2->fields["pulse_ops"] = pops;
+    popt2->fields["program"] = pg2;
+    const mxArray *pp2[9] = {I, Q, R, rho0, coil, grid, scalar(1e-5), scalar(5), popt2};
+    expect(1, 9, pp2, "Spinach:spinach_powder_gpu:program");
+    expect(2, 9, pp, "Spinach:spinach_powder_gpu:nlhs");
     mxArray *o2[2] = {nullptr, nullptr};
     expect(2, 8, pc, "Spinach:spinach_powder_gpu:nlhs");
     (void)o2;
