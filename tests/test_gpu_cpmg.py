@@ -119,3 +119,19 @@ def test_hp_acquire_echo_program_matches_oracle(gpu_engine, wname, spin):
         assert rel_err(res.fid, ref) <= tol, prec
     with pytest.raises(E.SpxError):                          # pulse index out of range
         gpu_engine.run_sequence(*g, [Py], prog)
+
+
+def test_program_identities(gpu_engine):
+    """A zero-step segment and a zero-angle pulse leave the state alone: the
+    program's recorded segments tile the plain acquisition."""
+    w = W.c0()
+    L = W.build(w)
+    gpu_engine.upload(L.I, L.terms, L.R, L.rho0, L.coil)
+    g = W.zcwn_grid(10)
+    plain = gpu_engine.run(*g, w.dt, 40, precision=E.FP64).fid
+    P = L.I * 0 + L.terms[sorted(L.terms)[0]]              # any operator: used with angle 0
+    prog = [('evolve', 0, w.dt), ('pulse', 0, 0.0), ('evolve', 15, w.dt), ('evolve', 25, w.dt)]
+    res = gpu_engine.run_sequence(*g, [P], prog, precision=E.FP64)
+    assert res.fid.shape == (1 + 16 + 26,)
+    want = np.concatenate([plain[:1], plain[:16], plain[15:41]])
+    assert rel_err(res.fid, want) <= 1e-13
