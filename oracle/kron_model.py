@@ -50,6 +50,12 @@ class KronModel:
             H += (Z[2, 2] - ss.basefrqs[s]) * self.ops[s]['z']
         for (a, b), A in ss.coupling.items():
             Ar = Rm @ A @ Rm.T
+            if a == b:
+                # quadratic coupling L.A.L, secular part (A_zz/2)(3 Lz^2 - L^2)
+                Lz = self.ops[a]['z']
+                s_ = (self.mults[a] - 1) / 2
+                H += (Ar[2, 2] / 2) * (3 * Lz @ Lz - s_ * (s_ + 1) * np.eye(self.dim))
+                continue
             iso = np.trace(A) / 3
             Oa, Ob = self.ops[a], self.ops[b]
             zz = Oa['z'] @ Ob['z']

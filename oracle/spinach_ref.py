@@ -605,7 +605,25 @@ def hamiltonian(ss: SpinSystem):
             isov = iso if op == 'Lz' else 0.0
             irrv = irr if aniso else np.zeros(8, complex)
             rows.append((isov, ist[op], irrv, [op], [s]))
-        # quadratic couplings (NQI) are not used on this path
+        # quadratic couplings (hamiltonian.m:191-257): rank-2 operators of the
+        # spin itself, all five ('strong') or T(2,0) alone ('secular')
+        Mq = ss.coupling.get((s, s))
+        if Mq is not None and np.linalg.norm(Mq, 2) > 2 * np.pi * ss.tols['inter_cutoff']:
+            iq, lq, pq = mat2sphten(Mq)
+            if np.linalg.norm(iq) > 1e-6 * np.linalg.norm(pq) or np.linalg.norm(lq) > 1e-6 * np.linalg.norm(pq):
+                raise ValueError('quadratic couplings must be traceless and symmetric.')
+            irrq = np.concatenate([np.zeros(3, complex), pq])
+            stq = ss.coupling_strength[(s, s)]
+            if stq == 'strong':
+                qops = [('T2,+2', 3), ('T2,+1', 4), ('T2,0', 5), ('T2,-1', 6), ('T2,-2', 7)]
+            elif stq == 'secular':
+                qops = [('T2,0', 5)]
+            else:
+                raise ValueError('unknown strength specification for the quadratic coupling.')
+            for op, idx in qops:
+                istq = np.zeros(8, complex)
+                istq[idx] = 1.0
+                rows.append((0.0, istq, irrq, [op], [s]))
     cutoff = 2 * np.pi * ss.tols['inter_cutoff']
     pairs = sorted([k for k, M in ss.coupling.items() if k[0] != k[1] and np.linalg.norm(M, 2) > cutoff],
                    key=lambda ab: (ab[1], ab[0]))

@@ -162,6 +162,7 @@ def make_spin_system(isotopes, magnet, zeeman_eigs=None, zeeman_euler=None,
     tols = dict(DEFAULT_TOLS, **(tols or {}))
     n = len(isotopes)
     gam = np.array([NUCLEI[i][1] for i in isotopes])
+    mult = [NUCLEI[i][0] for i in isotopes]
     carrier = -gam * magnet
     zee = []
     for s in range(n):
@@ -205,8 +206,11 @@ def make_spin_system(isotopes, magnet, zeeman_eigs=None, zeeman_euler=None,
     for key, j in (coupling_scalar or {}).items():
         if abs(j) > tols['inter_cutoff']:
             add(key, 2 * math.pi * j * np.eye(3))
-    cpl = {k: M for k, M in cpl.items()
-           if k[0] != k[1] and np.linalg.norm(M, 2) >= 2 * math.pi * tols['inter_cutoff']}
+    # (a, a): quadratic coupling of spin a (quadrupolar or zero-field splitting)
+    cpl = {k: M for k, M in cpl.items() if np.linalg.norm(M, 2) >= 2 * math.pi * tols['inter_cutoff']}
+    for (a, b) in cpl:
+        if a == b and mult[a] < 3:
+            raise ValueError(f'spin {a} has multiplicity {mult[a]}: no quadratic coupling')
     relax = r1 is not None or r2 is not None
     r1 = np.zeros(n) if r1 is None else np.asarray(r1, float)
     r2 = np.zeros(n) if r2 is None else np.asarray(r2, float)
@@ -373,11 +377,14 @@ class OperatorFactory:
         return np.concatenate([rl, rr]), np.concatenate([cl, cr]), np.concatenate([vl, -vr])
 
     # Human-readable product operators: lists of (op, spin) with op in
-    # E, Lz, L+, L-, Lx, Ly (kernel/utilities/human2opspec.m conventions).
+    # E, Lz, L+, L-, Lx, Ly and the rank-2 tensors T2,m (kernel/utilities/
+    # human2opspec.m conventions; T(l,m) is state code l*l+l-m, coefficient 1).
     _CODE = {'E': ((0, 1.0),), 'Lz': ((2, 1.0),), 'L+': ((1, -math.sqrt(2)),),
              'L-': ((3, math.sqrt(2)),),
              'Lx': ((1, -math.sqrt(2) / 2), (3, math.sqrt(2) / 2)),
-             'Ly': ((1, -math.sqrt(2) / 2j), (3, -math.sqrt(2) / 2j))}
+             'Ly': ((1, -math.sqrt(2) / 2j), (3, -math.sqrt(2) / 2j)),
+             'T2,+2': ((4, 1.0),), 'T2,+1': ((5, 1.0),), 'T2,0': ((6, 1.0),), 'T2,-1': ((7, 1.0),),
+             'T2,-2': ((8, 1.0),)}
 
     def operator(self, ops, kind: str = 'comm') -> sp.csr_matrix:
         r, c, v = self.operator_coo(ops, kind)
@@ -524,6 +531,18 @@ def interaction_terms(ss: SpinSystem, assumptions: str):
     for (a, b), M in ss.couplings.items():
         strength = cs[(a, b)]
         j, r1, r2 = sph_components(M)
+        if a == b:
+            # quadratic coupling (hamiltonian.m:191-257): traceless symmetric,
+            # rank-2 operators of the spin itself
+            if abs(j) > 1e-6 * np.linalg.norm(r2) or np.linalg.norm(r1) > 1e-6 * np.linalg.norm(r2):
+                raise ValueError('quadratic couplings must be traceless and symmetric')
+            irr = np.concatenate([np.zeros(3, complex), r2])
+            ops = (['T2,+2', 'T2,+1', 'T2,0', 'T2,-1', 'T2,-2'] if strength == 'strong' else ['T2,0'])
+            for op in ops:
+                ist = np.zeros(8)
+                ist[3 + 2 - int(op[3:])] = 1.0
+                ani_terms.append((ist, irr, [(op, a)]))
+            continue
         if abs(j) > cut:
             if strength in ('strong', 'secular'):
                 iso_terms += [(j, [('Lz', a), ('Lz', b)]), (j / 2, [('L+', a), ('L-', b)]),

@@ -113,6 +113,35 @@ def nmr_molecule(name, n_spins, seed, approximation, level, dt, nsteps, n_orient
                     'nmr', ('Lx', '13C'), ('L+', '13C'), dt, nsteps, n_orient, seed)
 
 
+def deuterium(seed: int = 5) -> Workload:
+    """Static 2H powder pattern: a C-D group with one proton (2H at 1.09 A from
+    the 13C, the proton at 1.09 A on another bond) at 14.1 T, 2H quadratic
+    coupling with C_Q about 170 kHz and asymmetry up to 0.2 along the C-D bond,
+    13C and 2H shift tensors, dipolar couplings from the geometry; full basis
+    (dim 144), 'nmr'; Lx(2H) detected with L+(2H), 400 orientations x 1024
+    steps of 2 us."""
+    rng = np.random.default_rng(seed)
+    cd = _unit(rng)
+    ch = _unit(rng)
+    while abs(float(cd @ ch)) > 0.5:
+        ch = _unit(rng)
+    coords = [1.09 * cd, np.zeros(3), 1.09 * ch]
+    eigs, eul = [], []
+    for rng_iso in ((0, 5), (0, 200), (0, 10)):
+        e, u = _csa(rng, rng_iso)
+        eigs.append(e)
+        eul.append(u)
+    cq = rng.uniform(160e3, 180e3)
+    eta = rng.uniform(0.0, 0.2)
+    # principal axis of the quadratic coupling along the C-D bond
+    bet = math.acos(float(np.clip(cd[2], -1, 1)))
+    alp = math.atan2(float(cd[1]), float(cd[0]))
+    ceigs = {(0, 0): [-(1 - eta) * cq / 6, -(1 + eta) * cq / 6, cq / 3]}
+    ceul = {(0, 0): [alp, bet, rng.uniform(0, 2 * np.pi)]}
+    return Workload('deuterium', ['2H', '13C', '1H'], 14.1, eigs, eul, coords, ceigs, ceul, None, None, 'none', 0,
+                    'nmr', ('Lx', '2H'), ('L+', '2H'), 2e-6, 1024, 400, seed)
+
+
 def c0(seed: int = 0) -> Workload:
     return nmr_molecule('c0', 3, seed, 'none', 0, 10e-6, 1024, 200, relax=False)
 

@@ -1,8 +1,8 @@
 """Generate the FP64 oracle fixtures used by the GPU parity tests.
 
 Run from the repository root:  python tests/golden/make_golden.py
-(and ``python tests/golden/make_golden.py large`` for the cluster-sized
-systems).  Writes tests/golden/*.npz.  Inputs are the seeded workloads of
+(``python tests/golden/make_golden.py large`` for the cluster-sized
+systems, ``... deuterium`` for the quadratic-coupling workload).  Writes tests/golden/*.npz.  Inputs are the seeded workloads of
 spinach_gb300.workloads; FIDs come from the oracle (oracle/spinach_ref.py).
 """
 import os
@@ -46,9 +46,19 @@ def large_systems():
          nsteps=w.nsteps)
 
 
+def deuterium():
+    """Static 2H powder pattern (quadratic coupling), dim 144 < 200: expm branch, full grid."""
+    w = W.deuterium()
+    g = W.zcwn_grid(w.n_orient)
+    fid = oracle_powder(w, g)
+    save('deuterium_powder_fp64.npz', fid=fid, seed=w.seed, nsteps=w.nsteps, n_orient=w.n_orient)
+
+
 def main():
     if 'large' in sys.argv[1:]:
         return large_systems()
+    if 'deuterium' in sys.argv[1:]:
+        return deuterium()
     t = time.time()
     # c0: full 200-point grid, 1024 steps, default tolerances (expm branch, dim < 200)
     w = W.c0()

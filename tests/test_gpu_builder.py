@@ -22,7 +22,7 @@ def _pair(gpu_engine, w, grid, nsteps):
     return ref, got, ms
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c4_small', 'c4'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c4_small', 'c4', 'deuterium'])
 def test_built_system_matches_host_builder(gpu_engine, name):
     w = getattr(W, name)()
     grid = W.zcwn_grid(24)

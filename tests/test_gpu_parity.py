@@ -37,6 +37,19 @@ def test_c0_full_powder_fp64_and_fp32(gpu_engine):
     assert r64.stats['orientations_failed'] == 0 and r32.stats['matvecs'] > 0
 
 
+def test_deuterium_powder_fp64_and_fp32(gpu_engine):
+    """Static 2H powder pattern (quadratic coupling T(2,0), dim 144, 400
+    orientations, 1024 steps) vs the oracle's expm branch."""
+    w = W.deuterium()
+    _upload(gpu_engine, w)
+    g = W.zcwn_grid(w.n_orient)
+    ref = np.load(os.path.join(GOLD, 'deuterium_powder_fp64.npz'))['fid']
+    r64 = gpu_engine.run(*g, w.dt, w.nsteps, precision=E.FP64)
+    assert rel_err(r64.fid, ref) <= FP64_TOL
+    r32 = gpu_engine.run(*g, w.dt, w.nsteps, precision=E.FP32)
+    assert rel_err(r32.fid, ref) <= FP32_TOL
+
+
 def test_c1_orientations_vs_krylov_branch(gpu_engine):
     """Config c1 (IK-0(3), dim 1156, T1/T2, 2048 steps), per orientation, vs step.m/krylov.m."""
     w = W.c1()

@@ -39,7 +39,7 @@ def test_full_basis_fid_matches_kron_model(relax):
         assert rel_err(f_st, f_kr) < 1e-8, ang
 
 
-@pytest.mark.parametrize('wl', ['c0', 'c4'])
+@pytest.mark.parametrize('wl', ['c0', 'c4', 'deuterium'])
 def test_builder_matches_oracle_operators(wl):
     w = getattr(W, wl)()
     if wl == 'c4':            # keep the CPU suite fast: electron, 14N, three protons
@@ -141,3 +141,27 @@ def test_eseem_matches_kron_model(relax):
         assert f_st.shape == (24,)
         assert np.abs(f_kr).max() > 0.1
         assert rel_err(f_st, f_kr) < 1e-8, ang
+
+
+def test_quadratic_coupling_matches_kron_model():
+    """The 2H quadratic coupling (hamiltonian.m:191-257, T(2,0) under 'nmr')
+    against L.A.L's secular part (A_zz/2)(3Lz^2 - L^2) in Hilbert space."""
+    w = W.deuterium()
+    ss, I, Q = oracle_system(w)
+    km = KronModel(ss)
+    rho_h = km.spin_op('Lx', '2H') / np.sqrt(km.dim)
+    coil_h = km.spin_op('L+', '2H') / np.sqrt(km.dim)
+    par = dict(rho0=R.state(ss, 'Lx', '2H'), coil=R.state(ss, 'L+', '2H'), sweep=1 / w.dt, npoints=129)
+    for ang in [(0.0, 0.7, 1.3), (0.4, 1.0, -0.3), (0.0, 2.5, 4.0)]:
+        f_st = R.powder_orientation_fid(ss, I, Q, par, ang)
+        f_kr = km.fid(ang, rho_h, coil_h, w.dt, 128)
+        assert rel_err(f_st, f_kr) < 1e-9, ang
+
+
+def test_quadratic_coupling_rules():
+    from spinach_gb300 import spin_system as S
+    with pytest.raises(ValueError):                      # spin-1/2 has no rank-2 operators
+        S.make_spin_system(['1H', '13C'], 14.1, coupling_eigs={(0, 0): [-1e3, -1e3, 2e3]})
+    ss = S.make_spin_system(['2H'], 14.1, coupling_eigs={(0, 0): [-1e4, -1e4, 3e4]})   # not traceless
+    with pytest.raises(ValueError):
+        S.interaction_terms(ss, 'nmr')
