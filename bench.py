@@ -49,11 +49,14 @@ WORKLOAD_TEXT = {
     'c0': 'c0: 13C+2x1H, full basis dim 64, 200-orientation zcwn grid, 1024 steps of 10 us',
     'c1': 'c1: 13C+6x1H, IK-0(3) dim 1156, T1/T2, 1000-orientation zcwn grid, 2048 steps of 5 us',
     'c4': 'c4: e + 14N + 10 1H at 0.34 T, IK-1(3) dim 2736, T2e, 4000-orientation zcwn grid, 4096 steps of 1 ns',
+    'deuterium': 'static 2H powder pattern: 2H (quadratic coupling C_Q ~170 kHz) + 13C + 1H at 14.1 T, full basis '
+                 'dim 144, 400-orientation zcwn grid, 1024 steps of 2 us',
 }
 BRANCH_TEXT = {
     'c0': 'expm below dim 200 (propagator.m:40-42), then P*rho (evolution.m:563-566)',
     'c1': 'propagator.m chopped Taylor + squaring, then P*rho (evolution.m:537-566)',
     'c4': 'propagator.m chopped Taylor + squaring, then P*rho (evolution.m:537-566)',
+    'deuterium': 'expm below dim 200 (propagator.m:40-42), then P*rho (evolution.m:563-566)',
 }
 
 
@@ -560,7 +563,7 @@ def main():
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    ap.add_argument('--workload', default='c1', choices=['c0', 'c1', 'c4'])
+    ap.add_argument('--workload', default='c1', choices=['c0', 'c1', 'c4', 'deuterium'])
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-surrogate', action='store_true', help='skip the learned-surrogate leg')
