@@ -165,3 +165,44 @@ def test_quadratic_coupling_rules():
     ss = S.make_spin_system(['2H'], 14.1, coupling_eigs={(0, 0): [-1e4, -1e4, 3e4]})   # not traceless
     with pytest.raises(ValueError):
         S.interaction_terms(ss, 'nmr')
+
+
+def test_strong_quadratic_coupling_matches_hilbert_space():
+    """'esr' assumptions keep the whole quadratic coupling of a nucleus
+    (hamiltonian.m:216-229, five T(2,m)) and its full Zeeman interaction: one
+    14N against H = L.Z.e_z + L.A.L built from spin matrices."""
+    import scipy.linalg as sla
+    from oracle.kron_model import KronModel
+    sys_ = dict(isotopes=['14N'], magnet=0.34, enable=[])
+    A = 2 * np.pi * np.array([[-0.4e6, 0.1e6, 0.05e6], [0.1e6, -0.6e6, 0.2e6], [0.05e6, 0.2e6, 1.0e6]])
+    evals, evecs = np.linalg.eigh(A / (2 * np.pi))
+    inter = dict(zeeman=dict(eigs=[[10.0, 20.0, 40.0]], euler=[[0.1, 0.2, 0.3]]),
+                 coupling=dict(eigs={(0, 0): list(evals)}))
+    ss = R.create(sys_, inter)
+    # put the coupling in as the full matrix (create.m adds 2*pi*S*diag(eigs)*S')
+    ss.coupling[(0, 0)] = A
+    ss = R.basis(ss, dict(approximation='none', level=0, space_level=1))
+    ss, I, Q = R.powder_setup(ss, 'esr')
+    km = KronModel(ss)
+    Lx, Ly, Lz = (km.ops[0][k] for k in ('x', 'y', 'z'))
+    Lv = [Lx, Ly, Lz]
+    rho = R.state(ss, 'Lx', '14N')
+    coil = R.state(ss, 'L+', '14N')
+    rho_h = km.spin_op('Lx', '14N') / np.sqrt(km.dim)
+    coil_h = km.spin_op('L+', '14N') / np.sqrt(km.dim)
+    dt, n = 2e-8, 96
+    par = dict(rho0=rho, coil=coil, sweep=1 / dt, npoints=n + 1)
+    for ang in [(0.0, 0.0, 0.0), (0.3, 1.1, -0.7)]:
+        Rm = R.euler2dcm(*ang)
+        Z = Rm @ ss.zeeman[0] @ Rm.T
+        Ar = Rm @ A @ Rm.T
+        H = sum(Z[i, 2] * Lv[i] for i in range(3)) + sum(Ar[i, j] * Lv[i] @ Lv[j] for i in range(3) for j in range(3))
+        Lh = np.kron(H, np.eye(3)) - np.kron(np.eye(3), H.T)
+        P = sla.expm(-1j * dt * Lh)
+        r = rho_h.reshape(-1).astype(complex)
+        f_h = []
+        for _ in range(n + 1):
+            f_h.append(np.vdot(coil_h.reshape(-1), r))
+            r = P @ r
+        f_st = R.powder_orientation_fid(ss, I, Q, par, ang)
+        assert rel_err(f_st, np.array(f_h)) < 1e-9, ang
