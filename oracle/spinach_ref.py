@@ -946,6 +946,26 @@ def grid_fib(parm: int):
     return np.zeros(n), bets, gams, np.full(n, 1.0 / n)
 
 
+def frqoffset(ss: SpinSystem, H, spins, offsets):
+    """kernel/frqoffset.m:27-55: H + 2*pi*offset*Lz(isotope) per channel;
+    channels naming the same isotope must carry the same offset."""
+    if not spins:
+        raise ValueError('parameters.spins variable cannot be empty.')
+    if len(offsets) != len(spins):
+        raise ValueError('parameters.offset must have the same number of elements as parameters.spins')
+    if any(s not in ss.isotopes for s in spins):
+        raise ValueError('parameters.spins refers to a spin that is not present in the system.')
+    seen = {}
+    for s, off in zip(spins, offsets):
+        if s in seen and seen[s] != off:
+            raise ValueError('offsets on channels referring to the same spin must be the same.')
+        seen[s] = off
+    for s in sorted(seen, key=spins.index):
+        if seen[s] != 0:
+            H = H + 2 * np.pi * seen[s] * operator(ss, 'Lz', s)
+    return H
+
+
 def powder_setup(ss: SpinSystem, assumptions: str):
     """kernel/contexts/powder.m:148-161: assume, then [I,Q]=hamiltonian once."""
     ss = assume(ss, assumptions)

@@ -213,7 +213,22 @@ def build(w: Workload) -> Liouvillian:
     fac = ssm.factory_for(ss, basis)
     H = ssm.rotational_hamiltonian(ss, basis, w.assumptions, fac)
     R = sp.diags(ssm.relaxation_diagonal(ss, basis)).tocsr().astype(complex)
-    return Liouvillian(H.iso, H.aniso, R, fac.state(*w.rho0), fac.state(*w.coil), basis.dim)
+    iso = H.iso
+    for s, off in _offsets(w):
+        iso = iso + 2 * math.pi * off * fac.operator([('Lz', s)])
+    return Liouvillian(iso, H.aniso, R, fac.state(*w.rho0), fac.state(*w.coil), basis.dim)
+
+
+def _offsets(w: Workload):
+    """(spin, offset Hz) of w.extra['offset'] = {isotope: Hz}: the frequency
+    offsets of powder.m's frqoffset call (kernel/frqoffset.m)."""
+    out = []
+    for iso_name, off in (w.extra.get('offset') or {}).items():
+        if iso_name not in w.isotopes:
+            raise ValueError(f'offset for {iso_name}, which is not in the system')
+        if off != 0:
+            out += [(s, float(off)) for s, name in enumerate(w.isotopes) if name == iso_name]
+    return out
 
 
 @dataclass
@@ -232,6 +247,12 @@ def build_spec(w: Workload) -> BuildSpec:
     basis = ssm.build_basis(ss, w.approximation, w.level)
     fac = ssm.factory_for(ss, basis)
     hm = ssm.hamiltonian_monomials(ss, basis, w.assumptions)
+    offs = _offsets(w)
+    if offs:                                    # Lz of each spin: code 2, coefficient 2*pi*offset
+        hm.mono_term = np.concatenate([hm.mono_term, np.zeros(len(offs), np.int32)])
+        hm.mono_spins = np.concatenate([hm.mono_spins, np.array([[s, -1] for s, _ in offs], np.int32)])
+        hm.mono_codes = np.concatenate([hm.mono_codes, np.array([[2, 0] for _ in offs], np.int32)])
+        hm.mono_coefs = np.concatenate([hm.mono_coefs, np.array([2 * math.pi * o for _, o in offs], np.complex128)])
     return BuildSpec(hm, ssm.relaxation_diagonal(ss, basis), fac.state(*w.rho0), fac.state(*w.coil), basis.dim)
 
 

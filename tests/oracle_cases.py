@@ -18,6 +18,9 @@ def oracle_system(w, tol_mode='default', krylov=False):
     ss = R.create(sys_, inter, tol_mode)
     ss = R.basis(ss, dict(approximation=w.approximation, level=w.level, space_level=1))
     ss, I, Q = R.powder_setup(ss, w.assumptions)
+    if w.extra.get('offset'):                   # powder.m:157, frqoffset.m
+        spins = list(w.extra['offset'])
+        I = R.frqoffset(ss, I, spins, [w.extra['offset'][s] for s in spins])
     return ss, I, Q
 
 

@@ -130,3 +130,20 @@ def test_invalid_inputs_raise(gpu_engine):
         gpu_engine.run([0.0], [0.1], [0.0], [1.0], -1.0, 4)
     with pytest.raises(E.SpxError):
         gpu_engine.run([0.0], [0.1], [0.0], [1.0], 1e3, 4)    # |L dt| too large
+
+
+def test_frequency_offsets(gpu_engine):
+    """powder.m's frqoffset: offsets on both isotopes, host and GPU builders."""
+    import copy
+    w = copy.deepcopy(W.c0())
+    w.extra['offset'] = {'13C': 1500.0, '1H': -300.0}
+    al, be, ga, _ = W.zcwn_grid(w.n_orient)
+    sel = np.array([2, 50, 123, 177])
+    g = (al[sel], be[sel], ga[sel], np.full(sel.size, 0.25))
+    ref = oracle_powder(w, g, nsteps=400)
+    _upload(gpu_engine, w)
+    assert rel_err(gpu_engine.run(*g, w.dt, 400, precision=E.FP64).fid, ref) <= FP64_TOL
+    assert rel_err(gpu_engine.run(*g, w.dt, 400, precision=E.FP32).fid, ref) <= FP32_TOL
+    bs = W.build_spec(w)
+    gpu_engine.build_system(bs.monomials, bs.r_diag, bs.rho0, bs.coil)
+    assert rel_err(gpu_engine.run(*g, w.dt, 400, precision=E.FP64).fid, ref) <= FP64_TOL

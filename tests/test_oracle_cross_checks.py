@@ -206,3 +206,19 @@ def test_strong_quadratic_coupling_matches_hilbert_space():
             r = P @ r
         f_st = R.powder_orientation_fid(ss, I, Q, par, ang)
         assert rel_err(f_st, np.array(f_h)) < 1e-9, ang
+
+
+def test_frequency_offsets_match_oracle():
+    """powder.m:157 frqoffset (kernel/frqoffset.m): 2*pi*offset*Lz per isotope."""
+    import copy
+    w = copy.deepcopy(W.c0())
+    w.extra['offset'] = {'13C': 1500.0, '1H': -300.0}
+    ss, I, Q = oracle_system(w)
+    L = W.build(w)
+    assert abs(L.I - I).max() <= 1e-14 * abs(I).max()
+    w0 = W.c0()
+    assert abs(W.build(w0).I - L.I).max() > 1e3             # the offsets are there
+    with pytest.raises(ValueError):
+        R.frqoffset(ss, I, ['13C', '13C'], [1.0, 2.0])
+    with pytest.raises(ValueError):
+        R.frqoffset(ss, I, ['15N'], [1.0])
