@@ -272,6 +272,7 @@ def create(sys: dict, inter: dict, tol_mode: str = 'default') -> SpinSystem:
     rl = inter.get('relaxation', [])
     ss.theories = list(rl)
     ss.r1 = list(inter.get('r1_rates', [0.0] * n))
+    ss.damp_rate = inter.get('damp_rate', 0.0)
     ss.r2 = list(inter.get('r2_rates', [0.0] * n))
     return ss
 
@@ -692,10 +693,26 @@ def orientation(Q: dict, angles) -> sp.csc_matrix:
 
 
 def relaxation(ss: SpinSystem) -> sp.csc_matrix:
-    """kernel/relaxation.m:72-93 with kernel/utilities/rlx_t1_t2.m:32-178 (scalar rates)."""
+    """kernel/relaxation.m:72-93 with kernel/utilities/rlx_t1_t2.m:32-178
+    (scalar rates), plus :638-684 ('damp', isotropic: RD = -rate*1, then
+    R + RD - (U'*RD*U)*(U*U') so that the unit state U is not damped)."""
     dim = ss.basis.shape[0]
-    if 't1_t2' not in ss.theories:
-        return sp.csc_matrix((dim, dim), dtype=complex)
+    R = sp.csc_matrix((dim, dim), dtype=complex)
+    if 't1_t2' in ss.theories:
+        R = R + _rlx_t1_t2(ss)
+    if 'damp' in ss.theories:
+        dr = np.asarray(getattr(ss, 'damp_rate', 0.0), float)
+        rate = float(np.mean(np.diag(dr))) if dr.ndim == 2 else float(dr)
+        RD = -rate * sp.identity(dim, dtype=complex, format='csc')
+        u = np.zeros(dim, complex)
+        u[np.where((ss.basis == 0).all(axis=1))[0][0]] = 1.0
+        U = sp.csc_matrix(u.reshape(-1, 1))
+        R = R + RD - (U.conj().T @ RD @ U).toarray()[0, 0] * (U @ U.conj().T)
+    return sp.csc_matrix(R)
+
+
+def _rlx_t1_t2(ss: SpinSystem) -> sp.csc_matrix:
+    """kernel/utilities/rlx_t1_t2.m:32-178 with scalar R1/R2 per spin."""
     L, M = lin2lm(ss.basis)
     mask = L != 0
     r1 = np.asarray(ss.r1, float); r2 = np.asarray(ss.r2, float)

@@ -652,16 +652,21 @@ def rotational_hamiltonian(ss: SpinSystem, basis: Basis, assumptions: str,
     return RotationalHamiltonian(dim, I, aniso)
 
 
-def relaxation_diagonal(ss: SpinSystem, basis: Basis) -> np.ndarray:
+def relaxation_diagonal(ss: SpinSystem, basis: Basis, damp_rate: float = 0.0) -> np.ndarray:
     """Diagonal of the T1/T2 relaxation superoperator (kernel/utilities/rlx_t1_t2.m:145-176):
     each state decays at the sum of R1 over its longitudinal spins and R2 over its
-    transverse spins.  Returned with the reference's sign (non-positive)."""
-    if not ss.relaxation:
-        return np.zeros(basis.dim)
+    transverse spins; with ``damp_rate`` (kernel/relaxation.m:638-684, 'damp',
+    isotropic) every state but the unit state also decays at that rate.
+    Returned with the reference's sign (non-positive)."""
     c = basis.codes.astype(np.int64)
-    l = np.floor(np.sqrt(c)).astype(np.int64)
-    m = l * l + l - c
-    active = l != 0
-    longi = active & (m == 0)
-    trans = active & (m != 0)
-    return -(longi @ ss.r1 + trans @ ss.r2)
+    out = np.zeros(basis.dim)
+    if ss.relaxation:
+        l = np.floor(np.sqrt(c)).astype(np.int64)
+        m = l * l + l - c
+        active = l != 0
+        longi = active & (m == 0)
+        trans = active & (m != 0)
+        out = -(longi @ ss.r1 + trans @ ss.r2)
+    if damp_rate:
+        out = out - float(damp_rate) * (c != 0).any(axis=1)
+    return out

@@ -212,7 +212,7 @@ def build(w: Workload) -> Liouvillian:
     basis = ssm.build_basis(ss, w.approximation, w.level)
     fac = ssm.factory_for(ss, basis)
     H = ssm.rotational_hamiltonian(ss, basis, w.assumptions, fac)
-    R = sp.diags(ssm.relaxation_diagonal(ss, basis)).tocsr().astype(complex)
+    R = sp.diags(ssm.relaxation_diagonal(ss, basis, w.extra.get('damp_rate', 0.0))).tocsr().astype(complex)
     iso = H.iso
     for s, off in _offsets(w):
         iso = iso + 2 * math.pi * off * fac.operator([('Lz', s)])
@@ -253,7 +253,7 @@ def build_spec(w: Workload) -> BuildSpec:
         hm.mono_spins = np.concatenate([hm.mono_spins, np.array([[s, -1] for s, _ in offs], np.int32)])
         hm.mono_codes = np.concatenate([hm.mono_codes, np.array([[2, 0] for _ in offs], np.int32)])
         hm.mono_coefs = np.concatenate([hm.mono_coefs, np.array([2 * math.pi * o for _, o in offs], np.complex128)])
-    return BuildSpec(hm, ssm.relaxation_diagonal(ss, basis), fac.state(*w.rho0), fac.state(*w.coil), basis.dim)
+    return BuildSpec(hm, ssm.relaxation_diagonal(ss, basis, w.extra.get('damp_rate', 0.0)), fac.state(*w.rho0), fac.state(*w.coil), basis.dim)
 
 
 def c4_small(seed: int = 4, n_protons: int = 2) -> Workload:

@@ -10,8 +10,11 @@ def oracle_system(w, tol_mode='default', krylov=False):
         inter['coordinates'] = w.coordinates
     if w.coupling_eigs is not None:
         inter['coupling'] = dict(eigs=w.coupling_eigs, euler=w.coupling_euler or {})
+    if w.extra.get('damp_rate'):
+        inter.setdefault('relaxation', []).append('damp')
+        inter['damp_rate'] = w.extra['damp_rate']
     if w.r1 is not None:
-        inter['relaxation'] = ['t1_t2']
+        inter.setdefault('relaxation', []).append('t1_t2')
         inter['r1_rates'] = w.r1
         inter['r2_rates'] = w.r2
     sys_ = dict(isotopes=w.isotopes, magnet=w.magnet, enable=['krylov'] if krylov else [])

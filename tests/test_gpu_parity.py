@@ -147,3 +147,19 @@ def test_frequency_offsets(gpu_engine):
     bs = W.build_spec(w)
     gpu_engine.build_system(bs.monomials, bs.r_diag, bs.rho0, bs.coil)
     assert rel_err(gpu_engine.run(*g, w.dt, 400, precision=E.FP64).fid, ref) <= FP64_TOL
+
+
+def test_isotropic_damping(gpu_engine):
+    """relaxation.m 'damp' with T1/T2 on the c0 system."""
+    import copy
+    w = copy.deepcopy(W.c0())
+    rng = np.random.default_rng(4)
+    w.r1, w.r2 = list(rng.uniform(1, 5, 3)), list(rng.uniform(5, 20, 3))
+    w.extra['damp_rate'] = 37.0
+    al, be, ga, _ = W.zcwn_grid(w.n_orient)
+    sel = np.array([9, 88, 140])
+    g = (al[sel], be[sel], ga[sel], np.full(sel.size, 1 / 3))
+    ref = oracle_powder(w, g, nsteps=600)
+    _upload(gpu_engine, w)
+    assert rel_err(gpu_engine.run(*g, w.dt, 600, precision=E.FP64).fid, ref) <= FP64_TOL
+    assert rel_err(gpu_engine.run(*g, w.dt, 600, precision=E.FP32).fid, ref) <= FP32_TOL

@@ -222,3 +222,19 @@ def test_frequency_offsets_match_oracle():
         R.frqoffset(ss, I, ['13C', '13C'], [1.0, 2.0])
     with pytest.raises(ValueError):
         R.frqoffset(ss, I, ['15N'], [1.0])
+
+
+def test_isotropic_damping_matches_oracle():
+    """relaxation.m 'damp' (isotropic): every state but the unit state decays
+    at damp_rate, on top of T1/T2."""
+    import copy
+    w = copy.deepcopy(W.c0())
+    rng = np.random.default_rng(4)
+    w.r1, w.r2 = list(rng.uniform(1, 5, 3)), list(rng.uniform(5, 20, 3))
+    w.extra['damp_rate'] = 37.0
+    ss, I, Q = oracle_system(w)
+    L = W.build(w)
+    Ro = R.relaxation(ss)
+    assert abs(Ro - sp.diags(Ro.diagonal())).max() == 0
+    assert np.abs(L.R.diagonal() - Ro.diagonal()).max() <= 1e-12
+    assert L.R.diagonal()[0] == 0 and abs(Ro.diagonal()[0]) == 0
