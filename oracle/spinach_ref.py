@@ -845,10 +845,34 @@ def evolution_observable(ss: SpinSystem, L, coil, rho, dt: float, nsteps: int) -
     return krylov_observable(ss, L, coil, rho, dt, nsteps)
 
 
+def decouple(ss: SpinSystem, L, rho, spins):
+    """kernel/decouple.m:46-95 (sphten-liouv, one spatial point): rows and
+    columns of L and entries of rho of every state in which a decoupled spin
+    is not in its unit state are zeroed."""
+    if not spins:
+        return L, rho
+    if any(s not in ss.isotopes for s in spins):
+        raise ValueError('the system does not contain the spins specified.')
+    dec = np.array([iso in spins for iso in ss.isotopes])
+    zero = ss.basis[:, dec].sum(axis=1) != 0
+    keep = sp.diags((~zero).astype(float))
+    L = clean_up(ss, sp.csc_matrix(keep @ L @ keep), ss.tols['liouv_zero'])
+    rho = np.where(zero, 0.0, np.asarray(rho, complex))
+    return L, rho
+
+
 def acquire(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
-    """experiments/acquire.m:42-73: L=H+iR, evolution(...,1/sweep,npoints-1,'observable')."""
+    """experiments/acquire.m:42-73: L=H+iR, the decoupling (:51), the
+    homodecoupling L + 2*pi*pwr*oper (:54-62), the dead time (:65-67), then
+    evolution(...,1/sweep,npoints-1,'observable')."""
     L = H + 1j * R
-    return evolution_observable(ss, L, parameters['coil'], parameters['rho0'],
+    rho0 = parameters['rho0']
+    L, rho0 = decouple(ss, L, rho0, parameters.get('decouple', []))
+    if 'homodec_oper' in parameters:
+        L = L + 2 * np.pi * parameters['homodec_pwr'] * parameters['homodec_oper']
+    if 'dead_time' in parameters:
+        rho0 = step(ss, sp.csr_matrix(L), rho0, parameters['dead_time'])
+    return evolution_observable(ss, L, parameters['coil'], rho0,
                                 1.0 / parameters['sweep'], parameters['npoints'] - 1)
 
 

@@ -273,6 +273,20 @@ def _clusters(ss: SpinSystem, approximation: str, level: int, space_level: int) 
     raise ValueError(f'unsupported basis approximation {approximation!r}')
 
 
+def decoupled_basis(ss: SpinSystem, basis: Basis, spins) -> Basis:
+    """The basis without the states in which a decoupled spin is active
+    (kernel/decouple.m zeroes their rows and columns of L and their
+    populations, so they never take part; dropping them gives the same
+    dynamics on a smaller problem)."""
+    if not spins:
+        return basis
+    if any(s not in ss.isotopes for s in spins):
+        raise ValueError('the system does not contain the spins specified')
+    dec = np.array([iso in spins for iso in ss.isotopes])
+    keep = basis.codes[:, dec].sum(axis=1) == 0
+    return Basis(basis.codes[keep], basis.radix, basis.keys[keep])
+
+
 def build_basis(ss: SpinSystem, approximation: str = 'none', level: int = 0,
                 space_level: int = 1, projections=None) -> Basis:
     """Union of all product states over spin clusters (kernel/basis.m:186-465)."""

@@ -209,13 +209,17 @@ def spin_system_of(w: Workload) -> ssm.SpinSystem:
 def build(w: Workload) -> Liouvillian:
     """Host setup of a workload: I, Q{r}{k,m}, R, rho0, coil."""
     ss = spin_system_of(w)
-    basis = ssm.build_basis(ss, w.approximation, w.level)
+    basis = ssm.decoupled_basis(ss, ssm.build_basis(ss, w.approximation, w.level), w.extra.get('decouple'))
     fac = ssm.factory_for(ss, basis)
     H = ssm.rotational_hamiltonian(ss, basis, w.assumptions, fac)
     R = sp.diags(ssm.relaxation_diagonal(ss, basis, w.extra.get('damp_rate', 0.0))).tocsr().astype(complex)
     iso = H.iso
     for s, off in _offsets(w):
         iso = iso + 2 * math.pi * off * fac.operator([('Lz', s)])
+    if w.extra.get('homodec'):                  # acquire.m:54-62: L + 2*pi*pwr*oper
+        op, name, pwr = w.extra['homodec']
+        for s in [i for i, x in enumerate(w.isotopes) if x == name]:
+            iso = iso + 2 * math.pi * pwr * fac.operator([(op, s)])
     return Liouvillian(iso, H.aniso, R, fac.state(*w.rho0), fac.state(*w.coil), basis.dim)
 
 
@@ -244,15 +248,19 @@ class BuildSpec:
 def build_spec(w: Workload) -> BuildSpec:
     """Host half of the on-GPU setup: basis, monomials, relaxation, states."""
     ss = spin_system_of(w)
-    basis = ssm.build_basis(ss, w.approximation, w.level)
+    basis = ssm.decoupled_basis(ss, ssm.build_basis(ss, w.approximation, w.level), w.extra.get('decouple'))
     fac = ssm.factory_for(ss, basis)
     hm = ssm.hamiltonian_monomials(ss, basis, w.assumptions)
-    offs = _offsets(w)
-    if offs:                                    # Lz of each spin: code 2, coefficient 2*pi*offset
-        hm.mono_term = np.concatenate([hm.mono_term, np.zeros(len(offs), np.int32)])
-        hm.mono_spins = np.concatenate([hm.mono_spins, np.array([[s, -1] for s, _ in offs], np.int32)])
-        hm.mono_codes = np.concatenate([hm.mono_codes, np.array([[2, 0] for _ in offs], np.int32)])
-        hm.mono_coefs = np.concatenate([hm.mono_coefs, np.array([2 * math.pi * o for _, o in offs], np.complex128)])
+    extra = [(s, 2, 2 * math.pi * o) for s, o in _offsets(w)]          # Lz: code 2
+    if w.extra.get('homodec'):
+        op, name, pwr = w.extra['homodec']
+        for s in [i for i, x in enumerate(w.isotopes) if x == name]:
+            extra += [(s, code, 2 * math.pi * pwr * f) for code, f in ssm.OperatorFactory._CODE[op]]
+    if extra:                                   # isotropic one-spin monomials
+        hm.mono_term = np.concatenate([hm.mono_term, np.zeros(len(extra), np.int32)])
+        hm.mono_spins = np.concatenate([hm.mono_spins, np.array([[s, -1] for s, _, _ in extra], np.int32)])
+        hm.mono_codes = np.concatenate([hm.mono_codes, np.array([[c, 0] for _, c, _ in extra], np.int32)])
+        hm.mono_coefs = np.concatenate([hm.mono_coefs, np.array([v for _, _, v in extra], np.complex128)])
     return BuildSpec(hm, ssm.relaxation_diagonal(ss, basis, w.extra.get('damp_rate', 0.0)), fac.state(*w.rho0), fac.state(*w.coil), basis.dim)
 
 

@@ -31,6 +31,12 @@ def oracle_powder(w, grid, nsteps=None, tol_mode='default', krylov=False, sum_up
     ss, I, Q = oracle_system(w, tol_mode, krylov)
     nsteps = w.nsteps if nsteps is None else nsteps
     par = dict(rho0=R.state(ss, *w.rho0), coil=R.state(ss, *w.coil), sweep=1 / w.dt, npoints=nsteps + 1)
+    if w.extra.get('decouple'):
+        par['decouple'] = list(w.extra['decouple'])
+    if w.extra.get('homodec'):
+        op, iso, pwr = w.extra['homodec']
+        par['homodec_oper'] = R.operator(ss, op, iso)
+        par['homodec_pwr'] = pwr
     return R.powder(ss, par, w.assumptions, grid, setup=(I, Q), sum_up=sum_up)
 
 

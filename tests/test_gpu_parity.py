@@ -163,3 +163,38 @@ def test_isotropic_damping(gpu_engine):
     _upload(gpu_engine, w)
     assert rel_err(gpu_engine.run(*g, w.dt, 600, precision=E.FP64).fid, ref) <= FP64_TOL
     assert rel_err(gpu_engine.run(*g, w.dt, 600, precision=E.FP32).fid, ref) <= FP32_TOL
+
+
+@pytest.mark.parametrize('extra', [{'decouple': ['1H']}, {'homodec': ('Lx', '1H', 2500.0)}])
+def test_acquire_options(gpu_engine, extra):
+    """acquire.m's decoupling (:51, as a smaller basis) and homodecoupling (:54-62)."""
+    import copy
+    w = copy.deepcopy(W.c0())
+    w.extra.update(extra)
+    al, be, ga, _ = W.zcwn_grid(w.n_orient)
+    sel = np.array([4, 77, 150])
+    g = (al[sel], be[sel], ga[sel], np.full(sel.size, 1 / 3))
+    ref = oracle_powder(w, g, nsteps=300)
+    _upload(gpu_engine, w)
+    assert rel_err(gpu_engine.run(*g, w.dt, 300, precision=E.FP64).fid, ref) <= FP64_TOL
+    assert rel_err(gpu_engine.run(*g, w.dt, 300, precision=E.FP32).fid, ref) <= FP32_TOL
+    bs = W.build_spec(w)
+    gpu_engine.build_system(bs.monomials, bs.r_diag, bs.rho0, bs.coil)
+    assert rel_err(gpu_engine.run(*g, w.dt, 300, precision=E.FP64).fid, ref) <= FP64_TOL
+
+
+def test_dead_time_as_a_program(gpu_engine):
+    """acquire.m:65-67 (rho0 <- step(L, rho0, dead_time)) as a silent one-step segment."""
+    from oracle_cases import oracle_system
+    from oracle import spinach_ref as R
+    w = W.c0()
+    ss, I, Q = oracle_system(w)
+    al, be, ga, _ = W.zcwn_grid(w.n_orient)
+    sel = np.array([11, 99])
+    g = (al[sel], be[sel], ga[sel], np.array([0.4, 0.6]))
+    dead = 23.7e-6
+    par = dict(rho0=R.state(ss, *w.rho0), coil=R.state(ss, *w.coil), sweep=1 / w.dt, npoints=201, dead_time=dead)
+    ref = sum(g[3][i] * R.powder_orientation_fid(ss, I, Q, par, (g[0][i], g[1][i], g[2][i])) for i in range(2))
+    _upload(gpu_engine, w)
+    res = gpu_engine.run_sequence(*g, [], [('evolve', 1, dead, False), ('evolve', 200, w.dt)], precision=E.FP64)
+    assert rel_err(res.fid, ref) <= FP64_TOL

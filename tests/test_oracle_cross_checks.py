@@ -238,3 +238,46 @@ def test_isotropic_damping_matches_oracle():
     assert abs(Ro - sp.diags(Ro.diagonal())).max() == 0
     assert np.abs(L.R.diagonal() - Ro.diagonal()).max() <= 1e-12
     assert L.R.diagonal()[0] == 0 and abs(Ro.diagonal()[0]) == 0
+
+
+def _dense_fid(L, g, dt, nsteps):
+    """FID of the product-built system at one orientation by dense expm."""
+    import scipy.linalg as sla
+    from spinach_gb300 import singlerot as SRt
+    H = L.I.toarray().astype(complex)
+    for (r, k, m), Qm in L.terms.items():
+        H = H + SRt.wigner_d(r, *g)[k, m] * Qm.toarray()
+    H = (H + H.conj().T) / 2
+    P = sla.expm(-1j * dt * (H + 1j * L.R.toarray()))
+    rho, out = L.rho0.copy(), []
+    for _ in range(nsteps + 1):
+        out.append(np.vdot(L.coil, rho))
+        rho = P @ rho
+    return np.array(out)
+
+
+def test_decoupling_as_a_smaller_basis_matches_the_masked_liouvillian():
+    """acquire.m:51 / decouple.m zero the rows and columns of the states in
+    which a decoupled spin is active; the builder drops those states."""
+    import copy
+    w = copy.deepcopy(W.c0())
+    w.extra['decouple'] = ['1H']
+    ss, I, Q = oracle_system(w)
+    L = W.build(w)
+    assert L.dim == 4 and ss.basis.shape[0] == 64            # 13C alone survives
+    par = dict(rho0=R.state(ss, *w.rho0), coil=R.state(ss, *w.coil), sweep=1 / w.dt, npoints=65,
+               decouple=['1H'])
+    for ang in [(0.0, 0.7, 1.3), (0.2, 2.0, -1.0)]:
+        assert rel_err(_dense_fid(L, ang, w.dt, 64), R.powder_orientation_fid(ss, I, Q, par, ang)) < 1e-12
+
+
+def test_homodecoupling_matches_oracle():
+    import copy
+    w = copy.deepcopy(W.c0())
+    w.extra['homodec'] = ('Lx', '1H', 2500.0)
+    ss, I, Q = oracle_system(w)
+    L = W.build(w)
+    par = dict(rho0=R.state(ss, *w.rho0), coil=R.state(ss, *w.coil), sweep=1 / w.dt, npoints=65,
+               homodec_oper=R.operator(ss, 'Lx', '1H'), homodec_pwr=2500.0)
+    ang = (0.0, 1.1, 0.4)
+    assert rel_err(_dense_fid(L, ang, w.dt, 64), R.powder_orientation_fid(ss, I, Q, par, ang)) < 1e-10
