@@ -732,13 +732,16 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     for (int e = tid; e < ell_loc; e += blockDim.x) s_col[e] = sys.ell_col[eb + e];
     // Slices to warps, longest-processing-time first: slices are stored in
     // non-increasing width, each goes to the least-loaded warp with room, so a
-    // warp's slices also come in non-increasing width.  Cost ~ width + 5.
+    // warp's slices also come in non-increasing width.  Cost ~ width + 5; the
+    // last warp starts with 6, the detection moment it folds every term
+    // (c1: handicap 0 -> 67.5 ms, 3 -> 65.7, 6 -> 65.5, 10 -> 66.6, 24 -> 68.7).
     __shared__ short s_wsl[32 * 8];
     __shared__ int s_wcnt[32];
     __shared__ int s_wload[32];
     csync<CLU>();             // every CTA of the cluster has started before any remote access
     if (tid == 0) {
         for (int w = 0; w < nwarps; ++w) { s_wcnt[w] = 0; s_wload[w] = 0; }
+        if (nwarps > 1) s_wload[nwarps - 1] = 6;
         bool fits = true;
         for (int sl = 0; sl < nsl; ++sl) {
             const int cost = ((s_soff[sl + 1] - s_soff[sl]) >> 5) + 5;
