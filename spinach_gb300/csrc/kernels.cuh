@@ -734,7 +734,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     // non-increasing width, each goes to the least-loaded warp with room, so a
     // warp's slices also come in non-increasing width.  Cost ~ width + 5; the
     // last warp starts with 6, the detection moment it folds every term
-    // (c1: handicap 0 -> 67.5 ms, 3 -> 65.7, 6 -> 65.5, 10 -> 66.6, 24 -> 68.7).
+    // (c1: handicap 0 -> 67.5 ms, 3 -> 65.7, 6 -> 65.5, 10 -> 66.6, 24 -> 68.7;
+    // per-slice constant 2 -> 66.5, 10 -> 68.8).
     __shared__ short s_wsl[32 * 8];
     __shared__ int s_wcnt[32];
     __shared__ int s_wload[32];
