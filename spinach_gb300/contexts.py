@@ -1,0 +1,250 @@
+"""Spinach's calling convention on the GPU engine.
+
+``create(sys, inter)`` and ``basis(spin_system, bas)`` take the reference's
+input structures (kernel/create.m, kernel/basis.m) as dicts, with 0-based spin
+indices in the coupling keys; ``state`` and ``operator`` build Liouville
+vectors and commutation superoperators (kernel/state.m, kernel/operator.m);
+``powder(spin_system, pulse_sequence, parameters, assumptions)`` and
+``singlerot(...)`` run the contexts (kernel/contexts/powder.m, singlerot.m)
+with the pulse sequences ``'acquire'``, ``'hp_acquire'``, ``'cpmg'`` and
+``'eseem'`` (experiments/*.m), the parameters named as there.  Every
+orientation runs on the GPU; the host only prepares the system.
+
+Supported fields.  sys: isotopes, magnet.  inter: zeeman.eigs/euler (ppm, or
+g for electrons), coordinates (Angstrom), coupling.eigs/euler/scalar (Hz,
+keys (a, b); (a, a) is a quadratic coupling), relaxation (['t1_t2'],
+['damp']), r1_rates, r2_rates, damp_rate.  bas: approximation ('none',
+'IK-0', 'IK-1'), level, projections.  parameters: grid (alphas, betas,
+gammas, weights), rho0 / coil (vectors, or (operator, isotope) pairs), sweep,
+npoints, spins + offset, decouple, homodec_oper + homodec_pwr, dead_time,
+sum_up, pulse_op, pulse_angle, echo_time, echo_oper, echo_angle, nloops,
+timestep; singlerot adds rate, axis, max_rank.  ``engine`` (an Engine) and
+``precision`` (engine.FP64 or FP32) are optional keyword arguments.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import engine as E
+from . import singlerot as SR
+from . import spin_system as S
+
+
+@dataclass
+class System:
+    """A spin system with its basis (the reference's ``spin_system`` after
+    create() and basis())."""
+    ss: S.SpinSystem
+    basis: S.Basis | None = None
+    damp_rate: float = 0.0
+
+    @property
+    def isotopes(self) -> list:
+        return self.ss.isotopes
+
+    def factory(self) -> S.OperatorFactory:
+        if self.basis is None:
+            raise ValueError('call basis() before building states or operators')
+        return S.factory_for(self.ss, self.basis)
+
+
+def create(sys: dict, inter: dict) -> System:
+    """kernel/create.m: interaction tensors from the sys / inter structures."""
+    isotopes = list(sys['isotopes'])
+    z = inter.get('zeeman', {})
+    cpl = inter.get('coupling', {})
+    rl = list(inter.get('relaxation', []))
+    unknown = [t for t in rl if t not in ('t1_t2', 'damp')]
+    if unknown:
+        raise ValueError(f'relaxation theories {unknown} are not supported')
+    r1 = inter.get('r1_rates') if 't1_t2' in rl else None
+    r2 = inter.get('r2_rates') if 't1_t2' in rl else None
+    ss = S.make_spin_system(isotopes, float(sys['magnet']), zeeman_eigs=z.get('eigs'),
+                            zeeman_euler=z.get('euler'), coordinates=inter.get('coordinates'),
+                            coupling_scalar=cpl.get('scalar'), coupling_eigs=cpl.get('eigs'),
+                            coupling_euler=cpl.get('euler'), r1=r1, r2=r2)
+    damp = float(np.mean(np.diag(np.atleast_2d(inter.get('damp_rate', 0.0))))) if 'damp' in rl else 0.0
+    return System(ss, None, damp)
+
+
+def basis(spin_system: System, bas: dict) -> System:
+    """kernel/basis.m: the spherical-tensor Liouville basis."""
+    b = S.build_basis(spin_system.ss, bas.get('approximation', 'none'), int(bas.get('level', 0)),
+                      projections=bas.get('projections'))
+    return System(spin_system.ss, b, spin_system.damp_rate)
+
+
+def state(spin_system: System, op: str, isotope: str) -> np.ndarray:
+    """kernel/state.m: sum over the spins of an isotope of op, as a Liouville vector."""
+    return spin_system.factory().state(op, isotope)
+
+
+def operator(spin_system: System, op: str, isotope: str) -> sp.csr_matrix:
+    """kernel/operator.m ('comm'): the commutation superoperator of sum_s op(s)."""
+    spins = [i for i, x in enumerate(spin_system.isotopes) if x == isotope]
+    if not spins:
+        raise ValueError('no such spins in the system')
+    f = spin_system.factory()
+    return sum(f.operator([(op, s)]) for s in spins)
+
+
+def _vector(spin_system: System, v) -> np.ndarray:
+    if isinstance(v, (tuple, list)) and len(v) == 2 and isinstance(v[0], str):
+        return state(spin_system, v[0], v[1])
+    return np.asarray(v, complex)
+
+
+def _matrix(spin_system: System, m):
+    if isinstance(m, (tuple, list)) and len(m) == 2 and isinstance(m[0], str):
+        return operator(spin_system, m[0], m[1])
+    return m
+
+
+def _restrict(spin_system: System, full: System, v: np.ndarray) -> np.ndarray:
+    """A vector of the full basis on the decoupled (smaller) basis."""
+    if full.basis is spin_system.basis or v.shape[0] == spin_system.basis.dim:
+        return v
+    idx = np.searchsorted(full.basis.keys, spin_system.basis.keys)
+    return v[idx]
+
+
+def _name(pulse_sequence) -> str:
+    return pulse_sequence if isinstance(pulse_sequence, str) else getattr(pulse_sequence, '__name__', '')
+
+
+def _setup(spin_system: System, parameters: dict, assumptions: str, sequence: str):
+    """[I,Q]=hamiltonian(assume(...)), frqoffset (powder.m:148-161), the
+    relaxation (powder.m:263), acquire.m's decoupling and homodecoupling."""
+    if spin_system.basis is None:
+        raise ValueError('call basis() first')
+    full = spin_system
+    dec = list(parameters.get('decouple') or [])
+    # acquire.m decouples (and homodecouples) the whole evolution, which the
+    # smaller basis reproduces; hp_acquire.m decouples after its pulses
+    if dec and sequence != 'acquire':
+        raise ValueError('decoupling is supported for acquire')
+    if 'homodec_oper' in parameters and sequence != 'acquire':
+        raise ValueError('homodecoupling is part of acquire')
+    work = System(full.ss, S.decoupled_basis(full.ss, full.basis, dec), full.damp_rate) if dec else full
+    f = work.factory()
+    H = S.rotational_hamiltonian(work.ss, work.basis, assumptions, f)
+    iso = H.iso
+    spins = list(parameters.get('spins') or [])
+    offs = list(np.atleast_1d(parameters.get('offset', np.zeros(len(spins)))))
+    if spins:
+        if len(offs) != len(spins):
+            raise ValueError('parameters.offset must have the same number of elements as parameters.spins')
+        seen = {}
+        for name, off in zip(spins, offs):
+            if name not in work.isotopes:
+                raise ValueError('parameters.spins refers to a spin that is not present in the system')
+            if name in seen and seen[name] != off:
+                raise ValueError('offsets on channels referring to the same spin must be the same')
+            seen[name] = off
+        for name, off in seen.items():
+            if off:
+                iso = iso + 2 * math.pi * float(off) * operator(work, 'Lz', name)
+    if 'homodec_oper' in parameters:
+        iso = iso + 2 * math.pi * float(parameters['homodec_pwr']) * _restrict_matrix(
+            work, full, _matrix(full, parameters['homodec_oper']))
+    R = sp.diags(S.relaxation_diagonal(work.ss, work.basis, work.damp_rate)).tocsr().astype(complex)
+    rho0 = _restrict(work, full, _vector(full, parameters['rho0']))
+    coil = _restrict(work, full, _vector(full, parameters['coil']))
+    return work, full, iso, H.aniso, R, rho0, coil
+
+
+def _restrict_matrix(work: System, full: System, M):
+    if work.basis is full.basis:
+        return M
+    idx = np.searchsorted(full.basis.keys, work.basis.keys)
+    return sp.csr_matrix(M)[idx][:, idx]
+
+
+def _grid(parameters: dict):
+    g = parameters['grid']
+    if isinstance(g, dict):
+        g = (g['alphas'], g['betas'], g['gammas'], g['weights'])
+    return tuple(np.ascontiguousarray(np.ravel(a), np.float64) for a in g)
+
+
+def _run(eng, pulse_sequence, parameters, work, full, grid, precision):
+    al, be, ga, w = grid
+    name = _name(pulse_sequence)
+    if name == 'acquire':
+        dt, n = 1.0 / float(parameters['sweep']), int(parameters['npoints']) - 1
+        if 'dead_time' in parameters:
+            prog = [('evolve', 1, float(parameters['dead_time']), False), ('evolve', n, dt)]
+            return eng.run_sequence(al, be, ga, w, [], prog, precision=precision)
+        return eng.run(al, be, ga, w, dt, n, precision=precision, per_orientation=not parameters.get('sum_up', 1))
+    if name == 'hp_acquire':
+        ops = [_restrict_matrix(work, full, _matrix(full, parameters['pulse_op']))]
+        prog = [('pulse', 0, float(parameters['pulse_angle']))]
+        if 'echo_time' in parameters:
+            ops.append(_restrict_matrix(work, full, _matrix(full, parameters['echo_oper'])))
+            et = float(parameters['echo_time'])
+            prog += [('evolve', 1, et, False), ('pulse', 1, float(parameters['echo_angle'])), ('evolve', 1, et, False)]
+        prog.append(('evolve', int(parameters['npoints']) - 1, 1.0 / float(parameters['sweep'])))
+        return eng.run_sequence(al, be, ga, w, ops, prog, precision=precision)
+    if name == 'cpmg':
+        P = _restrict_matrix(work, full, _matrix(full, parameters['pulse_op']))
+        return eng.run_cpmg(al, be, ga, w, float(parameters['timestep']), int(parameters['npoints']),
+                            int(parameters['nloops']), P, precision=precision)
+    if name == 'eseem':
+        P = _restrict_matrix(work, full, _matrix(full, parameters['pulse_op']))
+        return eng.run_eseem(al, be, ga, w, float(parameters['timestep']), int(parameters['npoints']), P,
+                             precision=precision)
+    raise ValueError(f'pulse sequence {pulse_sequence!r} is not supported on this engine')
+
+
+def _answer(res, parameters):
+    if parameters.get('sum_up', 1):
+        return res.fid
+    if res.fids is None:
+        raise ValueError('sum_up = 0 is available for acquire without a dead time')
+    return list(res.fids)
+
+
+def powder(spin_system: System, pulse_sequence, parameters: dict, assumptions: str, engine=None,
+           precision: int = E.FP64):
+    """kernel/contexts/powder.m:99-309: returns (answer, grid), the answer the
+    weighted sum of the orientations' outputs (sum_up, default) or their list."""
+    if parameters.get('needs'):
+        raise ValueError("parameters.needs: evaluate the states and pass one rho0 per orientation "
+                         "(Engine.set_initial_states) instead")
+    work, full, I, Q, R, rho0, coil = _setup(spin_system, parameters, assumptions, _name(pulse_sequence))
+    grid = _grid(parameters)
+    eng = engine or E.Engine(0)
+    try:
+        eng.upload(I, Q, R, rho0, coil)
+        res = _run(eng, pulse_sequence, parameters, work, full, grid, precision)
+    finally:
+        if engine is None:
+            eng.close()
+    return _answer(res, parameters), grid
+
+
+def singlerot(spin_system: System, pulse_sequence, parameters: dict, assumptions: str, engine=None,
+              precision: int = E.FP64):
+    """kernel/contexts/singlerot.m with acquire: the Fokker-Planck problem of
+    rate, axis and max_rank, in the engine's upload form.  A grid named
+    'single_crystal' (or single_crystal=True) starts from one rotor point."""
+    if _name(pulse_sequence) != 'acquire':
+        raise ValueError('singlerot runs acquire on this engine')
+    work, full, I, Q, R, rho0, coil = _setup(spin_system, parameters, assumptions, 'acquire')
+    single = bool(parameters.get('single_crystal')) or parameters.get('grid') == 'single_crystal'
+    grid = ((np.zeros(1), np.zeros(1), np.zeros(1), np.ones(1)) if parameters.get('grid') == 'single_crystal'
+            else _grid(parameters))
+    fp = SR.fokker_planck(I, Q, R, rho0, coil, int(parameters['max_rank']), float(parameters['rate']),
+                          parameters['axis'], single_crystal=single)
+    eng = engine or E.Engine(0)
+    try:
+        eng.upload(*fp)
+        res = _run(eng, 'acquire', parameters, work, full, grid, precision)
+    finally:
+        if engine is None:
+            eng.close()
+    return _answer(res, parameters), grid

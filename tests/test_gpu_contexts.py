@@ -1,0 +1,83 @@
+"""Spinach's calling convention (spinach_gb300.contexts): the same sys / inter /
+bas / parameters structures go to the oracle and to the GPU engine."""
+import numpy as np
+import pytest
+
+from spinach_gb300 import contexts as X, engine as E, workloads as W
+from oracle_cases import rel_err
+from oracle import spinach_ref as R
+
+pytestmark = pytest.mark.gpu
+
+
+def _structures():
+    sys_ = dict(isotopes=['13C', '1H', '1H'], magnet=14.1)
+    inter = dict(zeeman=dict(eigs=[[10.0, 70.0, 180.0], [1.0, 3.0, 8.0], [2.0, 2.5, 6.0]],
+                             euler=[[0.1, 0.7, 1.9], [0.4, 1.2, 0.3], [2.0, 0.5, 1.0]]),
+                 coordinates=[[0.0, 0.0, 0.0], [1.09, 0.0, 0.0], [-0.36, 1.03, 0.0]],
+                 coupling=dict(scalar={(0, 1): 140.0, (0, 2): 135.0}),
+                 relaxation=['t1_t2'], r1_rates=[2.0, 5.0, 5.0], r2_rates=[20.0, 40.0, 45.0])
+    bas = dict(approximation='none', level=0)
+    return sys_, inter, bas
+
+
+def _oracle(sys_, inter, bas, krylov=False):
+    ss = R.create(dict(sys_, enable=['krylov'] if krylov else []), inter)
+    ss = R.basis(ss, dict(bas, space_level=1))
+    return R.powder_setup(ss, 'nmr')
+
+
+def test_powder_acquire(gpu_engine):
+    sys_, inter, bas = _structures()
+    spin_system = X.basis(X.create(sys_, inter), bas)
+    grid = W.zcwn_grid(40)
+    parameters = dict(grid=grid, rho0=('Lx', '13C'), coil=('L+', '13C'), sweep=2e4, npoints=257,
+                      spins=['13C', '1H'], offset=[800.0, -150.0])
+    fid, _ = X.powder(spin_system, 'acquire', parameters, 'nmr', engine=gpu_engine)
+    ss, I, Q = _oracle(sys_, inter, bas)
+    I = R.frqoffset(ss, I, ['13C', '1H'], [800.0, -150.0])
+    par = dict(rho0=R.state(ss, 'Lx', '13C'), coil=R.state(ss, 'L+', '13C'), sweep=2e4, npoints=257)
+    ref = R.powder(ss, par, 'nmr', grid, setup=(I, Q))
+    assert rel_err(fid, ref) <= 1e-10
+    # sum_up = 0: one FID per orientation (powder.m:291-297)
+    fids, _ = X.powder(spin_system, 'acquire', dict(parameters, sum_up=0), 'nmr', engine=gpu_engine)
+    assert len(fids) == 40 and rel_err(sum(w * f for w, f in zip(grid[3], fids)), ref) <= 1e-10
+
+
+def test_powder_hp_acquire_with_echo_and_decoupled_acquire(gpu_engine):
+    sys_, inter, bas = _structures()
+    spin_system = X.basis(X.create(sys_, inter), bas)
+    grid = W.zcwn_grid(24)
+    ss, I, Q = _oracle(sys_, inter, bas)
+    par = dict(rho0=R.state(ss, 'Lz', '13C'), coil=R.state(ss, 'L+', '13C'), pulse_op=R.operator(ss, 'Ly', '13C'),
+               pulse_angle=np.pi / 2, echo_time=3e-4, echo_oper=R.operator(ss, 'Lx', '13C'), echo_angle=np.pi,
+               sweep=2e4, npoints=200)
+    ref = sum(grid[3][i] * R.powder_orientation_hp_acquire(ss, I, Q, par, (grid[0][i], grid[1][i], grid[2][i]))
+              for i in range(24))
+    parameters = dict(grid=grid, rho0=('Lz', '13C'), coil=('L+', '13C'), pulse_op=('Ly', '13C'),
+                      pulse_angle=np.pi / 2, echo_time=3e-4, echo_oper=('Lx', '13C'), echo_angle=np.pi,
+                      sweep=2e4, npoints=200)
+    fid, _ = X.powder(spin_system, 'hp_acquire', parameters, 'nmr', engine=gpu_engine)
+    assert rel_err(fid, ref) <= 1e-10
+    # proton-decoupled 13C acquisition (acquire.m:51)
+    par2 = dict(rho0=R.state(ss, 'Lx', '13C'), coil=R.state(ss, 'L+', '13C'), sweep=2e4, npoints=200,
+                decouple=['1H'])
+    ref2 = R.powder(ss, par2, 'nmr', grid, setup=(I, Q))
+    fid2, _ = X.powder(spin_system, 'acquire', dict(grid=grid, rho0=('Lx', '13C'), coil=('L+', '13C'), sweep=2e4,
+                                                     npoints=200, decouple=['1H']), 'nmr', engine=gpu_engine)
+    assert rel_err(fid2, ref2) <= 1e-10
+    with pytest.raises(ValueError):
+        X.powder(spin_system, 'cpmg', dict(parameters, decouple=['1H'], nloops=2, timestep=1e-4), 'nmr',
+                 engine=gpu_engine)
+
+
+def test_singlerot_reference_single_crystal_case(gpu_engine):
+    """tests/kernel/test_ctx_singlerot_acquire.m through the context API."""
+    spin_system = X.basis(X.create(dict(isotopes=['1H'], magnet=14.1),
+                                   dict(zeeman=dict(eigs=[[-2.0, -2.0, 4.0]], euler=[[0.0, 0.0, 0.0]]))),
+                          dict(approximation='none', projections=[1]))
+    rho = X.state(spin_system, 'L+', '1H')
+    parameters = dict(rho0=rho, coil=rho, sweep=2000.0, npoints=3, rate=1000.0, axis=(1, 1, 1), max_rank=1,
+                      grid='single_crystal')
+    fid, _ = X.singlerot(spin_system, 'acquire', parameters, 'nmr', engine=gpu_engine)
+    assert fid.shape == (3,) and abs(fid[0] - np.vdot(rho, rho)) <= 1e-12 and np.all(np.isfinite(fid))
