@@ -164,8 +164,24 @@ def _restrict_matrix(work: System, full: System, M):
     return sp.csr_matrix(M)[idx][:, idx]
 
 
+def load_grid(path: str):
+    """A spherical grid file of the reference (kernel/grids/*.mat, MATLAB v5
+    format): (alphas, betas, gammas, weights) as flat float64 arrays."""
+    import scipy.io as sio
+    try:
+        d = sio.loadmat(path)
+    except NotImplementedError as e:              # v7.3 (HDF5) files
+        raise ValueError(f'{path}: MATLAB v7.3 grid files are not readable here') from e
+    missing = [k for k in ('alphas', 'betas', 'gammas', 'weights') if k not in d]
+    if missing:
+        raise ValueError(f'{path}: no {missing} in the grid file')
+    return tuple(np.ascontiguousarray(np.ravel(d[k]), np.float64) for k in ('alphas', 'betas', 'gammas', 'weights'))
+
+
 def _grid(parameters: dict):
     g = parameters['grid']
+    if isinstance(g, str):
+        g = load_grid(g)
     if isinstance(g, dict):
         g = (g['alphas'], g['betas'], g['gammas'], g['weights'])
     return tuple(np.ascontiguousarray(np.ravel(a), np.float64) for a in g)

@@ -2,7 +2,9 @@
 
 Run from the repository root:  python tests/golden/make_golden.py
 (``python tests/golden/make_golden.py large`` for the cluster-sized
-systems, ``... deuterium`` for the quadratic-coupling workload).  Writes tests/golden/*.npz.  Inputs are the seeded workloads of
+systems, ``... deuterium`` for the quadratic-coupling workload, ``... grids``
+to copy the reference's 14-point Lebedev grid out of its grid file, which
+needs the reference source tree).  Writes tests/golden/*.npz.  Inputs are the seeded workloads of
 spinach_gb300.workloads; FIDs come from the oracle (oracle/spinach_ref.py).
 """
 import os
@@ -54,7 +56,17 @@ def deuterium():
     save('deuterium_powder_fp64.npz', fid=fid, seed=w.seed, nsteps=w.nsteps, n_orient=w.n_orient)
 
 
+def grids():
+    """kernel/grids/leb_2ang_rank_5.mat of the reference (the grid of
+    tests/kernel/test_ctx_powder_average.m) as arrays."""
+    from spinach_gb300 import contexts as X
+    al, be, ga, w = X.load_grid('/root/reference/kernel/grids/leb_2ang_rank_5.mat')
+    save('grid_leb_2ang_rank_5.npz', alphas=al, betas=be, gammas=ga, weights=w)
+
+
 def main():
+    if 'grids' in sys.argv[1:]:
+        return grids()
     if 'large' in sys.argv[1:]:
         return large_systems()
     if 'deuterium' in sys.argv[1:]:

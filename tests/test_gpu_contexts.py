@@ -81,3 +81,30 @@ def test_singlerot_reference_single_crystal_case(gpu_engine):
                       grid='single_crystal')
     fid, _ = X.singlerot(spin_system, 'acquire', parameters, 'nmr', engine=gpu_engine)
     assert fid.shape == (3,) and abs(fid[0] - np.vdot(rho, rho)) <= 1e-12 and np.all(np.isfinite(fid))
+
+
+def test_reference_powder_average_case(gpu_engine):
+    """tests/kernel/test_ctx_powder_average.m: on the reference's 14-point
+    Lebedev grid (kernel/grids/leb_2ang_rank_5.mat, copied into a fixture)
+    the powder answer equals the explicit weighted sum of the per-orientation
+    answers to 1e-12, and matches the oracle."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'grid_leb_2ang_rank_5.npz'))
+    grid = (d['alphas'], d['betas'], d['gammas'], d['weights'])
+    sys_ = dict(isotopes=['1H'], magnet=14.1)
+    inter = dict(zeeman=dict(eigs=[[-2.0, -2.0, 4.0]], euler=[[0.0, 0.0, 0.0]]))
+    bas = dict(approximation='none', projections=[1])
+    spin_system = X.basis(X.create(sys_, inter), bas)
+    rho = X.state(spin_system, 'L+', '1H')
+    parameters = dict(spins=['1H'], rho0=rho, coil=rho, decouple=[], offset=[0.0], sweep=2000.0, npoints=3,
+                      grid=grid)
+    fid_avg, g = X.powder(spin_system, 'acquire', parameters, 'nmr', engine=gpu_engine)
+    fid_cells, _ = X.powder(spin_system, 'acquire', dict(parameters, sum_up=False), 'nmr', engine=gpu_engine)
+    fid_ref = g[3][0] * fid_cells[0]
+    for n in range(1, len(fid_cells)):
+        fid_ref = fid_ref + g[3][n] * fid_cells[n]
+    assert np.abs(fid_avg - fid_ref).max() <= 1e-12
+    ss = R.basis(R.create(dict(sys_, enable=[]), inter), dict(bas, space_level=1))
+    ss, I, Q = R.powder_setup(ss, 'nmr')
+    par = dict(rho0=R.state(ss, 'L+', '1H'), coil=R.state(ss, 'L+', '1H'), sweep=2000.0, npoints=3)
+    assert rel_err(fid_avg, R.powder(ss, par, 'nmr', grid, setup=(I, Q))) <= 1e-10

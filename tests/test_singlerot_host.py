@@ -87,3 +87,19 @@ def test_powder_rotor_averaging_preserves_the_zero_time_signal():
                axis=(1, 1, 1), max_rank=2)
     fid = R.singlerot_orientation_fid(ss, I, Q, par, (0.0, 0.9, 2.0))
     assert abs(fid[0] - np.vdot(par['coil'], par['rho0'])) <= 1e-12 * abs(fid[0])
+
+
+def test_grid_file_round_trip(tmp_path):
+    """contexts.load_grid reads the reference's grid-file layout (MATLAB v5
+    with alphas, betas, gammas, weights columns)."""
+    import scipy.io as sio
+    from spinach_gb300 import contexts as X
+    rng = np.random.default_rng(1)
+    cols = {k: rng.uniform(0, 1, (7, 1)) for k in ('alphas', 'betas', 'gammas', 'weights')}
+    path = str(tmp_path / 'g.mat')
+    sio.savemat(path, cols)
+    g = X.load_grid(path)
+    assert all(np.array_equal(a, cols[k].ravel()) for a, k in zip(g, ('alphas', 'betas', 'gammas', 'weights')))
+    sio.savemat(path, {'alphas': cols['alphas']})
+    with pytest.raises(ValueError):
+        X.load_grid(path)
