@@ -234,8 +234,9 @@ const char *spx_surrogate_last_error(const spx_surrogate *s);
  *   SPX_SEQ_EVOLVE  nsteps steps of dt under the orientation's Liouvillian
  *                   (kernel/evolution.m); record != 0 appends the powder FID
  *                   coil'*rho at steps 0..nsteps to fid
- * Every orientation starts from rho0; fid receives sum over recorded
- * segments of (nsteps+1) complex values.  Needs one coil and the single rho0.
+ * Every orientation starts from rho0 (or its own state after
+ * spx_set_initial_states); fid receives sum over recorded segments of
+ * (nsteps+1) complex values.  Needs one coil.
  */
 enum { SPX_SEQ_PULSE = 0, SPX_SEQ_EVOLVE = 1 };
 typedef struct spx_seq_op {

@@ -269,6 +269,7 @@ def create(sys: dict, inter: dict, tol_mode: str = 'default') -> SpinSystem:
     for key, M in cpl.items():
         if np.linalg.norm(M, 2) >= 2 * np.pi * ss.tols['inter_cutoff']:
             ss.coupling[key] = M
+    ss.temperature = inter.get('temperature', None)
     rl = inter.get('relaxation', [])
     ss.theories = list(rl)
     ss.r1 = list(inter.get('r1_rates', [0.0] * n))
@@ -320,8 +321,14 @@ def assume(ss: SpinSystem, assumptions: str) -> SpinSystem:
                     cs[(a, b)] = 'secular'
                 else:
                     cs[(a, b)] = 'strong'
+    elif assumptions == 'labframe':
+        # kernel/assume.m:278-300: everything in full
+        zs = ['full'] * n
+        for a in range(n):
+            for b in range(n):
+                cs[(a, b)] = 'strong'
     else:
-        raise ValueError('only nmr and esr assumptions are restated')
+        raise ValueError('only nmr, esr and labframe assumptions are restated')
     ss.zeeman_strength, ss.coupling_strength = zs, cs
     return ss
 
@@ -575,8 +582,10 @@ def _coupling_terms(strength: str):
     return table[strength]
 
 
-def hamiltonian(ss: SpinSystem):
-    """kernel/hamiltonian.m:44-790 -> (I, Q) with Q[r][k][m] (0-based k, m).
+def hamiltonian(ss: SpinSystem, operator_type: str = 'comm'):
+    """kernel/hamiltonian.m:44-790 -> (I, Q) with Q[r][k][m] (0-based k, m);
+    operator_type 'left' gives left-side product superoperators (the 'left'
+    argument of hamiltonian.m, used for thermal equilibria).
 
     Descriptor rows are (isotropic, ist[8], irr[8], operator spec); I and Q are
     assembled as in :705-790 and cleaned to liouv_zero."""
@@ -657,7 +666,7 @@ def hamiltonian(ss: SpinSystem):
         mc = np.sum(np.abs(ist)) < tz
         if not (ma and (mb or mc)):
             kept.append((isov, ist, irr, ops, spins))
-    opers = [operator(ss, ops, spins, 'comm') for _, _, _, ops, spins in kept]
+    opers = [operator(ss, ops, spins, operator_type) for _, _, _, ops, spins in kept]
     dim = ss.basis.shape[0]
     I = sp.csc_matrix((dim, dim), dtype=complex)
     for (isov, _, _, _, _), O in zip(kept, opers):
@@ -1005,6 +1014,25 @@ def frqoffset(ss: SpinSystem, H, spins, offsets):
         if seen[s] != 0:
             H = H + 2 * np.pi * seen[s] * operator(ss, 'Lz', s)
     return H
+
+
+def equilibrium(ss: SpinSystem, I, Q, angles) -> np.ndarray:
+    """kernel/states/equilibrium.m:53-100 (sphten-liouv, four arguments):
+    H = I + orientation(Q, angles), rho = step(H, unit, -1i*beta) =
+    exp(-beta*H) unit with beta = hbar/(k*T), normalised to <unit|rho> = 1.
+    I and Q are left-side product superoperators of the lab-frame Hamiltonian."""
+    if ss.temperature is None or ss.temperature == 0:
+        raise ValueError('temperature must be specified (and non-zero)')
+    beta = HBAR / (1.380649e-23 * ss.temperature)
+    A = orientation(Q, angles)
+    H = I if A is None else I + A
+    dim = H.shape[0]
+    unit = np.zeros(dim, complex)
+    unit[0] = 1.0
+    if np.abs(H @ unit).sum() < 1e-10:
+        raise ValueError('H and Q must be left side product superops, not commutation superops.')
+    rho = step(ss, sp.csr_matrix(H), unit, -1j * beta)
+    return rho / np.vdot(unit, rho)
 
 
 def powder_setup(ss: SpinSystem, assumptions: str):

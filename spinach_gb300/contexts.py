@@ -17,6 +17,7 @@ keys (a, b); (a, a) is a quadratic coupling), relaxation (['t1_t2'],
 'IK-0', 'IK-1'), level, projections.  parameters: grid (alphas, betas,
 gammas, weights), rho0 / coil (vectors, or (operator, isotope) pairs), sweep,
 npoints, spins + offset, decouple, homodec_oper + homodec_pwr, dead_time,
+needs (['iso_eq'] or ['aniso_eq'], with inter temperature),
 sum_up, pulse_op, pulse_angle, echo_time, echo_oper, echo_angle, nloops,
 timestep; singlerot adds rate, axis, max_rank.  ``engine`` (an Engine) and
 ``precision`` (engine.FP64 or FP32) are optional keyword arguments.
@@ -41,6 +42,7 @@ class System:
     ss: S.SpinSystem
     basis: S.Basis | None = None
     damp_rate: float = 0.0
+    temperature: float | None = None
 
     @property
     def isotopes(self) -> list:
@@ -68,14 +70,14 @@ def create(sys: dict, inter: dict) -> System:
                             coupling_scalar=cpl.get('scalar'), coupling_eigs=cpl.get('eigs'),
                             coupling_euler=cpl.get('euler'), r1=r1, r2=r2)
     damp = float(np.mean(np.diag(np.atleast_2d(inter.get('damp_rate', 0.0))))) if 'damp' in rl else 0.0
-    return System(ss, None, damp)
+    return System(ss, None, damp, inter.get('temperature'))
 
 
 def basis(spin_system: System, bas: dict) -> System:
     """kernel/basis.m: the spherical-tensor Liouville basis."""
     b = S.build_basis(spin_system.ss, bas.get('approximation', 'none'), int(bas.get('level', 0)),
                       projections=bas.get('projections'))
-    return System(spin_system.ss, b, spin_system.damp_rate)
+    return System(spin_system.ss, b, spin_system.damp_rate, spin_system.temperature)
 
 
 def state(spin_system: System, op: str, isotope: str) -> np.ndarray:
@@ -129,7 +131,8 @@ def _setup(spin_system: System, parameters: dict, assumptions: str, sequence: st
         raise ValueError('decoupling is supported for acquire')
     if 'homodec_oper' in parameters and sequence != 'acquire':
         raise ValueError('homodecoupling is part of acquire')
-    work = System(full.ss, S.decoupled_basis(full.ss, full.basis, dec), full.damp_rate) if dec else full
+    work = (System(full.ss, S.decoupled_basis(full.ss, full.basis, dec), full.damp_rate, full.temperature)
+            if dec else full)
     f = work.factory()
     H = S.rotational_hamiltonian(work.ss, work.basis, assumptions, f)
     iso = H.iso
@@ -152,9 +155,20 @@ def _setup(spin_system: System, parameters: dict, assumptions: str, sequence: st
         iso = iso + 2 * math.pi * float(parameters['homodec_pwr']) * _restrict_matrix(
             work, full, _matrix(full, parameters['homodec_oper']))
     R = sp.diags(S.relaxation_diagonal(work.ss, work.basis, work.damp_rate)).tocsr().astype(complex)
-    rho0 = _restrict(work, full, _vector(full, parameters['rho0']))
+    needs = list(parameters.get('needs') or [])
+    if any(n not in ('iso_eq', 'aniso_eq') for n in needs):
+        raise ValueError("parameters.needs may contain 'iso_eq' and 'aniso_eq'")
+    if needs and 'rho0' in parameters:
+        raise ValueError('thermal equilibrium request conflicts with user-specified initial condition.')
+    if needs:
+        # powder.m:128-147: the lab-frame Hamiltonian as left-side products
+        HL = S.rotational_hamiltonian(work.ss, work.basis, 'labframe', work.factory(), kind='left')
+        rho0 = S.equilibrium_states(S.RotationalHamiltonian(HL.dim, HL.iso, {}), work.temperature)
+    else:
+        HL = None
+        rho0 = _restrict(work, full, _vector(full, parameters['rho0']))
     coil = _restrict(work, full, _vector(full, parameters['coil']))
-    return work, full, iso, H.aniso, R, rho0, coil
+    return work, full, iso, H.aniso, R, rho0, coil, HL
 
 
 def _restrict_matrix(work: System, full: System, M):
@@ -231,12 +245,18 @@ def powder(spin_system: System, pulse_sequence, parameters: dict, assumptions: s
     if parameters.get('needs'):
         raise ValueError("parameters.needs: evaluate the states and pass one rho0 per orientation "
                          "(Engine.set_initial_states) instead")
-    work, full, I, Q, R, rho0, coil = _setup(spin_system, parameters, assumptions, _name(pulse_sequence))
+    work, full, I, Q, R, rho0, coil, HL = _setup(spin_system, parameters, assumptions, _name(pulse_sequence))
     grid = _grid(parameters)
     eng = engine or E.Engine(0)
     try:
         eng.upload(I, Q, R, rho0, coil)
-        res = _run(eng, pulse_sequence, parameters, work, full, grid, precision)
+        if 'aniso_eq' in (parameters.get('needs') or []):
+            # powder.m:244-248: the equilibrium at every orientation
+            eng.set_initial_states(S.equilibrium_states(HL, work.temperature, *grid[:3]))
+        try:
+            res = _run(eng, pulse_sequence, parameters, work, full, grid, precision)
+        finally:
+            eng.set_initial_states(None)
     finally:
         if engine is None:
             eng.close()
@@ -250,7 +270,9 @@ def singlerot(spin_system: System, pulse_sequence, parameters: dict, assumptions
     'single_crystal' (or single_crystal=True) starts from one rotor point."""
     if _name(pulse_sequence) != 'acquire':
         raise ValueError('singlerot runs acquire on this engine')
-    work, full, I, Q, R, rho0, coil = _setup(spin_system, parameters, assumptions, 'acquire')
+    if parameters.get('needs'):
+        raise ValueError('singlerot takes an explicit rho0 on this engine')
+    work, full, I, Q, R, rho0, coil, _ = _setup(spin_system, parameters, assumptions, 'acquire')
     single = bool(parameters.get('single_crystal')) or parameters.get('grid') == 'single_crystal'
     grid = ((np.zeros(1), np.zeros(1), np.zeros(1), np.ones(1)) if parameters.get('grid') == 'single_crystal'
             else _grid(parameters))

@@ -1013,8 +1013,9 @@ void apply_pulse(spx_handle *h, const PulseOp &op, double theta, int64_t n_state
 // A pulse program on the evolution core: hard pulses exp(-1i*angle*P) and
 // evolution segments, each segment one powder run that starts from the
 // previous segment's final states (per orientation; before the first segment
-// the pulses act on the single rho0).  Recorded segments append their powder
-// FID (nsteps+1 points) to fid.
+// the pulses act on the single rho0, or on the per-orientation initial
+// states when they are set).  Recorded segments append their powder FID
+// (nsteps+1 points) to fid.
 void upload_grid(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
                  const double *weights) {
     h->d_grid.reserve(4 * (size_t)n_orient);
@@ -1029,8 +1030,9 @@ void upload_grid(spx_handle *h, int64_t n_orient, const double *alphas, const do
 void run_sequence(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
                   const double *weights, int32_t n_pulse, const spx_csc *pulse_ops, int32_t n_ops,
                   const spx_seq_op *ops, const spx_options &o, double *fid) {
-    if (h->nchan != 1 || h->n_states != 0)
-        throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil and one initial state");
+    if (h->nchan != 1) throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil");
+    if (h->n_states > 0 && h->n_states != n_orient)
+        throw SpxError(SPX_ERR_INVALID_ARGUMENT, "the grid size differs from the number of per-orientation initial states");
     if (n_pulse < 0 || n_ops < 0 || (n_pulse > 0 && !pulse_ops) || (n_ops > 0 && !ops))
         throw SpxError(SPX_ERR_INVALID_ARGUMENT, "bad pulse or operation arrays");
     int64_t max_steps = 0;
@@ -1061,7 +1063,12 @@ void run_sequence(spx_handle *h, int64_t n_orient, const double *alphas, const d
     h->d_fid.reserve((size_t)max_steps + 1);
     SPX_CUDA(cudaMemcpyAsync(h->d_seq_rho.p, h->d_rho0.p, h->n_pad * sizeof(double2), cudaMemcpyDeviceToDevice,
                              h->stream));
-    bool per_orient = false;        // states differ per orientation after the first segment
+    // states differ per orientation after the first segment, or from the
+    // start with per-orientation initial states (n_states == n_orient, checked)
+    bool per_orient = h->n_states > 0;
+    if (per_orient)
+        SPX_CUDA(cudaMemcpyAsync(h->d_seq[0].p, h->d_rho0s.p, ns * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                 h->stream));
     int cur = 0;
     size_t at = 0;
     for (int i = 0; i < n_ops; ++i) {

@@ -328,9 +328,14 @@ class OperatorFactory:
     def comm_coo(self, ops) -> sp.coo_matrix:
         """Commutation superoperator of a product of single-spin operators,
         cached (it depends only on the basis and the spins' multiplicities)."""
-        key = tuple(ops)
+        return self.coo(ops, 'comm')
+
+    def coo(self, ops, kind: str) -> sp.coo_matrix:
+        """The superoperator of a product of single-spin operators ('comm',
+        'left' or 'right'), cached."""
+        key = tuple(ops) if kind == 'comm' else (kind,) + tuple(ops)
         if key not in self.op_cache:
-            self.op_cache[key] = self.operator(ops, 'comm').tocoo()
+            self.op_cache[key] = self.operator(ops, kind).tocoo()
         return self.op_cache[key]
 
     def product(self, codes: dict, side: str) -> sp.csr_matrix:
@@ -487,8 +492,11 @@ def interaction_strengths(ss: SpinSystem, assumptions: str):
                 cs[(a, b)] = 'secular'
             else:
                 cs[(a, b)] = 'strong'
+    elif assumptions == 'labframe':
+        zs = ['full'] * ss.nspins
+        cs = {(a, b): 'strong' for (a, b) in ss.couplings}
     else:
-        raise ValueError("assumptions must be 'nmr' or 'esr'")
+        raise ValueError("assumptions must be 'nmr', 'esr' or 'labframe'")
     return zs, cs
 
 
@@ -634,11 +642,13 @@ def hamiltonian_monomials(ss: SpinSystem, basis: Basis, assumptions: str) -> Ham
 
 
 def rotational_hamiltonian(ss: SpinSystem, basis: Basis, assumptions: str,
-                           factory: OperatorFactory | None = None) -> RotationalHamiltonian:
-    """Isotropic part and rotational basis (kernel/hamiltonian.m:59-790)."""
+                           factory: OperatorFactory | None = None, kind: str = 'comm') -> RotationalHamiltonian:
+    """Isotropic part and rotational basis (kernel/hamiltonian.m:59-790);
+    kind 'left' gives left-side product superoperators (hamiltonian.m's
+    'left' argument, for thermal equilibria)."""
     f = factory or OperatorFactory(ss, basis)
     groups = _term_groups(ss, assumptions)
-    op = f.comm_coo        # one superoperator per distinct operator product
+    op = lambda ops: f.coo(ops, kind)        # one superoperator per distinct operator product
 
     dim = basis.dim
 
@@ -664,6 +674,67 @@ def rotational_hamiltonian(ss: SpinSystem, basis: Basis, assumptions: str,
         if acc is not None and acc.nnz:
             aniso[key] = acc
     return RotationalHamiltonian(dim, I, aniso)
+
+
+HBAR = 6.62607015e-34 / (2 * math.pi)      # J s (kernel/utilities/tolerances.m:348)
+KBOL = 1.380649e-23                        # J/K (kernel/utilities/tolerances.m:351)
+
+
+def _wigner_all(terms, alphas, betas, gammas) -> np.ndarray:
+    """D^r_{km}(alpha_o, beta_o, gamma_o) for every term (r, k, m) and
+    orientation o, (n_terms, n_orient) complex."""
+    from .singlerot import wigner_d
+    out = np.zeros((len(terms), len(alphas)), complex)
+    for o, (a, b, g) in enumerate(zip(alphas, betas, gammas)):
+        cache = {}
+        for t, (r, k, m) in enumerate(terms):
+            if r not in cache:
+                cache[r] = wigner_d(r, a, b, g)
+            out[t, o] = cache[r][k, m]
+    return out
+
+
+def equilibrium_states(H: RotationalHamiltonian, temperature: float, alphas=None, betas=None, gammas=None):
+    """Thermal equilibrium exp(-beta H(Omega)) unit / <unit|...> for every
+    orientation (kernel/states/equilibrium.m, sphten-liouv; H made of
+    left-side product superoperators of the lab-frame Hamiltonian,
+    H(Omega) = I + herm(sum D Q) as orientation.m builds it; beta = hbar/kT).
+    Without angles: the isotropic state exp(-beta I) unit.  Taylor series in
+    substeps of at most 2 in the 1-norm, stopped below the FP64 epsilon, as
+    kernel/step.m does.  Returns (n_orient, dim), or (dim,) without angles."""
+    if not temperature:
+        raise ValueError('temperature must be specified (and non-zero)')
+    beta = HBAR / (KBOL * float(temperature))
+    dim = H.dim
+    keys = sorted(H.aniso) if alphas is not None else []
+    Qs = [sp.csr_matrix(H.aniso[k]) for k in keys]
+    QHs = [Q.conj().T.tocsr() for Q in Qs]
+    I = sp.csr_matrix(H.iso)
+    n_or = 1 if alphas is None else len(alphas)
+    D = _wigner_all(keys, alphas, betas, gammas) if keys else np.zeros((0, n_or), complex)
+    norm1 = abs(I).sum(axis=0).max() + sum(abs(Q).sum(axis=0).max() for Q in Qs)
+    nsub = max(1, int(math.ceil(float(norm1) * beta / 2)))
+    h = beta / nsub
+
+    def apply(V):
+        out = I @ V
+        for t in range(len(keys)):
+            out = out + 0.5 * ((Qs[t] @ V) * D[t][None, :] + (QHs[t] @ V) * np.conj(D[t])[None, :])
+        return out
+
+    rho = np.zeros((dim, n_or), complex)
+    rho[0] = 1.0
+    for _ in range(nsub):
+        term = rho.copy()
+        k = 1
+        while True:
+            term = (-h / k) * apply(term)
+            rho = rho + term
+            k += 1
+            if np.abs(term).max() <= np.finfo(float).eps * np.abs(rho).max() or k > 200:
+                break
+    rho = rho / rho[0][None, :]
+    return rho[:, 0] if alphas is None else rho.T.copy()
 
 
 def relaxation_diagonal(ss: SpinSystem, basis: Basis, damp_rate: float = 0.0) -> np.ndarray:

@@ -108,3 +108,34 @@ def test_reference_powder_average_case(gpu_engine):
     ss, I, Q = R.powder_setup(ss, 'nmr')
     par = dict(rho0=R.state(ss, 'L+', '1H'), coil=R.state(ss, 'L+', '1H'), sweep=2000.0, npoints=3)
     assert rel_err(fid_avg, R.powder(ss, par, 'nmr', grid, setup=(I, Q))) <= 1e-10
+
+
+def test_anisotropic_thermal_equilibrium_hp_acquire(gpu_engine):
+    """powder.m 'aniso_eq' (powder.m:244-248, states/equilibrium.m): a
+    radical at 4 K with an anisotropic g tensor starts every orientation from
+    its own Boltzmann state; a 90-degree pulse (hp_acquire.m) reads it out."""
+    import copy
+    sys_ = dict(isotopes=['E', '14N'], magnet=0.34)
+    inter = dict(zeeman=dict(eigs=[[2.0020, 2.0060, 2.0100], [0.0, 0.0, 0.0]], euler=[[0.3, 0.8, 1.1], [0, 0, 0]]),
+                 coupling=dict(eigs={(0, 1): [15e6, 15e6, 90e6]}, euler={(0, 1): [0.0, 0.4, 0.0]}),
+                 relaxation=['t1_t2'], r1_rates=[1e5, 0.0], r2_rates=[5e6, 0.0], temperature=4.0)
+    bas = dict(approximation='none', level=0)
+    spin_system = X.basis(X.create(sys_, inter), bas)
+    grid = W.zcwn_grid(16)
+    parameters = dict(grid=grid, coil=('L+', 'E'), pulse_op=('Ly', 'E'), pulse_angle=np.pi / 2, sweep=2e8,
+                      npoints=128, needs=['aniso_eq'])
+    fid, _ = X.powder(spin_system, 'hp_acquire', parameters, 'esr', engine=gpu_engine)
+    fid_iso, _ = X.powder(spin_system, 'hp_acquire', dict(parameters, needs=['iso_eq']), 'esr', engine=gpu_engine)
+    # the oracle: labframe left-product Hamiltonian, equilibrium per orientation
+    ss = R.basis(R.create(dict(sys_, enable=['krylov']), inter), dict(bas, space_level=1))
+    ssL = R.assume(copy.deepcopy(ss), 'labframe')
+    IL, QL = R.hamiltonian(ssL, 'left')
+    ss, I, Q = R.powder_setup(ss, 'esr')
+    ref = 0
+    for n in range(16):
+        ang = (grid[0][n], grid[1][n], grid[2][n])
+        par = dict(rho0=R.equilibrium(ssL, IL, QL, ang), coil=R.state(ss, 'L+', 'E'),
+                   pulse_op=R.operator(ss, 'Ly', 'E'), pulse_angle=np.pi / 2, sweep=2e8, npoints=128)
+        ref = ref + grid[3][n] * R.powder_orientation_hp_acquire(ss, I, Q, par, ang)
+    assert rel_err(fid, ref) <= 1e-10
+    assert rel_err(fid_iso, ref) > 1e-4          # the anisotropy of the equilibrium is visible
