@@ -242,9 +242,6 @@ def powder(spin_system: System, pulse_sequence, parameters: dict, assumptions: s
            precision: int = E.FP64):
     """kernel/contexts/powder.m:99-309: returns (answer, grid), the answer the
     weighted sum of the orientations' outputs (sum_up, default) or their list."""
-    if parameters.get('needs'):
-        raise ValueError("parameters.needs: evaluate the states and pass one rho0 per orientation "
-                         "(Engine.set_initial_states) instead")
     work, full, I, Q, R, rho0, coil, HL = _setup(spin_system, parameters, assumptions, _name(pulse_sequence))
     grid = _grid(parameters)
     eng = engine or E.Engine(0)
