@@ -15,7 +15,8 @@ g for electrons), coordinates (Angstrom), coupling.eigs/euler/scalar (Hz,
 keys (a, b); (a, a) is a quadratic coupling), relaxation (['t1_t2'],
 ['damp']), r1_rates, r2_rates, damp_rate.  bas: approximation ('none',
 'IK-0', 'IK-1'), level, projections.  parameters: grid (alphas, betas,
-gammas, weights), rho0 / coil (vectors, or (operator, isotope) pairs), sweep,
+gammas, weights, or a grid file), rho0 / coil (vectors, or (operator,
+isotope) pairs; rho0 may be a function of (alpha, beta, gamma)), sweep,
 npoints, spins + offset, decouple, homodec_oper + homodec_pwr, dead_time,
 needs (['iso_eq'] or ['aniso_eq'], with inter temperature),
 sum_up, pulse_op, pulse_angle, echo_time, echo_oper, echo_angle, nloops,
@@ -164,6 +165,12 @@ def _setup(spin_system: System, parameters: dict, assumptions: str, sequence: st
         # powder.m:128-147: the lab-frame Hamiltonian as left-side products
         HL = S.rotational_hamiltonian(work.ss, work.basis, 'labframe', work.factory(), kind='left')
         rho0 = S.equilibrium_states(S.RotationalHamiltonian(HL.dim, HL.iso, {}), work.temperature)
+    elif callable(parameters['rho0']):
+        # powder.m:250-252: a function handle evaluated at every orientation;
+        # the single rho0 is a placeholder (the states replace it)
+        HL = None
+        rho0 = np.zeros(work.basis.dim, complex)
+        rho0[0] = 1.0
     else:
         HL = None
         rho0 = _restrict(work, full, _vector(full, parameters['rho0']))
@@ -250,6 +257,10 @@ def powder(spin_system: System, pulse_sequence, parameters: dict, assumptions: s
         if 'aniso_eq' in (parameters.get('needs') or []):
             # powder.m:244-248: the equilibrium at every orientation
             eng.set_initial_states(S.equilibrium_states(HL, work.temperature, *grid[:3]))
+        elif callable(parameters.get('rho0')):
+            f = parameters['rho0']
+            eng.set_initial_states(np.array([_restrict(work, full, _vector(full, f(a, b, g)))
+                                             for a, b, g in zip(*grid[:3])]))
         try:
             res = _run(eng, pulse_sequence, parameters, work, full, grid, precision)
         finally:

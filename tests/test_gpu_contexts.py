@@ -139,3 +139,20 @@ def test_anisotropic_thermal_equilibrium_hp_acquire(gpu_engine):
         ref = ref + grid[3][n] * R.powder_orientation_hp_acquire(ss, I, Q, par, ang)
     assert rel_err(fid, ref) <= 1e-10
     assert rel_err(fid_iso, ref) > 1e-4          # the anisotropy of the equilibrium is visible
+
+
+def test_function_handle_rho0(gpu_engine):
+    """powder.m:250-252: rho0 given as a function of the orientation."""
+    sys_, inter, bas = _structures()
+    spin_system = X.basis(X.create(sys_, inter), bas)
+    grid = W.zcwn_grid(20)
+    lx, lz = X.state(spin_system, 'Lx', '13C'), X.state(spin_system, 'Lz', '1H')
+    rho_f = lambda a, b, g: np.cos(b) * lx + np.sin(g) * lz
+    parameters = dict(grid=grid, rho0=rho_f, coil=('L+', '13C'), sweep=2e4, npoints=150)
+    fid, _ = X.powder(spin_system, 'acquire', parameters, 'nmr', engine=gpu_engine)
+    ref = 0
+    for n in range(20):
+        one = dict(parameters, rho0=rho_f(grid[0][n], grid[1][n], grid[2][n]),
+                   grid=(grid[0][n:n + 1], grid[1][n:n + 1], grid[2][n:n + 1], np.ones(1)))
+        ref = ref + grid[3][n] * X.powder(spin_system, 'acquire', one, 'nmr', engine=gpu_engine)[0]
+    assert rel_err(fid, ref) <= 1e-12
