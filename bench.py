@@ -20,7 +20,8 @@ Reported:
              sample, one process per core);
   clocks     nvidia-smi samples during the timed steps;
   gpu_launches  kernels of this library launched in the timed region;
-  c4 / c2 / mas / sequences / surrogate  the other workloads, once each.
+  c4 / c2 / mas / sequences / deuterium / surrogate  the other workloads,
+             once each.
 
 --impl reference times the reference algorithm (the oracle's restatement of
 Spinach's default CPU branch, propagator.m + P*rho) on the host cores.
@@ -342,7 +343,7 @@ def run_gpu(args):
             cpu = {'value': nn / t, 'unit': UNIT, 'cores': cores, 'kind': 'port',
                    'sample': f'{nn} orientations of {args.workload} (one per core, all time steps), '
                              f'oracle restatement in FP64: {BRANCH_TEXT[args.workload]}'}
-        sur = c2 = c4 = mas = echoes = None
+        sur = c2 = c4 = mas = echoes = deut = None
         if not args.no_surrogate and world == 1 and args.workload == 'c1':
             sur = surrogate_leg(eng, w, local)
         if not args.no_extra and world == 1 and args.workload == 'c1':
@@ -350,6 +351,7 @@ def run_gpu(args):
             c2 = c2_leg(local)
             mas = mas_leg(local)
             echoes = echo_legs(local)
+            deut = deuterium_leg(local)
         line = {
             'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': statistics.mean(step_ms), 'higher_is_better': True,
@@ -381,6 +383,7 @@ def run_gpu(args):
             'c2': c2,
             'mas': mas,
             'sequences': echoes,
+            'deuterium': deut,
             'clocks': clk,
             'gpu_launches': 3 * args.steps,
         }
@@ -449,6 +452,28 @@ def mas_leg(device):
            'nnz': res[E.FP32][1].stats['nnz'], 'rotor_space_setup_s': t_fp}
     eng.close()
     return out
+
+
+def deuterium_leg(device):
+    """Static 2H powder pattern (quadratic coupling, dim 144, 400 orientations x 1024 steps of 2 us),
+    upload + run with host buffers, FP32 and FP64."""
+    from spinach_gb300 import engine as E, workloads as W
+    w = W.deuterium()
+    L = W.build(w)
+    eng = E.Engine(device)
+    g = W.zcwn_grid(w.n_orient)
+    eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
+    eng.run(*g, w.dt, w.nsteps, precision=E.FP32)                               # warm-up
+    res = {}
+    for p in (E.FP32, E.FP64):
+        t0 = time.perf_counter()
+        eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
+        r = eng.run(*g, w.dt, w.nsteps, precision=p)
+        res[p] = (time.perf_counter() - t0, r)
+    eng.close()
+    return {'workload': WORKLOAD_TEXT['deuterium'] + ', upload + run', 'value': w.n_orient / res[E.FP32][0],
+            'unit': UNIT, 'rel_err_vs_fp64_gpu': _rel(res[E.FP32][1].fid, res[E.FP64][1].fid),
+            'fp64_gpu': {'value': w.n_orient / res[E.FP64][0]}, 'kernel_ms': res[E.FP32][1].stats['kernel_ms']}
 
 
 def echo_legs(device):
