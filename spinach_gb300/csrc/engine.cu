@@ -1279,16 +1279,22 @@ void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const doub
     h->d_fid.reserve((size_t)npoints);
     for (int64_t b0 = 0; b0 < n_orient; b0 += batch) {
         const int64_t nb = std::min(batch, n_orient - b0);
+        // the longest chunk among those needing the fewest CTAs per orientation
+        // (FP64 accumulators of 4-step chunks push c4 from 2- to 4-CTA clusters)
         Config c{};
+        bool have = false;
         for (int m : {kTrajChunk, 2, 1}) {
             o1.chunk_steps = m;
             try {
-                c = choose_config(h, nb, tau, nsteps, o1, 0, 256, true);
-                break;
+                const Config cm = choose_config(h, nb, tau, nsteps, o1, 0, 256, true);
+                if (!have || cm.cl < c.cl) c = cm;
+                have = true;
             } catch (const SpxError &e) {
-                if (m == 1 || e.code != SPX_ERR_UNSUPPORTED) throw;
+                if (e.code != SPX_ERR_UNSUPPORTED) throw;
             }
         }
+        if (!have) throw SpxError(SPX_ERR_UNSUPPORTED, "the trajectory does not fit a cluster of 8 SMs");
+        o1.chunk_steps = c.M;
         for (int dir = 0; dir < 2; ++dir) {
             RunIO io;
             io.rho0 = dir == 0 ? h->d_seq_rho.p : h->d_coil.p;
