@@ -260,7 +260,8 @@ spx_status spx_run_sequence(spx_handle *handle, int64_t n_orient, const double *
  * fid receives the concatenated powder FIDs, npoints*(1 + 2*nloops) complex
  * values.  pulse_op is the pulse's commutation superoperator in the basis of
  * the uploaded system (operator(spin_system,'Lx',...) in Spinach).  Needs one
- * coil and the single rho0.
+ * coil; per-orientation initial states (spx_set_initial_states) are used
+ * when set.  A program on spx_run_sequence.
  */
 spx_status spx_run_cpmg(spx_handle *handle, int64_t n_orient, const double *alphas, const double *betas,
                         const double *gammas, const double *weights, double dt, int64_t npoints, int32_t nloops,
