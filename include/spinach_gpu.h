@@ -236,7 +236,8 @@ const char *spx_surrogate_last_error(const spx_surrogate *s);
  *                   coil'*rho at steps 0..nsteps to fid
  * Every orientation starts from rho0 (or its own state after
  * spx_set_initial_states); fid receives sum over recorded segments of
- * (nsteps+1) complex values.  Needs one coil.
+ * (nsteps+1) complex values; fids_per_orient (or NULL) the same for every
+ * orientation, orientation-major (powder.m sum_up = false).  Needs one coil.
  */
 enum { SPX_SEQ_PULSE = 0, SPX_SEQ_EVOLVE = 1 };
 typedef struct spx_seq_op {
@@ -251,7 +252,8 @@ typedef struct spx_seq_op {
 
 spx_status spx_run_sequence(spx_handle *handle, int64_t n_orient, const double *alphas, const double *betas,
                             const double *gammas, const double *weights, int32_t n_pulse, const spx_csc *pulse_ops,
-                            int32_t n_ops, const spx_seq_op *ops, const spx_options *opt, double *fid);
+                            int32_t n_ops, const spx_seq_op *ops, const spx_options *opt, double *fid,
+                            double *fids_per_orient);
 
 /*
  * CPMG echo train on the same evolution core (experiments/cpmg.m): a hard

@@ -215,7 +215,8 @@ def _run(eng, pulse_sequence, parameters, work, full, grid, precision):
         dt, n = 1.0 / float(parameters['sweep']), int(parameters['npoints']) - 1
         if 'dead_time' in parameters:
             prog = [('evolve', 1, float(parameters['dead_time']), False), ('evolve', n, dt)]
-            return eng.run_sequence(al, be, ga, w, [], prog, precision=precision)
+            return eng.run_sequence(al, be, ga, w, [], prog, precision=precision,
+                                    per_orientation=not parameters.get('sum_up', 1))
         return eng.run(al, be, ga, w, dt, n, precision=precision, per_orientation=not parameters.get('sum_up', 1))
     if name == 'hp_acquire':
         ops = [_restrict_matrix(work, full, _matrix(full, parameters['pulse_op']))]
@@ -225,7 +226,8 @@ def _run(eng, pulse_sequence, parameters, work, full, grid, precision):
             et = float(parameters['echo_time'])
             prog += [('evolve', 1, et, False), ('pulse', 1, float(parameters['echo_angle'])), ('evolve', 1, et, False)]
         prog.append(('evolve', int(parameters['npoints']) - 1, 1.0 / float(parameters['sweep'])))
-        return eng.run_sequence(al, be, ga, w, ops, prog, precision=precision)
+        return eng.run_sequence(al, be, ga, w, ops, prog, precision=precision,
+                                per_orientation=not parameters.get('sum_up', 1))
     if name == 'cpmg':
         P = _restrict_matrix(work, full, _matrix(full, parameters['pulse_op']))
         return eng.run_cpmg(al, be, ga, w, float(parameters['timestep']), int(parameters['npoints']),
@@ -241,7 +243,7 @@ def _answer(res, parameters):
     if parameters.get('sum_up', 1):
         return res.fid
     if res.fids is None:
-        raise ValueError('sum_up = 0 is available for acquire without a dead time')
+        raise ValueError('sum_up = 0 is available for acquire and hp_acquire')
     return list(res.fids)
 
 

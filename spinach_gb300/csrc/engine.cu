@@ -1029,15 +1029,16 @@ void upload_grid(spx_handle *h, int64_t n_orient, const double *alphas, const do
 
 void run_sequence(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
                   const double *weights, int32_t n_pulse, const spx_csc *pulse_ops, int32_t n_ops,
-                  const spx_seq_op *ops, const spx_options &o, double *fid) {
+                  const spx_seq_op *ops, const spx_options &o, double *fid, double *fids_per_orient = nullptr) {
     if (h->nchan != 1) throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil");
     if (h->n_states > 0 && h->n_states != n_orient)
         throw SpxError(SPX_ERR_INVALID_ARGUMENT, "the grid size differs from the number of per-orientation initial states");
     if (n_pulse < 0 || n_ops < 0 || (n_pulse > 0 && !pulse_ops) || (n_ops > 0 && !ops))
         throw SpxError(SPX_ERR_INVALID_ARGUMENT, "bad pulse or operation arrays");
-    int64_t max_steps = 0;
+    int64_t max_steps = 0, total = 0;
     for (int i = 0; i < n_ops; ++i) {
         const spx_seq_op &q = ops[i];
+        if (q.kind == SPX_SEQ_EVOLVE && q.record) total += q.nsteps + 1;
         if (q.kind == SPX_SEQ_PULSE) {
             if (q.pulse < 0 || q.pulse >= n_pulse) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "pulse index out of range");
             if (!std::isfinite(q.angle)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite pulse angle");
@@ -1087,9 +1088,26 @@ void run_sequence(spx_handle *h, int64_t n_orient, const double *alphas, const d
                       c, 0, true, io);
         finish_run(h);
         if (q.record) {
-            SPX_CUDA(cudaMemcpy(fid + 2 * at, h->d_fid.p, ((size_t)q.nsteps + 1) * sizeof(double2),
-                                cudaMemcpyDeviceToHost));
-            at += (size_t)q.nsteps + 1;
+            const size_t np = (size_t)q.nsteps + 1;
+            SPX_CUDA(cudaMemcpy(fid + 2 * at, h->d_fid.p, np * sizeof(double2), cudaMemcpyDeviceToHost));
+            if (fids_per_orient) {
+                // this segment's FIDs of every orientation, into each orientation's row
+                std::vector<double2> tmp(np * (size_t)n_orient);
+                if (o.precision == SPX_FP64) {
+                    SPX_CUDA(cudaMemcpy(tmp.data(), h->d_fids.p, tmp.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+                } else {
+                    std::vector<float2> t32(tmp.size());
+                    SPX_CUDA(cudaMemcpy(t32.data(), h->d_fids.p, t32.size() * sizeof(float2), cudaMemcpyDeviceToHost));
+                    for (size_t i = 0; i < t32.size(); ++i) tmp[i] = make_double2(t32[i].x, t32[i].y);
+                }
+                for (int64_t or_ = 0; or_ < n_orient; ++or_)
+                    for (size_t j = 0; j < np; ++j) {
+                        const double2 v = tmp[(size_t)or_ * np + j];
+                        fids_per_orient[2 * ((size_t)or_ * total + at + j)] = v.x;
+                        fids_per_orient[2 * ((size_t)or_ * total + at + j) + 1] = v.y;
+                    }
+            }
+            at += np;
         }
         cur ^= 1;
         per_orient = true;
@@ -1761,7 +1779,8 @@ spx_status spx_run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, c
 
 spx_status spx_run_sequence(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
                             const double *gammas, const double *weights, int32_t n_pulse, const spx_csc *pulse_ops,
-                            int32_t n_ops, const spx_seq_op *ops, const spx_options *opt, double *fid) {
+                            int32_t n_ops, const spx_seq_op *ops, const spx_options *opt, double *fid,
+                            double *fids_per_orient) {
     if (!h) return SPX_ERR_INVALID_ARGUMENT;
     return guarded(h, [&] {
         if (!alphas || !betas || !gammas || !weights || !fid) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL argument");
@@ -1775,7 +1794,8 @@ spx_status spx_run_sequence(spx_handle *h, int64_t n_orient, const double *alpha
             throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
         o = apply_tuned(h, o);
         SPX_CUDA(cudaSetDevice(h->device));
-        run_sequence(h, n_orient, alphas, betas, gammas, weights, n_pulse, pulse_ops, n_ops, ops, o, fid);
+        run_sequence(h, n_orient, alphas, betas, gammas, weights, n_pulse, pulse_ops, n_ops, ops, o, fid,
+                     fids_per_orient);
     });
 }
 

@@ -74,7 +74,7 @@ SIGNATURES = {
                                    C.POINTER(C.c_int32), C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_int32), _D, _D, _D, _D, _D]),
     'spx_run_sequence': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_int32, C.POINTER(SpxCsc), C.c_int32,
-                                   C.POINTER(SpxSeqOp), C.POINTER(SpxOptions), _D]),
+                                   C.POINTER(SpxSeqOp), C.POINTER(SpxOptions), _D, _D]),
     'spx_run_eseem': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.POINTER(SpxCsc),
                                 C.POINTER(SpxOptions), _D]),
     'spx_upload_coils': (C.c_int, [_P, C.c_int32, _D]),
@@ -295,7 +295,7 @@ class Engine:
         return PowderResult(fid.view(np.complex128), None, self.stats())
 
     def run_sequence(self, alphas, betas, gammas, weights, pulse_ops, program, precision: int = FP32,
-                     threads: int = 0, cluster: int = 0) -> PowderResult:
+                     threads: int = 0, cluster: int = 0, per_orientation: bool = False) -> PowderResult:
         """A pulse program (spx_run_sequence): ``pulse_ops`` a list of
         commutation superoperators, ``program`` a list of ``('pulse', index,
         angle)`` and ``('evolve', nsteps, dt[, record])`` entries.  ``fid`` is
@@ -319,10 +319,13 @@ class Engine:
                 raise ValueError(f'unknown program entry {op[0]!r}')
         oarr = (SpxSeqOp * max(1, len(ops)))(*ops)
         fid = np.zeros(2 * max(npts, 1))
+        fids = np.zeros(2 * max(npts, 1) * al.size) if per_orientation else None
         opt = SpxOptions(precision, 0, threads, cluster, 0.0, 0.0, 0, 0)
         self._check(self.lib.spx_run_sequence(self.h, al.size, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
-                                              len(holders), parr, len(ops), oarr, C.byref(opt), _dptr(fid)), self.h)
-        return PowderResult(fid.view(np.complex128)[:npts], None, self.stats())
+                                              len(holders), parr, len(ops), oarr, C.byref(opt), _dptr(fid),
+                                              _dptr(fids) if fids is not None else None), self.h)
+        fs = None if fids is None else fids.view(np.complex128)[:npts * al.size].reshape(al.size, npts)
+        return PowderResult(fid.view(np.complex128)[:npts], fs, self.stats())
 
     def run_eseem(self, alphas, betas, gammas, weights, timestep: float, npoints: int, pulse_op,
                   precision: int = FP32, threads: int = 0, cluster: int = 0) -> PowderResult:

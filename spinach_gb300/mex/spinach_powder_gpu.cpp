@@ -303,7 +303,7 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
         for (auto &c : prog_pulses) views.push_back(c.view);
         std::vector<double> fid(2 * (size_t)std::max<int64_t>(npts, 1));
         st = spx_run_sequence(g_handle, no, al.data(), be.data(), ga.data(), wt.data(), (int32_t)views.size(),
-                              views.data(), (int32_t)prog.size(), prog.data(), &opt, fid.data());
+                              views.data(), (int32_t)prog.size(), prog.data(), &opt, fid.data(), nullptr);
         if (st != SPX_OK)
             throw GatewayError{"Spinach:spinach_powder_gpu:run", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
         plhs[0] = mxCreateDoubleMatrix((mwSize)npts, 1, mxCOMPLEX);

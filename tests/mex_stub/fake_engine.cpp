@@ -103,7 +103,7 @@ spx_status spx_run_cpmg(spx_handle *, int64_t no, const double *, const double *
 }
 spx_status spx_run_sequence(spx_handle *, int64_t no, const double *, const double *, const double *,
                             const double *, int32_t n_pulse, const spx_csc *P, int32_t n_ops, const spx_seq_op *ops,
-                            const spx_options *opt, double *fid) {
+                            const spx_options *opt, double *fid, double *) {
     g_rec.n_orient = no;
     g_rec.precision = opt ? opt->precision : -1;
     g_rec.nloops = -2;

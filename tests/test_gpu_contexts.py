@@ -156,3 +156,24 @@ def test_function_handle_rho0(gpu_engine):
                    grid=(grid[0][n:n + 1], grid[1][n:n + 1], grid[2][n:n + 1], np.ones(1)))
         ref = ref + grid[3][n] * X.powder(spin_system, 'acquire', one, 'nmr', engine=gpu_engine)[0]
     assert rel_err(fid, ref) <= 1e-12
+
+
+def test_per_orientation_outputs_of_a_program(gpu_engine):
+    """powder.m sum_up = false for hp_acquire (a pulse program)."""
+    sys_, inter, bas = _structures()
+    spin_system = X.basis(X.create(sys_, inter), bas)
+    grid = W.zcwn_grid(12)
+    parameters = dict(grid=grid, rho0=('Lz', '13C'), coil=('L+', '13C'), pulse_op=('Ly', '13C'),
+                      pulse_angle=np.pi / 2, echo_time=2e-4, echo_oper=('Lx', '13C'), echo_angle=np.pi,
+                      sweep=2e4, npoints=90)
+    fid, _ = X.powder(spin_system, 'hp_acquire', parameters, 'nmr', engine=gpu_engine)
+    cells, _ = X.powder(spin_system, 'hp_acquire', dict(parameters, sum_up=0), 'nmr', engine=gpu_engine)
+    assert len(cells) == 12 and cells[0].shape == (90,)
+    assert np.abs(sum(w * c for w, c in zip(grid[3], cells)) - fid).max() <= 1e-12 * np.abs(fid).max()
+    ss, I, Q = _oracle(sys_, inter, bas)
+    par = dict(rho0=R.state(ss, 'Lz', '13C'), coil=R.state(ss, 'L+', '13C'), pulse_op=R.operator(ss, 'Ly', '13C'),
+               pulse_angle=np.pi / 2, echo_time=2e-4, echo_oper=R.operator(ss, 'Lx', '13C'), echo_angle=np.pi,
+               sweep=2e4, npoints=90)
+    for n in (0, 7):
+        ref = R.powder_orientation_hp_acquire(ss, I, Q, par, (grid[0][n], grid[1][n], grid[2][n]))
+        assert rel_err(cells[n], ref) <= 1e-10
