@@ -263,23 +263,25 @@ spx_status spx_run_sequence(spx_handle *handle, int64_t n_orient, const double *
  * values.  pulse_op is the pulse's commutation superoperator in the basis of
  * the uploaded system (operator(spin_system,'Lx',...) in Spinach).  Needs one
  * coil; per-orientation initial states (spx_set_initial_states) are used
- * when set.  A program on spx_run_sequence.
+ * when set.  A program on spx_run_sequence; fids_per_orient (or NULL) as
+ * there.
  */
 spx_status spx_run_cpmg(spx_handle *handle, int64_t n_orient, const double *alphas, const double *betas,
                         const double *gammas, const double *weights, double dt, int64_t npoints, int32_t nloops,
-                        const spx_csc *pulse_op, const spx_options *opt, double *fid);
+                        const spx_csc *pulse_op, const spx_options *opt, double *fid, double *fids_per_orient);
 
 /*
  * Two-pulse echo (experiments/esr_dipolar/eseem.m): a 90-degree pulse
  * exp(-1i*(pi/2)*pulse_op) on rho0, a trajectory of npoints-1 steps of
  * timestep/2, a 180-degree pulse on every state of it and the refocusing of
  * state n by n more steps; fid[n] = coil' * that state, powder-summed
- * (npoints complex values).  Needs one coil and the single rho0; the
- * dimension is limited to 8192.
+ * (npoints complex values); fids_per_orient (or NULL) receives every
+ * orientation's echoes, orientation-major.  Needs one coil and the single
+ * rho0; the dimension is limited to 8192.
  */
 spx_status spx_run_eseem(spx_handle *handle, int64_t n_orient, const double *alphas, const double *betas,
                          const double *gammas, const double *weights, double timestep, int64_t npoints,
-                         const spx_csc *pulse_op, const spx_options *opt, double *fid);
+                         const spx_csc *pulse_op, const spx_options *opt, double *fid, double *fids_per_orient);
 
 /*
  * Per-orientation initial states (kernel/contexts/powder.m:244-254: the

@@ -231,11 +231,12 @@ def _run(eng, pulse_sequence, parameters, work, full, grid, precision):
     if name == 'cpmg':
         P = _restrict_matrix(work, full, _matrix(full, parameters['pulse_op']))
         return eng.run_cpmg(al, be, ga, w, float(parameters['timestep']), int(parameters['npoints']),
-                            int(parameters['nloops']), P, precision=precision)
+                            int(parameters['nloops']), P, precision=precision,
+                            per_orientation=not parameters.get('sum_up', 1))
     if name == 'eseem':
         P = _restrict_matrix(work, full, _matrix(full, parameters['pulse_op']))
         return eng.run_eseem(al, be, ga, w, float(parameters['timestep']), int(parameters['npoints']), P,
-                             precision=precision)
+                             precision=precision, per_orientation=not parameters.get('sum_up', 1))
     raise ValueError(f'pulse sequence {pulse_sequence!r} is not supported on this engine')
 
 
@@ -243,7 +244,7 @@ def _answer(res, parameters):
     if parameters.get('sum_up', 1):
         return res.fid
     if res.fids is None:
-        raise ValueError('sum_up = 0 is available for acquire and hp_acquire')
+        raise ValueError('no per-orientation outputs for this sequence')
     return list(res.fids)
 
 

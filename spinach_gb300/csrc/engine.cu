@@ -1119,7 +1119,7 @@ void run_sequence(spx_handle *h, int64_t n_orient, const double *alphas, const d
 // (npoints + 2*npoints*nloops points).
 void run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
               const double *weights, double dt, int64_t npoints, int32_t nloops, const spx_csc *pulse_op,
-              const spx_options &o, double *fid) {
+              const spx_options &o, double *fid, double *fids_per_orient) {
     // experiments/cpmg.m:77-90: both positive integers
     if (npoints < 1 || nloops < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "npoints and nloops must be positive");
     std::vector<spx_seq_op> prog;
@@ -1144,7 +1144,8 @@ void run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, const doubl
         pulse(M_PI);
         evolve(2 * npoints - 1);
     }
-    run_sequence(h, n_orient, alphas, betas, gammas, weights, 1, pulse_op, (int32_t)prog.size(), prog.data(), o, fid);
+    run_sequence(h, n_orient, alphas, betas, gammas, weights, 1, pulse_op, (int32_t)prog.size(), prog.data(), o, fid,
+                 fids_per_orient);
 }
 
 // Echo detection (experiments/esr_dipolar/eseem.m): the stack of half-echo
@@ -1223,7 +1224,7 @@ constexpr int kTrajChunk = 4;       // steps per chunk of trajectory outputs (fa
 
 void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
                const double *weights, double timestep, int64_t npoints, const spx_csc *pulse_op,
-               const spx_options &o, double *fid) {
+               const spx_options &o, double *fid, double *fids_per_orient) {
     if (h->nchan != 1 || h->n_states != 0)
         throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil and one initial state");
     if (npoints < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "npoints must be positive");
@@ -1333,6 +1334,9 @@ void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const doub
         (int)n_orient, (int)npoints, h->d_echo_f.p, g + 3 * n_orient, h->d_fid.p);
     SPX_CUDA(cudaGetLastError());
     SPX_CUDA(cudaMemcpyAsync(fid, h->d_fid.p, (size_t)npoints * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    if (fids_per_orient)
+        SPX_CUDA(cudaMemcpyAsync(fids_per_orient, h->d_echo_f.p, (size_t)n_orient * npoints * sizeof(double2),
+                                 cudaMemcpyDeviceToHost, h->stream));
     SPX_CUDA(cudaStreamSynchronize(h->stream));
 }
 
@@ -1758,7 +1762,7 @@ const char *spx_version(void) { return "spinach-gb300 0.1 (sm_103a)"; }
 
 spx_status spx_run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
                         const double *gammas, const double *weights, double dt, int64_t npoints, int32_t nloops,
-                        const spx_csc *pulse_op, const spx_options *opt, double *fid) {
+                        const spx_csc *pulse_op, const spx_options *opt, double *fid, double *fids_per_orient) {
     if (!h) return SPX_ERR_INVALID_ARGUMENT;
     return guarded(h, [&] {
         if (!alphas || !betas || !gammas || !weights || !fid || !pulse_op)
@@ -1773,7 +1777,7 @@ spx_status spx_run_cpmg(spx_handle *h, int64_t n_orient, const double *alphas, c
             throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
         o = apply_tuned(h, o);
         SPX_CUDA(cudaSetDevice(h->device));
-        run_cpmg(h, n_orient, alphas, betas, gammas, weights, dt, npoints, nloops, pulse_op, o, fid);
+        run_cpmg(h, n_orient, alphas, betas, gammas, weights, dt, npoints, nloops, pulse_op, o, fid, fids_per_orient);
     });
 }
 
@@ -1801,7 +1805,7 @@ spx_status spx_run_sequence(spx_handle *h, int64_t n_orient, const double *alpha
 
 spx_status spx_run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
                          const double *gammas, const double *weights, double timestep, int64_t npoints,
-                         const spx_csc *pulse_op, const spx_options *opt, double *fid) {
+                         const spx_csc *pulse_op, const spx_options *opt, double *fid, double *fids_per_orient) {
     if (!h) return SPX_ERR_INVALID_ARGUMENT;
     return guarded(h, [&] {
         if (!alphas || !betas || !gammas || !weights || !fid || !pulse_op)
@@ -1815,7 +1819,7 @@ spx_status spx_run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, 
         if (o.precision != SPX_FP32 && o.precision != SPX_FP64)
             throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
         SPX_CUDA(cudaSetDevice(h->device));
-        run_eseem(h, n_orient, alphas, betas, gammas, weights, timestep, npoints, pulse_op, o, fid);
+        run_eseem(h, n_orient, alphas, betas, gammas, weights, timestep, npoints, pulse_op, o, fid, fids_per_orient);
     });
 }
 

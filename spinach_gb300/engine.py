@@ -68,7 +68,7 @@ SIGNATURES = {
     'spx_run_powder_noalloc': (C.c_int, [_P, C.c_int64, _P, _P, _P, _P, C.c_double, C.c_int64,
                                          C.c_int32, _P]),
     'spx_run_cpmg': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.c_int32,
-                               C.POINTER(SpxCsc), C.POINTER(SpxOptions), _D]),
+                               C.POINTER(SpxCsc), C.POINTER(SpxOptions), _D, _D]),
     'spx_build_system': (C.c_int, [_P, C.c_int32, C.POINTER(C.c_int32), C.c_int64, C.POINTER(C.c_int64),
                                    C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_int32), C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
@@ -76,7 +76,7 @@ SIGNATURES = {
     'spx_run_sequence': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_int32, C.POINTER(SpxCsc), C.c_int32,
                                    C.POINTER(SpxSeqOp), C.POINTER(SpxOptions), _D, _D]),
     'spx_run_eseem': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.POINTER(SpxCsc),
-                                C.POINTER(SpxOptions), _D]),
+                                C.POINTER(SpxOptions), _D, _D]),
     'spx_upload_coils': (C.c_int, [_P, C.c_int32, _D]),
     'spx_set_initial_states': (C.c_int, [_P, C.c_int64, _D]),
     'spx_autotune': (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_double, C.c_int64, C.c_int32,
@@ -277,7 +277,8 @@ class Engine:
         return PowderResult(f, fs, self.stats())
 
     def run_cpmg(self, alphas, betas, gammas, weights, dt: float, npoints: int, nloops: int, pulse_op,
-                 precision: int = FP32, threads: int = 0, cluster: int = 0) -> PowderResult:
+                 precision: int = FP32, threads: int = 0, cluster: int = 0,
+                 per_orientation: bool = False) -> PowderResult:
         """CPMG echo train (experiments/cpmg.m): 90-degree pulse about ``pulse_op``
         (a commutation superoperator), npoints-1 steps, then ``nloops`` times a
         180-degree pulse and 2*npoints-1 steps.  ``fid`` holds the concatenated
@@ -286,13 +287,16 @@ class Engine:
         be = np.ascontiguousarray(betas, np.float64)
         ga = np.ascontiguousarray(gammas, np.float64)
         w = np.ascontiguousarray(weights, np.float64)
-        fid = np.zeros(2 * npoints * (1 + 2 * nloops))
+        npts = npoints * (1 + 2 * nloops)
+        fid = np.zeros(2 * npts)
+        fids = np.zeros(2 * npts * al.size) if per_orientation else None
         P = _CscHolder(pulse_op, self.dim)
         opt = SpxOptions(precision, 0, threads, cluster, 0.0, 0.0, 0, 0)
         self._check(self.lib.spx_run_cpmg(self.h, al.size, _dptr(al), _dptr(be), _dptr(ga), _dptr(w), float(dt),
-                                          int(npoints), int(nloops), C.byref(P.struct), C.byref(opt), _dptr(fid)),
-                    self.h)
-        return PowderResult(fid.view(np.complex128), None, self.stats())
+                                          int(npoints), int(nloops), C.byref(P.struct), C.byref(opt), _dptr(fid),
+                                          _dptr(fids) if fids is not None else None), self.h)
+        fs = None if fids is None else fids.view(np.complex128).reshape(al.size, npts)
+        return PowderResult(fid.view(np.complex128), fs, self.stats())
 
     def run_sequence(self, alphas, betas, gammas, weights, pulse_ops, program, precision: int = FP32,
                      threads: int = 0, cluster: int = 0, per_orientation: bool = False) -> PowderResult:
@@ -328,7 +332,8 @@ class Engine:
         return PowderResult(fid.view(np.complex128)[:npts], fs, self.stats())
 
     def run_eseem(self, alphas, betas, gammas, weights, timestep: float, npoints: int, pulse_op,
-                  precision: int = FP32, threads: int = 0, cluster: int = 0) -> PowderResult:
+                  precision: int = FP32, threads: int = 0, cluster: int = 0,
+                  per_orientation: bool = False) -> PowderResult:
         """Two-pulse echo (experiments/esr_dipolar/eseem.m): ``fid[n]`` is the powder
         echo after a 90-degree pulse, n steps of timestep/2, a 180-degree pulse
         and n more steps (npoints values)."""
@@ -337,12 +342,14 @@ class Engine:
         ga = np.ascontiguousarray(gammas, np.float64)
         w = np.ascontiguousarray(weights, np.float64)
         fid = np.zeros(2 * npoints)
+        fids = np.zeros(2 * npoints * al.size) if per_orientation else None
         P = _CscHolder(pulse_op, self.dim)
         opt = SpxOptions(precision, 0, threads, cluster, 0.0, 0.0, 0, 0)
         self._check(self.lib.spx_run_eseem(self.h, al.size, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
                                            float(timestep), int(npoints), C.byref(P.struct), C.byref(opt),
-                                           _dptr(fid)), self.h)
-        return PowderResult(fid.view(np.complex128), None, self.stats())
+                                           _dptr(fid), _dptr(fids) if fids is not None else None), self.h)
+        fs = None if fids is None else fids.view(np.complex128).reshape(al.size, npoints)
+        return PowderResult(fid.view(np.complex128), fs, self.stats())
 
     def run_device(self, d_alphas: int, d_betas: int, d_gammas: int, d_weights: int, n_orient: int,
                    dt: float, nsteps: int, d_fid: int, precision: int = FP32, chunk_steps: int = 0,

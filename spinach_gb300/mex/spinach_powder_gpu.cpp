@@ -314,7 +314,7 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     if (eseem) {
         std::vector<double> fid(2 * (size_t)(nsteps + 1));
         st = spx_run_eseem(g_handle, no, al.data(), be.data(), ga.data(), wt.data(), dt, nsteps + 1, &pulse.view, &opt,
-                           fid.data());
+                           fid.data(), nullptr);
         if (st != SPX_OK)
             throw GatewayError{"Spinach:spinach_powder_gpu:run", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
         plhs[0] = mxCreateDoubleMatrix((mwSize)(nsteps + 1), 1, mxCOMPLEX);
@@ -326,7 +326,7 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
         const int64_t npts = (nsteps + 1) * (1 + 2 * (int64_t)nloops);
         std::vector<double> fid(2 * (size_t)npts);
         st = spx_run_cpmg(g_handle, no, al.data(), be.data(), ga.data(), wt.data(), dt, nsteps + 1, nloops,
-                          &pulse.view, &opt, fid.data());
+                          &pulse.view, &opt, fid.data(), nullptr);
         if (st != SPX_OK)
             throw GatewayError{"Spinach:spinach_powder_gpu:run", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
         plhs[0] = mxCreateDoubleMatrix((mwSize)npts, 1, mxCOMPLEX);

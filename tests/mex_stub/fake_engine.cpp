@@ -91,7 +91,7 @@ spx_status spx_run_powder(spx_handle *, int64_t no, const double *a, const doubl
 }
 spx_status spx_run_cpmg(spx_handle *, int64_t no, const double *, const double *, const double *, const double *,
                         double dt, int64_t npoints, int32_t nloops, const spx_csc *P, const spx_options *opt,
-                        double *fid) {
+                        double *fid, double *) {
     g_rec.n_orient = no;
     g_rec.dt = dt;
     g_rec.npoints = npoints;
@@ -125,7 +125,8 @@ spx_status spx_run_sequence(spx_handle *, int64_t no, const double *, const doub
     return SPX_OK;
 }
 spx_status spx_run_eseem(spx_handle *, int64_t no, const double *, const double *, const double *, const double *,
-                         double dt, int64_t npoints, const spx_csc *P, const spx_options *opt, double *fid) {
+                         double dt, int64_t npoints, const spx_csc *P, const spx_options *opt, double *fid,
+                         double *) {
     g_rec.n_orient = no;
     g_rec.dt = dt;
     g_rec.npoints = npoints;

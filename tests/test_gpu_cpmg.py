@@ -135,3 +135,13 @@ def test_program_identities(gpu_engine):
     assert res.fid.shape == (1 + 16 + 26,)
     want = np.concatenate([plain[:1], plain[:16], plain[15:41]])
     assert rel_err(res.fid, want) <= 1e-13
+
+
+def test_cpmg_per_orientation_fids(gpu_engine):
+    w = W.c0()
+    L, ss, I, Q, pulse, pulse_o, rho0 = _case(w, krylov=False)
+    g = W.zcwn_grid(7)
+    gpu_engine.upload(L.I, L.terms, L.R, rho0, L.coil)
+    res = gpu_engine.run_cpmg(*g, w.dt, 16, 2, pulse, precision=E.FP64, per_orientation=True)
+    assert res.fids.shape == (7, 80)
+    assert np.abs((g[3][:, None] * res.fids).sum(axis=0) - res.fid).max() <= 1e-12 * np.abs(res.fid).max()

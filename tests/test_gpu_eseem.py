@@ -68,3 +68,13 @@ def test_eseem_argument_checks(gpu_engine):
     gpu_engine.upload_coils([coil, coil])
     with pytest.raises(E.SpxError):
         gpu_engine.run_eseem(*g, 1e-5, 8, pulse)
+
+
+def test_eseem_per_orientation_echoes(gpu_engine):
+    w = W.c0()
+    L, ss, I, Q, pulse, rho0, coil = _case(w, '13C', krylov=False)
+    g = W.zcwn_grid(9)
+    gpu_engine.upload(L.I, L.terms, L.R, rho0, coil)
+    res = gpu_engine.run_eseem(*g, 20e-6, 40, pulse, precision=E.FP64, per_orientation=True)
+    assert res.fids.shape == (9, 40)
+    assert np.abs((g[3][:, None] * res.fids).sum(axis=0) - res.fid).max() <= 1e-12 * np.abs(res.fid).max()
