@@ -1128,6 +1128,46 @@ def powder_orientation_eseem(ss, I, Q, parameters, angles) -> np.ndarray:
     return eseem(ss, parameters, H, relaxation(ss))
 
 
+def floquet_orientation_fid(ss, I, Q, parameters, angles) -> np.ndarray:
+    """One orientation of kernel/contexts/floquet.m:94-186 with @acquire:
+    Fourier components of the rotor-frame Hamiltonian up to the highest
+    interaction rank, F = sum_h kron(spdiags(1, h), T_h) + M, states in the
+    zeroth Fourier component."""
+    int_ranks = [r for r in sorted(Q) if any(q is not None and q.nnz for row in Q[r] for q in row)]
+    max_int = max(int_ranks + [2])
+    mr = parameters['max_rank']
+    N = 2 * mr + 1
+    dim = I.shape[0]
+    x, y, z = parameters['axis']
+    phi = math.atan2(y, x)
+    theta = math.pi / 2 - math.atan2(z, math.hypot(x, y))
+    M = 2 * np.pi * parameters['rate'] * sp.kron(sp.diags(np.arange(-mr, mr + 1, dtype=float)), sp.identity(dim))
+    T = [sp.csc_matrix((dim, dim), dtype=complex) for _ in range(2 * max_int + 1)]
+    for r in int_ranks:
+        L2R = wigner(r, phi, theta, 0)
+        R2L = L2R.conj().T
+        Dm = L2R @ wigner(r, *angles) @ R2L
+        for n in range(2 * r + 1):
+            Dr = np.zeros((2 * r + 1, 2 * r + 1))
+            Dr[n, n] = 1.0
+            D = L2R @ Dr @ R2L @ Dm
+            for m in range(2 * r + 1):
+                for k in range(2 * r + 1):
+                    if Q[r][k][m] is not None:
+                        T[n - r + max_int] = T[n - r + max_int] + Q[r][k][m] * D[k, m]
+    T[max_int] = T[max_int] + I
+    F = sp.csc_matrix((N * dim, N * dim), dtype=complex)
+    for h in range(2 * max_int + 1):
+        d = h - max_int
+        F = F + sp.kron(sp.diags(np.ones(N - abs(d)), d, shape=(N, N)), T[h])
+    F = clean_up(ss, sp.csc_matrix(F + M), ss.tols['liouv_zero'])
+    Rf = sp.kron(sp.identity(N), relaxation(ss))
+    e = np.zeros(N)
+    e[(N - 1) // 2] = 1.0
+    par = dict(parameters, rho0=np.kron(e, parameters['rho0']), coil=np.kron(e, parameters['coil']))
+    return acquire(ss, par, F, Rf)
+
+
 def powder(ss: SpinSystem, parameters: dict, assumptions: str, grid, setup=None,
            sum_up: bool = True):
     """kernel/contexts/powder.m:99-309 with pulse_sequence=@acquire, serial order.

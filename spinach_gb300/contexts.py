@@ -4,8 +4,9 @@
 input structures (kernel/create.m, kernel/basis.m) as dicts, with 0-based spin
 indices in the coupling keys; ``state`` and ``operator`` build Liouville
 vectors and commutation superoperators (kernel/state.m, kernel/operator.m);
-``powder(spin_system, pulse_sequence, parameters, assumptions)`` and
-``singlerot(...)`` run the contexts (kernel/contexts/powder.m, singlerot.m)
+``powder(spin_system, pulse_sequence, parameters, assumptions)``,
+``singlerot(...)`` and ``floquet(...)`` run the contexts
+(kernel/contexts/powder.m, singlerot.m, floquet.m)
 with the pulse sequences ``'acquire'``, ``'hp_acquire'``, ``'cpmg'`` and
 ``'eseem'`` (experiments/*.m), the parameters named as there.  Every
 orientation runs on the GPU; the host only prepares the system.
@@ -292,6 +293,30 @@ def singlerot(spin_system: System, pulse_sequence, parameters: dict, assumptions
     eng = engine or E.Engine(0)
     try:
         eng.upload(*fp)
+        res = _run(eng, 'acquire', parameters, work, full, grid, precision)
+    finally:
+        if engine is None:
+            eng.close()
+    return _answer(res, parameters), grid
+
+
+def floquet(spin_system: System, pulse_sequence, parameters: dict, assumptions: str, engine=None,
+            precision: int = E.FP64):
+    """kernel/contexts/floquet.m with acquire: the Floquet problem of rate,
+    axis and max_rank (Fourier components of the rotor-frame Hamiltonian), in
+    the engine's upload form."""
+    if _name(pulse_sequence) != 'acquire':
+        raise ValueError('floquet runs acquire on this engine')
+    if parameters.get('needs'):
+        raise ValueError('floquet takes an explicit rho0 on this engine')
+    work, full, I, Q, R, rho0, coil, _ = _setup(spin_system, parameters, assumptions, 'acquire')
+    grid = ((np.zeros(1), np.zeros(1), np.zeros(1), np.ones(1)) if parameters.get('grid') == 'single_crystal'
+            else _grid(parameters))
+    fs = SR.floquet_system(I, Q, R, rho0, coil, int(parameters['max_rank']), float(parameters['rate']),
+                           parameters['axis'])
+    eng = engine or E.Engine(0)
+    try:
+        eng.upload(*fs)
         res = _run(eng, 'acquire', parameters, work, full, grid, precision)
     finally:
         if engine is None:

@@ -118,3 +118,65 @@ def fokker_planck(I, terms: dict, R, rho0, coil, max_rank: int, rate: float, axi
     rho0_fp = np.kron(space, np.asarray(rho0, complex))
     coil_fp = np.kron(np.ones(N), np.asarray(coil, complex))
     return I_fp, out, R_fp, rho0_fp, coil_fp
+
+
+def floquet_system(I, terms: dict, R, rho0, coil, max_rank: int, rate: float, axis):
+    """Floquet MAS (kernel/contexts/floquet.m:94-186) in the engine's upload
+    form.  The Floquet Liouvillian of an orientation is
+
+        F = sum_h kron(S_h, T_h(Omega)) + M,  M = 2*pi*rate*kron(diag(-N..N), 1),
+
+    S_h the shift by h in the (2N+1)-dimensional Fourier space, T_0 containing
+    I, and T_{n-r} (n = 0..2r) += sum_{k,m} D(k,m) Q{r}{k,m} with
+    D = D_lab2rot P_n D_rot2lab (D_lab2rot D_mol2rot(Omega) D_rot2lab).  With
+    A_n = D_lab2rot P_n D_rot2lab D_lab2rot and B = D_rot2lab,
+    D(k,m) = sum_{j,l} A_n(k,j) D_mol2rot(j,l) B(l,m): the orientation enters
+    through D_mol2rot alone, so F = I' + sum D_mol2rot(j,l) Q'{r}{j,l}.  The
+    states live in the zeroth Fourier component (floquet.m:142-148)."""
+    if max_rank < 0 or int(max_rank) != max_rank:
+        raise ValueError('max_rank must be a non-negative integer')
+    ranks = sorted({key[0] for key in terms})
+    max_int = max(ranks + [2])
+    if max_int > max_rank:
+        raise ValueError('max_rank must be at least the highest interaction rank')
+    N = 2 * int(max_rank) + 1
+    dim = I.shape[0]
+    phi, theta = rotor_axis_angles(axis)
+    def shift(d):
+        return sp.diags(np.ones(N - abs(d)), d, shape=(N, N), format='csr')
+    M = 2 * np.pi * rate * sp.kron(sp.diags(np.arange(-max_rank, max_rank + 1, dtype=float)), sp.identity(dim))
+    I_f = (sp.kron(sp.identity(N), sp.csr_matrix(I)) + M).tocsr()
+    out = {}
+    for r in ranks:
+        L2R = wigner_d(r, phi, theta, 0.0)
+        R2L = L2R.conj().T
+        A = []
+        for n in range(2 * r + 1):
+            Pn = np.zeros((2 * r + 1, 2 * r + 1))
+            Pn[n, n] = 1.0
+            A.append(L2R @ Pn @ R2L @ L2R)
+        for j in range(2 * r + 1):
+            for l in range(2 * r + 1):
+                acc = None
+                for n in range(2 * r + 1):
+                    blk = None
+                    for k in range(2 * r + 1):
+                        for m in range(2 * r + 1):
+                            Q = terms.get((r, k, m))
+                            c = A[n][k, j] * R2L[l, m]
+                            if Q is None or abs(c) == 0:
+                                continue
+                            blk = c * Q if blk is None else blk + c * Q
+                    if blk is None:
+                        continue
+                    term = sp.kron(shift(n - r), sp.csr_matrix(blk))
+                    acc = term if acc is None else acc + term
+                if acc is not None:
+                    acc = sp.csr_matrix(acc)
+                    acc.eliminate_zeros()
+                    if acc.nnz:
+                        out[(r, j, l)] = acc
+    R_f = None if R is None else sp.kron(sp.identity(N), sp.csr_matrix(R), format='csr')
+    centre = np.zeros(N)
+    centre[N // 2] = 1.0
+    return I_f, out, R_f, np.kron(centre, np.asarray(rho0, complex)), np.kron(centre, np.asarray(coil, complex))

@@ -83,6 +83,34 @@ def test_singlerot_reference_single_crystal_case(gpu_engine):
     assert fid.shape == (3,) and abs(fid[0] - np.vdot(rho, rho)) <= 1e-12 and np.all(np.isfinite(fid))
 
 
+def test_floquet_context_matches_oracle(gpu_engine):
+    """kernel/contexts/floquet.m through the context API on the reference's
+    14-point Lebedev grid, against the oracle's per-orientation Floquet
+    restatement."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'grid_leb_2ang_rank_5.npz'))
+    grid = (d['alphas'], d['betas'], d['gammas'], d['weights'])
+    sys_ = dict(isotopes=['1H', '13C'], magnet=14.1)
+    inter = dict(zeeman=dict(eigs=[[-20.0, -10.0, 30.0], [40.0, -60.0, 20.0]],
+                             euler=[[0.0, 0.0, 0.0], [0.3, 0.9, 1.7]]),
+                 coordinates=[[0.0, 0.0, 0.0], [1.1, 0.0, 0.2]])
+    bas = dict(approximation='none')
+    spin_system = X.basis(X.create(sys_, inter), bas)
+    parameters = dict(rho0=X.state(spin_system, 'Lx', '13C'), coil=X.state(spin_system, 'L+', '13C'),
+                      sweep=50e3, npoints=64, rate=10e3, axis=(1, 1, 1), max_rank=3, grid=grid)
+    fid, g = X.floquet(spin_system, 'acquire', parameters, 'nmr', engine=gpu_engine)
+    ss = R.basis(R.create(dict(sys_, enable=[]), inter), bas)
+    ss, I, Q = R.powder_setup(ss, 'nmr')
+    par = dict(rho0=R.state(ss, 'Lx', '13C'), coil=R.state(ss, 'L+', '13C'), sweep=50e3, npoints=64,
+               rate=10e3, axis=(1, 1, 1), max_rank=3)
+    ref = sum(g[3][i] * R.floquet_orientation_fid(ss, I, Q, par, (g[0][i], g[1][i], g[2][i]))
+              for i in range(g[3].size))
+    assert np.abs(ref).max() > 0.05
+    assert rel_err(fid, ref) <= 1e-10
+    one, _ = X.floquet(spin_system, 'acquire', dict(parameters, grid='single_crystal'), 'nmr', engine=gpu_engine)
+    assert rel_err(one, R.floquet_orientation_fid(ss, I, Q, par, (0.0, 0.0, 0.0))) <= 1e-10
+
+
 def test_reference_powder_average_case(gpu_engine):
     """tests/kernel/test_ctx_powder_average.m: on the reference's 14-point
     Lebedev grid (kernel/grids/leb_2ang_rank_5.mat, copied into a fixture)

@@ -1,5 +1,7 @@
 """Magic-angle spinning (kernel/contexts/singlerot.m, Fokker-Planck) through the
 engine: the rotor-space Liouvillian in upload form runs on the same kernels."""
+import math
+
 import numpy as np
 import pytest
 
@@ -47,3 +49,42 @@ def test_reference_single_crystal_case(gpu_engine):
     assert fid.shape == (3,)
     assert abs(fid[0] - np.vdot(rho0, rho0)) <= 1e-12
     assert np.all(np.isfinite(fid))
+
+
+def _rotor_frame_angles(angles, axis):
+    """Euler angles of the rotation whose Wigner matrix is
+    D(angles) * D_rot2lab: floquet.m moves the crystallite into the rotor
+    frame with a trailing D_rot2lab that singlerot.m does not apply, so the
+    same crystallite carries these angles in singlerot.m."""
+    phi, theta = SR.rotor_axis_angles(axis)
+    D = SR.wigner_d(1, *angles) @ SR.wigner_d(1, phi, theta, 0.0).conj().T
+    b = math.acos(max(-1.0, min(1.0, D[1, 1].real)))
+    d = SR.wigner_d(1, 0.0, b, 0.0)
+    return -np.angle(D[0, 1] / d[0, 1]), b, -np.angle(D[1, 0] / d[1, 0])
+
+
+def test_floquet_mas_matches_oracle_and_fokker_planck(gpu_engine):
+    """floquet.m (Fourier components) on the engine against the oracle's
+    restatement, and against the Fokker-Planck rotor grid of singlerot.m for
+    the same crystallites, which describes the same spinning sample."""
+    w = W.c0()
+    L = W.build(w)
+    axis, rate = (1.0, 1.0, 1.0), 12.5e3
+    ss, I, Q = oracle_system(w, krylov=True)
+    al, be, ga, _ = W.zcwn_grid(w.n_orient)
+    sel = np.array([7, 66, 131])
+    g = (al[sel], be[sel], ga[sel], np.array([0.25, 0.35, 0.4]))
+    nsteps = 160
+    par = dict(rho0=R.state(ss, *w.rho0), coil=R.state(ss, *w.coil), sweep=1 / w.dt, npoints=nsteps + 1,
+               rate=rate, axis=axis, max_rank=4)
+    ref = sum(g[3][i] * R.floquet_orientation_fid(ss, I, Q, par, (g[0][i], g[1][i], g[2][i])) for i in range(3))
+    gpu_engine.upload(*SR.floquet_system(L.I, L.terms, L.R, L.rho0, L.coil, 4, rate, axis))
+    for prec, tol in ((E.FP64, 1e-10), (E.FP32, 1e-5)):
+        assert rel_err(gpu_engine.run(*g, w.dt, nsteps, precision=prec).fid, ref) <= tol, prec
+    # both MAS treatments, converged in the rotor rank, give the same signal
+    gpu_engine.upload(*SR.floquet_system(L.I, L.terms, L.R, L.rho0, L.coil, 12, rate, axis))
+    f_fl = gpu_engine.run(*g, w.dt, nsteps, precision=E.FP64).fid
+    mapped = np.array([_rotor_frame_angles((g[0][i], g[1][i], g[2][i]), axis) for i in range(3)])
+    gpu_engine.upload(*SR.fokker_planck(L.I, L.terms, L.R, L.rho0, L.coil, 12, rate, axis))
+    f_fp = gpu_engine.run(mapped[:, 0], mapped[:, 1], mapped[:, 2], g[3], w.dt, nsteps, precision=E.FP64).fid
+    assert rel_err(f_fl, f_fp) <= 1e-5

@@ -103,3 +103,38 @@ def test_grid_file_round_trip(tmp_path):
     sio.savemat(path, {'alphas': cols['alphas']})
     with pytest.raises(ValueError):
         X.load_grid(path)
+
+
+def test_floquet_liouvillian_matches_oracle():
+    """floquet.m's F = sum_h kron(S_h, T_h) + M assembled from the upload form
+    equals the oracle's literal construction at an orientation, and F is
+    Hermitian (the engine's Hermitisation leaves it unchanged)."""
+    w = W.c0()
+    L = W.build(w)
+    par = dict(max_rank=3, rate=12.5e3, axis=(1.0, 1.0, 1.0))
+    I_f, terms, R_f, rho0, coil = SR.floquet_system(L.I, L.terms, L.R, L.rho0, L.coil, **par)
+    ss, I, Q = oracle_system(w)
+    ang = (0.3, 1.1, -0.7)
+    A = I_f.toarray().astype(complex)
+    for (r, j, m), Qp in terms.items():
+        A += SR.wigner_d(r, *ang)[j, m] * Qp.toarray()
+    # the oracle's Floquet matrix, rebuilt the same way floquet_orientation_fid does
+    N, dim = 7, L.dim
+    phi, th = SR.rotor_axis_angles(par['axis'])
+    T = [np.zeros((dim, dim), complex) for _ in range(5)]
+    for r in sorted(Q):
+        L2R = R.wigner(r, phi, th, 0)
+        Dm = L2R @ R.wigner(r, *ang) @ L2R.conj().T
+        for n in range(2 * r + 1):
+            Dr = np.zeros((2 * r + 1, 2 * r + 1)); Dr[n, n] = 1
+            D = L2R @ Dr @ L2R.conj().T @ Dm
+            for k in range(2 * r + 1):
+                for mm in range(2 * r + 1):
+                    if Q[r][k][mm] is not None:
+                        T[n - r + 2] += D[k, mm] * Q[r][k][mm].toarray()
+    T[2] += I.toarray()
+    F = sum(np.kron(np.eye(N, k=h - 2), T[h]) for h in range(5))
+    F = F + 2 * np.pi * par['rate'] * np.kron(np.diag(np.arange(-3, 4, dtype=float)), np.eye(dim))
+    assert np.abs(A - F).max() <= 1e-12 * np.abs(F).max()
+    assert np.abs(F - F.conj().T).max() <= 1e-10 * np.abs(F).max()
+    assert rho0.shape == (N * dim,) and np.isclose(np.vdot(coil, rho0), np.vdot(L.coil, L.rho0))
