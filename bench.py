@@ -424,32 +424,50 @@ def c4_leg(device):
 
 
 def mas_leg(device):
-    """Magic-angle spinning (singlerot.m Fokker-Planck): the c0 system at 10 kHz about (1,1,1), rotor
-    rank 8 (17 rotor points, dim 1088), 200-orientation zcwn grid, 1024 steps of 10 us; upload and run
-    with host buffers, FP32 and FP64."""
+    """Magic-angle spinning, the c0 system at 10 kHz about (1,1,1), rotor rank 8, 200-orientation zcwn
+    grid, 1024 steps of 10 us; upload and run with host buffers, FP32 and FP64.  The Fokker-Planck
+    problem of singlerot.m (17 rotor points, dim 1088) is the headline; the Floquet problem of
+    floquet.m (17 Fourier components, dim 1088) is reported beside it."""
     from spinach_gb300 import engine as E, singlerot as SR, workloads as W
     w = W.c0()
     L = W.build(w)
+    g = W.zcwn_grid(w.n_orient)
+    eng = E.Engine(device)
+
+    def timed(system):
+        eng.upload(*system)
+        eng.run(*[a[:16] for a in g], w.dt, w.nsteps, precision=E.FP32)       # warm-up
+        res = {}
+        for p in (E.FP32, E.FP64):
+            t0 = time.perf_counter()
+            eng.upload(*system)
+            r = eng.run(*g, w.dt, w.nsteps, precision=p)
+            res[p] = (time.perf_counter() - t0, r)
+        return res
+
     t0 = time.perf_counter()
     fp = SR.fokker_planck(L.I, L.terms, L.R, L.rho0, L.coil, 8, 10e3, (1.0, 1.0, 1.0))
     t_fp = time.perf_counter() - t0
-    eng = E.Engine(device)
-    g = W.zcwn_grid(w.n_orient)
-    eng.upload(*fp)
-    eng.run(*[a[:16] for a in g], w.dt, w.nsteps, precision=E.FP32)           # warm-up
-    res = {}
-    for p in (E.FP32, E.FP64):
-        t0 = time.perf_counter()
-        eng.upload(*fp)
-        r = eng.run(*g, w.dt, w.nsteps, precision=p)
-        res[p] = (time.perf_counter() - t0, r)
+    res = timed(fp)
+    t0 = time.perf_counter()
+    fl = SR.floquet_system(L.I, L.terms, L.R, L.rho0, L.coil, 8, 10e3, (1.0, 1.0, 1.0))
+    t_fl = time.perf_counter() - t0
+    rfl = timed(fl)
     out = {'workload': 'MAS (singlerot.m, Fokker-Planck): c0 system at 10 kHz about (1,1,1), rotor rank 8 '
                        '(dim 17 x 64 = 1088), 200-orientation zcwn grid, 1024 steps of 10 us, upload + run',
            'value': w.n_orient / res[E.FP32][0], 'unit': UNIT,
            'rel_err_vs_fp64_gpu': _rel(res[E.FP32][1].fid, res[E.FP64][1].fid),
            'fp64_gpu': {'value': w.n_orient / res[E.FP64][0]},
            'kernel_ms': res[E.FP32][1].stats['kernel_ms'], 'cluster': res[E.FP32][1].stats['cluster'],
-           'nnz': res[E.FP32][1].stats['nnz'], 'rotor_space_setup_s': t_fp}
+           'nnz': res[E.FP32][1].stats['nnz'], 'rotor_space_setup_s': t_fp,
+           'floquet': {'workload': 'floquet.m: the same system, rate, axis, grid and steps, 17 Fourier '
+                                   'components (dim 1088), upload + run',
+                       'value': w.n_orient / rfl[E.FP32][0], 'unit': UNIT,
+                       'rel_err_vs_fp64_gpu': _rel(rfl[E.FP32][1].fid, rfl[E.FP64][1].fid),
+                       'fp64_gpu': {'value': w.n_orient / rfl[E.FP64][0]},
+                       'kernel_ms': rfl[E.FP32][1].stats['kernel_ms'],
+                       'cluster': rfl[E.FP32][1].stats['cluster'], 'nnz': rfl[E.FP32][1].stats['nnz'],
+                       'setup_s': t_fl}}
     eng.close()
     return out
 
