@@ -907,14 +907,23 @@ def evolution_trajectory(ss: SpinSystem, L, rho, dt: float, nsteps: int) -> np.n
     return clean_up(ss, ans, ss.tols['zte_tol'])
 
 
+def _spatial(parameters: dict, op):
+    """kron(speye(spc_dim), op): an operator of the spin space projected into
+    a context's spatial (rotor or Fourier) space; spc_dim = 1 by default."""
+    n = int(parameters.get('spc_dim', 1))
+    return op if n == 1 else sp.kron(sp.identity(n), sp.csr_matrix(op), format='csr')
+
+
 def cpmg(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
     """experiments/cpmg.m:29-63 (K = 0, one spatial point): a 90-degree pulse
     step(pulse_op, rho0, pi/2), a half-echo of npoints-1 steps, then nloops
     times a 180-degree pulse on the last state and an echo of 2*npoints-1
-    steps; the detected trajectories concatenated."""
+    steps; the detected trajectories concatenated.  The pulse operator is
+    projected into the spatial space first, kron(speye(spc_dim), pulse_op)
+    (:33; spc_dim = 1 in the powder context)."""
     L = H + 1j * R
     coil = np.asarray(parameters['coil'], complex)
-    P = parameters['pulse_op']
+    P = _spatial(parameters, parameters['pulse_op'])
     dt = parameters['timestep']
     rho = step(ss, P, parameters['rho0'], np.pi / 2)
     traj = evolution_trajectory(ss, L, rho, dt, parameters['npoints'] - 1)
@@ -930,12 +939,13 @@ def hp_acquire(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
     """experiments/hp_acquire.m (K = 0, no decoupling): pulse_op by
     pulse_angle; if echo_time is given, echo_time of evolution ('final', one
     step), echo_oper by echo_angle, echo_time again; then the observable of
-    npoints-1 steps of 1/sweep."""
+    npoints-1 steps of 1/sweep.  Both operators are projected into the
+    spatial space, kron(speye(spc_dim), op) (:57,69)."""
     L = H + 1j * R
-    rho = step(ss, parameters['pulse_op'], parameters['rho0'], parameters['pulse_angle'])
+    rho = step(ss, _spatial(parameters, parameters['pulse_op']), parameters['rho0'], parameters['pulse_angle'])
     if 'echo_time' in parameters:
         rho = evolution_trajectory(ss, L, rho, parameters['echo_time'], 1)[:, -1]
-        rho = step(ss, parameters['echo_oper'], rho, parameters['echo_angle'])
+        rho = step(ss, _spatial(parameters, parameters['echo_oper']), rho, parameters['echo_angle'])
         rho = evolution_trajectory(ss, L, rho, parameters['echo_time'], 1)[:, -1]
     return evolution_observable(ss, L, parameters['coil'], rho, 1.0 / parameters['sweep'],
                                 parameters['npoints'] - 1)
@@ -1077,8 +1087,18 @@ def fourdif1(N: int):
     return x, sla.toeplitz(col1, row1)
 
 
-def singlerot_orientation_fid(ss, I, Q, parameters, angles) -> np.ndarray:
-    """One orientation of kernel/contexts/singlerot.m:134-307 with @acquire,
+_MAS_SEQUENCES = {'acquire': 'acquire', 'hp_acquire': 'hp_acquire', 'cpmg': 'cpmg'}
+
+
+def _mas_sequence(name):
+    if name not in _MAS_SEQUENCES:
+        raise ValueError(f'sequence {name!r} is not restated for the MAS contexts')
+    return globals()[_MAS_SEQUENCES[name]]
+
+
+def singlerot_orientation_fid(ss, I, Q, parameters, angles, sequence: str = 'acquire') -> np.ndarray:
+    """One orientation of kernel/contexts/singlerot.m:134-307 with @acquire
+    (or @hp_acquire / @cpmg, which project their pulses with spc_dim),
     sphten-liouv, no rotating frames: H_n = I + sum D_comp(k,m) Q{r}{k,m} with
     D_comp = D_lab2rot*D_rotor(phi_n)*D_mol2rot (:269-283, not Hermitised
     without rframes), G = clean_up(blkdiag(H)+1i*M, liouv_zero) (:298),
@@ -1108,8 +1128,8 @@ def singlerot_orientation_fid(ss, I, Q, parameters, angles) -> np.ndarray:
     else:
         space = np.full(N, 1.0 / N)
     par = dict(parameters, rho0=np.kron(space, parameters['rho0']),
-               coil=np.kron(np.ones(N), parameters['coil']))
-    return acquire(ss, par, G, R)
+               coil=np.kron(np.ones(N), parameters['coil']), spc_dim=N)
+    return _mas_sequence(sequence)(ss, par, G, R)
 
 
 def powder_orientation_hp_acquire(ss, I, Q, parameters, angles) -> np.ndarray:
@@ -1128,8 +1148,9 @@ def powder_orientation_eseem(ss, I, Q, parameters, angles) -> np.ndarray:
     return eseem(ss, parameters, H, relaxation(ss))
 
 
-def floquet_orientation_fid(ss, I, Q, parameters, angles) -> np.ndarray:
-    """One orientation of kernel/contexts/floquet.m:94-186 with @acquire:
+def floquet_orientation_fid(ss, I, Q, parameters, angles, sequence: str = 'acquire') -> np.ndarray:
+    """One orientation of kernel/contexts/floquet.m:94-186 with @acquire (or
+    @hp_acquire / @cpmg, which project their pulses with spc_dim):
     Fourier components of the rotor-frame Hamiltonian up to the highest
     interaction rank, F = sum_h kron(spdiags(1, h), T_h) + M, states in the
     zeroth Fourier component."""
@@ -1164,8 +1185,8 @@ def floquet_orientation_fid(ss, I, Q, parameters, angles) -> np.ndarray:
     Rf = sp.kron(sp.identity(N), relaxation(ss))
     e = np.zeros(N)
     e[(N - 1) // 2] = 1.0
-    par = dict(parameters, rho0=np.kron(e, parameters['rho0']), coil=np.kron(e, parameters['coil']))
-    return acquire(ss, par, F, Rf)
+    par = dict(parameters, rho0=np.kron(e, parameters['rho0']), coil=np.kron(e, parameters['coil']), spc_dim=N)
+    return _mas_sequence(sequence)(ss, par, F, Rf)
 
 
 def powder(ss: SpinSystem, parameters: dict, assumptions: str, grid, setup=None,

@@ -209,9 +209,17 @@ def _grid(parameters: dict):
     return tuple(np.ascontiguousarray(np.ravel(a), np.float64) for a in g)
 
 
-def _run(eng, pulse_sequence, parameters, work, full, grid, precision):
+def _run(eng, pulse_sequence, parameters, work, full, grid, precision, spc_dim: int = 1):
+    """Runs the sequence on the uploaded system.  Pulse operators are
+    projected into the context's spatial space, kron(speye(spc_dim), op), as
+    hp_acquire.m:57,69 and cpmg.m:33 do (spc_dim = 1 for powder.m)."""
     al, be, ga, w = grid
     name = _name(pulse_sequence)
+
+    def op(key):
+        P = _restrict_matrix(work, full, _matrix(full, parameters[key]))
+        return P if spc_dim == 1 else sp.kron(sp.identity(spc_dim), P, format='csr')
+
     if name == 'acquire':
         dt, n = 1.0 / float(parameters['sweep']), int(parameters['npoints']) - 1
         if 'dead_time' in parameters:
@@ -220,22 +228,24 @@ def _run(eng, pulse_sequence, parameters, work, full, grid, precision):
                                     per_orientation=not parameters.get('sum_up', 1))
         return eng.run(al, be, ga, w, dt, n, precision=precision, per_orientation=not parameters.get('sum_up', 1))
     if name == 'hp_acquire':
-        ops = [_restrict_matrix(work, full, _matrix(full, parameters['pulse_op']))]
+        ops = [op('pulse_op')]
         prog = [('pulse', 0, float(parameters['pulse_angle']))]
         if 'echo_time' in parameters:
-            ops.append(_restrict_matrix(work, full, _matrix(full, parameters['echo_oper'])))
+            ops.append(op('echo_oper'))
             et = float(parameters['echo_time'])
             prog += [('evolve', 1, et, False), ('pulse', 1, float(parameters['echo_angle'])), ('evolve', 1, et, False)]
         prog.append(('evolve', int(parameters['npoints']) - 1, 1.0 / float(parameters['sweep'])))
         return eng.run_sequence(al, be, ga, w, ops, prog, precision=precision,
                                 per_orientation=not parameters.get('sum_up', 1))
     if name == 'cpmg':
-        P = _restrict_matrix(work, full, _matrix(full, parameters['pulse_op']))
+        P = op('pulse_op')
         return eng.run_cpmg(al, be, ga, w, float(parameters['timestep']), int(parameters['npoints']),
                             int(parameters['nloops']), P, precision=precision,
                             per_orientation=not parameters.get('sum_up', 1))
     if name == 'eseem':
-        P = _restrict_matrix(work, full, _matrix(full, parameters['pulse_op']))
+        if spc_dim != 1:
+            raise ValueError('eseem runs in the powder context on this engine')
+        P = op('pulse_op')
         return eng.run_eseem(al, be, ga, w, float(parameters['timestep']), int(parameters['npoints']), P,
                              precision=precision, per_orientation=not parameters.get('sum_up', 1))
     raise ValueError(f'pulse sequence {pulse_sequence!r} is not supported on this engine')
@@ -275,16 +285,23 @@ def powder(spin_system: System, pulse_sequence, parameters: dict, assumptions: s
     return _answer(res, parameters), grid
 
 
+def _mas_name(pulse_sequence, context: str, parameters: dict) -> str:
+    name = _name(pulse_sequence)
+    if name not in ('acquire', 'hp_acquire', 'cpmg'):
+        raise ValueError(f'{context} runs acquire, hp_acquire or cpmg on this engine')
+    if parameters.get('needs'):
+        raise ValueError(f'{context} takes an explicit rho0 on this engine')
+    return name
+
+
 def singlerot(spin_system: System, pulse_sequence, parameters: dict, assumptions: str, engine=None,
               precision: int = E.FP64):
-    """kernel/contexts/singlerot.m with acquire: the Fokker-Planck problem of
-    rate, axis and max_rank, in the engine's upload form.  A grid named
-    'single_crystal' (or single_crystal=True) starts from one rotor point."""
-    if _name(pulse_sequence) != 'acquire':
-        raise ValueError('singlerot runs acquire on this engine')
-    if parameters.get('needs'):
-        raise ValueError('singlerot takes an explicit rho0 on this engine')
-    work, full, I, Q, R, rho0, coil, _ = _setup(spin_system, parameters, assumptions, 'acquire')
+    """kernel/contexts/singlerot.m with acquire, hp_acquire or cpmg: the
+    Fokker-Planck problem of rate, axis and max_rank, in the engine's upload
+    form.  A grid named 'single_crystal' (or single_crystal=True) starts from
+    one rotor point."""
+    name = _mas_name(pulse_sequence, 'singlerot', parameters)
+    work, full, I, Q, R, rho0, coil, _ = _setup(spin_system, parameters, assumptions, name)
     single = bool(parameters.get('single_crystal')) or parameters.get('grid') == 'single_crystal'
     grid = ((np.zeros(1), np.zeros(1), np.zeros(1), np.ones(1)) if parameters.get('grid') == 'single_crystal'
             else _grid(parameters))
@@ -293,7 +310,7 @@ def singlerot(spin_system: System, pulse_sequence, parameters: dict, assumptions
     eng = engine or E.Engine(0)
     try:
         eng.upload(*fp)
-        res = _run(eng, 'acquire', parameters, work, full, grid, precision)
+        res = _run(eng, name, parameters, work, full, grid, precision, spc_dim=2 * int(parameters['max_rank']) + 1)
     finally:
         if engine is None:
             eng.close()
@@ -302,14 +319,11 @@ def singlerot(spin_system: System, pulse_sequence, parameters: dict, assumptions
 
 def floquet(spin_system: System, pulse_sequence, parameters: dict, assumptions: str, engine=None,
             precision: int = E.FP64):
-    """kernel/contexts/floquet.m with acquire: the Floquet problem of rate,
-    axis and max_rank (Fourier components of the rotor-frame Hamiltonian), in
-    the engine's upload form."""
-    if _name(pulse_sequence) != 'acquire':
-        raise ValueError('floquet runs acquire on this engine')
-    if parameters.get('needs'):
-        raise ValueError('floquet takes an explicit rho0 on this engine')
-    work, full, I, Q, R, rho0, coil, _ = _setup(spin_system, parameters, assumptions, 'acquire')
+    """kernel/contexts/floquet.m with acquire, hp_acquire or cpmg: the
+    Floquet problem of rate, axis and max_rank (Fourier components of the
+    rotor-frame Hamiltonian), in the engine's upload form."""
+    name = _mas_name(pulse_sequence, 'floquet', parameters)
+    work, full, I, Q, R, rho0, coil, _ = _setup(spin_system, parameters, assumptions, name)
     grid = ((np.zeros(1), np.zeros(1), np.zeros(1), np.ones(1)) if parameters.get('grid') == 'single_crystal'
             else _grid(parameters))
     fs = SR.floquet_system(I, Q, R, rho0, coil, int(parameters['max_rank']), float(parameters['rate']),
@@ -317,7 +331,7 @@ def floquet(spin_system: System, pulse_sequence, parameters: dict, assumptions: 
     eng = engine or E.Engine(0)
     try:
         eng.upload(*fs)
-        res = _run(eng, 'acquire', parameters, work, full, grid, precision)
+        res = _run(eng, name, parameters, work, full, grid, precision, spc_dim=2 * int(parameters['max_rank']) + 1)
     finally:
         if engine is None:
             eng.close()

@@ -55,3 +55,92 @@ def test_equilibrium_states_match_oracle():
         assert np.abs(st[i] - ref).max() <= 1e-12 * np.abs(dev).max()
     iso = S.equilibrium_states(S.RotationalHamiltonian(HL.dim, HL.iso, {}), 300.0)
     assert iso.shape == (HL.dim,) and iso[0] == 1.0
+
+
+class _DenseEngine:
+    """Exact dense stand-in for the engine's run semantics, used to check the
+    host side of the contexts on CPU: L(Omega) = Herm(I + sum D(Omega)(j,m)
+    Q{r}{j,m}) + iR propagated with expm, pulses exp(-1i*angle*P), a segment
+    of n steps records n+1 points unless record is False."""
+
+    class _Res:
+        def __init__(self, fids, w):
+            self.fids = np.array(fids)
+            self.fid = (np.asarray(w)[:, None] * self.fids).sum(axis=0)
+
+    def upload(self, I, terms, Rx, rho0, coil):
+        self.sys = (I, terms, Rx, np.asarray(rho0, complex), np.asarray(coil, complex))
+
+    def _L(self, a, b, g):
+        from spinach_gb300 import singlerot as SR
+        I, terms, Rx, _, _ = self.sys
+        H = I.toarray().astype(complex)
+        D = {r: SR.wigner_d(r, a, b, g) for r in {k[0] for k in terms}}
+        for (r, j, m), T in terms.items():
+            H = H + D[r][j, m] * T.toarray()
+        L = (H + H.conj().T) / 2
+        return L if Rx is None else L + 1j * Rx.toarray()
+
+    def _program(self, al, be, ga, w, ops, prog):
+        from scipy.linalg import expm
+        _, _, _, rho0, coil = self.sys
+        fids = []
+        for a, b, g in zip(al, be, ga):
+            L, rho, out = self._L(a, b, g), rho0.copy(), []
+            for item in prog:
+                if item[0] == 'pulse':
+                    rho = expm(-1j * item[2] * ops[item[1]].toarray()) @ rho
+                    continue
+                n, dt, record = item[1], item[2], (item[3] if len(item) > 3 else True)
+                P = expm(-1j * L * dt)
+                if record:
+                    out.append(np.vdot(coil, rho))
+                for _ in range(n):
+                    rho = P @ rho
+                    if record:
+                        out.append(np.vdot(coil, rho))
+            fids.append(out)
+        return self._Res(fids, w)
+
+    def run_sequence(self, al, be, ga, w, ops, prog, precision=None, per_orientation=False):
+        return self._program(al, be, ga, w, ops, prog)
+
+    def run_cpmg(self, al, be, ga, w, dt, npoints, nloops, P, precision=None, per_orientation=False):
+        prog = [('pulse', 0, np.pi / 2), ('evolve', npoints - 1, dt)]
+        for _ in range(nloops):
+            prog += [('pulse', 0, np.pi), ('evolve', 2 * npoints - 1, dt)]
+        return self._program(al, be, ga, w, [P], prog)
+
+    def close(self):
+        pass
+
+
+@pytest.mark.parametrize('context,sequence', [('singlerot', 'hp_acquire'), ('floquet', 'cpmg'),
+                                              ('singlerot', 'cpmg'), ('floquet', 'hp_acquire')])
+def test_mas_contexts_project_pulses_into_rotor_space(context, sequence):
+    """singlerot.m / floquet.m with @hp_acquire and @cpmg: the pulses act on
+    every rotor point or Fourier component, kron(speye(spc_dim), op)
+    (hp_acquire.m:57,69, cpmg.m:33); the context's uploaded system and
+    programs, run exactly, against the oracle."""
+    sys_, inter, spin_system = _system()
+    al, be, ga = np.array([0.0, 0.0, 0.0]), np.array([0.4, 1.3, 2.5]), np.array([0.3, 2.0, 4.1])
+    w = np.array([0.2, 0.5, 0.3])
+    base = dict(rate=8e3, axis=(1, 1, 1), max_rank=2, grid=(al, be, ga, w))
+    if sequence == 'hp_acquire':
+        seq = dict(pulse_op=('Ly', '13C'), pulse_angle=np.pi / 2, echo_time=3e-5, echo_oper=('Lx', '13C'),
+                   echo_angle=np.pi, sweep=2e4, npoints=12)
+    else:
+        seq = dict(pulse_op=('Ly', '13C'), timestep=5e-5, npoints=6, nloops=2)
+    parameters = dict(base, rho0=('Lz', '13C'), coil=('L+', '13C'), **seq)
+    fid, _ = getattr(X, context)(spin_system, sequence, parameters, 'nmr', engine=_DenseEngine())
+    ss = R.basis(R.create(dict(sys_, enable=[]), inter), dict(approximation='none', level=0, space_level=1))
+    ss, I, Q = R.powder_setup(ss, 'nmr')
+    par = dict(base, rho0=R.state(ss, 'Lz', '13C'), coil=R.state(ss, 'L+', '13C'))
+    for k in ('pulse_op', 'echo_oper'):
+        if k in seq:
+            par[k] = R.operator(ss, seq[k][0], seq[k][1])
+    par.update({k: v for k, v in seq.items() if k not in ('pulse_op', 'echo_oper')})
+    one = R.singlerot_orientation_fid if context == 'singlerot' else R.floquet_orientation_fid
+    ref = sum(w[i] * one(ss, I, Q, par, (al[i], be[i], ga[i]), sequence=sequence) for i in range(3))
+    assert np.abs(ref).max() > 0.05
+    assert np.abs(fid - ref).max() <= 1e-9 * np.abs(ref).max()

@@ -1,5 +1,7 @@
-"""Magic-angle spinning (kernel/contexts/singlerot.m, Fokker-Planck) through the
-engine: the rotor-space Liouvillian in upload form runs on the same kernels."""
+"""Magic-angle spinning (kernel/contexts/singlerot.m, Fokker-Planck, and
+kernel/contexts/floquet.m) through the engine: the rotor-space and Floquet
+Liouvillians in upload form run on the same kernels, with acquire and with
+the hard-pulse sequences."""
 import math
 
 import numpy as np
@@ -88,3 +90,38 @@ def test_floquet_mas_matches_oracle_and_fokker_planck(gpu_engine):
     gpu_engine.upload(*SR.fokker_planck(L.I, L.terms, L.R, L.rho0, L.coil, 12, rate, axis))
     f_fp = gpu_engine.run(mapped[:, 0], mapped[:, 1], mapped[:, 2], g[3], w.dt, nsteps, precision=E.FP64).fid
     assert rel_err(f_fl, f_fp) <= 1e-5
+
+
+@pytest.mark.parametrize('context,sequence', [('singlerot', 'hp_acquire'), ('floquet', 'cpmg'),
+                                              ('singlerot', 'cpmg'), ('floquet', 'hp_acquire')])
+def test_mas_contexts_with_pulse_sequences(gpu_engine, context, sequence):
+    """singlerot.m / floquet.m with @hp_acquire (echo) and @cpmg: pulses
+    projected into the rotor or Fourier space, kron(speye(spc_dim), op)
+    (hp_acquire.m:57,69, cpmg.m:33), on the engine against the oracle."""
+    from spinach_gb300 import contexts as X
+    sys_ = dict(isotopes=['13C', '1H'], magnet=14.1)
+    inter = dict(zeeman=dict(eigs=[[10.0, 70.0, 180.0], [1.0, 3.0, 8.0]], euler=[[0.1, 0.7, 1.9], [0, 0, 0]]),
+                 coupling=dict(scalar={(0, 1): 140.0}))
+    spin_system = X.basis(X.create(sys_, inter), dict(approximation='none'))
+    al, be, ga = np.zeros(3), np.array([0.4, 1.3, 2.5]), np.array([0.3, 2.0, 4.1])
+    w = np.array([0.2, 0.5, 0.3])
+    base = dict(rate=8e3, axis=(1, 1, 1), max_rank=3, grid=(al, be, ga, w))
+    if sequence == 'hp_acquire':
+        seq = dict(pulse_op=('Ly', '13C'), pulse_angle=np.pi / 2, echo_time=3e-5, echo_oper=('Lx', '13C'),
+                   echo_angle=np.pi, sweep=2e4, npoints=40)
+    else:
+        seq = dict(pulse_op=('Ly', '13C'), timestep=5e-5, npoints=16, nloops=2)
+    parameters = dict(base, rho0=('Lz', '13C'), coil=('L+', '13C'), **seq)
+    ss = R.basis(R.create(dict(sys_, enable=[]), inter), dict(approximation='none', level=0, space_level=1))
+    ss, I, Q = R.powder_setup(ss, 'nmr')
+    par = dict(base, rho0=R.state(ss, 'Lz', '13C'), coil=R.state(ss, 'L+', '13C'))
+    for k in ('pulse_op', 'echo_oper'):
+        if k in seq:
+            par[k] = R.operator(ss, seq[k][0], seq[k][1])
+    par.update({k: v for k, v in seq.items() if k not in ('pulse_op', 'echo_oper')})
+    one = R.singlerot_orientation_fid if context == 'singlerot' else R.floquet_orientation_fid
+    ref = sum(w[i] * one(ss, I, Q, par, (al[i], be[i], ga[i]), sequence=sequence) for i in range(3))
+    assert np.abs(ref).max() > 0.05
+    for prec, tol in ((E.FP64, 1e-10), (E.FP32, 1e-5)):
+        fid, _ = getattr(X, context)(spin_system, sequence, parameters, 'nmr', engine=gpu_engine, precision=prec)
+        assert rel_err(fid, ref) <= tol, prec
