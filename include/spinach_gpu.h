@@ -284,6 +284,23 @@ spx_status spx_run_eseem(spx_handle *handle, int64_t n_orient, const double *alp
                          const spx_csc *pulse_op, const spx_options *opt, double *fid, double *fids_per_orient);
 
 /*
+ * Three-pulse DEER with hard pulses (experiments/esr_dipolar/
+ * deer_3p_hard_deer.m, 'brief' output; replaces the orientation loop of
+ * powder.m:226-287 around it): a 90-degree pulse exp(-1i*(pi/2)*ex_prob) on
+ * rho0, a trajectory of nsteps steps of stepsize, a 180-degree pump pulse
+ * exp(-1i*pi*ex_pump) on every state of it, the refocusing of state j by
+ * nsteps-j more steps, a 180-degree probe pulse and nsteps more steps;
+ * fid[j] = coil' * that state / norm(coil, 2), powder-summed, j = 0..nsteps
+ * (nsteps+1 complex values; the coil is the probe coil).  fids_per_orient
+ * (or NULL) receives every orientation's trace, orientation-major.  Needs one
+ * coil and the single rho0; the dimension is limited to 8192.
+ */
+spx_status spx_run_deer(spx_handle *handle, int64_t n_orient, const double *alphas, const double *betas,
+                        const double *gammas, const double *weights, double stepsize, int64_t nsteps,
+                        const spx_csc *ex_prob, const spx_csc *ex_pump, const spx_options *opt, double *fid,
+                        double *fids_per_orient);
+
+/*
  * Per-orientation initial states (kernel/contexts/powder.m:244-254: the
  * 'aniso_eq' equilibrium or a function-handle rho0 evaluated at every grid
  * point).  states holds n_states Liouville vectors, orientation after

@@ -174,6 +174,33 @@ class KronModel:
             r = P @ r
         return np.array(out)
 
+    def deer_3p(self, angles, rho0, coil, ex_prob, ex_pump, stepsize, nsteps):
+        """Three-pulse DEER with hard pulses U rho U^dagger: probe 90 degrees,
+        j steps, pump 180 degrees, nsteps-j steps, probe 180 degrees, nsteps
+        steps; point j is <coil, state> (not normalised), j = 0..nsteps."""
+        H = self.hamiltonian(angles)
+        I = np.eye(self.dim)
+        L = np.kron(H, I) - np.kron(I, H.T) + 1j * self.relaxation()
+        P = sla.expm(-1j * stepsize * L)
+
+        def pulse(r, op, theta):
+            U = sla.expm(-1j * theta * op)
+            return (U @ r.reshape(self.dim, self.dim) @ U.conj().T).reshape(-1)
+
+        r = pulse(rho0.reshape(-1).astype(complex), ex_prob, np.pi / 2)
+        c = coil.reshape(-1)
+        out = []
+        for j in range(nsteps + 1):
+            x = pulse(r, ex_pump, np.pi)
+            for _ in range(nsteps - j):
+                x = P @ x
+            x = pulse(x, ex_prob, np.pi)
+            for _ in range(nsteps):
+                x = P @ x
+            out.append(np.vdot(c, x))
+            r = P @ r
+        return np.array(out)
+
 
 def gamma_of(isotope):
     return ISOTOPES[isotope][1]

@@ -983,6 +983,44 @@ def eseem(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
     return np.asarray(parameters['coil'], complex).conj() @ stack
 
 
+def evolution_final(ss: SpinSystem, L, rho, dt: float, nsteps: int) -> np.ndarray:
+    """kernel/evolution.m:168-246 ('final', one subspace): below krylov_tol the
+    user timing is replaced by nsteps_opt = max(1, ceil(log2(dim/(ncols*log 2))))
+    steps of total_time/nsteps_opt with one propagator (:196-234); otherwise
+    kernel/krylov.m:84-90, one step() of the whole time.  rho may be a stack."""
+    L = clean_up(ss, sp.csc_matrix(L), ss.tols['liouv_zero'])
+    rho = clean_up(ss, np.array(rho, complex), ss.tols['zte_tol'])
+    dim = L.shape[0]
+    total = dt * nsteps
+    if dim < ss.tols['krylov_tol'] and 'krylov' not in ss.enable:
+        ncols = 1 if rho.ndim == 1 else rho.shape[1]
+        n_opt = max(1, math.ceil(math.log2(dim / (ncols * math.log(2)))))
+        P = propagator(ss, L, total / n_opt)
+        for _ in range(n_opt):
+            rho = P @ rho
+    else:
+        rho = step(ss, sp.csr_matrix(L), rho, total)
+    return clean_up(ss, rho, ss.tols['zte_tol'])
+
+
+def deer_3p_hard(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
+    """experiments/esr_dipolar/deer_3p_hard_deer.m ('brief' output, K = 0):
+    probe 90-degree pulse, trajectory of nsteps steps of stepsize, pump
+    180-degree pulse on every column, the reversed stack refocused, probe
+    180-degree pulse, nsteps more steps ('final'), detection on coil_prob
+    divided by its 2-norm."""
+    L = H + 1j * R
+    dt, n = parameters['stepsize'], parameters['nsteps']
+    rho = step(ss, parameters['ex_prob'], parameters['rho0'], np.pi / 2)
+    stack = evolution_trajectory(ss, L, rho, dt, n)
+    stack = step(ss, parameters['ex_pump'], stack, np.pi)
+    stack[:, ::-1] = evolution_refocus(ss, stack[:, ::-1], L, dt)
+    stack = step(ss, parameters['ex_prob'], stack, np.pi)
+    stack = evolution_final(ss, L, stack, dt, n)
+    coil = np.asarray(parameters['coil_prob'], complex)
+    return coil.conj() @ stack / np.linalg.norm(coil)
+
+
 # --------------------------------------------------------------------------
 # Grids and the powder context
 # --------------------------------------------------------------------------
@@ -1146,6 +1184,14 @@ def powder_orientation_eseem(ss, I, Q, parameters, angles) -> np.ndarray:
     H = I if A is None else I + A
     H = (H + H.conj().T) / 2
     return eseem(ss, parameters, H, relaxation(ss))
+
+
+def powder_orientation_deer(ss, I, Q, parameters, angles) -> np.ndarray:
+    """One iteration of kernel/contexts/powder.m:226-274 with @deer_3p_hard_deer."""
+    A = orientation(Q, angles)
+    H = I if A is None else I + A
+    H = (H + H.conj().T) / 2
+    return deer_3p_hard(ss, parameters, H, relaxation(ss))
 
 
 def floquet_orientation_fid(ss, I, Q, parameters, angles, sequence: str = 'acquire') -> np.ndarray:

@@ -242,6 +242,13 @@ def _run(eng, pulse_sequence, parameters, work, full, grid, precision, spc_dim: 
         return eng.run_cpmg(al, be, ga, w, float(parameters['timestep']), int(parameters['npoints']),
                             int(parameters['nloops']), P, precision=precision,
                             per_orientation=not parameters.get('sum_up', 1))
+    if name == 'deer_3p_hard_deer':
+        if spc_dim != 1:
+            raise ValueError('deer_3p_hard_deer runs in the powder context on this engine')
+        if parameters.get('output', 'brief') != 'brief':
+            raise ValueError("deer_3p_hard_deer runs output='brief' on this engine")
+        return eng.run_deer(al, be, ga, w, float(parameters['stepsize']), int(parameters['nsteps']), op('ex_prob'),
+                            op('ex_pump'), precision=precision, per_orientation=not parameters.get('sum_up', 1))
     if name == 'eseem':
         if spc_dim != 1:
             raise ValueError('eseem runs in the powder context on this engine')
@@ -262,7 +269,11 @@ def _answer(res, parameters):
 def powder(spin_system: System, pulse_sequence, parameters: dict, assumptions: str, engine=None,
            precision: int = E.FP64):
     """kernel/contexts/powder.m:99-309: returns (answer, grid), the answer the
-    weighted sum of the orientations' outputs (sum_up, default) or their list."""
+    weighted sum of the orientations' outputs (sum_up, default) or their list.
+    For deer_3p_hard_deer the answer is the DEER trace (deer.deer_trace of
+    the 'brief' output), detected on parameters['coil_prob']."""
+    if _name(pulse_sequence) == 'deer_3p_hard_deer':
+        parameters = dict(parameters, coil=parameters['coil_prob'])
     work, full, I, Q, R, rho0, coil, HL = _setup(spin_system, parameters, assumptions, _name(pulse_sequence))
     grid = _grid(parameters)
     eng = engine or E.Engine(0)

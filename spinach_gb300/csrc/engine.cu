@@ -1180,12 +1180,15 @@ __global__ void identity_kernel(int n_pad, double2 *a) {
 // out[o][n] = sum_i conj(v[o][n][i]) * (Pi u[o][n])[i], one warp per (o, n).
 __global__ void echo_form_kernel(int n_orient, int npoints, int n_pad, const int *__restrict__ ptr,
                                  const int *__restrict__ col, const double2 *__restrict__ val,
-                                 const double2 *__restrict__ u, const double2 *__restrict__ v, double2 *out) {
+                                 const double2 *__restrict__ u, const double2 *__restrict__ v, int reverse,
+                                 double2 *out) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = (int64_t)n_orient * npoints;
     for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw;
          w += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-        const double2 *uu = u + w * n_pad, *vv = v + w * n_pad;
+        // v point npoints-1-j of the same orientation when reverse
+        const int64_t wv = reverse ? w - 2 * (w % npoints) + npoints - 1 : w;
+        const double2 *uu = u + w * n_pad, *vv = v + wv * n_pad;
         double re = 0.0, im = 0.0;
         for (int i = lane; i < n_pad; i += 32) {
             double wr = 0.0, wi = 0.0;
@@ -1222,65 +1225,58 @@ __global__ void echo_powder_kernel(int n_orient, int npoints, const double2 *f, 
 
 constexpr int kTrajChunk = 4;       // steps per chunk of trajectory outputs (falls back to 2, 1)
 
-void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
-               const double *weights, double timestep, int64_t npoints, const spx_csc *pulse_op,
-               const spx_options &o, double *fid, double *fids_per_orient) {
-    if (h->nchan != 1 || h->n_states != 0)
-        throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil and one initial state");
-    if (npoints < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "npoints must be positive");
-    const double tau = timestep / 2;                // eseem.m: steps of timestep/2
-    const int64_t nsteps = npoints - 1;
-    validate_run(h, n_orient, tau, nsteps);
+// Pi = exp(-1i*theta*P) column by column, kept as CSR in the echo buffers
+// (entries above 1e-15; Pi is unitary, so they are at most 1).
+void upload_echo_propagator(spx_handle *h, const PulseOp &P, double theta) {
     const int n_pad = h->n_pad;
-    if (n_pad > 8192) throw SpxError(SPX_ERR_UNSUPPORTED, "echo detection is limited to dimension 8192");
-    h->pulses.clear();
-    h->pulses.push_back(std::make_unique<PulseOp>());
-    const PulseOp &P = *h->pulses.back();
-    upload_pulse(h, pulse_op, *h->pulses.back());
-    upload_grid(h, n_orient, alphas, betas, gammas, weights);
-    double *g = h->d_grid.p;
-    // rho1 = exp(-1i pi/2 P) rho0
-    h->d_seq_rho.reserve(n_pad);
-    SPX_CUDA(cudaMemcpyAsync(h->d_seq_rho.p, h->d_rho0.p, n_pad * sizeof(double2), cudaMemcpyDeviceToDevice,
-                             h->stream));
-    apply_pulse(h, P, M_PI / 2, 1, h->d_seq_rho.p);
-    // Pi = exp(-1i pi P) column by column, kept as CSR (entries above 1e-15;
-    // Pi is unitary, so they are at most 1)
-    {
-        DevBuf<double2> dense;
-        dense.reserve((size_t)n_pad * n_pad);
-        identity_kernel<<<h->sm_count * 4, 256, 0, h->stream>>>(n_pad, dense.p);
-        SPX_CUDA(cudaGetLastError());
-        apply_pulse(h, P, M_PI, n_pad, dense.p);
-        std::vector<double2> hd((size_t)n_pad * n_pad);
-        SPX_CUDA(cudaMemcpyAsync(hd.data(), dense.p, hd.size() * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
-        SPX_CUDA(cudaStreamSynchronize(h->stream));
-        std::vector<int> ptr(n_pad + 1, 0), col;
-        std::vector<double2> val;
-        for (int i = 0; i < n_pad; ++i) {
-            for (int j = 0; j < n_pad; ++j) {
-                const double2 v = hd[(size_t)j * n_pad + i];         // column j holds Pi e_j
-                if (std::fabs(v.x) > 1e-15 || std::fabs(v.y) > 1e-15) {
-                    col.push_back(j);
-                    val.push_back(v);
-                }
+    DevBuf<double2> dense;
+    dense.reserve((size_t)n_pad * n_pad);
+    identity_kernel<<<h->sm_count * 4, 256, 0, h->stream>>>(n_pad, dense.p);
+    SPX_CUDA(cudaGetLastError());
+    apply_pulse(h, P, theta, n_pad, dense.p);
+    std::vector<double2> hd((size_t)n_pad * n_pad);
+    SPX_CUDA(cudaMemcpyAsync(hd.data(), dense.p, hd.size() * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    SPX_CUDA(cudaStreamSynchronize(h->stream));
+    std::vector<int> ptr(n_pad + 1, 0), col;
+    std::vector<double2> val;
+    for (int i = 0; i < n_pad; ++i) {
+        for (int j = 0; j < n_pad; ++j) {
+            const double2 v = hd[(size_t)j * n_pad + i];         // column j holds Pi e_j
+            if (std::fabs(v.x) > 1e-15 || std::fabs(v.y) > 1e-15) {
+                col.push_back(j);
+                val.push_back(v);
             }
-            ptr[i + 1] = (int)col.size();
         }
-        if (col.empty()) { col.push_back(0); val.push_back(make_double2(0, 0)); }
-        h->d_echo_ptr.upload(ptr, h->stream);
-        h->d_echo_col.upload(col, h->stream);
-        h->d_echo_val.upload(val, h->stream);
+        ptr[i + 1] = (int)col.size();
     }
-    // adjoint generator
-    const int64_t n_ell = (int64_t)h->nstreams * h->ell_len, n_diag = (int64_t)h->nstreams * n_pad;
+    if (col.empty()) { col.push_back(0); val.push_back(make_double2(0, 0)); }
+    h->d_echo_ptr.upload(ptr, h->stream);
+    h->d_echo_col.upload(col, h->stream);
+    h->d_echo_val.upload(val, h->stream);
+}
+
+// The adjoint generator -H + 1i R in the d_neg_* streams: propagating under it
+// is propagating under the adjoint of exp(-1i L dt).
+void negate_generator(spx_handle *h) {
+    const int64_t n_ell = (int64_t)h->nstreams * h->ell_len, n_diag = (int64_t)h->nstreams * h->n_pad;
     h->d_neg_re.reserve((size_t)std::max<int64_t>(n_ell, 1));
     if (h->cplx) h->d_neg_im.reserve((size_t)std::max<int64_t>(n_ell, 1));
     h->d_neg_diag.reserve((size_t)n_diag);
     negate_streams_kernel<<<h->sm_count * 4, 256, 0, h->stream>>>(
         n_ell, h->d_ell_re.p, h->cplx ? h->d_ell_im.p : nullptr, h->d_neg_re.p, h->cplx ? h->d_neg_im.p : nullptr,
-        n_diag, n_pad, h->d_diag.p, h->d_neg_diag.p);
+        n_diag, h->n_pad, h->d_diag.p, h->d_neg_diag.p);
     SPX_CUDA(cudaGetLastError());
+}
+
+// The echo core: the forward trajectory u from d_seq_rho and the adjoint
+// trajectory v from the coil (adj0 null) or from per-orientation states adj0
+// (n_orient x n_pad), nsteps steps of tau each; echo_f[o][j] =
+// conj(v[o][k]) * Pi * u[o][j] with k = j, or k = nsteps - j when reverse;
+// d_fid = their weighted sum in orientation order.
+void echo_trajectories(spx_handle *h, int64_t n_orient, const double *g, double tau, int64_t nsteps,
+                       const spx_options &o, const double2 *adj0, bool reverse) {
+    const int n_pad = h->n_pad;
+    const int64_t npoints = nsteps + 1;
     // the states at every step come from chunks of a few steps (their
     // intermediate states accumulated in shared memory: one-step chunks spend
     // most of their series on the truncation tail); orientations in batches
@@ -1316,7 +1312,9 @@ void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const doub
         o1.chunk_steps = c.M;
         for (int dir = 0; dir < 2; ++dir) {
             RunIO io;
-            io.rho0 = dir == 0 ? h->d_seq_rho.p : h->d_coil.p;
+            if (dir == 0) io.rho0 = h->d_seq_rho.p;
+            else if (adj0) io.rho0s = adj0 + (size_t)b0 * n_pad;
+            else io.rho0 = h->d_coil.p;
             io.traj_out = h->d_traj[dir].p;
             io.adjoint = dir == 1;
             launch_powder(h, nb, g + b0, g + n_orient + b0, g + 2 * n_orient + b0, g + 3 * n_orient + b0, tau, nsteps,
@@ -1327,17 +1325,109 @@ void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const doub
         const int blocks = (int)std::min<int64_t>((warps + 7) / 8, (int64_t)h->sm_count * 16);
         echo_form_kernel<<<blocks, 256, 0, h->stream>>>((int)nb, (int)npoints, n_pad, h->d_echo_ptr.p, h->d_echo_col.p,
                                                         h->d_echo_val.p, h->d_traj[0].p, h->d_traj[1].p,
-                                                        h->d_echo_f.p + b0 * npoints);
+                                                        reverse ? 1 : 0, h->d_echo_f.p + b0 * npoints);
         SPX_CUDA(cudaGetLastError());
     }
     echo_powder_kernel<<<(unsigned)((npoints + 127) / 128), 128, 0, h->stream>>>(
         (int)n_orient, (int)npoints, h->d_echo_f.p, g + 3 * n_orient, h->d_fid.p);
     SPX_CUDA(cudaGetLastError());
+}
+
+// Copies the powder echo (and every orientation's) to the host, times scale.
+void echo_outputs(spx_handle *h, int64_t n_orient, int64_t npoints, double scale, double *fid,
+                  double *fids_per_orient) {
     SPX_CUDA(cudaMemcpyAsync(fid, h->d_fid.p, (size_t)npoints * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
     if (fids_per_orient)
         SPX_CUDA(cudaMemcpyAsync(fids_per_orient, h->d_echo_f.p, (size_t)n_orient * npoints * sizeof(double2),
                                  cudaMemcpyDeviceToHost, h->stream));
     SPX_CUDA(cudaStreamSynchronize(h->stream));
+    if (scale != 1.0) {
+        for (int64_t i = 0; i < 2 * npoints; ++i) fid[i] *= scale;
+        if (fids_per_orient)
+            for (int64_t i = 0; i < 2 * n_orient * npoints; ++i) fids_per_orient[i] *= scale;
+    }
+}
+
+void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
+               const double *weights, double timestep, int64_t npoints, const spx_csc *pulse_op,
+               const spx_options &o, double *fid, double *fids_per_orient) {
+    if (h->nchan != 1 || h->n_states != 0)
+        throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil and one initial state");
+    if (npoints < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "npoints must be positive");
+    const double tau = timestep / 2;                // eseem.m: steps of timestep/2
+    const int64_t nsteps = npoints - 1;
+    validate_run(h, n_orient, tau, nsteps);
+    if (h->n_pad > 8192) throw SpxError(SPX_ERR_UNSUPPORTED, "echo detection is limited to dimension 8192");
+    h->pulses.clear();
+    h->pulses.push_back(std::make_unique<PulseOp>());
+    upload_pulse(h, pulse_op, *h->pulses.back());
+    const PulseOp &P = *h->pulses.back();
+    upload_grid(h, n_orient, alphas, betas, gammas, weights);
+    // rho1 = exp(-1i pi/2 P) rho0
+    h->d_seq_rho.reserve(h->n_pad);
+    SPX_CUDA(cudaMemcpyAsync(h->d_seq_rho.p, h->d_rho0.p, h->n_pad * sizeof(double2), cudaMemcpyDeviceToDevice,
+                             h->stream));
+    apply_pulse(h, P, M_PI / 2, 1, h->d_seq_rho.p);
+    upload_echo_propagator(h, P, M_PI);
+    negate_generator(h);
+    echo_trajectories(h, n_orient, h->d_grid.p, tau, nsteps, o, nullptr, false);
+    echo_outputs(h, n_orient, npoints, 1.0, fid, fids_per_orient);
+}
+
+// Three-pulse DEER with hard pulses (experiments/esr_dipolar/deer_3p_hard_deer.m,
+// 'brief' output): with U = exp(-1i L stepsize), N = nsteps and
+// rho1 = exp(-1i (pi/2) X_prob) rho0,
+//   trace[j] = coil' U^N P_prob U^(N-j) Pi_pump U^j rho1 / |coil|_2,  j = 0..N,
+// P_prob = exp(-1i pi X_prob), Pi_pump = exp(-1i pi X_pump).  With
+// w = P_prob' (U')^N coil (an adjoint run of N steps, then the pulse by -pi),
+// trace[j] = conj((U')^(N-j) w) Pi_pump U^j rho1: the adjoint trajectory from
+// w read backwards against the forward trajectory from rho1.
+void run_deer(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
+              const double *weights, double stepsize, int64_t nsteps, const spx_csc *ex_prob,
+              const spx_csc *ex_pump, const spx_options &o, double *fid, double *fids_per_orient) {
+    if (h->nchan != 1 || h->n_states != 0)
+        throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil and one initial state");
+    if (nsteps < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "nsteps must be a positive integer");
+    validate_run(h, n_orient, stepsize, nsteps);
+    const int n_pad = h->n_pad;
+    if (n_pad > 8192) throw SpxError(SPX_ERR_UNSUPPORTED, "echo detection is limited to dimension 8192");
+    h->pulses.clear();
+    for (const spx_csc *q : {ex_prob, ex_pump}) {
+        h->pulses.push_back(std::make_unique<PulseOp>());
+        upload_pulse(h, q, *h->pulses.back());
+    }
+    const PulseOp &prob = *h->pulses[0], &pump = *h->pulses[1];
+    upload_grid(h, n_orient, alphas, betas, gammas, weights);
+    const double *g = h->d_grid.p;
+    h->d_seq_rho.reserve(n_pad);
+    SPX_CUDA(cudaMemcpyAsync(h->d_seq_rho.p, h->d_rho0.p, n_pad * sizeof(double2), cudaMemcpyDeviceToDevice,
+                             h->stream));
+    apply_pulse(h, prob, M_PI / 2, 1, h->d_seq_rho.p);
+    upload_echo_propagator(h, pump, M_PI);
+    negate_generator(h);
+    // w = P_prob' (U')^N coil for every orientation
+    h->d_seq[0].reserve((size_t)n_orient * n_pad);
+    h->d_fid.reserve((size_t)nsteps + 1);
+    {
+        RunIO io;
+        io.rho0 = h->d_coil.p;
+        io.state_out = h->d_seq[0].p;
+        io.adjoint = true;
+        const Config c = choose_config(h, n_orient, stepsize, nsteps, o, 0);
+        launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, stepsize, nsteps, o,
+                      h->d_fid.p, c, 0, true, io);
+        finish_run(h);
+    }
+    apply_pulse(h, prob, -M_PI, n_orient, h->d_seq[0].p);
+    echo_trajectories(h, n_orient, g, stepsize, nsteps, o, h->d_seq[0].p, true);
+    // deer_3p_hard_deer.m divides by the 2-norm of the probe coil
+    std::vector<double2> coil(n_pad);
+    SPX_CUDA(cudaMemcpyAsync(coil.data(), h->d_coil.p, n_pad * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    SPX_CUDA(cudaStreamSynchronize(h->stream));
+    double nrm = 0.0;
+    for (const double2 &v : coil) nrm += v.x * v.x + v.y * v.y;
+    if (!(nrm > 0.0)) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "the probe coil is zero");
+    echo_outputs(h, n_orient, nsteps + 1, 1.0 / std::sqrt(nrm), fid, fids_per_orient);
 }
 
 // ---------------------------------------------------------------------------
@@ -1820,6 +1910,28 @@ spx_status spx_run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, 
             throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
         SPX_CUDA(cudaSetDevice(h->device));
         run_eseem(h, n_orient, alphas, betas, gammas, weights, timestep, npoints, pulse_op, o, fid, fids_per_orient);
+    });
+}
+
+spx_status spx_run_deer(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
+                        const double *gammas, const double *weights, double stepsize, int64_t nsteps,
+                        const spx_csc *ex_prob, const spx_csc *ex_pump, const spx_options *opt, double *fid,
+                        double *fids_per_orient) {
+    if (!h) return SPX_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (!alphas || !betas || !gammas || !weights || !fid || !ex_prob || !ex_pump)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "NULL argument");
+        for (int64_t o = 0; o < n_orient; ++o)
+            if (!std::isfinite(alphas[o]) || !std::isfinite(betas[o]) || !std::isfinite(gammas[o]) ||
+                !std::isfinite(weights[o]))
+                throw SpxError(SPX_ERR_INVALID_ARGUMENT, "non-finite grid entry");
+        spx_options o{};
+        if (opt) o = *opt;
+        if (o.precision != SPX_FP32 && o.precision != SPX_FP64)
+            throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
+        SPX_CUDA(cudaSetDevice(h->device));
+        run_deer(h, n_orient, alphas, betas, gammas, weights, stepsize, nsteps, ex_prob, ex_pump, o, fid,
+                 fids_per_orient);
     });
 }
 

@@ -77,6 +77,8 @@ SIGNATURES = {
                                    C.POINTER(SpxSeqOp), C.POINTER(SpxOptions), _D, _D]),
     'spx_run_eseem': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.POINTER(SpxCsc),
                                 C.POINTER(SpxOptions), _D, _D]),
+    'spx_run_deer': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.POINTER(SpxCsc),
+                               C.POINTER(SpxCsc), C.POINTER(SpxOptions), _D, _D]),
     'spx_upload_coils': (C.c_int, [_P, C.c_int32, _D]),
     'spx_set_initial_states': (C.c_int, [_P, C.c_int64, _D]),
     'spx_autotune': (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_double, C.c_int64, C.c_int32,
@@ -349,6 +351,29 @@ class Engine:
                                            float(timestep), int(npoints), C.byref(P.struct), C.byref(opt),
                                            _dptr(fid), _dptr(fids) if fids is not None else None), self.h)
         fs = None if fids is None else fids.view(np.complex128).reshape(al.size, npoints)
+        return PowderResult(fid.view(np.complex128), fs, self.stats())
+
+    def run_deer(self, alphas, betas, gammas, weights, stepsize: float, nsteps: int, ex_prob, ex_pump,
+                 precision: int = FP32, threads: int = 0, cluster: int = 0,
+                 per_orientation: bool = False) -> PowderResult:
+        """Three-pulse DEER with hard pulses (experiments/esr_dipolar/deer_3p_hard_deer.m,
+        'brief'): ``fid[j]`` is the powder DEER trace with the pump pulse j steps
+        after the first probe pulse (nsteps+1 values), divided by the 2-norm of
+        the uploaded (probe) coil."""
+        al = np.ascontiguousarray(alphas, np.float64)
+        be = np.ascontiguousarray(betas, np.float64)
+        ga = np.ascontiguousarray(gammas, np.float64)
+        w = np.ascontiguousarray(weights, np.float64)
+        npts = int(nsteps) + 1
+        fid = np.zeros(2 * npts)
+        fids = np.zeros(2 * npts * al.size) if per_orientation else None
+        Pp, Pu = _CscHolder(ex_prob, self.dim), _CscHolder(ex_pump, self.dim)
+        opt = SpxOptions(precision, 0, threads, cluster, 0.0, 0.0, 0, 0)
+        self._check(self.lib.spx_run_deer(self.h, al.size, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
+                                          float(stepsize), int(nsteps), C.byref(Pp.struct), C.byref(Pu.struct),
+                                          C.byref(opt), _dptr(fid), _dptr(fids) if fids is not None else None),
+                    self.h)
+        fs = None if fids is None else fids.view(np.complex128).reshape(al.size, npts)
         return PowderResult(fid.view(np.complex128), fs, self.stats())
 
     def run_device(self, d_alphas: int, d_betas: int, d_gammas: int, d_weights: int, n_orient: int,

@@ -111,6 +111,26 @@ class _DenseEngine:
             prog += [('pulse', 0, np.pi), ('evolve', 2 * npoints - 1, dt)]
         return self._program(al, be, ga, w, [P], prog)
 
+    def run_deer(self, al, be, ga, w, stepsize, nsteps, ex_prob, ex_pump, precision=None, per_orientation=False):
+        from scipy.linalg import expm
+        _, _, _, rho0, coil = self.sys
+        fids = []
+        for a, b, g in zip(al, be, ga):
+            U = expm(-1j * self._L(a, b, g) * stepsize)
+            Pp, Pu = expm(-1j * np.pi * ex_prob.toarray()), expm(-1j * np.pi * ex_pump.toarray())
+            r = expm(-1j * np.pi / 2 * ex_prob.toarray()) @ rho0
+            out = []
+            for j in range(nsteps + 1):
+                x = np.linalg.matrix_power(U, nsteps) @ Pp @ np.linalg.matrix_power(U, nsteps - j) @ Pu @ r
+                out.append(np.vdot(coil, x) / np.linalg.norm(coil))
+                r = U @ r
+            fids.append(out)
+        return self._Res(fids, w)
+
+    def set_initial_states(self, states):
+        if states is not None:
+            raise NotImplementedError('per-orientation states are not modelled here')
+
     def close(self):
         pass
 
@@ -144,3 +164,23 @@ def test_mas_contexts_project_pulses_into_rotor_space(context, sequence):
     ref = sum(w[i] * one(ss, I, Q, par, (al[i], be[i], ga[i]), sequence=sequence) for i in range(3))
     assert np.abs(ref).max() > 0.05
     assert np.abs(fid - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+def test_powder_deer_context_matches_oracle():
+    """powder(..., @deer_3p_hard_deer, ...): the probe coil is the detection
+    state and the answer is the 'brief' DEER trace."""
+    sys_, inter, spin_system = _system()
+    g = (np.zeros(3), np.array([0.4, 1.3, 2.5]), np.array([0.3, 2.0, 4.1]), np.array([0.2, 0.5, 0.3]))
+    parameters = dict(grid=g, rho0=('Lz', '13C'), coil_prob=('L+', '13C'), ex_prob=('Ly', '13C'),
+                      ex_pump=('Ly', '1H'), stepsize=2e-4, nsteps=10, output='brief')
+    trace, _ = X.powder(spin_system, 'deer_3p_hard_deer', parameters, 'nmr', engine=_DenseEngine())
+    ss = R.basis(R.create(dict(sys_, enable=[]), inter), dict(approximation='none', level=0, space_level=1))
+    ss, I, Q = R.powder_setup(ss, 'nmr')
+    par = dict(rho0=R.state(ss, 'Lz', '13C'), coil_prob=R.state(ss, 'L+', '13C'),
+               ex_prob=R.operator(ss, 'Ly', '13C'), ex_pump=R.operator(ss, 'Ly', '1H'), stepsize=2e-4, nsteps=10)
+    ref = sum(g[3][i] * R.powder_orientation_deer(ss, I, Q, par, (g[0][i], g[1][i], g[2][i])) for i in range(3))
+    assert np.abs(ref).max() > 0.05
+    assert np.abs(trace - ref).max() <= 1e-9 * np.abs(ref).max()
+    with pytest.raises(ValueError):
+        X.powder(spin_system, 'deer_3p_hard_deer', dict(parameters, output='detailed'), 'nmr',
+                 engine=_DenseEngine())

@@ -143,6 +143,27 @@ def test_eseem_matches_kron_model(relax):
         assert rel_err(f_st, f_kr) < 1e-8, ang
 
 
+@pytest.mark.parametrize('relax', [False, True])
+def test_deer_matches_kron_model(relax):
+    """experiments/esr_dipolar/deer_3p_hard_deer.m restated on the
+    spherical-tensor basis (trajectory, stacked pump pulse, reversed
+    refocusing, probe pulse, 'final' evolution) vs Hilbert-space pulses, the
+    probe on 13C and the pump on the protons."""
+    w = _c0_like(relax)
+    ss, I, Q = oracle_system(w)
+    km = KronModel(ss)
+    rho_h = km.spin_op('Lz', '13C') / np.sqrt(km.dim)
+    coil_h = km.spin_op('L+', '13C') / np.sqrt(km.dim)
+    par = dict(rho0=R.state(ss, 'Lz', '13C'), coil_prob=R.state(ss, 'L+', '13C'),
+               ex_prob=R.operator(ss, 'Ly', '13C'), ex_pump=R.operator(ss, 'Ly', '1H'), stepsize=w.dt, nsteps=20)
+    for ang in [(0.0, 0.7, 1.3), (0.4, 1.0, -0.3)]:
+        f_st = R.powder_orientation_deer(ss, I, Q, par, ang) * np.linalg.norm(par['coil_prob'])
+        f_kr = km.deer_3p(ang, rho_h, coil_h, km.spin_op('Ly', '13C'), km.spin_op('Ly', '1H'), w.dt, 20)
+        assert f_st.shape == (21,)
+        assert np.abs(f_kr).max() > 0.05
+        assert rel_err(f_st, f_kr) < 1e-8, ang
+
+
 def test_quadratic_coupling_matches_kron_model():
     """The 2H quadratic coupling (hamiltonian.m:191-257, T(2,0) under 'nmr')
     against L.A.L's secular part (A_zz/2)(3Lz^2 - L^2) in Hilbert space."""
