@@ -496,11 +496,12 @@ def deuterium_leg(device):
 
 def echo_legs(device):
     """Pulse sequences on the evolution core, FP32 with host buffers: CPMG on the c1 system (1000
-    orientations, 128-point half-echoes, 8 loops: 2176 points) and the two-pulse echo on the c4 radical
-    (4000 orientations, 256 points of 8 ns), each against the same run in FP64."""
+    orientations, 128-point half-echoes, 8 loops: 2176 points), the two-pulse echo on the c4 radical
+    (4000 orientations, 256 points of 8 ns) and three-pulse hard DEER on the same radical (probe E,
+    pump 1H, 4000 orientations, 256 pump positions of 8 ns), each against the same run in FP64."""
     from spinach_gb300 import engine as E, spin_system as S, workloads as W
     out = {}
-    for name, w, spin in (('cpmg', W.c1(), '13C'), ('eseem', W.c4(), 'E')):
+    for name, w, spin in (('cpmg', W.c1(), '13C'), ('eseem', W.c4(), 'E'), ('deer', W.c4(), 'E')):
         L = W.build(w)
         ss = W.spin_system_of(w)
         fac = S.factory_for(ss, S.build_basis(ss, w.approximation, w.level))
@@ -512,10 +513,15 @@ def echo_legs(device):
             run = lambda p: eng.run_cpmg(*g, w.dt, 128, 8, pulse, precision=p)
             text = ('CPMG (cpmg.m) on the c1 system: Lz(13C), Ly(13C) pulses, 1000 orientations, '
                     '128-point half-echoes of 5 us, 8 loops (2176 points)')
-        else:
+        elif name == 'eseem':
             run = lambda p: eng.run_eseem(*g, 8e-9, 256, pulse, precision=p)
             text = ('two-pulse echo (eseem.m) on the c4 radical: Lz(E), Ly(E) pulses, 4000 orientations, '
                     '256 echo points, timestep 8 ns')
+        else:
+            pump = sum(fac.operator([('Ly', i)]) for i, iso in enumerate(w.isotopes) if iso == '1H')
+            run = lambda p: eng.run_deer(*g, 8e-9, 255, pulse, pump, precision=p)
+            text = ('three-pulse hard DEER (deer_3p_hard_deer.m) on the c4 radical: Lz(E), probe Ly(E), pump '
+                    'Ly(1H), 4000 orientations, 256 pump positions, stepsize 8 ns')
         run(E.FP32)                                                           # warm-up
         t0 = time.perf_counter()
         r32 = run(E.FP32)

@@ -18,7 +18,10 @@
 //          instead of acquire.m: npoints = nsteps+1 per half-echo, fid
 //          npoints*(1+2*nloops) x 1; pulse_op and sequence = 'eseem' run
 //          experiments/esr_dipolar/eseem.m with timestep = dt and
-//          npoints = nsteps+1 (fid (nsteps+1) x 1); pulse_ops (cell of
+//          npoints = nsteps+1 (fid (nsteps+1) x 1); ex_prob, ex_pump and
+//          sequence = 'deer' run experiments/esr_dipolar/deer_3p_hard_deer.m
+//          ('brief') with stepsize = dt, nsteps pump positions and the probe
+//          coil as coil (fid the (nsteps+1) x 1 DEER trace); pulse_ops (cell of
 //          sparse dim x dim) and program (n x 6: kind 0 = pulse / 1 =
 //          evolution, pulse index (1-based), angle, nsteps, dt, record) run a
 //          pulse program (dt and nsteps of the call are then unused; fid the
@@ -202,6 +205,8 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     CscCopy pulse;
     int32_t nloops = 0;                 // > 0: a CPMG echo train (experiments/cpmg.m)
     bool eseem = false;                 // a two-pulse echo (experiments/esr_dipolar/eseem.m)
+    bool deer = false;                  // three-pulse DEER (experiments/esr_dipolar/deer_3p_hard_deer.m)
+    CscCopy pump;
     std::vector<CscCopy> prog_pulses;   // a pulse program: its operators and operations
     std::vector<spx_seq_op> prog;
     bool program = false;
@@ -245,11 +250,25 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
         if (sq) {
             char buf[16] = {0};
             if (!mxIsChar(sq) || mxGetString(sq, buf, sizeof buf) != 0 ||
-                (std::strcmp(buf, "eseem") != 0 && std::strcmp(buf, "cpmg") != 0))
-                throw GatewayError{"Spinach:spinach_powder_gpu:sequence", "opts.sequence must be 'cpmg' or 'eseem'."};
+                (std::strcmp(buf, "eseem") != 0 && std::strcmp(buf, "cpmg") != 0 && std::strcmp(buf, "deer") != 0))
+                throw GatewayError{"Spinach:spinach_powder_gpu:sequence",
+                                   "opts.sequence must be 'cpmg', 'eseem' or 'deer'."};
             eseem = std::strcmp(buf, "eseem") == 0;
+            deer = std::strcmp(buf, "deer") == 0;
         }
-        if (eseem) {
+        if (deer) {
+            const mxArray *xp = mxGetField(prhs[8], 0, "ex_prob");
+            const mxArray *xu = mxGetField(prhs[8], 0, "ex_pump");
+            if (!xp || !xu || po || nl)
+                throw GatewayError{"Spinach:spinach_powder_gpu:sequence",
+                                   "DEER takes opts.ex_prob and opts.ex_pump, and no opts.pulse_op or opts.nloops."};
+            if (nsteps < 1)
+                throw GatewayError{"Spinach:spinach_powder_gpu:nsteps", "DEER needs a positive nsteps."};
+            fill_csc(xp, n, "opts.ex_prob", pulse);
+            fill_csc(xu, n, "opts.ex_pump", pump);
+            if (nlhs > 1)
+                throw GatewayError{"Spinach:spinach_powder_gpu:nlhs", "DEER returns the powder trace only."};
+        } else if (eseem) {
             if (!po || nl)
                 throw GatewayError{"Spinach:spinach_powder_gpu:sequence", "an echo takes opts.pulse_op and no opts.nloops."};
             fill_csc(po, n, "opts.pulse_op", pulse);
@@ -258,7 +277,7 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
         } else if ((po == nullptr) != (nl == nullptr)) {
             throw GatewayError{"Spinach:spinach_powder_gpu:cpmg", "opts.pulse_op and opts.nloops go together."};
         }
-        if (po && !eseem) {
+        if (po && !eseem && !deer) {
             fill_csc(po, n, "opts.pulse_op", pulse);
             const double v = scalar(nl, "opts.nloops");
             if (v < 1 || v != (double)(int32_t)v)
@@ -309,6 +328,17 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
         plhs[0] = mxCreateDoubleMatrix((mwSize)npts, 1, mxCOMPLEX);
         mxComplexDouble *out = mxGetComplexDoubles(plhs[0]);
         for (int64_t i = 0; i < npts; ++i) { out[i].real = fid[2 * i]; out[i].imag = fid[2 * i + 1]; }
+        return;
+    }
+    if (deer) {
+        std::vector<double> fid(2 * (size_t)(nsteps + 1));
+        st = spx_run_deer(g_handle, no, al.data(), be.data(), ga.data(), wt.data(), dt, nsteps, &pulse.view,
+                          &pump.view, &opt, fid.data(), nullptr);
+        if (st != SPX_OK)
+            throw GatewayError{"Spinach:spinach_powder_gpu:run", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
+        plhs[0] = mxCreateDoubleMatrix((mwSize)(nsteps + 1), 1, mxCOMPLEX);
+        mxComplexDouble *out = mxGetComplexDoubles(plhs[0]);
+        for (int64_t i = 0; i <= nsteps; ++i) { out[i].real = fid[2 * i]; out[i].imag = fid[2 * i + 1]; }
         return;
     }
     if (eseem) {

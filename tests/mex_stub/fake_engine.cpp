@@ -23,7 +23,7 @@ struct Recorded {
     int precision = -1;
     bool want_per = false;
     int fail_run = 0;
-    std::vector<double> pulse;
+    std::vector<double> pulse, pump;
     int64_t npoints = 0;
     int nloops = 0;
 } g_rec;
@@ -134,6 +134,19 @@ spx_status spx_run_eseem(spx_handle *, int64_t no, const double *, const double 
     g_rec.precision = opt ? opt->precision : -1;
     g_rec.pulse.assign(P->values, P->values + 2 * P->colptr[P->n]);
     for (int64_t i = 0; i < npoints; ++i) { fid[2 * i] = 3.0 * i; fid[2 * i + 1] = -1.0; }
+    return SPX_OK;
+}
+spx_status spx_run_deer(spx_handle *, int64_t no, const double *, const double *, const double *, const double *,
+                        double dt, int64_t nsteps, const spx_csc *Pp, const spx_csc *Pu, const spx_options *opt,
+                        double *fid, double *) {
+    g_rec.n_orient = no;
+    g_rec.dt = dt;
+    g_rec.nsteps = nsteps;
+    g_rec.nloops = -3;
+    g_rec.precision = opt ? opt->precision : -1;
+    g_rec.pulse.assign(Pp->values, Pp->values + 2 * Pp->colptr[Pp->n]);
+    g_rec.pump.assign(Pu->values, Pu->values + 2 * Pu->colptr[Pu->n]);
+    for (int64_t i = 0; i <= nsteps; ++i) { fid[2 * i] = 7.0 * i; fid[2 * i + 1] = 0.5; }
     return SPX_OK;
 }
 spx_status spx_run_powder_device(spx_handle *, int64_t, const double *, const double *, const double *,

@@ -22,7 +22,7 @@ struct Recorded {
     int precision;
     bool want_per;
     int fail_run;
-    std::vector<double> pulse;
+    std::vector<double> pulse, pump;
     int64_t npoints;
     int nloops;
 };
@@ -185,6 +185,25 @@ int main() {
     eopt3->fields["sequence"] = str("eseem");
     const mxArray *pe3[9] = {I, Q, R, rho0, coil, grid, scalar(2e-8), scalar(7), eopt3};
     expect(1, 9, pe3, "Spinach:spinach_powder_gpu:sequence");
+    // opts.ex_prob + opts.ex_pump + opts.sequence = 'deer': three-pulse DEER
+    mxArray *dopt = strct();
+    dopt->fields["ex_prob"] = copt->fields["pulse_op"];
+    dopt->fields["ex_pump"] = sparse(n, {2}, {3}, {0.25}, {});
+    dopt->fields["sequence"] = str("deer");
+    const mxArray *pd[9] = {I, Q, R, rho0, coil, grid, scalar(4e-9), scalar(6), dopt};
+    mxArray *od[1] = {nullptr};
+    mexFunction(1, od, 9, pd);
+    CHECK(g_rec.nloops == -3 && g_rec.nsteps == 6 && g_rec.dt == 4e-9 && g_rec.precision == 1);
+    CHECK(g_rec.pump.size() == 2 && g_rec.pump[0] == 0.25);
+    CHECK(od[0] && od[0]->m == 7 && od[0]->n == 1 && od[0]->cx[2].real == 14.0 && od[0]->cx[2].imag == 0.5);
+    expect(2, 9, pd, "Spinach:spinach_powder_gpu:nlhs");
+    const mxArray *pd0[9] = {I, Q, R, rho0, coil, grid, scalar(4e-9), scalar(0), dopt};
+    expect(1, 9, pd0, "Spinach:spinach_powder_gpu:nsteps");
+    mxArray *dopt2 = strct();
+    dopt2->fields["ex_prob"] = copt->fields["pulse_op"];
+    dopt2->fields["sequence"] = str("deer");
+    const mxArray *pd2[9] = {I, Q, R, rho0, coil, grid, scalar(4e-9), scalar(6), dopt2};
+    expect(1, 9, pd2, "Spinach:spinach_powder_gpu:sequence");
     // opts.pulse_ops + opts.program: a pulse program (hp_acquire with an echo)
     mxArray *popt = strct();
     mxArray *pops = cell(1, 2);
