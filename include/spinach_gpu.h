@@ -284,6 +284,14 @@ spx_status spx_run_eseem(spx_handle *handle, int64_t n_orient, const double *alp
                          const spx_csc *pulse_op, const spx_options *opt, double *fid, double *fids_per_orient);
 
 /*
+ * Out-of-phase two-pulse echo (experiments/esr_dipolar/oopeseem.m): as
+ * spx_run_eseem with a 45-degree first pulse exp(-1i*(pi/4)*pulse_op).
+ */
+spx_status spx_run_oopeseem(spx_handle *handle, int64_t n_orient, const double *alphas, const double *betas,
+                            const double *gammas, const double *weights, double timestep, int64_t npoints,
+                            const spx_csc *pulse_op, const spx_options *opt, double *fid, double *fids_per_orient);
+
+/*
  * Three-pulse DEER with hard pulses (experiments/esr_dipolar/
  * deer_3p_hard_deer.m, 'brief' output; replaces the orientation loop of
  * powder.m:226-287 around it): a 90-degree pulse exp(-1i*(pi/2)*ex_prob) on

@@ -151,9 +151,10 @@ class KronModel:
                     r = P @ r
         return np.array(out)
 
-    def eseem(self, angles, rho0, coil, pulse_op, timestep, npoints):
-        """Two-pulse echo: U rho U^dagger pulses (90 then 180 degrees), point n
-        after n steps of timestep/2 on each side of the 180-degree pulse."""
+    def eseem(self, angles, rho0, coil, pulse_op, timestep, npoints, first_angle=np.pi / 2):
+        """Two-pulse echo: U rho U^dagger pulses (first_angle, 90 degrees by
+        default, then 180 degrees), point n after n steps of timestep/2 on
+        each side of the 180-degree pulse."""
         H = self.hamiltonian(angles)
         I = np.eye(self.dim)
         L = np.kron(H, I) - np.kron(I, H.T) + 1j * self.relaxation()
@@ -163,7 +164,7 @@ class KronModel:
             U = sla.expm(-1j * theta * pulse_op)
             return (U @ r.reshape(self.dim, self.dim) @ U.conj().T).reshape(-1)
 
-        r = pulse(rho0.reshape(-1).astype(complex), np.pi / 2)
+        r = pulse(rho0.reshape(-1).astype(complex), first_angle)
         c = coil.reshape(-1)
         out = []
         for n in range(npoints):

@@ -969,18 +969,24 @@ def evolution_refocus(ss: SpinSystem, stack, L, dt: float) -> np.ndarray:
     return clean_up(ss, stack, ss.tols['zte_tol'])
 
 
-def eseem(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
+def eseem(ss: SpinSystem, parameters: dict, H, R, first_angle: float = np.pi / 2) -> np.ndarray:
     """experiments/esr_dipolar/eseem.m:40-64 (K = 0, no screening): 90-degree
     pulse, trajectory of npoints-1 steps of timestep/2, 180-degree pulse on
     every column, refocusing, detection."""
     L = H + 1j * R
     P = parameters['pulse_op']
     tau = parameters['timestep'] / 2
-    rho = step(ss, P, parameters['rho0'], np.pi / 2)
+    rho = step(ss, P, parameters['rho0'], first_angle)
     stack = evolution_trajectory(ss, L, rho, tau, parameters['npoints'] - 1)
     stack = step(ss, P, stack, np.pi)
     stack = evolution_refocus(ss, stack, L, tau)
     return np.asarray(parameters['coil'], complex).conj() @ stack
+
+
+def oopeseem(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
+    """experiments/esr_dipolar/oopeseem.m (K = 0, no screening): eseem.m with
+    a 45-degree first pulse."""
+    return eseem(ss, parameters, H, R, first_angle=np.pi / 4)
 
 
 def evolution_final(ss: SpinSystem, L, rho, dt: float, nsteps: int) -> np.ndarray:
@@ -1019,6 +1025,21 @@ def deer_3p_hard(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
     stack = evolution_final(ss, L, stack, dt, n)
     coil = np.asarray(parameters['coil_prob'], complex)
     return coil.conj() @ stack / np.linalg.norm(coil)
+
+
+def deer_3p_hard_echo(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
+    """experiments/esr_dipolar/deer_3p_hard_echo.m (K = 0): probe 90 degrees,
+    tb, pump 180 degrees, ta-tb, probe 180 degrees, ta-tc/2 (each 'final', one
+    step), then the echo observed over tc in nsteps steps."""
+    L = H + 1j * R
+    ta, tb, tc, n = parameters['ta'], parameters['tb'], parameters['tc'], parameters['nsteps']
+    rho = step(ss, parameters['ex_prob'], parameters['rho0'], np.pi / 2)
+    rho = evolution_final(ss, L, rho, tb, 1)
+    rho = step(ss, parameters['ex_pump'], rho, np.pi)
+    rho = evolution_final(ss, L, rho, ta - tb, 1)
+    rho = step(ss, parameters['ex_prob'], rho, np.pi)
+    rho = evolution_final(ss, L, rho, ta - 0.5 * tc, 1)
+    return evolution_observable(ss, L, parameters['coil'], rho, tc / n, n)
 
 
 # --------------------------------------------------------------------------
@@ -1184,6 +1205,15 @@ def powder_orientation_eseem(ss, I, Q, parameters, angles) -> np.ndarray:
     H = I if A is None else I + A
     H = (H + H.conj().T) / 2
     return eseem(ss, parameters, H, relaxation(ss))
+
+
+def powder_orientation_sequence(ss, I, Q, parameters, angles, sequence) -> np.ndarray:
+    """One iteration of kernel/contexts/powder.m:226-274 with any restated
+    sequence function(ss, parameters, H, R)."""
+    A = orientation(Q, angles)
+    H = I if A is None else I + A
+    H = (H + H.conj().T) / 2
+    return sequence(ss, parameters, H, relaxation(ss))
 
 
 def powder_orientation_deer(ss, I, Q, parameters, angles) -> np.ndarray:

@@ -249,12 +249,22 @@ def _run(eng, pulse_sequence, parameters, work, full, grid, precision, spc_dim: 
             raise ValueError("deer_3p_hard_deer runs output='brief' on this engine")
         return eng.run_deer(al, be, ga, w, float(parameters['stepsize']), int(parameters['nsteps']), op('ex_prob'),
                             op('ex_pump'), precision=precision, per_orientation=not parameters.get('sum_up', 1))
-    if name == 'eseem':
+    if name == 'deer_3p_hard_echo':
+        # deer_3p_hard_echo.m: three hard pulses, three silent delays, the echo over tc
+        ta, tb, tc, n = (float(parameters['ta']), float(parameters['tb']), float(parameters['tc']),
+                         int(parameters['nsteps']))
+        prog = [('pulse', 0, np.pi / 2), ('evolve', 1, tb, False), ('pulse', 1, np.pi),
+                ('evolve', 1, ta - tb, False), ('pulse', 0, np.pi), ('evolve', 1, ta - 0.5 * tc, False),
+                ('evolve', n, tc / n)]
+        return eng.run_sequence(al, be, ga, w, [op('ex_prob'), op('ex_pump')], prog, precision=precision,
+                                per_orientation=not parameters.get('sum_up', 1))
+    if name in ('eseem', 'oopeseem'):
         if spc_dim != 1:
-            raise ValueError('eseem runs in the powder context on this engine')
+            raise ValueError(f'{name} runs in the powder context on this engine')
         P = op('pulse_op')
         return eng.run_eseem(al, be, ga, w, float(parameters['timestep']), int(parameters['npoints']), P,
-                             precision=precision, per_orientation=not parameters.get('sum_up', 1))
+                             precision=precision, per_orientation=not parameters.get('sum_up', 1),
+                             out_of_phase=name == 'oopeseem')
     raise ValueError(f'pulse sequence {pulse_sequence!r} is not supported on this engine')
 
 

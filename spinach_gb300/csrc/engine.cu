@@ -1348,9 +1348,10 @@ void echo_outputs(spx_handle *h, int64_t n_orient, int64_t npoints, double scale
     }
 }
 
+// first_angle: pi/2 for eseem.m, pi/4 for oopeseem.m (the out-of-phase echo).
 void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas, const double *gammas,
                const double *weights, double timestep, int64_t npoints, const spx_csc *pulse_op,
-               const spx_options &o, double *fid, double *fids_per_orient) {
+               double first_angle, const spx_options &o, double *fid, double *fids_per_orient) {
     if (h->nchan != 1 || h->n_states != 0)
         throw SpxError(SPX_ERR_UNSUPPORTED, "pulse sequences take one coil and one initial state");
     if (npoints < 1) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "npoints must be positive");
@@ -1363,11 +1364,11 @@ void run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const doub
     upload_pulse(h, pulse_op, *h->pulses.back());
     const PulseOp &P = *h->pulses.back();
     upload_grid(h, n_orient, alphas, betas, gammas, weights);
-    // rho1 = exp(-1i pi/2 P) rho0
+    // rho1 = exp(-1i first_angle P) rho0
     h->d_seq_rho.reserve(h->n_pad);
     SPX_CUDA(cudaMemcpyAsync(h->d_seq_rho.p, h->d_rho0.p, h->n_pad * sizeof(double2), cudaMemcpyDeviceToDevice,
                              h->stream));
-    apply_pulse(h, P, M_PI / 2, 1, h->d_seq_rho.p);
+    apply_pulse(h, P, first_angle, 1, h->d_seq_rho.p);
     upload_echo_propagator(h, P, M_PI);
     negate_generator(h);
     echo_trajectories(h, n_orient, h->d_grid.p, tau, nsteps, o, nullptr, false);
@@ -1893,9 +1894,11 @@ spx_status spx_run_sequence(spx_handle *h, int64_t n_orient, const double *alpha
     });
 }
 
-spx_status spx_run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
-                         const double *gammas, const double *weights, double timestep, int64_t npoints,
-                         const spx_csc *pulse_op, const spx_options *opt, double *fid, double *fids_per_orient) {
+namespace {
+spx_status run_echo_entry(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
+                          const double *gammas, const double *weights, double timestep, int64_t npoints,
+                          const spx_csc *pulse_op, double first_angle, const spx_options *opt, double *fid,
+                          double *fids_per_orient) {
     if (!h) return SPX_ERR_INVALID_ARGUMENT;
     return guarded(h, [&] {
         if (!alphas || !betas || !gammas || !weights || !fid || !pulse_op)
@@ -1909,8 +1912,24 @@ spx_status spx_run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, 
         if (o.precision != SPX_FP32 && o.precision != SPX_FP64)
             throw SpxError(SPX_ERR_INVALID_ARGUMENT, "unknown precision");
         SPX_CUDA(cudaSetDevice(h->device));
-        run_eseem(h, n_orient, alphas, betas, gammas, weights, timestep, npoints, pulse_op, o, fid, fids_per_orient);
+        run_eseem(h, n_orient, alphas, betas, gammas, weights, timestep, npoints, pulse_op, first_angle, o, fid,
+                  fids_per_orient);
     });
+}
+}  // namespace
+
+spx_status spx_run_eseem(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
+                         const double *gammas, const double *weights, double timestep, int64_t npoints,
+                         const spx_csc *pulse_op, const spx_options *opt, double *fid, double *fids_per_orient) {
+    return run_echo_entry(h, n_orient, alphas, betas, gammas, weights, timestep, npoints, pulse_op, M_PI / 2, opt,
+                          fid, fids_per_orient);
+}
+
+spx_status spx_run_oopeseem(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,
+                            const double *gammas, const double *weights, double timestep, int64_t npoints,
+                            const spx_csc *pulse_op, const spx_options *opt, double *fid, double *fids_per_orient) {
+    return run_echo_entry(h, n_orient, alphas, betas, gammas, weights, timestep, npoints, pulse_op, M_PI / 4, opt,
+                          fid, fids_per_orient);
 }
 
 spx_status spx_run_deer(spx_handle *h, int64_t n_orient, const double *alphas, const double *betas,

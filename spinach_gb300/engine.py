@@ -77,6 +77,8 @@ SIGNATURES = {
                                    C.POINTER(SpxSeqOp), C.POINTER(SpxOptions), _D, _D]),
     'spx_run_eseem': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.POINTER(SpxCsc),
                                 C.POINTER(SpxOptions), _D, _D]),
+    'spx_run_oopeseem': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.POINTER(SpxCsc),
+                                   C.POINTER(SpxOptions), _D, _D]),
     'spx_run_deer': (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.c_double, C.c_int64, C.POINTER(SpxCsc),
                                C.POINTER(SpxCsc), C.POINTER(SpxOptions), _D, _D]),
     'spx_upload_coils': (C.c_int, [_P, C.c_int32, _D]),
@@ -335,10 +337,11 @@ class Engine:
 
     def run_eseem(self, alphas, betas, gammas, weights, timestep: float, npoints: int, pulse_op,
                   precision: int = FP32, threads: int = 0, cluster: int = 0,
-                  per_orientation: bool = False) -> PowderResult:
+                  per_orientation: bool = False, out_of_phase: bool = False) -> PowderResult:
         """Two-pulse echo (experiments/esr_dipolar/eseem.m): ``fid[n]`` is the powder
         echo after a 90-degree pulse, n steps of timestep/2, a 180-degree pulse
-        and n more steps (npoints values)."""
+        and n more steps (npoints values).  out_of_phase: the 45-degree first
+        pulse of experiments/esr_dipolar/oopeseem.m (spx_run_oopeseem)."""
         al = np.ascontiguousarray(alphas, np.float64)
         be = np.ascontiguousarray(betas, np.float64)
         ga = np.ascontiguousarray(gammas, np.float64)
@@ -347,9 +350,10 @@ class Engine:
         fids = np.zeros(2 * npoints * al.size) if per_orientation else None
         P = _CscHolder(pulse_op, self.dim)
         opt = SpxOptions(precision, 0, threads, cluster, 0.0, 0.0, 0, 0)
-        self._check(self.lib.spx_run_eseem(self.h, al.size, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
-                                           float(timestep), int(npoints), C.byref(P.struct), C.byref(opt),
-                                           _dptr(fid), _dptr(fids) if fids is not None else None), self.h)
+        fn = self.lib.spx_run_oopeseem if out_of_phase else self.lib.spx_run_eseem
+        self._check(fn(self.h, al.size, _dptr(al), _dptr(be), _dptr(ga), _dptr(w), float(timestep), int(npoints),
+                       C.byref(P.struct), C.byref(opt), _dptr(fid), _dptr(fids) if fids is not None else None),
+                    self.h)
         fs = None if fids is None else fids.view(np.complex128).reshape(al.size, npoints)
         return PowderResult(fid.view(np.complex128), fs, self.stats())
 

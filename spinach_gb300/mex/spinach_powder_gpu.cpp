@@ -18,7 +18,8 @@
 //          instead of acquire.m: npoints = nsteps+1 per half-echo, fid
 //          npoints*(1+2*nloops) x 1; pulse_op and sequence = 'eseem' run
 //          experiments/esr_dipolar/eseem.m with timestep = dt and
-//          npoints = nsteps+1 (fid (nsteps+1) x 1); ex_prob, ex_pump and
+//          npoints = nsteps+1 (fid (nsteps+1) x 1), sequence = 'oopeseem'
+//          the out-of-phase echo of oopeseem.m; ex_prob, ex_pump and
 //          sequence = 'deer' run experiments/esr_dipolar/deer_3p_hard_deer.m
 //          ('brief') with stepsize = dt, nsteps pump positions and the probe
 //          coil as coil (fid the (nsteps+1) x 1 DEER trace); pulse_ops (cell of
@@ -205,6 +206,7 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     CscCopy pulse;
     int32_t nloops = 0;                 // > 0: a CPMG echo train (experiments/cpmg.m)
     bool eseem = false;                 // a two-pulse echo (experiments/esr_dipolar/eseem.m)
+    bool out_of_phase = false;          // its 45-degree first pulse (experiments/esr_dipolar/oopeseem.m)
     bool deer = false;                  // three-pulse DEER (experiments/esr_dipolar/deer_3p_hard_deer.m)
     CscCopy pump;
     std::vector<CscCopy> prog_pulses;   // a pulse program: its operators and operations
@@ -250,10 +252,12 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
         if (sq) {
             char buf[16] = {0};
             if (!mxIsChar(sq) || mxGetString(sq, buf, sizeof buf) != 0 ||
-                (std::strcmp(buf, "eseem") != 0 && std::strcmp(buf, "cpmg") != 0 && std::strcmp(buf, "deer") != 0))
+                (std::strcmp(buf, "eseem") != 0 && std::strcmp(buf, "oopeseem") != 0 &&
+                 std::strcmp(buf, "cpmg") != 0 && std::strcmp(buf, "deer") != 0))
                 throw GatewayError{"Spinach:spinach_powder_gpu:sequence",
-                                   "opts.sequence must be 'cpmg', 'eseem' or 'deer'."};
-            eseem = std::strcmp(buf, "eseem") == 0;
+                                   "opts.sequence must be 'cpmg', 'eseem', 'oopeseem' or 'deer'."};
+            out_of_phase = std::strcmp(buf, "oopeseem") == 0;
+            eseem = out_of_phase || std::strcmp(buf, "eseem") == 0;
             deer = std::strcmp(buf, "deer") == 0;
         }
         if (deer) {
@@ -343,8 +347,9 @@ void run(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     }
     if (eseem) {
         std::vector<double> fid(2 * (size_t)(nsteps + 1));
-        st = spx_run_eseem(g_handle, no, al.data(), be.data(), ga.data(), wt.data(), dt, nsteps + 1, &pulse.view, &opt,
-                           fid.data(), nullptr);
+        st = (out_of_phase ? spx_run_oopeseem : spx_run_eseem)(g_handle, no, al.data(), be.data(), ga.data(),
+                                                               wt.data(), dt, nsteps + 1, &pulse.view, &opt,
+                                                               fid.data(), nullptr);
         if (st != SPX_OK)
             throw GatewayError{"Spinach:spinach_powder_gpu:run", std::string(spx_status_string(st)) + ": " + spx_last_error(g_handle)};
         plhs[0] = mxCreateDoubleMatrix((mwSize)(nsteps + 1), 1, mxCOMPLEX);

@@ -136,6 +136,13 @@ spx_status spx_run_eseem(spx_handle *, int64_t no, const double *, const double 
     for (int64_t i = 0; i < npoints; ++i) { fid[2 * i] = 3.0 * i; fid[2 * i + 1] = -1.0; }
     return SPX_OK;
 }
+spx_status spx_run_oopeseem(spx_handle *h, int64_t no, const double *a, const double *b, const double *c,
+                            const double *w, double dt, int64_t npoints, const spx_csc *P, const spx_options *opt,
+                            double *fid, double *per) {
+    spx_run_eseem(h, no, a, b, c, w, dt, npoints, P, opt, fid, per);
+    g_rec.nloops = -4;
+    return SPX_OK;
+}
 spx_status spx_run_deer(spx_handle *, int64_t no, const double *, const double *, const double *, const double *,
                         double dt, int64_t nsteps, const spx_csc *Pp, const spx_csc *Pu, const spx_options *opt,
                         double *fid, double *) {

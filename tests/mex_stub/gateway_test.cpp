@@ -176,6 +176,14 @@ int main() {
     CHECK(g_rec.npoints == 8 && g_rec.nloops == -1 && g_rec.precision == 0 && g_rec.dt == 2e-8);
     CHECK(oe[0] && oe[0]->m == 8 && oe[0]->n == 1 && oe[0]->cx[5].real == 15.0 && oe[0]->cx[5].imag == -1.0);
     expect(2, 9, pe, "Spinach:spinach_powder_gpu:nlhs");
+    mxArray *eoop = strct();
+    eoop->fields["pulse_op"] = copt->fields["pulse_op"];
+    eoop->fields["sequence"] = str("oopeseem");
+    const mxArray *peo[9] = {I, Q, R, rho0, coil, grid, scalar(2e-8), scalar(7), eoop};
+    mxArray *oeo[1] = {nullptr};
+    mexFunction(1, oeo, 9, peo);
+    CHECK(g_rec.nloops == -4 && g_rec.npoints == 8 && g_rec.precision == 1);
+    CHECK(oeo[0] && oeo[0]->m == 8 && oeo[0]->cx[5].real == 15.0);
     mxArray *eopt2 = strct();
     eopt2->fields["pulse_op"] = copt->fields["pulse_op"];
     eopt2->fields["sequence"] = str("hahn");

@@ -184,3 +184,22 @@ def test_powder_deer_context_matches_oracle():
     with pytest.raises(ValueError):
         X.powder(spin_system, 'deer_3p_hard_deer', dict(parameters, output='detailed'), 'nmr',
                  engine=_DenseEngine())
+
+
+def test_powder_deer_echo_context_matches_oracle():
+    """powder(..., @deer_3p_hard_echo, ...) as a pulse program (three hard
+    pulses, three silent delays, the echo over tc) against the oracle."""
+    sys_, inter, spin_system = _system()
+    g = (np.zeros(3), np.array([0.4, 1.3, 2.5]), np.array([0.3, 2.0, 4.1]), np.array([0.2, 0.5, 0.3]))
+    times = dict(ta=6e-4, tb=2e-4, tc=4e-4, nsteps=16)
+    parameters = dict(grid=g, rho0=('Lz', '13C'), coil=('L+', '13C'), ex_prob=('Ly', '13C'), ex_pump=('Ly', '1H'),
+                      **times)
+    echo, _ = X.powder(spin_system, 'deer_3p_hard_echo', parameters, 'nmr', engine=_DenseEngine())
+    ss = R.basis(R.create(dict(sys_, enable=[]), inter), dict(approximation='none', level=0, space_level=1))
+    ss, I, Q = R.powder_setup(ss, 'nmr')
+    par = dict(rho0=R.state(ss, 'Lz', '13C'), coil=R.state(ss, 'L+', '13C'), ex_prob=R.operator(ss, 'Ly', '13C'),
+               ex_pump=R.operator(ss, 'Ly', '1H'), **times)
+    ref = sum(g[3][i] * R.powder_orientation_sequence(ss, I, Q, par, (g[0][i], g[1][i], g[2][i]),
+                                                      R.deer_3p_hard_echo) for i in range(3))
+    assert echo.shape == (17,) and np.abs(ref).max() > 0.05
+    assert np.abs(echo - ref).max() <= 1e-9 * np.abs(ref).max()

@@ -63,3 +63,26 @@ def test_deer_identities_and_checks(gpu_engine):
     gpu_engine.upload_coils([L.coil, L.coil])
     with pytest.raises(E.SpxError):                      # one detection channel
         gpu_engine.run_deer(*g, 10e-6, 8, Xprob, Xpump)
+
+
+def test_deer_echo_program_matches_oracle(gpu_engine):
+    """experiments/esr_dipolar/deer_3p_hard_echo.m as a pulse program on the
+    c4 radical (probe E, pump 1H): three hard pulses, three silent delays and
+    the echo over tc."""
+    w = W.c4_small()
+    L, ss, I, Q, Xprob, Xpump, rho0, coil = _case(w, 'E', '1H', krylov=True)
+    ta, tb, tc, n = 200e-9, 60e-9, 120e-9, 24
+    g = W.zcwn_grid(4)
+    g = (g[0], g[1], g[2], np.array([0.3, 0.2, 0.4, 0.1]))
+    par = dict(rho0=R.state(ss, 'Lz', 'E'), coil=R.state(ss, 'L+', 'E'), ex_prob=R.operator(ss, 'Ly', 'E'),
+               ex_pump=R.operator(ss, 'Ly', '1H'), ta=ta, tb=tb, tc=tc, nsteps=n)
+    ref = sum(g[3][i] * R.powder_orientation_sequence(ss, I, Q, par, (g[0][i], g[1][i], g[2][i]),
+                                                      R.deer_3p_hard_echo) for i in range(4))
+    assert np.abs(ref).max() > 0.02
+    gpu_engine.upload(L.I, L.terms, L.R, rho0, coil)
+    prog = [('pulse', 0, np.pi / 2), ('evolve', 1, tb, False), ('pulse', 1, np.pi), ('evolve', 1, ta - tb, False),
+            ('pulse', 0, np.pi), ('evolve', 1, ta - 0.5 * tc, False), ('evolve', n, tc / n)]
+    for prec, tol in ((E.FP64, 1e-10), (E.FP32, 1e-5)):
+        res = gpu_engine.run_sequence(*g, [Xprob, Xpump], prog, precision=prec)
+        assert res.fid.shape == (n + 1,)
+        assert rel_err(res.fid, ref) <= tol, prec

@@ -78,3 +78,23 @@ def test_eseem_per_orientation_echoes(gpu_engine):
     res = gpu_engine.run_eseem(*g, 20e-6, 40, pulse, precision=E.FP64, per_orientation=True)
     assert res.fids.shape == (9, 40)
     assert np.abs((g[3][:, None] * res.fids).sum(axis=0) - res.fid).max() <= 1e-12 * np.abs(res.fid).max()
+
+
+@pytest.mark.parametrize('wname,spin,timestep,npoints', [('c0', '13C', 20e-6, 48),
+                                                         ('c4_small', 'E', 10e-9, 32)])
+def test_oopeseem_matches_oracle(gpu_engine, wname, spin, timestep, npoints):
+    """experiments/esr_dipolar/oopeseem.m: the echo core with a 45-degree
+    first pulse (spx_run_oopeseem)."""
+    w = getattr(W, wname)()
+    L, ss, I, Q, pulse, rho0, coil = _case(w, spin, krylov=(wname != 'c0'))
+    g = W.zcwn_grid(4)
+    g = (g[0], g[1], g[2], np.array([0.1, 0.4, 0.3, 0.2]))
+    par = dict(rho0=R.state(ss, 'Lz', spin), coil=R.state(ss, 'L+', spin), pulse_op=R.operator(ss, 'Ly', spin),
+               timestep=timestep, npoints=npoints)
+    ref = sum(g[3][i] * R.powder_orientation_sequence(ss, I, Q, par, (g[0][i], g[1][i], g[2][i]), R.oopeseem)
+              for i in range(4))
+    assert np.abs(ref).max() > 0.05
+    gpu_engine.upload(L.I, L.terms, L.R, rho0, coil)
+    for prec, tol in ((E.FP64, 1e-10), (E.FP32, 1e-5)):
+        res = gpu_engine.run_eseem(*g, timestep, npoints, pulse, precision=prec, out_of_phase=True)
+        assert rel_err(res.fid, ref) <= tol, prec

@@ -164,6 +164,25 @@ def test_deer_matches_kron_model(relax):
         assert rel_err(f_st, f_kr) < 1e-8, ang
 
 
+def test_oopeseem_matches_kron_model():
+    """experiments/esr_dipolar/oopeseem.m (the 45-degree first pulse)
+    restated on the spherical-tensor basis vs Hilbert-space pulses."""
+    w = _c0_like(True)
+    ss, I, Q = oracle_system(w)
+    km = KronModel(ss)
+    rho_h = km.spin_op('Lz', '13C') / np.sqrt(km.dim)
+    coil_h = km.spin_op(*w.coil) / np.sqrt(km.dim)
+    par = dict(rho0=R.state(ss, 'Lz', '13C'), coil=R.state(ss, *w.coil), pulse_op=R.operator(ss, 'Ly', '13C'),
+               timestep=2 * w.dt, npoints=24)
+    ang = (0.4, 1.0, -0.3)
+    f_st = R.powder_orientation_sequence(ss, I, Q, par, ang, R.oopeseem)
+    f_kr = km.eseem(ang, rho_h, coil_h, km.spin_op('Ly', '13C'), 2 * w.dt, 24, first_angle=np.pi / 4)
+    assert np.abs(f_kr).max() > 0.05
+    assert rel_err(f_st, f_kr) < 1e-8
+    # not the in-phase echo
+    assert rel_err(f_st, R.powder_orientation_eseem(ss, I, Q, par, ang)) > 0.1
+
+
 def test_quadratic_coupling_matches_kron_model():
     """The 2H quadratic coupling (hamiltonian.m:191-257, T(2,0) under 'nmr')
     against L.A.L's secular part (A_zz/2)(3Lz^2 - L^2) in Hilbert space."""
