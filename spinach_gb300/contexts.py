@@ -202,6 +202,9 @@ def load_grid(path: str):
 
 def _grid(parameters: dict):
     g = parameters['grid']
+    if isinstance(g, str) and g == 'single_crystal':
+        # kernel/grids/single_crystal.mat: one orientation at zero Euler angles, unit weight
+        return (np.zeros(1), np.zeros(1), np.zeros(1), np.ones(1))
     if isinstance(g, str):
         g = load_grid(g)
     if isinstance(g, dict):
@@ -304,6 +307,20 @@ def powder(spin_system: System, pulse_sequence, parameters: dict, assumptions: s
         if engine is None:
             eng.close()
     return _answer(res, parameters), grid
+
+
+def crystal(spin_system: System, pulse_sequence, parameters: dict, assumptions: str, engine=None,
+            precision: int = E.FP64):
+    """kernel/contexts/crystal.m:74-147: the sequence at the single
+    orientation parameters['orientation'] (three Euler angles), H Hermitised
+    as there; returns the answer alone.  A one-point powder on the engine."""
+    o = np.asarray(parameters.get('orientation', []), np.float64).ravel()
+    if o.size != 3 or not np.all(np.isfinite(o)):
+        raise ValueError('parameters.orientation must be a row vector with three numbers')
+    grid = (o[:1].copy(), o[1:2].copy(), o[2:3].copy(), np.ones(1))
+    answer, _ = powder(spin_system, pulse_sequence, dict(parameters, grid=grid), assumptions, engine=engine,
+                       precision=precision)
+    return answer
 
 
 def _mas_name(pulse_sequence, context: str, parameters: dict) -> str:

@@ -102,6 +102,9 @@ class _DenseEngine:
             fids.append(out)
         return self._Res(fids, w)
 
+    def run(self, al, be, ga, w, dt, nsteps, precision=None, per_orientation=False):
+        return self._program(al, be, ga, w, [], [('evolve', nsteps, dt)])
+
     def run_sequence(self, al, be, ga, w, ops, prog, precision=None, per_orientation=False):
         return self._program(al, be, ga, w, ops, prog)
 
@@ -203,3 +206,28 @@ def test_powder_deer_echo_context_matches_oracle():
                                                       R.deer_3p_hard_echo) for i in range(3))
     assert echo.shape == (17,) and np.abs(ref).max() > 0.05
     assert np.abs(echo - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+def test_powder_single_crystal_matches_crystal():
+    """tests/kernel/test_ctx_powder_crystal.m: powder() on the single_crystal
+    grid equals crystal() at zero Euler angles (1e-12), and the oracle."""
+    sys_ = dict(isotopes=['1H'], magnet=14.1)
+    inter = dict(zeeman=dict(eigs=[[-2.0, -2.0, 4.0]], euler=[[0.0, 0.0, 0.0]]))
+    bas = dict(approximation='none', projections=[1])
+    spin_system = X.basis(X.create(sys_, inter), bas)
+    rho = X.state(spin_system, 'L+', '1H')
+    parameters = dict(spins=['1H'], rho0=rho, coil=rho, decouple=[], offset=[0.0], sweep=2000.0, npoints=4,
+                      grid='single_crystal', orientation=[0.0, 0.0, 0.0])
+    fid_powder, g = X.powder(spin_system, 'acquire', parameters, 'nmr', engine=_DenseEngine())
+    fid_crystal = X.crystal(spin_system, 'acquire', parameters, 'nmr', engine=_DenseEngine())
+    assert g[3].tolist() == [1.0] and np.abs(fid_powder - fid_crystal).max() <= 1e-12
+    ss = R.basis(R.create(dict(sys_, enable=[]), inter), dict(bas, space_level=1))
+    ss, I, Q = R.powder_setup(ss, 'nmr')
+    par = dict(rho0=R.state(ss, 'L+', '1H'), coil=R.state(ss, 'L+', '1H'), sweep=2000.0, npoints=4)
+    assert np.abs(fid_crystal - R.powder_orientation_fid(ss, I, Q, par, (0.0, 0.0, 0.0))).max() <= 1e-12
+    # another orientation through crystal() against the oracle
+    ang = [0.3, 1.1, -0.4]
+    f = X.crystal(spin_system, 'acquire', dict(parameters, orientation=ang), 'nmr', engine=_DenseEngine())
+    assert np.abs(f - R.powder_orientation_fid(ss, I, Q, par, tuple(ang))).max() <= 1e-12
+    with pytest.raises(ValueError):                      # crystal.m: a row vector with three numbers
+        X.crystal(spin_system, 'acquire', dict(parameters, orientation=[0.0, 0.0]), 'nmr', engine=_DenseEngine())

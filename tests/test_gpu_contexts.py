@@ -83,6 +83,25 @@ def test_singlerot_reference_single_crystal_case(gpu_engine):
     assert fid.shape == (3,) and abs(fid[0] - np.vdot(rho, rho)) <= 1e-12 and np.all(np.isfinite(fid))
 
 
+def test_reference_powder_crystal_case(gpu_engine):
+    """tests/kernel/test_ctx_powder_crystal.m through the context API: powder()
+    on the single_crystal grid equals crystal() at zero Euler angles."""
+    sys_ = dict(isotopes=['1H'], magnet=14.1)
+    inter = dict(zeeman=dict(eigs=[[-2.0, -2.0, 4.0]], euler=[[0.0, 0.0, 0.0]]))
+    bas = dict(approximation='none', projections=[1])
+    spin_system = X.basis(X.create(sys_, inter), bas)
+    rho = X.state(spin_system, 'L+', '1H')
+    parameters = dict(spins=['1H'], rho0=rho, coil=rho, decouple=[], offset=[0.0], sweep=2000.0, npoints=4,
+                      grid='single_crystal', orientation=[0.0, 0.0, 0.0])
+    fid_powder, _ = X.powder(spin_system, 'acquire', parameters, 'nmr', engine=gpu_engine)
+    fid_crystal = X.crystal(spin_system, 'acquire', parameters, 'nmr', engine=gpu_engine)
+    assert np.abs(fid_powder - fid_crystal).max() <= 1e-12
+    ss = R.basis(R.create(dict(sys_, enable=[]), inter), dict(bas, space_level=1))
+    ss, I, Q = R.powder_setup(ss, 'nmr')
+    par = dict(rho0=R.state(ss, 'L+', '1H'), coil=R.state(ss, 'L+', '1H'), sweep=2000.0, npoints=4)
+    assert rel_err(fid_crystal, R.powder_orientation_fid(ss, I, Q, par, (0.0, 0.0, 0.0))) <= 1e-10
+
+
 def test_floquet_context_matches_oracle(gpu_engine):
     """kernel/contexts/floquet.m through the context API on the reference's
     14-point Lebedev grid, against the oracle's per-orientation Floquet

@@ -195,3 +195,28 @@ def test_powder_sum_equals_explicit_weighted_sum():
         w = -gam * 14.1 * 1e-6 * (0.0 + 4.0 * (3 * math.cos(b) ** 2 - 1) / 2)
         t = np.arange(3) / 2000
         close(cells[n], np.vdot(rho, rho) * np.exp(-1j * w * t), 1e-9, 1e-9)
+
+
+# test_orientation_average_suite.m (the orientation() part; average() is
+# average Hamiltonian theory, not on this path)
+def test_orientation_at_zero_euler_angles():
+    Q = {1: [[None] * 3 for _ in range(3)]}
+    Q[1][0][0] = sp.csc_matrix(np.array([[1.0, 0.0], [0.0, 0.0]]))
+    Q[1][1][1] = sp.csc_matrix(np.array([[0.0, 1.0], [1.0, 0.0]]))
+    Q[1][2][2] = sp.csc_matrix(np.array([[0.0, 0.0], [0.0, 2.0]]))
+    H = R.orientation(Q, (0.0, 0.0, 0.0))
+    close(H, Q[1][0][0] + Q[1][1][1] + Q[1][2][2], 1e-14, 1e-14)
+
+
+# test_step_matches_expm.m, restated in Liouville space: the sign convention
+# rho(t) = exp(-iHt) rho(0) exp(+iHt) of density-matrix evolution
+def test_step_sign_convention_in_liouville_space():
+    ss = R.basis(R.create(dict(isotopes=['1H'], magnet=0.0), dict()), dict(approximation='none'))
+    w, dt = 2 * math.pi * 123, 2.5e-3
+    L = w * R.operator(ss, 'Lz', '1H')
+    x, y = R.state(ss, 'Lx', '1H'), R.state(ss, 'Ly', '1H')
+    rho = x + 0.25 * y
+    c, s = math.cos(w * dt), math.sin(w * dt)
+    ref = (c * x + s * y) + 0.25 * (c * y - s * x)           # Lx -> Lx cos + Ly sin under exp(-iwt Lz)
+    close(R.step(ss, L, rho, dt), ref, 1e-13, 1e-13)
+    close(sla.expm(-1j * dt * L.toarray()) @ rho, ref, 1e-13, 1e-13)
