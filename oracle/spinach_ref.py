@@ -1027,6 +1027,30 @@ def deer_3p_hard(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
     return coil.conj() @ stack / np.linalg.norm(coil)
 
 
+def inv_rec(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
+    """experiments/inv_rec.m (K = 0): rho0 = equilibrium(spin_system), the
+    isotropic lab-frame equilibrium (equilibrium.m:63-67, hamiltonian.m with
+    one output builds no anisotropic part); Ly of spins{1} from L+; a
+    180-degree pulse, n_delays steps of max_delay/n_delays ('trajectory'), a
+    90-degree pulse on every column, then the observable of npoints-1 steps of
+    1/sweep on L+; the answer is npoints x (n_delays+1)."""
+    import copy
+    L = H + 1j * R
+    ssL = assume(copy.deepcopy(ss), 'labframe')
+    IL, _ = hamiltonian(ssL, 'left')
+    rho0 = equilibrium(ssL, IL, {}, (0.0, 0.0, 0.0))
+    spin = parameters['spins'][0]
+    coil = state(ss, 'L+', spin)
+    Lp = operator(ss, 'L+', spin)
+    Ly = (Lp - Lp.conj().T) / 2j
+    rho = step(ss, Ly, rho0, np.pi)
+    nd = parameters['n_delays']
+    stack = evolution_trajectory(ss, L, rho, parameters['max_delay'] / nd, nd)
+    stack = step(ss, Ly, stack, np.pi / 2)
+    return np.stack([evolution_observable(ss, L, coil, stack[:, k], 1.0 / parameters['sweep'],
+                                          parameters['npoints'] - 1) for k in range(nd + 1)], axis=1)
+
+
 def deer_3p_hard_echo(ss: SpinSystem, parameters: dict, H, R) -> np.ndarray:
     """experiments/esr_dipolar/deer_3p_hard_echo.m (K = 0): probe 90 degrees,
     tb, pump 180 degrees, ta-tb, probe 180 degrees, ta-tc/2 (each 'final', one

@@ -252,6 +252,21 @@ def _run(eng, pulse_sequence, parameters, work, full, grid, precision, spc_dim: 
             raise ValueError("deer_3p_hard_deer runs output='brief' on this engine")
         return eng.run_deer(al, be, ga, w, float(parameters['stepsize']), int(parameters['nsteps']), op('ex_prob'),
                             op('ex_pump'), precision=precision, per_orientation=not parameters.get('sum_up', 1))
+    if name == 'inv_rec':
+        # one program per recovery delay: the trajectory column k of inv_rec.m
+        nd = int(parameters['n_delays'])
+        if nd < 1:
+            raise ValueError('parameters.n_delays must be a positive integer')
+        dd, dt, n = float(parameters['max_delay']) / nd, 1.0 / float(parameters['sweep']), int(parameters['npoints']) - 1
+        P = op('pulse_op')
+        runs = []
+        for k in range(nd + 1):
+            prog = ([('pulse', 0, np.pi)] + ([('evolve', k, dd, False)] if k else []) +
+                    [('pulse', 0, np.pi / 2), ('evolve', n, dt)])
+            runs.append(eng.run_sequence(al, be, ga, w, [P], prog, precision=precision,
+                                         per_orientation=not parameters.get('sum_up', 1)))
+        return _Stacked(np.stack([r.fid for r in runs], axis=1),
+                        None if runs[0].fids is None else np.stack([r.fids for r in runs], axis=-1))
     if name == 'deer_3p_hard_echo':
         # deer_3p_hard_echo.m: three hard pulses, three silent delays, the echo over tc
         ta, tb, tc, n = (float(parameters['ta']), float(parameters['tb']), float(parameters['tc']),
@@ -271,6 +286,14 @@ def _run(eng, pulse_sequence, parameters, work, full, grid, precision, spc_dim: 
     raise ValueError(f'pulse sequence {pulse_sequence!r} is not supported on this engine')
 
 
+@dataclass
+class _Stacked:
+    """Several recorded programs side by side: fid is npoints x columns, fids
+    (per orientation) n_orient x npoints x columns."""
+    fid: np.ndarray
+    fids: np.ndarray | None
+
+
 def _answer(res, parameters):
     if parameters.get('sum_up', 1):
         return res.fid
@@ -287,6 +310,13 @@ def powder(spin_system: System, pulse_sequence, parameters: dict, assumptions: s
     the 'brief' output), detected on parameters['coil_prob']."""
     if _name(pulse_sequence) == 'deer_3p_hard_deer':
         parameters = dict(parameters, coil=parameters['coil_prob'])
+    if _name(pulse_sequence) == 'inv_rec':
+        # inv_rec.m makes its own rho0 (the isotropic equilibrium), coil (L+)
+        # and pulse operator (Ly) from parameters.spins{1}
+        if 'rho0' in parameters or parameters.get('needs'):
+            raise ValueError('inv_rec starts from the isotropic thermal equilibrium')
+        spin = list(parameters['spins'])[0]
+        parameters = dict(parameters, needs=['iso_eq'], coil=('L+', spin), pulse_op=('Ly', spin))
     work, full, I, Q, R, rho0, coil, HL = _setup(spin_system, parameters, assumptions, _name(pulse_sequence))
     grid = _grid(parameters)
     eng = engine or E.Engine(0)

@@ -231,3 +231,26 @@ def test_powder_single_crystal_matches_crystal():
     assert np.abs(f - R.powder_orientation_fid(ss, I, Q, par, tuple(ang))).max() <= 1e-12
     with pytest.raises(ValueError):                      # crystal.m: a row vector with three numbers
         X.crystal(spin_system, 'acquire', dict(parameters, orientation=[0.0, 0.0]), 'nmr', engine=_DenseEngine())
+
+
+def test_powder_inv_rec_context_matches_oracle():
+    """powder(..., @inv_rec, ...): the isotropic equilibrium, a 180-degree
+    pulse, n_delays+1 recovery times, a 90-degree pulse and one FID each
+    (npoints x (n_delays+1)), as one pulse program per delay."""
+    sys_, inter, _ = _system(temperature=300.0)
+    inter = dict(inter, relaxation=['damp'], damp_rate=3.0)       # damping: a recovery to see
+    spin_system = X.basis(X.create(sys_, inter), dict(approximation='none'))
+    g = (np.zeros(2), np.array([0.4, 1.3]), np.array([0.3, 2.0]), np.array([0.4, 0.6]))
+    parameters = dict(grid=g, spins=['13C'], n_delays=3, max_delay=0.3, sweep=2e3, npoints=8)
+    fids, _ = X.powder(spin_system, 'inv_rec', parameters, 'nmr', engine=_DenseEngine())
+    ss = R.basis(R.create(dict(sys_, enable=[]), inter), dict(approximation='none', level=0, space_level=1))
+    ss, I, Q = R.powder_setup(ss, 'nmr')
+    ref = sum(g[3][i] * R.powder_orientation_sequence(ss, I, Q, parameters, (g[0][i], g[1][i], g[2][i]), R.inv_rec)
+              for i in range(2))
+    # 13C thermal polarisation at 14.1 T and 300 K is of order 1e-5; the
+    # first point changes with the recovery delay
+    assert fids.shape == (8, 4) and np.abs(ref).max() > 1e-6
+    assert abs(ref[0, 0] - ref[0, -1]) > 0.1 * np.abs(ref).max()
+    assert np.abs(fids - ref).max() <= 1e-9 * np.abs(ref).max()
+    with pytest.raises(ValueError):
+        X.powder(spin_system, 'inv_rec', dict(parameters, rho0=('Lz', '13C')), 'nmr', engine=_DenseEngine())
