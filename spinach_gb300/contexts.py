@@ -5,24 +5,29 @@ input structures (kernel/create.m, kernel/basis.m) as dicts, with 0-based spin
 indices in the coupling keys; ``state`` and ``operator`` build Liouville
 vectors and commutation superoperators (kernel/state.m, kernel/operator.m);
 ``powder(spin_system, pulse_sequence, parameters, assumptions)``,
-``singlerot(...)`` and ``floquet(...)`` run the contexts
-(kernel/contexts/powder.m, singlerot.m, floquet.m)
-with the pulse sequences ``'acquire'``, ``'hp_acquire'``, ``'cpmg'`` and
-``'eseem'`` (experiments/*.m), the parameters named as there.  Every
-orientation runs on the GPU; the host only prepares the system.
+``crystal(...)``, ``singlerot(...)`` and ``floquet(...)`` run the contexts
+(kernel/contexts/powder.m, crystal.m, singlerot.m, floquet.m) with the pulse
+sequences ``'acquire'``, ``'hp_acquire'``, ``'cpmg'``, ``'eseem'``,
+``'oopeseem'``, ``'deer_3p_hard_deer'``, ``'deer_3p_hard_echo'`` and
+``'inv_rec'`` (experiments/*.m; the two MAS contexts run acquire,
+hp_acquire and cpmg), the parameters named as there.  Every orientation runs
+on the GPU; the host only prepares the system.
 
 Supported fields.  sys: isotopes, magnet.  inter: zeeman.eigs/euler (ppm, or
 g for electrons), coordinates (Angstrom), coupling.eigs/euler/scalar (Hz,
 keys (a, b); (a, a) is a quadratic coupling), relaxation (['t1_t2'],
-['damp']), r1_rates, r2_rates, damp_rate.  bas: approximation ('none',
-'IK-0', 'IK-1'), level, projections.  parameters: grid (alphas, betas,
-gammas, weights, or a grid file), rho0 / coil (vectors, or (operator,
-isotope) pairs; rho0 may be a function of (alpha, beta, gamma)), sweep,
-npoints, spins + offset, decouple, homodec_oper + homodec_pwr, dead_time,
-needs (['iso_eq'] or ['aniso_eq'], with inter temperature),
-sum_up, pulse_op, pulse_angle, echo_time, echo_oper, echo_angle, nloops,
-timestep; singlerot adds rate, axis, max_rank.  ``engine`` (an Engine) and
-``precision`` (engine.FP64 or FP32) are optional keyword arguments.
+['damp']), r1_rates, r2_rates, damp_rate, temperature.  bas: approximation
+('none', 'IK-0', 'IK-1'), level, projections.  parameters: grid (alphas,
+betas, gammas, weights, a grid file, or 'single_crystal'), rho0 / coil
+(vectors, or (operator, isotope) pairs; rho0 may be a function of (alpha,
+beta, gamma)), sweep, npoints, spins + offset, decouple, homodec_oper +
+homodec_pwr, dead_time, needs (['iso_eq'] or ['aniso_eq'], with inter
+temperature), sum_up, pulse_op, pulse_angle, echo_time, echo_oper,
+echo_angle, nloops, timestep; DEER: ex_prob, ex_pump, coil_prob, stepsize,
+nsteps, output ('brief'), ta, tb, tc; inv_rec: n_delays, max_delay;
+crystal: orientation; singlerot and floquet: rate, axis, max_rank.
+``engine`` (an Engine) and ``precision`` (engine.FP64 or FP32) are optional
+keyword arguments.
 """
 from __future__ import annotations
 
