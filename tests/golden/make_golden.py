@@ -2,7 +2,8 @@
 
 Run from the repository root:  python tests/golden/make_golden.py
 (``python tests/golden/make_golden.py large`` for the cluster-sized
-systems, ``... deuterium`` for the quadratic-coupling workload, ``... grids``
+systems, ``... deuterium`` for the quadratic-coupling workload,
+``... sequences`` for the pulse sequences and MAS contexts, ``... grids``
 to copy the reference's 14-point Lebedev grid out of its grid file, which
 needs the reference source tree).  Writes tests/golden/*.npz.  Inputs are the seeded workloads of
 spinach_gb300.workloads; FIDs come from the oracle (oracle/spinach_ref.py).
@@ -64,7 +65,54 @@ def grids():
     save('grid_leb_2ang_rank_5.npz', alphas=al, betas=be, gammas=ga, weights=w)
 
 
+SEQ_SEL = np.array([7, 66, 131, 180])
+SEQ_W = np.array([0.1, 0.4, 0.3, 0.2])
+
+
+def sequence_cases():
+    """The c0 system (13C + 2 1H, dim 64) at four zcwn orientations with
+    every restated pulse sequence and both MAS contexts: name -> (function of
+    (ss, I, Q, angles), parameters).  Shared with the regression test."""
+    from oracle import spinach_ref as R
+    from oracle_cases import oracle_system
+    w = W.c0()
+    ss, I, Q = oracle_system(w)
+    Ly = R.operator(ss, 'Ly', '13C')
+    base = dict(rho0=R.state(ss, 'Lz', '13C'), coil=R.state(ss, 'L+', '13C'))
+    cases = {
+        'hp_acquire': (R.hp_acquire, dict(base, pulse_op=Ly, pulse_angle=np.pi / 2, echo_time=37 * w.dt,
+                                          echo_oper=R.operator(ss, 'Lx', '13C'), echo_angle=np.pi,
+                                          sweep=1 / w.dt, npoints=64)),
+        'cpmg': (R.cpmg, dict(base, pulse_op=Ly, timestep=w.dt, npoints=24, nloops=2)),
+        'eseem': (R.eseem, dict(base, pulse_op=Ly, timestep=2 * w.dt, npoints=48)),
+        'oopeseem': (R.oopeseem, dict(base, pulse_op=Ly, timestep=2 * w.dt, npoints=48)),
+        'deer_3p_hard_deer': (R.deer_3p_hard, dict(base, coil_prob=base['coil'], ex_prob=Ly,
+                                                   ex_pump=R.operator(ss, 'Ly', '1H'), stepsize=w.dt,
+                                                   nsteps=40)),
+        'deer_3p_hard_echo': (R.deer_3p_hard_echo, dict(base, ex_prob=Ly, ex_pump=R.operator(ss, 'Ly', '1H'),
+                                                        ta=60 * w.dt, tb=20 * w.dt, tc=40 * w.dt, nsteps=40)),
+    }
+    out = {k: (lambda f, p: (lambda a: R.powder_orientation_sequence(ss, I, Q, p, a, f)))(f, p)
+           for k, (f, p) in cases.items()}
+    mas = dict(rho0=R.state(ss, *w.rho0), coil=R.state(ss, *w.coil), sweep=1 / w.dt, npoints=161,
+               rate=12.5e3, axis=(1.0, 1.0, 1.0), max_rank=4)
+    out['singlerot'] = lambda a: R.singlerot_orientation_fid(ss, I, Q, mas, a)
+    out['floquet'] = lambda a: R.floquet_orientation_fid(ss, I, Q, mas, a)
+    return w, out
+
+
+def sequences():
+    w, cases = sequence_cases()
+    al, be, ga, _ = W.zcwn_grid(w.n_orient)
+    res = {}
+    for name, f in cases.items():
+        res[name] = sum(SEQ_W[i] * f((al[j], be[j], ga[j])) for i, j in enumerate(SEQ_SEL))
+    save('c0_sequences_fp64.npz', sel=SEQ_SEL, weights=SEQ_W, seed=w.seed, **res)
+
+
 def main():
+    if 'sequences' in sys.argv[1:]:
+        return sequences()
     if 'grids' in sys.argv[1:]:
         return grids()
     if 'large' in sys.argv[1:]:
