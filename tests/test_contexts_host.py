@@ -252,5 +252,9 @@ def test_powder_inv_rec_context_matches_oracle():
     assert fids.shape == (8, 4) and np.abs(ref).max() > 1e-6
     assert abs(ref[0, 0] - ref[0, -1]) > 0.1 * np.abs(ref).max()
     assert np.abs(fids - ref).max() <= 1e-9 * np.abs(ref).max()
+    # sum_up = 0: one npoints x (n_delays+1) answer per orientation
+    cells, _ = X.powder(spin_system, 'inv_rec', dict(parameters, sum_up=0), 'nmr', engine=_DenseEngine())
+    assert len(cells) == 2 and all(c.shape == (8, 4) for c in cells)
+    assert np.abs(g[3][0] * cells[0] + g[3][1] * cells[1] - fids).max() <= 1e-12 * np.abs(fids).max()
     with pytest.raises(ValueError):
         X.powder(spin_system, 'inv_rec', dict(parameters, rho0=('Lz', '13C')), 'nmr', engine=_DenseEngine())
