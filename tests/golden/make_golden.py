@@ -3,9 +3,12 @@
 Run from the repository root:  python tests/golden/make_golden.py
 (``python tests/golden/make_golden.py large`` for the cluster-sized
 systems, ``... deuterium`` for the quadratic-coupling workload,
-``... sequences`` for the pulse sequences and MAS contexts, ``... grids``
-to copy the reference's 14-point Lebedev grid out of its grid file, which
-needs the reference source tree).  Writes tests/golden/*.npz.  Inputs are the seeded workloads of
+``... sequences`` for the pulse sequences and MAS contexts, ``... wide``
+for the full c1 powder, many c1/c4 orientations, every c2 dimension and the
+paranoia-mode propagator branch (parallel over the host cores), ``... grids
+<reference root>`` to copy the reference's 14-point Lebedev grid out of its
+grid file, which needs the reference source tree; the root can also come
+from the SPINACH_ROOT environment variable).  Writes tests/golden/*.npz.  Inputs are the seeded workloads of
 spinach_gb300.workloads; FIDs come from the oracle (oracle/spinach_ref.py).
 """
 import os
@@ -57,12 +60,109 @@ def deuterium():
     save('deuterium_powder_fp64.npz', fid=fid, seed=w.seed, nsteps=w.nsteps, n_orient=w.n_orient)
 
 
-def grids():
+def grids(root):
     """kernel/grids/leb_2ang_rank_5.mat of the reference (the grid of
-    tests/kernel/test_ctx_powder_average.m) as arrays."""
+    tests/kernel/test_ctx_powder_average.m) as arrays; ``root`` is the
+    reference's source tree."""
     from spinach_gb300 import contexts as X
-    al, be, ga, w = X.load_grid('/root/reference/kernel/grids/leb_2ang_rank_5.mat')
+    if not root:
+        raise SystemExit('give the reference source tree: make_golden.py grids <root> (or SPINACH_ROOT)')
+    al, be, ga, w = X.load_grid(os.path.join(root, 'kernel', 'grids', 'leb_2ang_rank_5.mat'))
     save('grid_leb_2ang_rank_5.npz', alphas=al, betas=be, gammas=ga, weights=w)
+
+
+_SYSTEMS = {}
+
+
+def _workload(kind, idx):
+    if kind == 'c2':
+        return W.c2()[idx]
+    return {'c1': W.c1, 'c4': W.c4}[kind]()
+
+
+def _orient_fids(task):
+    """Worker: per-orientation FP64 FIDs of grid points ``sel`` of a workload
+    (one oracle setup per worker and system)."""
+    from oracle import spinach_ref as R
+    from oracle_cases import oracle_system
+    kind, idx, sel, tol_mode, krylov = task
+    w = _workload(kind, idx)
+    key = (kind, idx, tol_mode, krylov)
+    if key not in _SYSTEMS:
+        _SYSTEMS[key] = oracle_system(w, tol_mode, krylov)
+    ss, I, Q = _SYSTEMS[key]
+    al, be, ga, _ = W.zcwn_grid(w.n_orient)
+    sel = np.asarray(sel)
+    par = dict(rho0=R.state(ss, *w.rho0), coil=R.state(ss, *w.coil), sweep=1 / w.dt, npoints=w.nsteps + 1)
+    grid = (al[sel], be[sel], ga[sel], np.ones(sel.size))
+    return sel, np.array(R.powder(ss, par, w.assumptions, grid, setup=(I, Q), sum_up=False))
+
+
+def _pool_fids(pool, kind, idx, sel, tol_mode='default', krylov=True, chunk=8):
+    """Per-orientation FIDs of the grid points ``sel``, computed in parallel,
+    returned in the order of ``sel``."""
+    sel = np.asarray(sel)
+    tasks = [(kind, idx, sel[i:i + chunk].tolist(), tol_mode, krylov) for i in range(0, sel.size, chunk)]
+    out = {}
+    for s, f in pool.imap_unordered(_orient_fids, tasks):
+        for j, fj in zip(s, f):
+            out[int(j)] = fj
+    return np.array([out[int(j)] for j in sel])
+
+
+def wide():
+    """Wide parity fixtures, parallel over the host cores (spawned workers,
+    one BLAS thread each):
+      * c1: the whole 1000-orientation powder FID (Krylov branch, summed in
+        grid order as powder.m:280-287 does) and 32 per-orientation FIDs;
+      * c1: two orientations of the default propagator branch with
+        prop_chop = eps ('paranoia', kernel/utilities/tolerances.m:97-100);
+      * c4: 24 per-orientation FIDs (Krylov branch);
+      * c2: four orientations of the first system of every dimension, and the
+        whole 400-orientation powder of the dim-64, -256 and -1024 systems."""
+    import multiprocessing as mp
+    for v in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
+        os.environ[v] = '1'
+    t0 = time.time()
+    with mp.get_context('spawn').Pool(os.cpu_count()) as pool:
+        w = W.c1()
+        fids = _pool_fids(pool, 'c1', 0, np.arange(w.n_orient), chunk=20)
+        _, _, _, wt = W.zcwn_grid(w.n_orient)
+        fid = wt[0] * fids[0]
+        for n in range(1, w.n_orient):
+            fid = fid + wt[n] * fids[n]
+        sel = np.linspace(0, w.n_orient - 1, 32).round().astype(int)
+        save('c1_powder_krylov_fp64.npz', fid=fid, sel=sel, fids=fids[sel], seed=w.seed, nsteps=w.nsteps,
+             n_orient=w.n_orient)
+        print('c1 powder', round(time.time() - t0, 1), 's')
+        psel = np.array([0, 611])
+        fp = _pool_fids(pool, 'c1', 0, psel, tol_mode='paranoia', krylov=False, chunk=1)
+        save('c1_orient_propagator_paranoia_fp64.npz', sel=psel, fids=fp, seed=w.seed, nsteps=w.nsteps)
+        print('c1 paranoia', round(time.time() - t0, 1), 's')
+        w = W.c4()
+        sel = np.linspace(7, w.n_orient - 1, 24).round().astype(int)
+        save('c4_orients_krylov_fp64.npz', sel=sel, fids=_pool_fids(pool, 'c4', 0, sel, chunk=1), seed=w.seed,
+             nsteps=w.nsteps)
+        print('c4', round(time.time() - t0, 1), 's')
+        ws = W.c2()
+        dims = {}
+        for i, x in enumerate(ws):
+            d = W.build(x).dim
+            dims.setdefault(d, i)
+        for d, i in sorted(dims.items()):
+            x = ws[i]
+            sel = np.array([13, 111, 257, 389])
+            kw = dict(system=i, dim=d, sel=sel, fids=_pool_fids(pool, 'c2', i, sel, chunk=1), seed=x.seed,
+                      nsteps=x.nsteps)
+            if d <= 1024:
+                _, _, _, wt = W.zcwn_grid(x.n_orient)
+                f = _pool_fids(pool, 'c2', i, np.arange(x.n_orient), chunk=10)
+                p = wt[0] * f[0]
+                for n in range(1, x.n_orient):
+                    p = p + wt[n] * f[n]
+                kw['fid'] = p
+            save(f'c2_dim{d}_krylov_fp64.npz', **kw)
+            print('c2 dim', d, round(time.time() - t0, 1), 's')
 
 
 SEQ_SEL = np.array([7, 66, 131, 180])
@@ -114,7 +214,10 @@ def main():
     if 'sequences' in sys.argv[1:]:
         return sequences()
     if 'grids' in sys.argv[1:]:
-        return grids()
+        rest = sys.argv[sys.argv.index('grids') + 1:]
+        return grids(rest[0] if rest else os.environ.get('SPINACH_ROOT'))
+    if 'wide' in sys.argv[1:]:
+        return wide()
     if 'large' in sys.argv[1:]:
         return large_systems()
     if 'deuterium' in sys.argv[1:]:
