@@ -321,3 +321,34 @@ def test_homodecoupling_matches_oracle():
                homodec_oper=R.operator(ss, 'Lx', '1H'), homodec_pwr=2500.0)
     ang = (0.0, 1.1, 0.4)
     assert rel_err(_dense_fid(L, ang, w.dt, 64), R.powder_orientation_fid(ss, I, Q, par, ang)) < 1e-10
+
+
+@pytest.mark.parametrize('approx', ['IK-0', 'IK-1'])
+def test_restricted_basis_at_full_level_is_the_full_basis(approx):
+    """basis.m:186-269: an IK-0 or IK-1 basis whose correlation level equals
+    the spin count keeps every product state, so the restricted-basis
+    machinery (oracle and product builder alike) must return the full basis,
+    and the FIDs computed in it must match the independent Zeeman-basis model
+    (oracle/kron_model.py) -- the check that pins the IK code paths of c1, c2
+    and c4 on a system small enough for the model."""
+    w = _c0_like(True)
+    w.approximation, w.level = approx, len(w.isotopes)
+    ss, I, Q = oracle_system(w)
+    assert ss.basis.shape[0] == 4 ** len(w.isotopes)
+    full = _c0_like(True)
+    ssf, _, _ = oracle_system(full)
+    assert sorted(map(tuple, ss.basis.tolist())) == sorted(map(tuple, ssf.basis.tolist()))
+    L = W.build(w)
+    pss = W.spin_system_of(w)
+    pb = S.build_basis(pss, w.approximation, w.level)
+    assert pb.dim == 4 ** len(w.isotopes)
+    assert sorted(map(tuple, pb.codes.tolist())) == sorted(map(tuple, ss.basis.tolist()))
+    km = KronModel(ss)
+    rho_h = km.spin_op(*w.rho0) / np.sqrt(km.dim)
+    coil_h = km.spin_op(*w.coil) / np.sqrt(km.dim)
+    par = dict(rho0=R.state(ss, *w.rho0), coil=R.state(ss, *w.coil), sweep=1 / w.dt, npoints=129)
+    for ang in [(0.0, 0.7, 1.3), (0.4, 1.9, -0.3)]:
+        f_st = R.powder_orientation_fid(ss, I, Q, par, ang)
+        f_kr = km.fid(ang, rho_h, coil_h, w.dt, 128)
+        assert rel_err(f_st, f_kr) < 1e-8, ang
+    assert L.dim == ss.basis.shape[0]

@@ -220,3 +220,24 @@ def test_step_sign_convention_in_liouville_space():
     ref = (c * x + s * y) + 0.25 * (c * y - s * x)           # Lx -> Lx cos + Ly sin under exp(-iwt Lz)
     close(R.step(ss, L, rho, dt), ref, 1e-13, 1e-13)
     close(sla.expm(-1j * dt * L.toarray()) @ rho, ref, 1e-13, 1e-13)
+
+
+def test_point_dipole_xyz2dd():
+    """tests/kernel/test_dynamic_physics_formulae_suite.m:38-44 (xyz2dd): a
+    1H-13C pair one Angstrom apart along z has the point-dipole constant
+    d = gamma1*gamma2*hbar*mu0/(4*pi*r^3) and the traceless tensor
+    d*diag(1, 1, -2).  The oracle (kernel/utilities/dipolar.m, half of the
+    tensor on each ordered pair) and the product's host builder must give it,
+    at the reference test's 1e-6 relative tolerance (its hbar and mu0 are
+    the older CODATA values)."""
+    from spinach_gb300 import spin_system as S
+    hbar, mu0 = 1.054571628e-34, 4 * np.pi * 1e-7
+    d_ref = R.ISOTOPES['1H'][1] * R.ISOTOPES['13C'][1] * hbar * mu0 / (4 * np.pi * (1e-10) ** 3)
+    M_ref = d_ref * np.diag([1.0, 1.0, -2.0])
+    ss = R.create(dict(isotopes=['1H', '13C'], magnet=14.1), dict(coordinates=[[0, 0, 0], [0, 0, 1]]))
+    M = ss.coupling[(0, 1)] + ss.coupling[(1, 0)]
+    assert np.abs(M - M_ref).max() <= 1e-6 * abs(d_ref)
+    pss = S.make_spin_system(['1H', '13C'], 14.1, coordinates=[[0, 0, 0], [0, 0, 1]])
+    P = pss.couplings[(0, 1)] + pss.couplings[(1, 0)]
+    assert np.abs(P - M_ref).max() <= 1e-6 * abs(d_ref)
+    assert np.abs(P - M).max() <= 1e-14 * abs(d_ref)

@@ -138,3 +138,23 @@ def test_floquet_liouvillian_matches_oracle():
     assert np.abs(A - F).max() <= 1e-12 * np.abs(F).max()
     assert np.abs(F - F.conj().T).max() <= 1e-10 * np.abs(F).max()
     assert rho0.shape == (N * dim,) and np.isclose(np.vdot(coil, rho0), np.vdot(L.coil, L.rho0))
+
+
+def test_reference_floquet_acquire_known_answers():
+    """tests/kernel/test_ctx_floquet_acquire.m:25-66: one 1H with an axial
+    shift tensor (projections +1 basis), max_rank 1, 1 kHz about (1,1,1),
+    three points at 2 kHz on the reference's 14-point Lebedev grid
+    (leb_2ang_rank_5): three points, the zero-time signal equals coil'*rho0
+    to 1e-12 (the Floquet projection preserves the initial overlap), all
+    finite."""
+    import os
+    ss, I, Q = _one_proton()
+    d = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'grid_leb_2ang_rank_5.npz'))
+    rho0 = R.state(ss, 'L+', '1H')
+    par = dict(rho0=rho0, coil=rho0, sweep=2000.0, npoints=3, rate=1000.0, axis=(1, 1, 1), max_rank=1)
+    fid = sum(d['weights'][i] * R.floquet_orientation_fid(ss, I, Q, par, (d['alphas'][i], d['betas'][i],
+                                                                          d['gammas'][i]))
+              for i in range(d['weights'].size))
+    assert fid.shape == (3,)
+    assert abs(fid[0] - np.vdot(rho0, rho0)) <= 1e-12
+    assert np.all(np.isfinite(fid))
