@@ -65,8 +65,26 @@ typedef struct {
                                   (the autotuned value, else the largest that fits) */
     int32_t lanczos_its;       /* Lanczos steps of the per-orientation spectral bound,
                                   0 = 32, else 2..48 (fewer: looser, cheaper bounds) */
-    int32_t reserved;
+    int32_t flags;             /* SPX_FLAG_* bits, 0 = defaults */
 } spx_options;
+
+/*
+ * FP32 runs of spx_run_powder and spx_run_powder_device re-run
+ * SPX_FP32_CHECKED_ORIENTATIONS orientations of the grid (evenly spaced) in
+ * FP64 on a second stream while the FP32 run proceeds on the other SMs, and
+ * report the largest relative 2-norm error of their FIDs in
+ * spx_stats.fp32_rel_error and the error it implies for the powder FID in
+ * spx_stats.fp32_powder_error.  When the error of what the caller receives
+ * (the powder FID, and every orientation's FID when fids_per_orient is
+ * given) exceeds half of SPX_FP32_ERROR_BAR (a margin for an estimate drawn
+ * from two orientations), spx_run_powder runs the whole grid again in FP64
+ * and returns that result (spx_stats.promoted_fp64 = 1);
+ * spx_run_powder_device only reports the errors.
+ */
+#define SPX_FP32_ERROR_BAR 1e-5
+#define SPX_FP32_CHECKED_ORIENTATIONS 2
+#define SPX_FLAG_NO_FP32_CHECK 1   /* skip the FP64 check of an FP32 run */
+#define SPX_FLAG_NO_PROMOTE 2      /* report the check, never re-run in FP64 */
 
 /* Statistics of the last spx_run_powder* call on a handle. */
 typedef struct {
@@ -92,6 +110,21 @@ typedef struct {
     int32_t channels;          /* detection channels of the run */
     int32_t retries;           /* 1 if spx_run_powder re-ran after a device status
                                   (wider series table and the safe spectral bound) */
+    int32_t fp32_checked;      /* orientations of the last FP32 run that were also run in
+                                  FP64 to measure its error (0: not measured) */
+    int64_t kernel_launches;   /* run kernels this handle has launched since spx_create
+                                  (propagation, powder sums, pulses, echo forms, checks;
+                                  spx_build_system's construction kernels not included) */
+    double fp32_rel_error;     /* largest relative 2-norm error ||f32 - f64|| / ||f64|| of
+                                  the checked orientations' FIDs (0 when not measured) */
+    int32_t promoted_fp64;     /* 1 if spx_run_powder found the FP32 error above the
+                                  bar and returned an FP64 re-run instead */
+    int32_t reserved;
+    double fp32_powder_error;  /* the error those imply for the powder FID, two parts in
+                                  quadrature: the checked orientations' running relative
+                                  error weighted by the powder FID's intensity over time,
+                                  and their rms error norm summed as independent errors
+                                  over the grid weights (0 when not measured) */
 } spx_stats;
 
 typedef struct spx_handle spx_handle;
@@ -177,15 +210,23 @@ spx_status spx_run_powder_device(spx_handle *handle, int64_t n_orient,
  * gpuArray pool already holds it, or instrument software that budgets memory
  * at start-up) and code that must not trigger the implicit device-wide
  * synchronisation a cudaMalloc/cudaFree can cause.  Uses the system already
- * uploaded on the handle; the grid (d_alphas, d_betas, d_gammas, d_weights:
- * n_orient doubles each) and d_fid (2*(nsteps+1) doubles) are caller-owned
- * device memory.  Every intermediate lives in one static device array of
+ * uploaded on the handle (with its detection channels and per-orientation
+ * initial states, if set); the grid (d_alphas, d_betas, d_gammas, d_weights:
+ * n_orient doubles each) and d_fid (2*(nsteps+1) doubles per channel, channel
+ * by channel) are caller-owned device memory.  Every intermediate lives in one static device array of
  * SPX_NOALLOC_SCRATCH_BYTES per GPU (held from library load until process
  * exit); runs needing more return SPX_ERR_UNSUPPORTED before any work is
- * queued.  Chunks are capped at 64 steps.  The first call on a device looks up
- * the array's address and should therefore come before any stream capture.
- * The call blocks until the run has finished.  Calls share the array: calls
- * that overlap on the GPU (other threads or handles on the same device) race.
+ * queued (a 1156-dimensional system over 2048 steps fits about 1.8k
+ * orientations in FP32 and 0.9k in FP64: the Bessel tables of the 152 CTAs
+ * take about 35 MB of the array).  Chunks are capped at 64 steps.  The
+ * first call on a device (and the first after the device's context was reset)
+ * looks up the array's address and should therefore come before any stream
+ * capture.  The call waits for its stream before it returns.  Calls share the
+ * array, which keeps the last call's contents: calls that overlap on the GPU
+ * (other threads or handles on the same device) race.  If an orientation fails
+ * its series checks the call returns SPX_ERR_SERIES and d_fid holds no usable
+ * result: unlike spx_run_powder it does not retry with conservative bounds,
+ * and it leaves the handle's spx_stats as they were.
  */
 #define SPX_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 spx_status spx_run_powder_noalloc(spx_handle *handle, int64_t n_orient,

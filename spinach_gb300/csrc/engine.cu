@@ -7,6 +7,7 @@
 // kernels of kernels.cuh for every orientation grid.  Also here: the launch
 // configuration (one CTA or a cluster per orientation), the autotuner, the
 // no-allocation entry point and batched CUDA graphs over many handles.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -124,6 +125,24 @@ struct spx_handle {
     DevBuf<long long> d_matvecs;
     DevBuf<double> d_halfwidth;
     DevBuf<int> d_counter;           // orientation work counter of the propagation kernel
+
+    int64_t launches = 0;           // kernels launched by this handle (spx_stats.kernel_launches)
+
+    // FP64 check of FP32 runs: a few orientations re-run in FP64 on a second
+    // stream while the FP32 run proceeds (spx_stats.fp32_rel_error)
+    cudaStream_t check_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    DevBuf<double> d_chk_grid;       // alpha | beta | gamma of the checked orientations
+    DevBuf<double2> d_chk_rho0s;     // their initial states when per-orientation states are set
+    DevBuf<unsigned char> d_chk_fids;
+    DevBuf<double> d_chk_table, d_chk_halfwidth;
+    DevBuf<int> d_chk_status, d_chk_kused, d_chk_mused, d_chk_counter;
+    DevBuf<long long> d_chk_matvecs;
+    int chk_pending = 0;             // checked orientations of the pending run (0: none)
+    std::vector<int> chk_index;      // their grid indices
+    const double2 *chk_out = nullptr;    // the pending run's powder FID (device)
+    const double *chk_w = nullptr;       // and its grid weights (device)
+    int64_t chk_nsteps = 0;
 
     // last run
     spx_stats stats{};
@@ -657,7 +676,9 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
             M = (int)std::min<int64_t>(M, nsteps + 1);
             M = std::max(M, 1);
             c.M = M;
-            const double xu = c.fixed ? std::max(h->g_upper * M * dt, 1.0) : c.chunk_x;
+            // a single step whose series argument exceeds the target (long
+            // delays of a pulse program) still gets a table that holds its series
+            const double xu = c.fixed ? std::max(h->g_upper * M * dt, 1.0) : std::max(c.chunk_x, h->g_upper * dt);
             int K = (int)host_series_terms(xu, std::min(lg, 0.05), c.tol) + 16;
             if (kmax_override > 0) K = std::max(K, kmax_override);
             c.Kmax = std::min(K, 8192);
@@ -708,16 +729,19 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
 }
 
 // Launch the propagation kernel (plain or cluster launch) on the handle's stream.
-void launch_chebyshev(spx_handle *h, bool f64, const Config &c, spx::DevSystem &sys, spx::DevRun &run) {
-    SPX_CUDA(cudaMemsetAsync(run.next_orient, 0, sizeof(int), h->stream));
+void launch_chebyshev(spx_handle *h, bool f64, const Config &c, spx::DevSystem &sys, spx::DevRun &run,
+                      cudaStream_t stream = nullptr) {
+    if (!stream) stream = h->stream;
+    SPX_CUDA(cudaMemsetAsync(run.next_orient, 0, sizeof(int), stream));
     run.cl = c.cl;
     run.nsl_loc = c.nsl_loc;
     run.ell_loc = c.ell_loc;
     for (int j = 0; j <= spx::kMaxCluster; ++j) run.cl_slices[j] = j <= c.cl ? c.slices[j] : 0;
     const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1, h->ncoil > 0, c.traj);
     void *args[] = {&sys, &run};
+    ++h->launches;
     if (c.cl == 1) {
-        SPX_CUDA(cudaLaunchKernel(kfn, dim3(c.grid), dim3(c.threads), args, c.smem, h->stream));
+        SPX_CUDA(cudaLaunchKernel(kfn, dim3(c.grid), dim3(c.threads), args, c.smem, stream));
         return;
     }
     cudaLaunchConfig_t lc{};
@@ -729,7 +753,7 @@ void launch_chebyshev(spx_handle *h, bool f64, const Config &c, spx::DevSystem &
     lc.gridDim = dim3((unsigned)c.grid);
     lc.blockDim = dim3((unsigned)c.threads);
     lc.dynamicSmemBytes = c.smem;
-    lc.stream = h->stream;
+    lc.stream = stream;
     lc.attrs = at;
     lc.numAttrs = 1;
     SPX_CUDA(cudaLaunchKernelExC(&lc, kfn, args));
@@ -762,11 +786,77 @@ struct RunIO {
     bool adjoint = false;              // propagate under -H + 1i R (the adjoint of L, negated)
 };
 
+spx_options apply_tuned(const spx_handle *h, spx_options o);
+
+constexpr int kCheckOrients = SPX_FP32_CHECKED_ORIENTATIONS;   // orientations of an FP32 run re-run in FP64
+
+// Orientation indices checked in FP64: evenly spaced over the grid.
+int check_index(int j, int S, int64_t n_orient) { return (int)(((2 * (int64_t)j + 1) * n_orient) / (2 * S)); }
+
+// Enqueue the FP64 re-run of the checked orientations on the check stream
+// (forked from the handle's stream) and return its CTA count, so that the
+// FP32 launch can leave those SMs to it.
+int launch_fp32_check(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be, const double *d_ga,
+                      double dt, int64_t nsteps, const spx_options &opt, const spx::DevSystem &sys32) {
+    const int S = (int)std::min<int64_t>(kCheckOrients, n_orient);
+    spx_options o64{};
+    o64.precision = SPX_FP64;
+    o64.lanczos_its = opt.lanczos_its;
+    o64 = apply_tuned(h, o64);
+    const Config c = choose_config(h, S, dt, nsteps, o64, 0);
+    const size_t npts = ((size_t)nsteps + 1) * h->nchan;
+    if (!h->check_stream) {
+        SPX_CUDA(cudaStreamCreateWithFlags(&h->check_stream, cudaStreamNonBlocking));
+        SPX_CUDA(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+        SPX_CUDA(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+    }
+    h->d_chk_grid.reserve(3 * (size_t)S);
+    h->d_chk_fids.reserve(npts * S * sizeof(double2));
+    h->d_chk_table.reserve((size_t)c.grid * c.Kmax * (c.M + 1));
+    h->d_chk_status.reserve(S);
+    h->d_chk_kused.reserve(S);
+    h->d_chk_mused.reserve(S);
+    h->d_chk_matvecs.reserve(S);
+    h->d_chk_halfwidth.reserve(S);
+    h->d_chk_counter.reserve(1);
+    if (sys32.rho0s) h->d_chk_rho0s.reserve((size_t)S * h->n_pad);
+    std::vector<int> &idx = h->chk_index;
+    idx.resize(S);
+    for (int j = 0; j < S; ++j) idx[j] = check_index(j, S, n_orient);
+    SPX_CUDA(cudaEventRecord(h->ev_fork, h->stream));
+    SPX_CUDA(cudaStreamWaitEvent(h->check_stream, h->ev_fork, 0));
+    double *g = h->d_chk_grid.p;
+    for (int j = 0; j < S; ++j) {
+        SPX_CUDA(cudaMemcpyAsync(g + j, d_al + idx[j], sizeof(double), cudaMemcpyDeviceToDevice, h->check_stream));
+        SPX_CUDA(cudaMemcpyAsync(g + S + j, d_be + idx[j], sizeof(double), cudaMemcpyDeviceToDevice, h->check_stream));
+        SPX_CUDA(cudaMemcpyAsync(g + 2 * S + j, d_ga + idx[j], sizeof(double), cudaMemcpyDeviceToDevice,
+                                 h->check_stream));
+        if (sys32.rho0s)
+            SPX_CUDA(cudaMemcpyAsync(h->d_chk_rho0s.p + (size_t)j * h->n_pad, sys32.rho0s + (size_t)idx[j] * h->n_pad,
+                                     h->n_pad * sizeof(double2), cudaMemcpyDeviceToDevice, h->check_stream));
+    }
+    spx::DevSystem sys = sys32;
+    if (sys32.rho0s) sys.rho0s = h->d_chk_rho0s.p;
+    spx::DevRun run{};
+    run.traj_m = c.traj_m;
+    run.n_orient = S; run.alpha = g; run.beta = g + S; run.gamma = g + 2 * S;
+    run.dt = dt; run.nsteps = (int)nsteps; run.M = c.M; run.Kmax = c.Kmax; run.tol = c.tol;
+    run.fixed_chunk = c.fixed ? 1 : 0; run.chunk_x = c.chunk_x;
+    run.lanczos_its = o64.lanczos_its > 0 ? o64.lanczos_its : 32;
+    run.safe_bounds = 0; run.fids = h->d_chk_fids.p; run.table = h->d_chk_table.p;
+    run.status = h->d_chk_status.p; run.matvecs = h->d_chk_matvecs.p; run.halfwidth = h->d_chk_halfwidth.p;
+    run.kused = h->d_chk_kused.p; run.mused = h->d_chk_mused.p; run.next_orient = h->d_chk_counter.p;
+    launch_chebyshev(h, true, c, sys, run, h->check_stream);
+    SPX_CUDA(cudaEventRecord(h->ev_join, h->check_stream));
+    return c.grid;
+}
+
 void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be,
                    const double *d_ga, const double *d_w, double dt, int64_t nsteps,
-                   const spx_options &opt, double2 *d_out, const Config &c, int safe_bounds = 0, bool timed = true,
-                   const RunIO &io = RunIO{}) {
+                   const spx_options &opt, double2 *d_out, const Config &c_in, int safe_bounds = 0, bool timed = true,
+                   const RunIO &io = RunIO{}, bool fp32_check = false) {
     const bool f64 = opt.precision == SPX_FP64;
+    Config c = c_in;
     const size_t npts = ((size_t)nsteps + 1) * h->nchan;   // the powder sum treats channels as more points
     reserve_run(h, n_orient, nsteps, f64, c);
 
@@ -802,6 +892,14 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     run.mused = h->d_mused.p;
     run.next_orient = h->d_counter.p;
 
+    int chk = 0;
+    if (fp32_check && !f64) {
+        // the FP64 re-run takes its CTAs' SMs; the FP32 run keeps the rest
+        const int chk_ctas = launch_fp32_check(h, n_orient, d_al, d_be, d_ga, dt, nsteps, opt, sys);
+        chk = (int)std::min<int64_t>(kCheckOrients, n_orient);
+        const int take = ((chk_ctas + c.cl - 1) / c.cl) * c.cl;
+        if (c.grid - take >= std::max(c.cl, c.grid / 2)) c.grid -= take;
+    }
     if (timed) SPX_CUDA(cudaEventRecord(h->ev[0], h->stream));
     launch_chebyshev(h, f64, c, sys, run);
     if (timed) SPX_CUDA(cudaEventRecord(h->ev[1], h->stream));
@@ -809,6 +907,7 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     const int group = kPowderGroup;
     const int ngroups = (int)((n_orient + group - 1) / group);
     const dim3 pb(256), pg((unsigned)((npts + 255) / 256), (unsigned)ngroups);
+    ++h->launches;  // powder partial sum
     if (f64)
         spx::powder_partial_kernel<double2><<<pg, pb, 0, h->stream>>>(
             reinterpret_cast<const double2 *>(h->d_fids.p), d_w, (int)n_orient, (int)npts, group, h->d_part.p);
@@ -816,9 +915,11 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
         spx::powder_partial_kernel<float2><<<pg, pb, 0, h->stream>>>(
             reinterpret_cast<const float2 *>(h->d_fids.p), d_w, (int)n_orient, (int)npts, group, h->d_part.p);
     SPX_CUDA(cudaGetLastError());
+    ++h->launches;
     spx::powder_combine_kernel<<<dim3((unsigned)((npts + 255) / 256)), dim3(256), 0, h->stream>>>(
         h->d_part.p, ngroups, (int)npts, d_out);
     SPX_CUDA(cudaGetLastError());
+    if (chk) SPX_CUDA(cudaStreamWaitEvent(h->stream, h->ev_join, 0));   // the FP64 re-run is part of the run
     if (timed) SPX_CUDA(cudaEventRecord(h->ev[2], h->stream));
     h->stats_timed = timed;
 
@@ -838,6 +939,65 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     h->stats.smem_bytes = (int32_t)c.smem;
     h->stats_pending = true;
     h->last_norient = n_orient;
+    h->chk_pending = chk;
+    h->chk_out = d_out;
+    h->chk_w = d_w;
+    h->chk_nsteps = nsteps;
+}
+
+// FP32 error of a run from its checked orientations (FP32 FIDs f32 and
+// their FP64 re-runs f64, S x npts each, channel by channel), its powder FID
+// pw and the sum of its squared grid weights w2:
+//   orientation  the largest relative 2-norm error of the checked FIDs;
+//   powder       the error these imply for the powder FID sum_o w_o f_o,
+//                split into two parts added in quadrature.  The part that
+//                follows the signal: an orientation's FP32 error acts like a
+//                phase error growing with time, so phi(t), the larger of the
+//                checked orientations' relative errors over [0, t], weighted
+//                by the powder FID's intensity: sqrt(sum |pw|^2 phi^2 /
+//                sum |pw|^2).  The part that does not: errors independent
+//                across orientations add in quadrature, sqrt(w2) times the
+//                checked orientations' rms error norm, over |pw|.
+struct FP32Error {
+    double orientation = 0.0, powder = 0.0;
+};
+FP32Error fp32_error(const std::vector<float2> &f32, const std::vector<double2> &f64, const std::vector<double2> &pw,
+                     double w2, int S, size_t len, int nchan) {
+    FP32Error out;
+    const size_t npts = len * nchan;
+    std::vector<double> phi(len);
+    for (int ch = 0; ch < nchan; ++ch) {
+        std::fill(phi.begin(), phi.end(), 0.0);
+        double err2 = 0.0;                  // sum over checked orientations of |delta f|^2
+        for (int j = 0; j < S; ++j) {
+            const size_t base = (size_t)j * npts + (size_t)ch * len;
+            double num = 0.0, den = 0.0;
+            for (size_t t = 0; t < len; ++t) {
+                const double2 b = f64[base + t];
+                const double dx = (double)f32[base + t].x - b.x, dy = (double)f32[base + t].y - b.y;
+                num += dx * dx + dy * dy;
+                den += b.x * b.x + b.y * b.y;
+                phi[t] = std::max(phi[t], den > 0.0 ? std::sqrt(num / den) : (num > 0.0 ? INFINITY : 0.0));
+            }
+            err2 += num;
+            out.orientation = std::max(out.orientation, den > 0.0 ? std::sqrt(num / den) : (num > 0.0 ? INFINITY : 0.0));
+        }
+        double num = 0.0, den = 0.0;
+        for (size_t t = 0; t < len; ++t) {
+            const double2 p = pw[(size_t)ch * len + t];
+            const double a = p.x * p.x + p.y * p.y;
+            num += a * phi[t] * phi[t];
+            den += a;
+        }
+        if (den > 0.0) {
+            const double coherent2 = num / den;
+            const double independent2 = w2 * (err2 / S) / den;
+            out.powder = std::max(out.powder, std::sqrt(coherent2 + independent2));
+        } else if (err2 > 0.0) {
+            out.powder = INFINITY;
+        }
+    }
+    return out;
 }
 
 // Synchronise, read per-orientation status and fill the statistics.
@@ -882,6 +1042,34 @@ spx_status finish_run(spx_handle *h) {
     h->stats.orientations_failed = failed;
     h->stats.min_half_width = hmin;
     h->stats.max_half_width = hmax;
+    if (h->chk_pending > 0) {
+        const int S = h->chk_pending;
+        h->chk_pending = 0;
+        std::vector<int> cst(S);
+        SPX_CUDA(cudaMemcpy(cst.data(), h->d_chk_status.p, S * sizeof(int), cudaMemcpyDeviceToHost));
+        bool ok = true;
+        for (int j = 0; j < S; ++j) ok = ok && cst[j] == spx::kDevOk;
+        // an FP64 re-run that failed its own series checks measures nothing
+        h->stats.fp32_checked = ok ? S : 0;
+        if (ok) {
+            const size_t len = (size_t)h->chk_nsteps + 1, npts = len * h->nchan;
+            std::vector<double2> f64((size_t)S * npts), pw(npts);
+            std::vector<float2> f32((size_t)S * npts);
+            SPX_CUDA(cudaMemcpy(f64.data(), h->d_chk_fids.p, f64.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+            for (int j = 0; j < S; ++j)
+                SPX_CUDA(cudaMemcpy(f32.data() + (size_t)j * npts,
+                                    reinterpret_cast<const float2 *>(h->d_fids.p) + (size_t)h->chk_index[j] * npts,
+                                    npts * sizeof(float2), cudaMemcpyDeviceToHost));
+            SPX_CUDA(cudaMemcpy(pw.data(), h->chk_out, npts * sizeof(double2), cudaMemcpyDeviceToHost));
+            std::vector<double> w(no);
+            SPX_CUDA(cudaMemcpy(w.data(), h->chk_w, no * sizeof(double), cudaMemcpyDeviceToHost));
+            double w2 = 0.0;
+            for (double x : w) w2 += x * x;
+            const FP32Error e = fp32_error(f32, f64, pw, w2, S, len, h->nchan);
+            h->stats.fp32_rel_error = e.orientation;
+            h->stats.fp32_powder_error = e.powder;
+        }
+    }
     if (failed) {
         static const char *why[] = {"ok", "series longer than the coefficient table", "state norm grew (spectral bound violated)",
                                     "non-finite state", "launch configuration has too few threads"};
@@ -1005,6 +1193,7 @@ void apply_pulse(spx_handle *h, const PulseOp &op, double theta, int64_t n_state
     SPX_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void *>(&pulse_kernel),
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = (int)std::min<int64_t>(n_states, (int64_t)h->sm_count * 2);
+    ++h->launches;
     pulse_kernel<<<grid, 256, smem, h->stream>>>((int)n_states, h->n_pad, op.ptr.p, op.col.p, op.val.p, theta / nsub,
                                                  nsub, nterms, states);
     SPX_CUDA(cudaGetLastError());
@@ -1231,6 +1420,7 @@ void upload_echo_propagator(spx_handle *h, const PulseOp &P, double theta) {
     const int n_pad = h->n_pad;
     DevBuf<double2> dense;
     dense.reserve((size_t)n_pad * n_pad);
+    ++h->launches;
     identity_kernel<<<h->sm_count * 4, 256, 0, h->stream>>>(n_pad, dense.p);
     SPX_CUDA(cudaGetLastError());
     apply_pulse(h, P, theta, n_pad, dense.p);
@@ -1262,6 +1452,7 @@ void negate_generator(spx_handle *h) {
     h->d_neg_re.reserve((size_t)std::max<int64_t>(n_ell, 1));
     if (h->cplx) h->d_neg_im.reserve((size_t)std::max<int64_t>(n_ell, 1));
     h->d_neg_diag.reserve((size_t)n_diag);
+    ++h->launches;
     negate_streams_kernel<<<h->sm_count * 4, 256, 0, h->stream>>>(
         n_ell, h->d_ell_re.p, h->cplx ? h->d_ell_im.p : nullptr, h->d_neg_re.p, h->cplx ? h->d_neg_im.p : nullptr,
         n_diag, h->n_pad, h->d_diag.p, h->d_neg_diag.p);
@@ -1323,11 +1514,13 @@ void echo_trajectories(spx_handle *h, int64_t n_orient, const double *g, double 
         }
         const int64_t warps = nb * npoints;
         const int blocks = (int)std::min<int64_t>((warps + 7) / 8, (int64_t)h->sm_count * 16);
+        ++h->launches;
         echo_form_kernel<<<blocks, 256, 0, h->stream>>>((int)nb, (int)npoints, n_pad, h->d_echo_ptr.p, h->d_echo_col.p,
                                                         h->d_echo_val.p, h->d_traj[0].p, h->d_traj[1].p,
                                                         reverse ? 1 : 0, h->d_echo_f.p + b0 * npoints);
         SPX_CUDA(cudaGetLastError());
     }
+    ++h->launches;
     echo_powder_kernel<<<(unsigned)((npoints + 127) / 128), 128, 0, h->stream>>>(
         (int)n_orient, (int)npoints, h->d_echo_f.p, g + 3 * n_orient, h->d_fid.p);
     SPX_CUDA(cudaGetLastError());
@@ -1565,20 +1758,54 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[SPX_NOALLOC_SCR
 namespace {
 
 std::mutex g_noalloc_mutex;
-void *g_noalloc_address[256] = {};
+struct NoallocAddress {
+    unsigned long long ctx_id = 0;   // context the address belongs to (0: none yet)
+    void *ptr = nullptr;
+};
+NoallocAddress g_noalloc_address[256];
 
-// Device address of g_noalloc_scratch on the current device, looked up once
-// per device (host code only sees a stand-in symbol, never the device address).
+// Identifier of the current context (driver entry points fetched through the
+// runtime, so the library needs no link against libcuda).  Context ids are
+// never reused within a process, so a reset primary context gets a new one.
+unsigned long long current_context_id() {
+    typedef CUresult (*GetCurrent)(CUcontext *);
+    typedef CUresult (*GetId)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    if (!get_current || !get_id) {
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        void *f1 = nullptr, *f2 = nullptr;
+        SPX_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1));
+        SPX_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2));
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            throw SpxError(SPX_ERR_CUDA, "the driver lacks cuCtxGetCurrent/cuCtxGetId");
+        get_current = reinterpret_cast<GetCurrent>(f1);
+        get_id = reinterpret_cast<GetId>(f2);
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        throw SpxError(SPX_ERR_CUDA, "no current CUDA context");
+    return id;
+}
+
+// Device address of g_noalloc_scratch on the current device.  Host code only
+// sees a stand-in symbol, never the device address, so the address is looked
+// up with cudaGetSymbolAddress once per device and context (again after
+// another part of the process has reset the device and its context).
 void *noalloc_scratch(int device) {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (device < 0 || device >= 256) throw SpxError(SPX_ERR_INVALID_ARGUMENT, "device ordinal out of range");
-    if (!g_noalloc_address[device]) {
+    const unsigned long long id = current_context_id();
+    NoallocAddress &a = g_noalloc_address[device];
+    if (!a.ptr || a.ctx_id != id) {
         void *ptr = nullptr;
         SPX_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
         if (!ptr) throw SpxError(SPX_ERR_CUDA, "no device address for the static scratch array");
-        g_noalloc_address[device] = ptr;
+        a.ptr = ptr;
+        a.ctx_id = id;
     }
-    return g_noalloc_address[device];
+    return a.ptr;
 }
 
 void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, const double *d_be,
@@ -1639,10 +1866,13 @@ void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, con
     run.halfwidth = reinterpret_cast<double *>(base + offs[6] + (size_t)n_orient * sizeof(long long));
     run.next_orient = reinterpret_cast<int *>(base + offs[8]);
     double2 *part = reinterpret_cast<double2 *>(base + offs[2]);
-    // the only value that must start at zero is the failure flag
+    // values that must start at zero: the failure flag here, the work counter
+    // (run.next_orient) in launch_chebyshev; everything else is written
+    // before it is read
     SPX_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
     launch_chebyshev(h, f64, c, sys, run);
     const dim3 pb(256), pg((unsigned)((npts + 255) / 256), (unsigned)ngroups);
+    ++h->launches;  // powder partial sum
     if (f64)
         spx::powder_partial_kernel<double2><<<pg, pb, 0, h->stream>>>(
             reinterpret_cast<const double2 *>(run.fids), d_w, (int)n_orient, (int)npts, group, part);
@@ -1650,9 +1880,11 @@ void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, con
         spx::powder_partial_kernel<float2><<<pg, pb, 0, h->stream>>>(
             reinterpret_cast<const float2 *>(run.fids), d_w, (int)n_orient, (int)npts, group, part);
     SPX_CUDA(cudaGetLastError());
+    ++h->launches;
     spx::powder_combine_kernel<<<dim3((unsigned)((npts + 255) / 256)), dim3(256), 0, h->stream>>>(
         part, ngroups, (int)npts, reinterpret_cast<double2 *>(d_fid));
     SPX_CUDA(cudaGetLastError());
+    ++h->launches;
     status_any_kernel<<<dim3(64), dim3(256), 0, h->stream>>>(run.status, (int)n_orient, flag);
     SPX_CUDA(cudaGetLastError());
     int failed = 0;
@@ -1709,6 +1941,10 @@ spx_status spx_destroy(spx_handle *h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
+    if (h->check_stream) cudaStreamSynchronize(h->check_stream);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->check_stream) cudaStreamDestroy(h->check_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return SPX_OK;
@@ -1748,7 +1984,9 @@ spx_status spx_run_powder(spx_handle *h, int64_t n_orient, const double *alphas,
         SPX_CUDA(cudaMemcpyAsync(g + 3 * n_orient, weights, b, cudaMemcpyHostToDevice, h->stream));
         h->d_fid.reserve(((size_t)nsteps + 1) * h->nchan);
         Config c = choose_config(h, n_orient, dt, nsteps, o, 0);
-        launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o, h->d_fid.p, c);
+        const bool check = o.precision == SPX_FP32 && !(o.flags & SPX_FLAG_NO_FP32_CHECK);
+        launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o, h->d_fid.p, c,
+                      0, true, RunIO{}, check);
         spx_status st = SPX_OK;
         bool retried = false;
         try {
@@ -1769,11 +2007,38 @@ spx_status spx_run_powder(spx_handle *h, int64_t n_orient, const double *alphas,
             c = choose_config(h, n_orient, dt, nsteps, o, 2 * kneed + 16);
             retried = true;
             launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o,
-                          h->d_fid.p, c, 1);
+                          h->d_fid.p, c, 1, true, RunIO{}, check);
             st = finish_run(h);
         }
         (void)st;
         h->stats.retries = retried ? 1 : 0;
+        // the bar applies to what the caller receives: the powder FID, and
+        // every orientation's FID when those are asked for too
+        const double err32 = fids_per_orient ? std::max(h->stats.fp32_rel_error, h->stats.fp32_powder_error)
+                                             : h->stats.fp32_powder_error;
+        // the estimate comes from two orientations: it has tracked the measured
+        // powder error within about 25 %, so the re-run starts at half the bar
+        if (check && h->stats.fp32_checked > 0 && !(err32 <= 0.5 * SPX_FP32_ERROR_BAR) &&
+            !(o.flags & SPX_FLAG_NO_PROMOTE)) {
+            // the FP32 result misses the bar on the checked orientations: run
+            // the whole grid again in FP64 and return that
+            const spx_stats s32 = h->stats;
+            spx_options o64 = o;
+            o64.precision = SPX_FP64;
+            o64.threads = o64.cluster = 0;
+            o64.chunk_target = 0.0;
+            o64 = apply_tuned(h, o64);
+            const Config c64 = choose_config(h, n_orient, dt, nsteps, o64, 0);
+            launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o64,
+                          h->d_fid.p, c64, 1);
+            finish_run(h);
+            h->stats.fp32_checked = s32.fp32_checked;
+            h->stats.fp32_rel_error = s32.fp32_rel_error;
+            h->stats.fp32_powder_error = s32.fp32_powder_error;
+            h->stats.promoted_fp64 = 1;
+            h->stats.retries = s32.retries;
+            o.precision = SPX_FP64;
+        }
         SPX_CUDA(cudaMemcpy(fid, h->d_fid.p, ((size_t)nsteps + 1) * h->nchan * sizeof(double2),
                             cudaMemcpyDeviceToHost));
         if (fids_per_orient) {
@@ -1807,8 +2072,9 @@ spx_status spx_run_powder_device(spx_handle *h, int64_t n_orient, const double *
         o = apply_tuned(h, o);
         SPX_CUDA(cudaSetDevice(h->device));
         const Config c = choose_config(h, n_orient, dt, nsteps, o, 0);
+        const bool check = o.precision == SPX_FP32 && !(o.flags & SPX_FLAG_NO_FP32_CHECK);
         launch_powder(h, n_orient, d_alphas, d_betas, d_gammas, d_weights, dt, nsteps, o,
-                      reinterpret_cast<double2 *>(d_fid), c);
+                      reinterpret_cast<double2 *>(d_fid), c, 0, true, RunIO{}, check);
     });
 }
 
@@ -1829,6 +2095,7 @@ spx_status spx_get_stats(spx_handle *h, spx_stats *stats) {
         finish_run(h);
     });
     *stats = h->stats;
+    stats->kernel_launches = h->launches;
     return st;
 }
 

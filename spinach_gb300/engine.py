@@ -26,7 +26,11 @@ class SpxCsc(C.Structure):
 class SpxOptions(C.Structure):
     _fields_ = [('precision', C.c_int32), ('chunk_steps', C.c_int32), ('threads', C.c_int32),
                 ('cluster', C.c_int32), ('series_tol', C.c_double), ('chunk_target', C.c_double),
-                ('lanczos_its', C.c_int32), ('reserved', C.c_int32)]
+                ('lanczos_its', C.c_int32), ('flags', C.c_int32)]
+
+
+FLAG_NO_FP32_CHECK, FLAG_NO_PROMOTE = 1, 2
+FP32_ERROR_BAR = 1e-5
 
 
 SEQ_PULSE, SEQ_EVOLVE = 0, 1
@@ -46,7 +50,9 @@ class SpxStats(C.Structure):
                 ('dim', C.c_int64), ('nnz', C.c_int64), ('ell_entries', C.c_int64),
                 ('value_streams', C.c_int32), ('real_offdiag', C.c_int32),
                 ('cluster', C.c_int32), ('smem_bytes', C.c_int32), ('channels', C.c_int32),
-                ('retries', C.c_int32)]
+                ('retries', C.c_int32), ('fp32_checked', C.c_int32), ('kernel_launches', C.c_int64),
+                ('fp32_rel_error', C.c_double), ('promoted_fp64', C.c_int32), ('reserved', C.c_int32),
+                ('fp32_powder_error', C.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -259,7 +265,12 @@ class Engine:
     def run(self, alphas, betas, gammas, weights, dt: float, nsteps: int, precision: int = FP32,
             per_orientation: bool = False, chunk_steps: int = 0, threads: int = 0,
             series_tol: float = 0.0, cluster: int = 0, chunk_target: float = 0.0,
-            lanczos_its: int = 0) -> PowderResult:
+            lanczos_its: int = 0, fp32_check: bool = True, promote: bool = True) -> PowderResult:
+        """spx_run_powder.  FP32 runs re-run two orientations in FP64 and report
+        their larger relative error (stats['fp32_rel_error']) and the powder
+        error it implies (stats['fp32_powder_error']); above half of 1e-5 the
+        whole grid is re-run in FP64 (stats['promoted_fp64']) unless
+        ``promote`` is false."""
         al = np.ascontiguousarray(alphas, np.float64)
         be = np.ascontiguousarray(betas, np.float64)
         ga = np.ascontiguousarray(gammas, np.float64)
@@ -268,7 +279,8 @@ class Engine:
         nch = getattr(self, 'nchan', 1)
         fid = np.zeros(2 * (nsteps + 1) * nch)
         fids = np.zeros(2 * (nsteps + 1) * nch * no) if per_orientation else None
-        opt = SpxOptions(precision, chunk_steps, threads, cluster, series_tol, chunk_target, lanczos_its, 0)
+        flags = (0 if fp32_check else FLAG_NO_FP32_CHECK) | (0 if promote else FLAG_NO_PROMOTE)
+        opt = SpxOptions(precision, chunk_steps, threads, cluster, series_tol, chunk_target, lanczos_its, flags)
         self._check(self.lib.spx_run_powder(self.h, no, _dptr(al), _dptr(be), _dptr(ga), _dptr(w),
                                             float(dt), int(nsteps), C.byref(opt), _dptr(fid),
                                             _dptr(fids) if fids is not None else None), self.h)
@@ -382,9 +394,11 @@ class Engine:
 
     def run_device(self, d_alphas: int, d_betas: int, d_gammas: int, d_weights: int, n_orient: int,
                    dt: float, nsteps: int, d_fid: int, precision: int = FP32, chunk_steps: int = 0,
-                   threads: int = 0, series_tol: float = 0.0, cluster: int = 0):
-        """Enqueue a run on device-resident buffers (raw device pointers); no sync."""
-        opt = SpxOptions(precision, chunk_steps, threads, cluster, series_tol, 0.0)
+                   threads: int = 0, series_tol: float = 0.0, cluster: int = 0, fp32_check: bool = True):
+        """Enqueue a run on device-resident buffers (raw device pointers); no
+        sync.  FP32 runs report their FP64-checked error in the stats."""
+        opt = SpxOptions(precision, chunk_steps, threads, cluster, series_tol, 0.0, 0,
+                         0 if fp32_check else FLAG_NO_FP32_CHECK)
         self._check(self.lib.spx_run_powder_device(self.h, n_orient, d_alphas, d_betas, d_gammas,
                                                    d_weights, float(dt), int(nsteps), C.byref(opt),
                                                    d_fid), self.h)

@@ -224,3 +224,31 @@ def test_per_orientation_outputs_of_a_program(gpu_engine):
     for n in (0, 7):
         ref = R.powder_orientation_hp_acquire(ss, I, Q, par, (grid[0][n], grid[1][n], grid[2][n]))
         assert rel_err(cells[n], ref) <= 1e-10
+
+
+def test_powder_inv_rec(gpu_engine):
+    """powder(..., @inv_rec, ...) on the GPU (experiments/inv_rec.m:50-66: the
+    isotropic equilibrium, a 180-degree pulse, n_delays+1 recovery times, a
+    90-degree pulse and one FID each) against the oracle's restatement, FP64
+    <= 1e-10 and FP32 <= 1e-5 per recovery column, and the per-orientation
+    cells (sum_up = 0)."""
+    sys_, inter, bas = _structures()
+    # fast longitudinal relaxation, so that the recovery shows within delays
+    # whose |L|*dt stays in range (2.5 ms steps)
+    inter = dict(inter, temperature=300.0, r1_rates=[200.0, 300.0, 300.0], r2_rates=[400.0, 500.0, 500.0])
+    spin_system = X.basis(X.create(sys_, inter), bas)
+    grid = W.zcwn_grid(16)
+    parameters = dict(grid=grid, spins=['13C'], n_delays=4, max_delay=0.01, sweep=2e4, npoints=96)
+    ss, I, Q = _oracle(sys_, inter, bas)
+    ref = sum(grid[3][i] * R.powder_orientation_sequence(ss, I, Q, parameters, (grid[0][i], grid[1][i], grid[2][i]),
+                                                         R.inv_rec) for i in range(16))
+    assert ref.shape == (96, 5) and abs(ref[0, 0] - ref[0, -1]) > 0.1 * np.abs(ref).max()
+    for prec, tol in ((E.FP64, 1e-10), (E.FP32, 1e-5)):
+        fids, _ = X.powder(spin_system, 'inv_rec', parameters, 'nmr', engine=gpu_engine, precision=prec)
+        assert fids.shape == (96, 5)
+        for k in range(5):
+            assert rel_err(fids[:, k], ref[:, k]) <= tol, (prec, k)
+    cells, _ = X.powder(spin_system, 'inv_rec', dict(parameters, sum_up=0), 'nmr', engine=gpu_engine)
+    assert len(cells) == 16 and cells[3].shape == (96, 5)
+    one = R.powder_orientation_sequence(ss, I, Q, parameters, (grid[0][3], grid[1][3], grid[2][3]), R.inv_rec)
+    assert rel_err(cells[3], one) <= 1e-10
