@@ -16,6 +16,13 @@ Steps (all on one GPU; torch holds device buffers and runs the SVD):
   6. judge: exact FIDs at held-out dense orientations.  The powder error is
      estimated as |sum_held w (s - f) - sum_coarse w (s - f)| / |P|; above the
      tolerance the exact path runs on the dense grid (fallback).
+Before any training a cheaper test can reject the network outright: the
+powders of the coarse grid's two interleaved halves (even and odd points)
+differ by the angular structure the coarse grid does not resolve.  When they
+differ by more than ``prejudge_factor`` times the tolerance, the FIDs vary on
+angular scales finer than the coarse grid, which a network over a few
+spherical-harmonic degrees fitted to it cannot recover, so training is
+skipped and the exact dense run follows at once.
 Weights of each grid are normalised to sum 1 before mixing grids (the
 powder weights of kernel/contexts/powder.m:280-287 sum to 1 already).
 """
@@ -40,6 +47,8 @@ class SurrogateResult:
     nearest_rel_err: float          # same for the nearest coarse orientation's exact FID
     loss: np.ndarray
     seconds: dict = field(default_factory=dict)
+    half_grid_rel_diff: float = 0.0     # |P_even - P_odd| / |P| of the coarse grid's halves
+    trained: bool = True                # False when the half-grid test rejected the network
 
 
 def _xyz(beta, gamma):
@@ -83,7 +92,8 @@ class SurrogatePowder:
         self.seed = seed
 
     def run(self, coarse_grid, dense_grid, holdout_idx, dt: float, nsteps: int, epochs: int = 1500,
-            lr: float = 1e-3, tol: float = 1e-5, precision: int = E.FP32) -> SurrogateResult:
+            lr: float = 1e-3, tol: float = 1e-5, precision: int = E.FP32,
+            prejudge_factor: float = 100.0) -> SurrogateResult:
         torch = self.torch
         sec = {}
         ca, cb, cg, cw = (np.asarray(a, float) for a in coarse_grid)
@@ -95,6 +105,20 @@ class SurrogatePowder:
         t0 = time.perf_counter()
         coarse = self.engine.run(ca, cb, cg, cw, dt, nsteps, precision=precision, per_orientation=True)
         sec['coarse_exact'] = time.perf_counter() - t0
+
+        # half-grid test: the powders of the even and odd coarse points
+        even, odd = coarse.fids[0::2], coarse.fids[1::2]
+        pe = (cw[0::2] / cw[0::2].sum()) @ even
+        po = (cw[1::2] / cw[1::2].sum()) @ odd
+        half = float(np.linalg.norm(pe - po) / max(np.linalg.norm(coarse.fid), 1e-300))
+        if prejudge_factor > 0 and half > prejudge_factor * tol:
+            t0 = time.perf_counter()
+            fid = self.engine.run(da, db, dg, dw, dt, nsteps, precision=precision).fid
+            sec['fallback'] = time.perf_counter() - t0
+            return SurrogateResult(fid=fid, surrogate_fid=coarse.fid, coarse_fid=coarse.fid, accepted=False,
+                                   judge_estimate=float('nan'), holdout_rel_err=float('nan'),
+                                   nearest_rel_err=float('nan'), loss=np.zeros(0), seconds=sec,
+                                   half_grid_rel_diff=half, trained=False)
 
         t0 = time.perf_counter()
         F = torch.from_numpy(coarse.fids).to(self.dev, torch.complex64)
@@ -162,4 +186,4 @@ class SurrogatePowder:
             sec['fallback'] = time.perf_counter() - t0
         return SurrogateResult(fid=fid, surrogate_fid=P, coarse_fid=coarse.fid, accepted=accepted,
                                judge_estimate=judge, holdout_rel_err=holdout_rel,
-                               nearest_rel_err=nearest_rel, loss=loss, seconds=sec)
+                               nearest_rel_err=nearest_rel, loss=loss, seconds=sec, half_grid_rel_diff=half)

@@ -102,7 +102,7 @@ def test_surrogate_gain_over_nearest_orientation(torch_cuda, engine_lib):
     eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
     sp = SG.SurrogatePowder(eng, rank=16, seed=0)
     dense = W.zcwn_grid(20000)
-    res = sp.run(W.zcwn_grid(2000), dense, np.arange(20, 20000, 40), w.dt, 16, epochs=1500)
+    res = sp.run(W.zcwn_grid(2000), dense, np.arange(20, 20000, 40), w.dt, 16, epochs=1500, prejudge_factor=0)
     assert res.loss[-1] < 1e-2 * res.loss[0]
     assert res.holdout_rel_err < 0.5 * res.nearest_rel_err, (res.holdout_rel_err, res.nearest_rel_err)
     exact = eng.run(*dense, w.dt, 16, precision=E.FP64).fid
@@ -110,3 +110,30 @@ def test_surrogate_gain_over_nearest_orientation(torch_cuda, engine_lib):
         assert np.linalg.norm(res.fid - exact) <= 1e-4 * np.linalg.norm(exact)
     else:
         assert np.linalg.norm(res.fid - exact) <= 1e-5 * np.linalg.norm(exact)
+
+
+def test_surrogate_on_the_full_c3_workload(torch_cuda, engine_lib):
+    """Workload c3 at its real length (the c1 system, 2048 steps; coarse 2000,
+    dense 20000, 500 held out): the FIDs dephase across orientations on
+    angular scales far finer than 2000 coarse orientations resolve, so the
+    half-grid test rejects the network before training, and the exact dense
+    run that follows is within 1e-5 of FP64.  Forced to train, the network
+    is rejected by the held-out judge too."""
+    from spinach_gb300 import engine as E, surrogate as SG, workloads as W
+    w = W.c1()
+    L = W.build(w)
+    eng = E.Engine(0)
+    try:
+        eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
+        coarse, dense = W.zcwn_grid(2000), W.zcwn_grid(20000)
+        held = np.arange(20, 20000, 40)
+        sp = SG.SurrogatePowder(eng, rank=64, seed=0)
+        res = sp.run(coarse, dense, held, w.dt, w.nsteps, epochs=1500)
+        assert not res.trained and not res.accepted and res.half_grid_rel_diff > 1e-3
+        exact = eng.run(*dense, w.dt, w.nsteps, precision=E.FP64).fid
+        assert np.linalg.norm(res.fid - exact) <= 1e-5 * np.linalg.norm(exact)
+        forced = sp.run(coarse, dense, held, w.dt, w.nsteps, epochs=300, prejudge_factor=0)
+        assert forced.trained and not forced.accepted and forced.judge_estimate > 1e-5
+        assert np.linalg.norm(forced.fid - exact) <= 1e-5 * np.linalg.norm(exact)
+    finally:
+        eng.close()
