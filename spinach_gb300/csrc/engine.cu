@@ -2030,7 +2030,7 @@ spx_status spx_run_powder(spx_handle *h, int64_t n_orient, const double *alphas,
             o64 = apply_tuned(h, o64);
             const Config c64 = choose_config(h, n_orient, dt, nsteps, o64, 0);
             launch_powder(h, n_orient, g, g + n_orient, g + 2 * n_orient, g + 3 * n_orient, dt, nsteps, o64,
-                          h->d_fid.p, c64, 1);
+                          h->d_fid.p, c64);
             finish_run(h);
             h->stats.fp32_checked = s32.fp32_checked;
             h->stats.fp32_rel_error = s32.fp32_rel_error;

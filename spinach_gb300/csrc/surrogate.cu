@@ -1,8 +1,9 @@
 // Orientation surrogate for the powder FID: a small MLP over real spherical
 // harmonics of the orientation (beta, gamma) that predicts the coefficients of
 // an orientation's FID in an SVD basis.  Training and inference run on the GPU
-// in the kernels below (tiled FP32-accumulate products with BF16 weights, GELU,
-// Adam); one training step is captured once in a CUDA graph and replayed.
+// in the kernels below (split-TF32 tensor-core products with FP32 accumulation
+// and BF16 weights, GELU, Adam); one training step is captured once in a CUDA
+// graph and replayed.
 //
 // Features follow kernel/utilities/spher_harmon.m (orthonormal Y_lm with the
 // Condon-Shortley phase): for each l, Re Y_l0, then Re Y_lm and Im Y_lm for
@@ -76,65 +77,113 @@ __global__ void sh_features_kernel(int64_t n, const double *__restrict__ beta, c
 }
 
 // ---------------------------------------------------------------------------
-// C[i,j] (+)= sum_k A(i,k) B(k,j), FP32 accumulation.
+// C[i,j] (+)= sum_k A(i,k) B(k,j) on the tensor cores with FP32 accumulation.
 // A(i,k) = TA ? A[k*lda+i] : A[i*lda+k];  B(k,j) = TB ? B[j*ldb+k] : B[k*ldb+j].
-// 64x64 tiles, 16-deep slabs staged in shared memory, 4x4 outputs per thread.
+// Operands are split into TF32 pairs (x = hi + lo, each TF32, 22 significant
+// bits together) and the products hi*hi + lo*hi (+ hi*lo for an FP32 B) run as
+// mma.sync m16n8k8 TF32 instructions: FP32-level accuracy from the tensor
+// pipe.  A BF16 B (the weights) is exact in TF32 and is not split.  64x64
+// tiles, 16-deep slabs staged in shared memory (rows padded to 20 floats, so
+// the fragment reads are conflict-free), four warps of 32x32; gridDim.z
+// splits K into slabs that write their own copies of C.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float tof(float v) { return v; }
 __device__ __forceinline__ float tof(__nv_bfloat16 v) { return __bfloat162float(v); }
 
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ void split_tf32(float x, uint32_t &hi, uint32_t &lo) {
+    hi = tf32_rna(x);
+    lo = tf32_rna(x - __uint_as_float(hi));
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <class T> struct IsF32 { static constexpr bool value = false; };
+template <> struct IsF32<float> { static constexpr bool value = true; };
+
 template <bool TA, bool TB, class BT>
-__global__ void __launch_bounds__(256) gemm_kernel(int M, int N, int K, const float *__restrict__ A, int lda,
+__global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, const float *__restrict__ A, int lda,
                                                    const BT *__restrict__ B, int ldb, float *__restrict__ C,
                                                    int ldc, int accumulate) {
-    __shared__ float As[16][64 + 1];
-    __shared__ float Bs[16][64 + 1];
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    constexpr bool kSplitB = IsF32<BT>::value;
+    __shared__ float As[64][20];     // [row of A][k]
+    __shared__ float Bs[64][20];     // [column of B][k]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, t = lane & 3;                   // fragment row group and thread in group
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
     const int i0 = blockIdx.y * 64, j0 = blockIdx.x * 64;
     // split-K: slab z covers k in [kb, ke) and writes its own copy of C
     const int kchunk = (((K + gridDim.z - 1) / gridDim.z) + 15) & ~15;
     const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
     C += (int64_t)blockIdx.z * M * ldc;
-    float acc[4][4] = {};
+    float acc[2][4][4] = {};
     for (int k0 = kb; k0 < ke; k0 += 16) {
-        for (int t = threadIdx.x; t < 16 * 64; t += 256) {
-            const int kk = t / 64, ii = t % 64;
-            const int i = i0 + ii, k = k0 + kk;
-            float av = 0.f;
-            if (i < M && k < ke) av = TA ? A[(int64_t)k * lda + i] : A[(int64_t)i * lda + k];
-            As[kk][ii] = av;
-            const int j = j0 + ii;
-            float bv = 0.f;
-            if (j < N && k < ke) bv = TB ? tof(B[(int64_t)j * ldb + k]) : tof(B[(int64_t)k * ldb + j]);
-            Bs[kk][ii] = bv;
+        for (int q = threadIdx.x; q < 64 * 16; q += 128) {
+            // consecutive threads follow the contiguous global index
+            const int ai = TA ? q % 64 : q / 16, ak = TA ? q / 64 : q % 16;
+            const int i = i0 + ai, k = k0 + ak;
+            As[ai][ak] = (i < M && k < ke) ? (TA ? A[(int64_t)k * lda + i] : A[(int64_t)i * lda + k]) : 0.f;
+            const int bj = TB ? q / 16 : q % 64, bk = TB ? q % 16 : q / 64;
+            const int j = j0 + bj, k2 = k0 + bk;
+            Bs[bj][bk] = (j < N && k2 < ke) ? (TB ? tof(B[(int64_t)j * ldb + k2]) : tof(B[(int64_t)k2 * ldb + j])) : 0.f;
         }
         __syncthreads();
 #pragma unroll
-        for (int kk = 0; kk < 16; ++kk) {
-            float a[4], b[4];
+        for (int ks = 0; ks < 16; ks += 8) {
+            uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
 #pragma unroll
-            for (int r = 0; r < 4; ++r) a[r] = As[kk][ty * 4 + r];
+            for (int mt = 0; mt < 2; ++mt) {
+                const int r = wm + mt * 16 + g;
+                split_tf32(As[r][ks + t], ah[mt][0], al[mt][0]);
+                split_tf32(As[r + 8][ks + t], ah[mt][1], al[mt][1]);
+                split_tf32(As[r][ks + t + 4], ah[mt][2], al[mt][2]);
+                split_tf32(As[r + 8][ks + t + 4], ah[mt][3], al[mt][3]);
+            }
 #pragma unroll
-            for (int c = 0; c < 4; ++c) b[c] = Bs[kk][tx * 4 + c];
+            for (int nt = 0; nt < 4; ++nt) {
+                const int cj = wn + nt * 8 + g;
+                if constexpr (kSplitB) {
+                    split_tf32(Bs[cj][ks + t], bh[nt][0], bl[nt][0]);
+                    split_tf32(Bs[cj][ks + t + 4], bh[nt][1], bl[nt][1]);
+                } else {
+                    bh[nt][0] = __float_as_uint(Bs[cj][ks + t]);
+                    bh[nt][1] = __float_as_uint(Bs[cj][ks + t + 4]);
+                }
+            }
 #pragma unroll
-            for (int r = 0; r < 4; ++r)
+            for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-                for (int c = 0; c < 4; ++c) acc[r][c] = fmaf(a[r], b[c], acc[r][c]);
+                for (int nt = 0; nt < 4; ++nt) {
+                    mma_tf32(acc[mt][nt], al[mt], bh[nt]);
+                    if constexpr (kSplitB) mma_tf32(acc[mt][nt], ah[mt], bl[nt]);
+                    mma_tf32(acc[mt][nt], ah[mt], bh[nt]);
+                }
         }
         __syncthreads();
     }
+    // accumulator fragment: c0 (g, 2t), c1 (g, 2t+1), c2 (g+8, 2t), c3 (g+8, 2t+1)
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        const int i = i0 + ty * 4 + r;
-        if (i >= M) continue;
+    for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const int j = j0 + tx * 4 + c;
-            if (j >= N) continue;
-            float *p = C + (int64_t)i * ldc + j;
-            *p = accumulate ? *p + acc[r][c] : acc[r][c];
-        }
-    }
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int i = i0 + wm + mt * 16 + g + (q >> 1) * 8;
+                const int j = j0 + wn + nt * 8 + 2 * t + (q & 1);
+                if (i < M && j < N) {
+                    float *p = C + (int64_t)i * ldc + j;
+                    *p = accumulate ? *p + acc[mt][nt][q] : acc[mt][nt][q];
+                }
+            }
 }
 
 __device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
@@ -293,7 +342,7 @@ template <bool TA, bool TB, class BT>
 void gemm(cudaStream_t st, int M, int N, int K, const float *A, int lda, const BT *B, int ldb, float *C, int ldc,
           bool acc) {
     dim3 grid((N + 63) / 64, (M + 63) / 64);
-    gemm_kernel<TA, TB, BT><<<grid, 256, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc, acc ? 1 : 0);
+    gemm_kernel<TA, TB, BT><<<grid, 128, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc, acc ? 1 : 0);
 }
 
 // weight gradient dW[dd x di] = dZ^T X over n samples, split along the samples
@@ -301,10 +350,10 @@ void weight_grad(spx_surrogate *s, int dd, int di, int64_t n, const float *dZ, c
     const int splits = (int)std::min<int64_t>(kMaxSplits, std::max<int64_t>(1, n / kSplitRows));
     dim3 grid((di + 63) / 64, (dd + 63) / 64, splits);
     if (splits == 1) {
-        gemm_kernel<true, false, float><<<grid, 256, 0, s->stream>>>(dd, di, (int)n, dZ, dd, X, di, dW, di, 0);
+        gemm_kernel<true, false, float><<<grid, 128, 0, s->stream>>>(dd, di, (int)n, dZ, dd, X, di, dW, di, 0);
         return;
     }
-    gemm_kernel<true, false, float><<<grid, 256, 0, s->stream>>>(dd, di, (int)n, dZ, dd, X, di, s->split.p, di, 0);
+    gemm_kernel<true, false, float><<<grid, 128, 0, s->stream>>>(dd, di, (int)n, dZ, dd, X, di, s->split.p, di, 0);
     const int64_t count = (int64_t)dd * di;
     split_reduce_kernel<<<blocks(count), 256, 0, s->stream>>>(count, splits, s->split.p, dW);
 }
