@@ -1003,15 +1003,18 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         // the last chunk only reaches j_last steps: its series can stop where the
         // Bessel column of j_last (times the growth from Im L) drops below tol
         const int nchunks = (nsteps + Mo) / Mo;      // ceil((nsteps+1)/Mo)
-        if (tid == 0) {
+        if (warp == 0) {
+            // one warp scans the column 32 terms at a time from the top
             const int j_last = nsteps - (nchunks - 1) * Mo;
             const double lg = 2.0 * imax / half;
             int kl = 2;
-            double grow = exp((K - 1) * lg);
-            const double shrink = exp(-lg);
-            for (int k = K - 1; k >= 2; --k, grow *= shrink)
-                if (fabs(table[(size_t)k * (Mo + 1) + j_last]) * grow > run.tol) { kl = k + 1; break; }
-            s_int[3] = min(K, kl + 2);
+            for (int top = K - 1; top >= 2; top -= 32) {
+                const int k = top - lane;
+                const bool sig = k >= 2 && fabs(table[(size_t)k * (Mo + 1) + j_last]) * exp(k * lg) > run.tol;
+                const unsigned m = __ballot_sync(0xffffffffu, sig);
+                if (m) { kl = top - (__ffs(m) - 1) + 1; break; }
+            }
+            if (lane == 0) s_int[3] = min(K, kl + 2);
         }
         // series coefficients of one chunk (tau = M dt), centre phase folded in
         {
@@ -1386,29 +1389,51 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             __syncthreads();
             // FID points of this chunk: f_j = ph_j * sum_k J_k(s j dt) (-i)^k mu_k
             if (!CLU || crank == 0) {
+              // the moments turned by (-i)^k, in place (nothing reads them after)
+              for (int q = tid; q < Kc * sys.nchan; q += blockDim.x) {
+                  const int k = q % Kc;
+                  Vec &m = s_mu[(q / Kc) * run.Kmax + k];
+                  const Vec mu = m;
+                  switch (k & 3) {
+                      case 1: m.x = mu.y; m.y = -mu.x; break;
+                      case 2: m.x = -mu.x; m.y = -mu.y; break;
+                      case 3: m.x = -mu.y; m.y = mu.x; break;
+                      default: break;
+                  }
+              }
+              __syncthreads();
               for (int ch = 0; ch < sys.nchan; ++ch) {
                 const Vec *mu_c = s_mu + ch * run.Kmax;
                 Vec *out_c = fid_out + (size_t)ch * (nsteps + 1);
                 if (ch > 0) __syncthreads();         // s_rec reused per channel
                 const int parts = max(1, (int)blockDim.x / Mo);
                 const int kper = (Kc + parts - 1) / parts;
+                const size_t ld = (size_t)(Mo + 1);
                 for (int jj = tid; jj < Mo * parts; jj += blockDim.x) {
                     const int j = jj % Mo, pidx = jj / Mo;
                     const int k0 = pidx * kper, k1 = min(Kc, k0 + kper);
-                    Vec f = vzero<Vec>();
-                    for (int k = k0; k < k1; ++k) {
-                        const Real jv = (Real)table[(size_t)k * (Mo + 1) + j];
-                        const Vec mu = mu_c[k];
-                        Real re, im;
-                        switch (k & 3) {
-                            case 0: re = mu.x; im = mu.y; break;
-                            case 1: re = mu.y; im = -mu.x; break;
-                            case 2: re = -mu.x; im = -mu.y; break;
-                            default: re = -mu.y; im = mu.x; break;
-                        }
-                        f.x += jv * re;
-                        f.y += jv * im;
+                    // the Bessel table sits in global memory (L2): four
+                    // independent loads per step keep its latency off the
+                    // critical path, two accumulators the adds
+                    const double *tcol = table + j;
+                    Vec f = vzero<Vec>(), g = vzero<Vec>();
+                    int k = k0;
+                    for (; k + 4 <= k1; k += 4) {
+                        const Real j0 = (Real)tcol[(size_t)k * ld], j1 = (Real)tcol[(size_t)(k + 1) * ld];
+                        const Real j2 = (Real)tcol[(size_t)(k + 2) * ld], j3 = (Real)tcol[(size_t)(k + 3) * ld];
+                        const Vec m0 = mu_c[k], m1 = mu_c[k + 1], m2 = mu_c[k + 2], m3 = mu_c[k + 3];
+                        f.x += j0 * m0.x; f.y += j0 * m0.y;
+                        g.x += j1 * m1.x; g.y += j1 * m1.y;
+                        f.x += j2 * m2.x; f.y += j2 * m2.y;
+                        g.x += j3 * m3.x; g.y += j3 * m3.y;
                     }
+                    for (; k < k1; ++k) {
+                        const Real jv = (Real)tcol[(size_t)k * ld];
+                        f.x += jv * mu_c[k].x;
+                        f.y += jv * mu_c[k].y;
+                    }
+                    f.x += g.x;
+                    f.y += g.y;
                     s_rec[jj] = f;
                 }
                 __syncthreads();
