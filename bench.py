@@ -652,6 +652,16 @@ def c2_leg(device):
             b.launch()
             ms.append(b.synchronize())
         f32 = B.powder_fids(bp)
+        # where the graph's time goes: every system alone on the whole GPU
+        # (same tuned shape, kernel time by the engine's events)
+        solo = []
+        for eng, g, f, dt, ns in zip(bp.engines, bp.grids, bp.fids, bp.dts, bp.nsteps):
+            eng.run_device(g[0].data_ptr(), g[1].data_ptr(), g[2].data_ptr(), g[3].data_ptr(), g.shape[1], dt, ns,
+                           f.data_ptr(), precision=E.FP32, fp32_check=False)
+            solo.append(eng.stats()['kernel_ms'])
+        solo_by_dim = {}
+        for d, t in zip(bp.dims, solo):
+            solo_by_dim.setdefault(str(d), []).append(t)
         B.capture(bp, E.FP64)
         bp.batch.launch()
         ms64 = bp.batch.synchronize()
@@ -669,6 +679,10 @@ def c2_leg(device):
                 'rel_err_vs_fp64_gpu_max': max(_rel(a, b_) for a, b_ in zip(f32, f64)),
                 'fp64_gpu': {'value': n_fids / (ms64 / 1e3), 'graph_ms': ms64},
                 'systems_by_dim': dims, 'tuned_shape_by_dim': shapes,
+                'solo_kernel_ms': {'sum': sum(solo), 'max': max(solo),
+                                   'by_dim_sum': {d: sum(v) for d, v in solo_by_dim.items()},
+                                   'note': 'each system alone on the whole GPU: the sum is the time of running '
+                                           'them one after another, the max the slowest system\'s own time'},
                 'setup_s': bp.setup_s, 'autotune_s': bp.tune_s}
     finally:
         bp.close()
