@@ -746,6 +746,29 @@ def surrogate_c4_leg(device):
         eng.close()
 
 
+def profile_surrogate():
+    """The c3 network (169 features, 4 x 256 GELU, 128 outputs) trained for 20
+    epochs on 2000 random orientations, then 20000 predictions."""
+    import torch
+    from spinach_gb300 import engine as E
+    from spinach_gb300.build import build_library
+    build_library()
+    net = E.Surrogate(0, lmax=12, hidden=256, layers=4, n_out=128, seed=1)
+    rng = np.random.default_rng(0)
+    n = 2000
+    db = torch.from_numpy(np.arccos(rng.uniform(-1, 1, n))).cuda()
+    dg = torch.from_numpy(rng.uniform(0, 2 * np.pi, n)).cuda()
+    T = torch.randn(n, 128, device='cuda', dtype=torch.float32)
+    loss = net.train(n, db.data_ptr(), dg.data_ptr(), T.data_ptr(), 20, 1e-3)
+    m = 20000
+    out = torch.empty(m, 128, device='cuda', dtype=torch.float32)
+    bb = torch.from_numpy(np.arccos(rng.uniform(-1, 1, m))).cuda()
+    gg = torch.from_numpy(rng.uniform(0, 2 * np.pi, m)).cuda()
+    net.predict(m, bb.data_ptr(), gg.data_ptr(), out.data_ptr())
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_surrogate': True, 'final_loss': float(loss[-1])}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -761,7 +784,12 @@ def main():
                     help='grid size per rank (default: the workload\'s own; smaller for profiling)')
     ap.add_argument('--profile-only', action='store_true',
                     help='warm-up and timed powder runs only (for ncu captures); no FP64/e2e/CPU legs')
+    ap.add_argument('--profile-surrogate', action='store_true',
+                    help='only the c3 network: 20 training epochs on 2000 orientations, then 20000 predictions '
+                         '(for ncu captures of its tensor-core products)')
     args = ap.parse_args()
+    if args.profile_surrogate:
+        return profile_surrogate()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == 'reference':

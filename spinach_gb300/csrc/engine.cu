@@ -894,11 +894,14 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
 
     int chk = 0;
     if (fp32_check && !f64) {
-        // the FP64 re-run takes its CTAs' SMs; the FP32 run keeps the rest
+        // the FP64 re-run takes its CTAs' SMs; an FP32 run of several waves
+        // keeps the rest (a single-wave grid keeps every CTA: fewer would add
+        // a wave)
         const int chk_ctas = launch_fp32_check(h, n_orient, d_al, d_be, d_ga, dt, nsteps, opt, sys);
         chk = (int)std::min<int64_t>(kCheckOrients, n_orient);
         const int take = ((chk_ctas + c.cl - 1) / c.cl) * c.cl;
-        if (c.grid - take >= std::max(c.cl, c.grid / 2)) c.grid -= take;
+        const bool waves = n_orient * c.cl > c.grid;
+        if (waves && c.grid - take >= std::max(c.cl, c.grid / 2)) c.grid -= take;
     }
     if (timed) SPX_CUDA(cudaEventRecord(h->ev[0], h->stream));
     launch_chebyshev(h, f64, c, sys, run);

@@ -5,7 +5,9 @@ Run from the repository root:  python tests/golden/make_golden.py
 systems, ``... deuterium`` for the quadratic-coupling workload,
 ``... sequences`` for the pulse sequences and MAS contexts, ``... wide``
 for the full c1 powder, many c1/c4 orientations, every c2 dimension and the
-paranoia-mode propagator branch (parallel over the host cores), ``... grids
+paranoia-mode propagator branch (parallel over the host cores), ``... powders``
+for the whole c4 powder and the remaining c2 whole powders (about an hour on
+8 cores), ``... grids
 <reference root>`` to copy the reference's 14-point Lebedev grid out of its
 grid file, which needs the reference source tree; the root can also come
 from the SPINACH_ROOT environment variable).  Writes tests/golden/*.npz.  Inputs are the seeded workloads of
@@ -165,6 +167,40 @@ def wide():
             print('c2 dim', d, round(time.time() - t0, 1), 's')
 
 
+def wide_powders():
+    """The whole powder FIDs the 'wide' fixtures leave out, parallel over the
+    host cores: config 4's 4000-orientation powder (Krylov branch, summed in
+    grid order) and the 400-orientation powders of the c2 systems of
+    dimension 1156, 1789 and 4096 (added to their c2_dim*_krylov_fp64.npz)."""
+    import multiprocessing as mp
+    for v in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
+        os.environ[v] = '1'
+    t0 = time.time()
+    with mp.get_context('spawn').Pool(os.cpu_count()) as pool:
+        ws = W.c2()
+        for d in (1156, 1789, 4096):
+            name = f'c2_dim{d}_krylov_fp64.npz'
+            old = dict(np.load(os.path.join(HERE, name)))
+            i = int(old['system'])
+            x = ws[i]
+            _, _, _, wt = W.zcwn_grid(x.n_orient)
+            f = _pool_fids(pool, 'c2', i, np.arange(x.n_orient), chunk=4)
+            p = wt[0] * f[0]
+            for n in range(1, x.n_orient):
+                p = p + wt[n] * f[n]
+            old['fid'] = p
+            save(name, **old)
+            print('c2 dim', d, round(time.time() - t0, 1), 's', flush=True)
+        w = W.c4()
+        _, _, _, wt = W.zcwn_grid(w.n_orient)
+        f = _pool_fids(pool, 'c4', 0, np.arange(w.n_orient), chunk=10)
+        fid = wt[0] * f[0]
+        for n in range(1, w.n_orient):
+            fid = fid + wt[n] * f[n]
+        save('c4_powder_krylov_fp64.npz', fid=fid, seed=w.seed, nsteps=w.nsteps, n_orient=w.n_orient)
+        print('c4 powder', round(time.time() - t0, 1), 's', flush=True)
+
+
 SEQ_SEL = np.array([7, 66, 131, 180])
 SEQ_W = np.array([0.1, 0.4, 0.3, 0.2])
 
@@ -218,6 +254,8 @@ def main():
         return grids(rest[0] if rest else os.environ.get('SPINACH_ROOT'))
     if 'wide' in sys.argv[1:]:
         return wide()
+    if 'powders' in sys.argv[1:]:
+        return wide_powders()
     if 'large' in sys.argv[1:]:
         return large_systems()
     if 'deuterium' in sys.argv[1:]:
