@@ -9,10 +9,11 @@ oracle fixtures of tests/golden/make_golden.py ('wide'):
   tolerances of kernel/utilities/tolerances.m:97-100, at two orientations: the
   chop quantisation is then below the bar, so the propagator branch itself is
   held to 1e-10;
-* c4 (EPR radical, IK-1(3), dim 2736, 4096 steps): 24 orientations;
+* c4 (EPR radical, IK-1(3), dim 2736, 4096 steps): the whole 4000-orientation
+  powder FID and 24 orientations;
 * c2: four orientations of one system of every dimension (64, 256, 1024,
-  1156, 1789, 4096), and the whole 400-orientation powder of the dim-64, -256
-  and -1024 systems through the batched graph with on-GPU construction.
+  1156, 1789, 4096), and the whole 400-orientation powder of each of those
+  six systems through the batched graph with on-GPU construction.
 
 Bars (relative 2-norm error, tests/lib/test_close.m metric): FP64 <= 1e-10,
 FP32 <= 1e-5.
@@ -77,6 +78,18 @@ def test_c1_default_propagator_branch_at_paranoia_chop(gpu_engine):
                         'c1 propagator branch')
 
 
+def test_c4_whole_powder_vs_oracle(gpu_engine):
+    """Config 4's powder FID (4000 orientations x 4096 steps)."""
+    w = W.c4()
+    _upload(gpu_engine, w)
+    gold = np.load(os.path.join(GOLD, 'c4_powder_krylov_fp64.npz'))
+    g = W.zcwn_grid(w.n_orient)
+    r64 = gpu_engine.run(*g, w.dt, w.nsteps, precision=E.FP64)
+    assert rel_err(r64.fid, gold['fid']) <= FP64_TOL
+    r32 = gpu_engine.run(*g, w.dt, w.nsteps, precision=E.FP32)
+    assert rel_err(r32.fid, gold['fid']) <= FP32_TOL
+
+
 def test_c4_twenty_four_orientations(gpu_engine):
     w = W.c4()
     _upload(gpu_engine, w)
@@ -97,15 +110,15 @@ def test_c2_every_dimension_four_orientations(gpu_engine, dim):
 
 def test_c2_whole_powders_through_the_batched_graph(engine_lib):
     """The c2 path itself (on-GPU construction of I and Q, one CUDA graph over
-    the systems) against the oracle's whole powders of the dim-64, -256 and
-    -1024 systems, FP64 and FP32."""
+    the systems) against the oracle's whole 400-orientation powders of one
+    system of every dimension, FP64 and FP32."""
     import torch
     from spinach_gb300 import batched as B
-    golds = [np.load(os.path.join(GOLD, f'c2_dim{d}_krylov_fp64.npz')) for d in (64, 256, 1024)]
+    golds = [np.load(os.path.join(GOLD, f'c2_dim{d}_krylov_fp64.npz')) for d in C2_DIMS]
     ws = W.c2()
     bp = B.prepare([ws[int(g['system'])] for g in golds], tune=False, precision=E.FP64)
     try:
-        assert bp.dims == [64, 256, 1024]
+        assert bp.dims == C2_DIMS
         for prec, tol in ((E.FP64, FP64_TOL), (E.FP32, FP32_TOL)):
             for f in bp.fids:
                 f.zero_()
