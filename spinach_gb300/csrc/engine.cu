@@ -97,6 +97,7 @@ struct spx_handle {
     int64_t nnz = 0;
     double g_upper = 0.0;      // upper bound of the spectral radius of H over all orientations
     double max_im_diag = 0.0;
+    double lo_scale = 1.0;     // power of two scaling every assembled off-diagonal entry into (-1, 1)
     DevBuf<int> d_slice_off, d_stream_coef, d_term_rkm;
     std::vector<int> slice_off_host;
     DevBuf<uint16_t> d_ell_col;
@@ -447,6 +448,10 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
     h->cplx = cplx;
     h->nnz = (int64_t)nk;
     h->g_upper = g_upper;
+    // every assembled off-diagonal entry is at most g_upper in magnitude (the
+    // rotational coefficients are at most 1): 2^-(floor(log2 g_upper) + 1)
+    // scales them into (-1, 1) for the packed FP32 layout
+    h->lo_scale = g_upper > 0.0 ? std::ldexp(1.0, -std::ilogb(g_upper) - 1) : 1.0;
     h->max_im_diag = max_im_diag;
     h->have_system = true;
 }
@@ -541,18 +546,20 @@ double host_series_terms(double x, double lg, double tol) {
 }
 
 template <bool F64, bool CPLX>
-size_t smem_bytes(const spx_handle *h, int nsl_loc, int ell_loc, int Kmax, int M, int threads, int traj_m) {
-    spx::SmemLayout<F64, CPLX> L(h->n_pad, nsl_loc, ell_loc, Kmax, M, threads, h->nchan, traj_m);
+size_t smem_bytes(const spx_handle *h, int nsl_loc, int ell_loc, int Kmax, int M, int threads, int traj_m, int cl) {
+    // cluster launches of FP32 real values keep each column in its value
+    const bool packed = !F64 && !CPLX && cl > 1;
+    spx::SmemLayout<F64, CPLX> L(h->n_pad, nsl_loc, ell_loc, Kmax, M, threads, h->nchan, traj_m, packed);
     return L.total;
 }
 
 size_t smem_for(const spx_handle *h, bool f64, int nsl_loc, int ell_loc, int Kmax, int M, int threads,
-                int traj_m = 1) {
+                int traj_m, int cl) {
     if (f64)
-        return h->cplx ? smem_bytes<true, true>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m)
-                       : smem_bytes<true, false>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m);
-    return h->cplx ? smem_bytes<false, true>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m)
-                   : smem_bytes<false, false>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m);
+        return h->cplx ? smem_bytes<true, true>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m, cl)
+                       : smem_bytes<true, false>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m, cl);
+    return h->cplx ? smem_bytes<false, true>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m, cl)
+                   : smem_bytes<false, false>(h, nsl_loc, ell_loc, Kmax, M, threads, traj_m, cl);
 }
 
 }  // namespace
@@ -647,11 +654,11 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     if (opt.chunk_target > 0) targets = {opt.chunk_target};
     bool placed = false;
     const int cls[] = {1, 2, 4, 8};
-    // first pass: at most 4 rows per lane (8 spill registers); second pass: 8 on one CTA
-    for (int pass = 0; pass < 2 && !placed; ++pass)
+    // up to 8 rows per lane on one CTA, at most 4 on a cluster (c4 on one CTA
+    // with 6 rows per lane: 323 ms per powder, on 2-CTA clusters with 3:
+    // 344 ms -- a cluster pays a barrier across SMs per term)
     for (int cl : cls) {
         if (opt.cluster > 0 && cl != opt.cluster) continue;       // cluster size set by the caller
-        if (pass == 1 && cl > 1) continue;
         if (!partition_slices(h, cl, c)) continue;
         // warps: one per 32-row slice, at most 16 (c1: 16 warps 118.9 ms,
         // 13 warps 121.3 ms per 1000-orientation powder; c2 dim 4096 on 8-CTA
@@ -663,7 +670,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
         else if (nws[0] > 4) nws.push_back((nws[0] + 1) / 2);
         for (int nwarps : nws) {
         const int rows = (c.nsl_loc + nwarps - 1) / nwarps;
-        if (rows > (pass == 0 ? 4 : 8)) continue;
+        if (rows > (cl > 1 ? 4 : 8)) continue;
         c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 8;
         c.threads = nwarps * 32;
         // dynamic shared memory may use what the kernel's static arrays leave
@@ -683,7 +690,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
             if (kmax_override > 0) K = std::max(K, kmax_override);
             c.Kmax = std::min(K, 8192);
             c.traj_m = traj ? c.M : 1;
-            c.smem = smem_for(h, f64, c.nsl_loc, c.ell_loc, c.Kmax, c.M, c.threads, c.traj_m);
+            c.smem = smem_for(h, f64, c.nsl_loc, c.ell_loc, c.Kmax, c.M, c.threads, c.traj_m, cl);
             if (c.smem <= budget) { placed = true; break; }
             if (c.fixed) break;
         }
@@ -866,7 +873,7 @@ void launch_powder(spx_handle *h, int64_t n_orient, const double *d_al, const do
     sys.ell_re = h->d_ell_re.p; sys.ell_im = h->cplx ? h->d_ell_im.p : nullptr;
     sys.diag = h->d_diag.p; sys.stream_coef = h->d_stream_coef.p; sys.nstreams = h->nstreams;
     sys.ncoef = 1 + 2 * h->nterms; sys.nterms = h->nterms; sys.term_rkm = h->d_term_rkm.p;
-    sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag;
+    sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag; sys.lo_scale = h->lo_scale;
     sys.ncoil = h->ncoil; sys.coil_rows = h->d_coil_rows.p; sys.coil_vals = h->d_coil_vals.p;
     sys.coil_chan = h->d_coil_chan.p; sys.nchan = h->nchan;
     sys.rho0s = h->n_states > 0 ? h->d_rho0s.p : nullptr;
@@ -1851,7 +1858,7 @@ void run_powder_noalloc(spx_handle *h, int64_t n_orient, const double *d_al, con
     sys.ell_re = h->d_ell_re.p; sys.ell_im = h->cplx ? h->d_ell_im.p : nullptr;
     sys.diag = h->d_diag.p; sys.stream_coef = h->d_stream_coef.p; sys.nstreams = h->nstreams;
     sys.ncoef = 1 + 2 * h->nterms; sys.nterms = h->nterms; sys.term_rkm = h->d_term_rkm.p;
-    sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag;
+    sys.rho0 = h->d_rho0.p; sys.coil = h->d_coil.p; sys.max_im_diag = h->max_im_diag; sys.lo_scale = h->lo_scale;
     sys.ncoil = h->ncoil; sys.coil_rows = h->d_coil_rows.p; sys.coil_vals = h->d_coil_vals.p;
     sys.coil_chan = h->d_coil_chan.p; sys.nchan = h->nchan;
     sys.rho0s = h->n_states > 0 ? h->d_rho0s.p : nullptr;

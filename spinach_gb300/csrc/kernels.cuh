@@ -30,9 +30,12 @@
 // double.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <stdint.h>
+
+#include <type_traits>
 
 namespace spx {
 
@@ -52,11 +55,22 @@ enum DeviceStatus : int {
 // FP32 shared-memory layouts.  Liouvillian values are stored compactly (hi
 // + lo float pairs) and expanded into f32x2 operand pairs in registers:
 //   ValR  real off-diagonal value (hi, lo)                          8 B
+//   ValRP real off-diagonal value with its column (cluster launches) 8 B:
+//         hi, the low part as a half in units u = 2^-24 / s, and the
+//         column index, so the column array is not stored.  s is a power
+//         of two with |v| s <= 1: before the rescale to L~ the system's
+//         lo_scale (1 / a bound on every assembled off-diagonal entry),
+//         after it 1 (an off-diagonal entry of the Hermitian L is at most
+//         half its spectral width, so the entries of L~ are below 1).
+//         |lo| <= ulp(hi) / 2 <= 2^-24 / s keeps lo / u within [-1, 1]; the
+//         half holds 11 bits of it, about 35 bits in all.
 //   ValC  complex value (re_hi, im_hi, re_lo, im_lo)               16 B
 //   DgS   diagonal (re_hi, re_lo, im, 0)                           16 B
 // Series coefficients are few and read by every row, so they stay pre-packed:
 //   PackA  h = (re_hi, re_hi, -im_hi, im_hi), l = same for the lo parts
 struct __align__(8) ValR { float hi, lo; };
+struct __align__(8) ValRP { float hi; __half lo; uint16_t col; };
+static_assert(sizeof(ValRP) == sizeof(ValR), "packed values keep the layout's size");
 struct __align__(16) ValC { float rh, ih, rl, il; };
 struct __align__(16) DgS { float rh, rl, im, pad; };
 struct __align__(16) PackC { float4 h, l; };
@@ -76,6 +90,13 @@ static __device__ __forceinline__ void split(double v, float &hi, float &lo) {
     lo = (float)(v - (double)hi);
 }
 static __device__ __forceinline__ void pack(ValR &o, double re, double) { split(re, o.hi, o.lo); }
+// writes the value in units 2^-24 / s (s: a power of two with |re| s <= 1),
+// keeps the column
+static __device__ __forceinline__ void pack_rp(ValRP &o, double re, double s) {
+    o.hi = (float)re;
+    const float l = (float)((re - (double)o.hi) * (16777216.0 * s));
+    o.lo = __float2half_rn(fminf(fmaxf(l, -65504.f), 65504.f));
+}
 static __device__ __forceinline__ void pack(ValC &o, double re, double im) {
     split(re, o.rh, o.rl);
     split(im, o.ih, o.il);
@@ -93,6 +114,14 @@ static __device__ __forceinline__ void pack(PackC &o, double re, double im) {
     o.l = make_float4(rl, rl, -il, il);
 }
 static __device__ __forceinline__ double2 unpack(const ValR &v) { return make_double2((double)v.hi + (double)v.lo, 0.0); }
+// value of a packed entry stored in units u
+static __device__ __forceinline__ double2 unpack_rp(const ValRP &v, float u) {
+    return make_double2((double)v.hi + (double)(__half2float(v.lo) * u), 0.0);
+}
+// column of ELL entry e: from the column array, or from a packed value
+template <class V>
+static __device__ __forceinline__ int col_of(const uint16_t *s_col, const V *, int e) { return s_col[e]; }
+static __device__ __forceinline__ int col_of(const uint16_t *, const ValRP *s_val, int e) { return s_val[e].col; }
 static __device__ __forceinline__ double2 unpack(const ValC &v) {
     return make_double2((double)v.rh + (double)v.rl, (double)v.ih + (double)v.il);
 }
@@ -109,6 +138,12 @@ static __device__ __forceinline__ void mac(float2 &y, const ValR &v, const float
     y.x = fmaf(v.hi, x.x, y.x); y.y = fmaf(v.hi, x.y, y.y);
     y.x = fmaf(v.lo, x.x, y.x); y.y = fmaf(v.lo, x.y, y.y);
 }
+// packed entry in units u
+static __device__ __forceinline__ void mac_rp(float2 &y, const ValRP &v, const float2 x, float u) {
+    const float lo = __half2float(v.lo) * u;
+    y.x = fmaf(v.hi, x.x, y.x); y.y = fmaf(v.hi, x.y, y.y);
+    y.x = fmaf(lo, x.x, y.x); y.y = fmaf(lo, x.y, y.y);
+}
 static __device__ __forceinline__ void mac(float2 &y, const ValC &v, const float2 x) {
     // (re + i im) x = re*x + (-im*x.y, im*x.x)
     y.x = fmaf(v.rh, x.x, y.x); y.y = fmaf(v.rh, x.y, y.y);
@@ -123,6 +158,13 @@ static __device__ __forceinline__ void mac(double2 &y, const double2 &v, const d
     y.x = fma(v.x, x.x, y.x); y.x = fma(-v.y, x.y, y.x);
     y.y = fma(v.x, x.y, y.y); y.y = fma(v.y, x.x, y.y);
 }
+// the same for any stored value; u: units of a packed entry's low part
+template <class V>
+static __device__ __forceinline__ double2 value_of(const V &v, float) { return unpack(v); }
+static __device__ __forceinline__ double2 value_of(const ValRP &v, float u) { return unpack_rp(v, u); }
+template <class Y, class V, class X>
+static __device__ __forceinline__ void mac_u(Y &y, const V &v, const X x, float) { mac(y, v, x); }
+static __device__ __forceinline__ void mac_u(float2 &y, const ValRP &v, const float2 x, float u) { mac_rp(y, v, x, u); }
 
 template <class V> __device__ __forceinline__ V vzero();
 template <> __device__ __forceinline__ float2 vzero<float2>() { return make_float2(0.f, 0.f); }
@@ -336,6 +378,7 @@ struct DevSystem {
     const int *coil_chan;       // ncoil detection channels (0 .. nchan-1)
     int nchan;                  // detection channels (evolution.m 'multichannel'); > 1 needs the listed coil
     double max_im_diag;         // largest |Im L_ii| (relaxation), rad/s
+    double lo_scale;            // power of two, at most 1 / (a bound on every assembled off-diagonal entry)
 };
 
 struct DevRun {
@@ -500,8 +543,9 @@ struct SmemLayout {
     // entries one CTA owns (all of them without a cluster)
     // traj_m > 1: trajectory outputs with chunks of traj_m steps (coefficients
     // and accumulators of the traj_m - 1 states inside a chunk)
+    // packed: FP32 real values carry their columns (ValRP), no column array
     __host__ __device__ SmemLayout(int n_pad, int nslices, int ell_len, int Kmax, int M, int nthreads, int nchan = 1,
-                                   int traj_m = 1) {
+                                   int traj_m = 1, bool packed = false) {
         size_t o = 0;
         coef = o; o = align(o + sizeof(double) * kMaxCoef);
         red = o; o = align(o + sizeof(double) * kRedSlots);
@@ -509,8 +553,8 @@ struct SmemLayout {
         alpha = o; o = align(o + sizeof(double) * kMaxLanczos);
         beta = o; o = align(o + sizeof(double) * kMaxLanczos);
         slice_off = o; o = align(o + sizeof(int) * (nslices + 1));
-        ell_col = o; o = align(o + sizeof(uint16_t) * ell_len);
-        ell_val = o; o = align(o + sizeof(typename P::Val) * ell_len);
+        ell_col = o; o = align(o + (packed ? 0 : sizeof(uint16_t) * ell_len));
+        ell_val = o; o = align(o + sizeof(typename P::Val) * ell_len);    // sizeof(ValRP) == sizeof(ValR)
         diag = o; o = align(o + sizeof(typename P::Dg) * 32 * (size_t)nslices);
         xa = o; o = align(o + sizeof(typename P::Vec) * n_pad);
         xb = o; o = align(o + sizeof(typename P::Vec) * n_pad);
@@ -673,7 +717,13 @@ __global__ void __launch_bounds__(512)
 powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     using P = Prec<F64, CPLX>;
     using Vec = typename P::Vec;
-    using Val = typename P::Val;
+    // cluster launches of FP32 real values keep each column in its value
+    // (ValRP), which leaves room for larger systems per CTA
+    constexpr bool PACKED = !F64 && !CPLX && CLU;
+    using Val = std::conditional_t<PACKED, ValRP, typename P::Val>;
+    // units of a packed entry's low part before the rescale to L~ (exact:
+    // lo_scale is a power of two)
+    const float lo_unit = (float)(5.9604644775390625e-8 / sys.lo_scale);
     using Dg = typename P::Dg;
     using Real = typename P::Real;
     using Acc = typename P::Acc;
@@ -681,7 +731,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 
     extern __shared__ __align__(16) unsigned char smem[];
     const SmemLayout<F64, CPLX> L(sys.n_pad, CLU ? run.nsl_loc : sys.nslices, CLU ? run.ell_loc : sys.ell_len,
-                                  run.Kmax, run.M, blockDim.x, sys.nchan, TRJ ? run.traj_m : 1);
+                                  run.Kmax, run.M, blockDim.x, sys.nchan, TRJ ? run.traj_m : 1, PACKED);
     double *s_coef = reinterpret_cast<double *>(smem + L.coef);
     double *s_red = reinterpret_cast<double *>(smem + L.red);
     double *s_cred = reinterpret_cast<double *>(smem + L.cred);
@@ -729,7 +779,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         s_cval[tid] = tovec(sys.coil_vals[tid], Vec());
         s_cchan[tid] = sys.coil_chan ? sys.coil_chan[tid] : 0;
     }
-    for (int e = tid; e < ell_loc; e += blockDim.x) s_col[e] = sys.ell_col[eb + e];
+    for (int e = tid; e < ell_loc; e += blockDim.x) {
+        if constexpr (PACKED) s_val[e].col = sys.ell_col[eb + e];
+        else s_col[e] = sys.ell_col[eb + e];
+    }
     // Slices to warps, longest-processing-time first: slices are stored in
     // non-increasing width, each goes to the least-loaded warp with room, so a
     // warp's slices also come in non-increasing width.  Cost ~ width + 5; the
@@ -790,7 +843,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 re = fma(c, sys.ell_re[(size_t)s * sys.ell_len + eb + e], re);
                 if (CPLX) im = fma(c, sys.ell_im[(size_t)s * sys.ell_len + eb + e], im);
             }
-            pack(s_val[e], re, im);
+            if constexpr (PACKED) pack_rp(s_val[e], re, sys.lo_scale);
+            else pack(s_val[e], re, im);
         }
         for (int i = tid; i < nrow_loc; i += blockDim.x) {
             double re = 0.0, im = 0.0;
@@ -811,7 +865,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
             const int off = s_soff[sl], w = (s_soff[sl + 1] - off) >> 5;
             double rad = 0.0;
             for (int c = 0; c < w; ++c) {
-                const double2 v = unpack(s_val[off + c * 32 + lane]);
+                const double2 v = value_of(s_val[off + c * 32 + lane], lo_unit);
                 rad += CPLX ? sqrt(v.x * v.x + v.y * v.y) : fabs(v.x);
             }
             const double dr = unpack(s_diag[lrow]).x;
@@ -869,7 +923,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 Vec y = vzero<Vec>();
                 for (int c = 0; c < w; ++c) {
                     const int e = off + c * 32 + lane;
-                    mac(y, s_val[e], s_xa[s_col[e]]);
+                    mac_u(y, s_val[e], s_xa[col_of(s_col, s_val, e)], lo_unit);
                 }
                 const Real dr = diag_re(s_diag[lrow]);
                 y.x += dr * q_cur[r].x;
@@ -988,8 +1042,9 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         {
             const double inv = 1.0 / half;
             for (int e = tid; e < ell_loc; e += blockDim.x) {
-                const double2 v = unpack(s_val[e]);
-                pack(s_val[e], v.x * inv, v.y * inv);
+                const double2 v = value_of(s_val[e], lo_unit);
+                if constexpr (PACKED) pack_rp(s_val[e], v.x * inv, 1.0);      // L~ entries below 1
+                else pack(s_val[e], v.x * inv, v.y * inv);
             }
             for (int i = tid; i < nrow_loc; i += blockDim.x) {
                 const double2 d = unpack(s_diag[i]);
@@ -1271,7 +1326,9 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                             const f2x X = tc[r];
                             Y[r] = mul2(f2pk(d.rh, d.rh), X);
                             kahan_add2(Y[r], C[r], mul2(f2pk(-d.im, d.im), swap2(X)));
-                            Lo[r] = mul2(f2pk(d.rl, d.rl), X);
+                            // packed values: the low parts are summed in units of 2^-24
+                            const float dl = PACKED ? d.rl * 16777216.f : d.rl;
+                            Lo[r] = mul2(f2pk(dl, dl), X);
                         }
                     }
                     int c = 0;
@@ -1283,7 +1340,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 #pragma unroll
                                 for (int r = 0; r < seg; ++r) {
                                     const int e = r_off[r] + c * 32;
-                                    const f2x X = src[s_col[e]];
+                                    const f2x X = src[col_of(s_col, s_val, e)];
                                     if constexpr (CPLX) {
                                         const ValC v = s_val[e];
                                         const f2x XS = swap2(X);
@@ -1292,9 +1349,12 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                                         Lo[r] = fma2(f2pk(v.rl, v.rl), X, Lo[r]);
                                         Lo[r] = fma2(f2pk(-v.il, v.il), XS, Lo[r]);
                                     } else {
-                                        const ValR v = s_val[e];
+                                        const Val v = s_val[e];
+                                        float lo;
+                                        if constexpr (PACKED) lo = __half2float(v.lo);
+                                        else lo = v.lo;
                                         kahan_add2(Y[r], C[r], mul2(f2pk(v.hi, v.hi), X));
-                                        Lo[r] = fma2(f2pk(v.lo, v.lo), X, Lo[r]);
+                                        Lo[r] = fma2(f2pk(lo, lo), X, Lo[r]);
                                     }
                                 }
                             }
@@ -1305,7 +1365,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     for (int r = 0; r < RMAX; ++r) {
                         if (r < nr) {
                             // t_k = TW * (Y + (Lo - C)) - t_{k-2}
-                            const f2x T = sub2(fma2(TW, Y[r], mul2(TW, sub2(Lo[r], C[r]))), tp[r]);
+                            const f2x LoR = PACKED ? mul2(Lo[r], f2pk(5.9604644775390625e-8f, 5.9604644775390625e-8f)) : Lo[r];
+                            const f2x T = sub2(fma2(TW, Y[r], mul2(TW, sub2(LoR, C[r]))), tp[r]);
                             tp[r] = tc[r];
                             tc[r] = T;
                             dst[r_row[r]] = T;
