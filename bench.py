@@ -775,7 +775,8 @@ def main():
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    ap.add_argument('--workload', default='c1', choices=['c0', 'c1', 'c4', 'deuterium'])
+    ap.add_argument('--workload', default='c1', choices=['c0', 'c1', 'c4', 'deuterium', 'c2_4096'],
+                    help="c2_4096 (one dim-4096 system of c2) only with --profile-only")
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-surrogate', action='store_true', help='skip the learned-surrogate leg')
@@ -790,6 +791,8 @@ def main():
     args = ap.parse_args()
     if args.profile_surrogate:
         return profile_surrogate()
+    if args.workload == 'c2_4096' and not args.profile_only:
+        ap.error('--workload c2_4096 is a profiling case: add --profile-only')
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == 'reference':

@@ -583,7 +583,7 @@ const void *spx_kernel_f64r_dc_t(int rmax, bool cluster);
 const void *spx_kernel_f64c_dc_t(int rmax, bool cluster);
 namespace {
 
-// Single-CTA kernels for RMAX 1, 2, 4, 8; cluster kernels for RMAX 1, 2, 4;
+// Single-CTA kernels for RMAX 1, 2, 4, 6; cluster kernels for RMAX 1, 2, 4;
 // sc: the coil is listed (at most 32 non-zeros), else the dense projection.
 const void *select_kernel(bool f64, bool cplx, int rmax, bool clu, bool sc, bool traj = false) {
     if (traj) {
@@ -654,8 +654,8 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     if (opt.chunk_target > 0) targets = {opt.chunk_target};
     bool placed = false;
     const int cls[] = {1, 2, 4, 8};
-    // up to 8 rows per lane on one CTA, at most 4 on a cluster (c4 on one CTA
-    // with 6 rows per lane: 323 ms per powder, on 2-CTA clusters with 3:
+    // up to 6 rows per lane on one CTA, at most 4 on a cluster (c4 on one CTA
+    // with 6 rows per lane: 195 ms per powder, on 2-CTA clusters with 3:
     // 344 ms -- a cluster pays a barrier across SMs per term)
     for (int cl : cls) {
         if (opt.cluster > 0 && cl != opt.cluster) continue;       // cluster size set by the caller
@@ -670,8 +670,8 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
         else if (nws[0] > 4) nws.push_back((nws[0] + 1) / 2);
         for (int nwarps : nws) {
         const int rows = (c.nsl_loc + nwarps - 1) / nwarps;
-        if (rows > (cl > 1 ? 4 : 8)) continue;
-        c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 8;
+        if (rows > (cl > 1 ? 4 : 6)) continue;
+        c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 6;
         c.threads = nwarps * 32;
         // dynamic shared memory may use what the kernel's static arrays leave
         cudaFuncAttributes fa{};

@@ -230,6 +230,15 @@ __device__ __forceinline__ void kahan_add2(f2x &Y, f2x &C, f2x P) {
     C = sub2(sub2(t, Y), y);
     Y = t;
 }
+// The same with the low-order part kept with the opposite sign: Y + L is the
+// sum, and products of the values' low parts can be added into L directly
+// (one accumulator per row fewer).
+__device__ __forceinline__ void kahan_add2l(f2x &Y, f2x &L, f2x P) {
+    const f2x y = add2(P, L);
+    const f2x t = add2(Y, y);
+    L = sub2(y, sub2(t, Y));
+    Y = t;
+}
 // a * t for a packed complex coefficient (PackC/PackA layout), hi and lo parts
 static __device__ __forceinline__ f2x cmul_pk(const PackC &a, f2x T) {
     const f2x TS = swap2(T);
@@ -713,13 +722,14 @@ static __device__ __noinline__ void traj_accumulate(Vec *acc, int stride, const 
 // into separate instantiations so that the other runs' term loop keeps its
 // registers (the out-of-line accumulation calls cost c1 5 % when present).
 template <bool F64, bool CPLX, int RMAX, bool CLU, bool SC, bool TRJ>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(512, 1)
 powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     using P = Prec<F64, CPLX>;
     using Vec = typename P::Vec;
     // cluster launches of FP32 real values keep each column in its value
     // (ValRP), which leaves room for larger systems per CTA
     constexpr bool PACKED = !F64 && !CPLX && CLU;
+    constexpr bool FOLD = RMAX > 4 && !PACKED;     // see the FP32 term loop
     using Val = std::conditional_t<PACKED, ValRP, typename P::Val>;
     // units of a packed entry's low part before the rescale to L~ (exact:
     // lo_scale is a power of two)
@@ -1118,19 +1128,25 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
         // accumulations are independent dependency chains.  A lane's slices come
         // in non-increasing width, so entry c is shared by rows 0..seg-1 while
         // c < width of row seg-1: each segment runs with a compile-time row count.
-        int r_row[RMAX], r_off[RMAX], r_w[RMAX];
+        // With 6 rows per lane a row (below 2^16: columns are uint16) and its
+        // ELL width share a register.
+        [[maybe_unused]] int r_rw[RMAX], r_rowv[RMAX], r_wv[RMAX];
+        int r_off[RMAX];
         int nr = 0;
 #pragma unroll
         for (int r = 0; r < RMAX; ++r) {
-            r_row[r] = 0; r_off[r] = 0; r_w[r] = 0;
+            r_rw[r] = 0; r_rowv[r] = 0; r_wv[r] = 0; r_off[r] = 0;
             if (r < rows_per_lane) {
                 const int sl = s_wsl[warp * RMAX + r];
                 nr = r + 1;
-                r_row[r] = row0 + sl * 32 + lane;
+                const int row = row0 + sl * 32 + lane, w = (s_soff[sl + 1] - s_soff[sl]) >> 5;
+                if constexpr (FOLD) r_rw[r] = row | (w << 16);
+                else { r_rowv[r] = row; r_wv[r] = w; }
                 r_off[r] = s_soff[sl] + lane;
-                r_w[r] = (s_soff[sl + 1] - s_soff[sl]) >> 5;
             }
         }
+        auto r_row = [&](int r) { if constexpr (FOLD) return r_rw[r] & 0xffff; else return r_rowv[r]; };
+        auto r_w = [&](int r) { if constexpr (FOLD) return (int)((unsigned)r_rw[r] >> 16); else return r_wv[r]; };
         Vec *fid_out = reinterpret_cast<Vec *>(run.fids) + (size_t)o * sys.nchan * (nsteps + 1);
         int status = kDevOk;
         [[maybe_unused]] Vec t_prev[RMAX], t_cur[RMAX], acc[RMAX], cc[RMAX];
@@ -1138,8 +1154,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 #pragma unroll
         for (int r = 0; r < RMAX; ++r) {
             const double2 x0 = r >= nr ? make_double2(0.0, 0.0)
-                               : sys.rho0s ? sys.rho0s[(size_t)o * sys.n_pad + r_row[r]] : sys.rho0[r_row[r]];
-            const double2 c0 = r < nr ? sys.coil[r_row[r]] : make_double2(0.0, 0.0);
+                               : sys.rho0s ? sys.rho0s[(size_t)o * sys.n_pad + r_row(r)] : sys.rho0[r_row(r)];
+            const double2 c0 = r < nr ? sys.coil[r_row(r)] : make_double2(0.0, 0.0);
             if constexpr (F64) {
                 t_prev[r] = vzero<Vec>(); acc[r] = vzero<Vec>();
                 t_cur[r] = tovec(x0, Vec());
@@ -1169,7 +1185,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                         double2 v;
                         if constexpr (F64) v = tod(t_cur[r]);
                         else v = tod(f2up(tc[r]));
-                        tr[r_row[r]] = v;
+                        tr[r_row(r)] = v;
                     }
                 }
             }
@@ -1199,12 +1215,12 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 #pragma unroll
                 for (int r = 0; r < RMAX; ++r) {
                     if (r < nr) {
-                        s_xa[r_row[r]] = t_cur[r];
-                        push_peers<CLU>(&s_xa[r_row[r]], t_cur[r], crank, CL);
+                        s_xa[r_row(r)] = t_cur[r];
+                        push_peers<CLU>(&s_xa[r_row(r)], t_cur[r], crank, CL);
                         if (!scoil) cdot_acc(mom, cc[r], t_cur[r]);
                         acc[r] = vzero<Vec>();
                         acc_add64(acc[r], s_atau[0], t_cur[r]);
-                        if (TRJ && TM1 > 0) traj_accumulate(s_tacc + (r_row[r] - row0), nrow_loc, s_tco, TM1, t_cur[r], true);
+                        if (TRJ && TM1 > 0) traj_accumulate(s_tacc + (r_row(r) - row0), nrow_loc, s_tco, TM1, t_cur[r], true);
                         start_n2 += t_cur[r].x * t_cur[r].x + t_cur[r].y * t_cur[r].y;
                         t_prev[r] = vzero<Vec>();
                     }
@@ -1230,13 +1246,13 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 #pragma unroll
                     for (int r = 0; r < RMAX; ++r) {
                         y[r] = vzero<Vec>();
-                        if (r < nr) cmac(y[r], s_diag[r_row[r] - row0], t_cur[r]);
+                        if (r < nr) cmac(y[r], s_diag[r_row(r) - row0], t_cur[r]);
                     }
                     int c = 0;
 #pragma unroll
                     for (int seg = RMAX; seg >= 1; --seg) {
                         if (seg <= nr) {
-                            const int cend = r_w[seg - 1];
+                            const int cend = r_w(seg - 1);
                             for (; c < cend; ++c) {
 #pragma unroll
                                 for (int r = 0; r < seg; ++r) {
@@ -1253,11 +1269,11 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                             const Vec tn = recur(y[r], two, t_prev[r]);
                             t_prev[r] = t_cur[r];
                             t_cur[r] = tn;
-                            dst[r_row[r]] = tn;
-                            push_peers<CLU>(&dst[r_row[r]], tn, crank, CL);
+                            dst[r_row(r)] = tn;
+                            push_peers<CLU>(&dst[r_row(r)], tn, crank, CL);
                             if (!scoil) cdot_acc(mom, cc[r], tn);
                             if (advance) acc_add64(acc[r], s_atau[k], tn);
-                            if (TRJ && TM1 > 0) traj_accumulate(s_tacc + (r_row[r] - row0), nrow_loc, s_tco + k * TM1, TM1, tn, false);
+                            if (TRJ && TM1 > 0) traj_accumulate(s_tacc + (r_row(r) - row0), nrow_loc, s_tco + k * TM1, TM1, tn, false);
                         }
                     }
                     if (!scoil) {
@@ -1284,14 +1300,14 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 for (int r = 0; r < RMAX; ++r) {
                     if (r < nr) {
                         const f2x T = tc[r];
-                        reinterpret_cast<f2x *>(s_xa)[r_row[r]] = T;
-                        push_peers<CLU>(reinterpret_cast<f2x *>(s_xa) + r_row[r], T, crank, CL);
+                        reinterpret_cast<f2x *>(s_xa)[r_row(r)] = T;
+                        push_peers<CLU>(reinterpret_cast<f2x *>(s_xa) + r_row(r), T, crank, CL);
                         if (!scoil) {
                             MOM = fma2(crr[r], T, MOM);
                             MOM = fma2(cim[r], swap2(T), MOM);
                         }
                         ac[r] = cmul_pk(s_atau[0], T);
-                        if (TRJ && TM1 > 0) traj_accumulate(s_tacc + (r_row[r] - row0), nrow_loc, s_tco, TM1, f2up(T), true);
+                        if (TRJ && TM1 > 0) traj_accumulate(s_tacc + (r_row(r) - row0), nrow_loc, s_tco, TM1, f2up(T), true);
                         cp[r] = 0ull;
                         tp[r] = 0ull;
                         const float2 t = f2up(T);
@@ -1315,27 +1331,39 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                         else if (scoil) coil_moment(reinterpret_cast<const Vec *>(src), sys.ncoil, s_crow, s_cval, lane, &s_mu[k - 1]);
                         else reduce_term(s_part + ((k - 1) & 1) * nwarps, nwarps, lane, &s_mu[k - 1]);
                     }
-                    f2x Y[RMAX], C[RMAX], Lo[RMAX];
+                    // Y + Lw + Lp is a row's sum: Y the running sum, Lw its
+                    // compensated low-order part, Lp the products of the values'
+                    // low parts (packed values: in units of 2^-24).  With 6 or 8
+                    // rows per lane those products go into Lw instead: one
+                    // accumulator per row fewer keeps the rows' state in
+                    // registers (c4: 195 ms per powder against 323 with spills),
+                    // at the cost of a longer dependency chain per entry (c1 4 %
+                    // slower, so fewer rows keep Lp).
+                    f2x Y[RMAX], Lw[RMAX];
+                    [[maybe_unused]] f2x Lp[RMAX];
 #pragma unroll
                     for (int r = 0; r < RMAX; ++r) {
                         Y[r] = 0ull;
-                        C[r] = 0ull;
-                        Lo[r] = 0ull;
+                        Lw[r] = 0ull;
+                        if constexpr (!FOLD) Lp[r] = 0ull;
                         if (r < nr) {
-                            const DgS d = s_diag[r_row[r] - row0];
+                            const DgS d = s_diag[r_row(r) - row0];
                             const f2x X = tc[r];
                             Y[r] = mul2(f2pk(d.rh, d.rh), X);
-                            kahan_add2(Y[r], C[r], mul2(f2pk(-d.im, d.im), swap2(X)));
-                            // packed values: the low parts are summed in units of 2^-24
-                            const float dl = PACKED ? d.rl * 16777216.f : d.rl;
-                            Lo[r] = mul2(f2pk(dl, dl), X);
+                            kahan_add2l(Y[r], Lw[r], mul2(f2pk(-d.im, d.im), swap2(X)));
+                            if constexpr (FOLD) {
+                                Lw[r] = fma2(f2pk(d.rl, d.rl), X, Lw[r]);
+                            } else {
+                                const float dl = PACKED ? d.rl * 16777216.f : d.rl;
+                                Lp[r] = mul2(f2pk(dl, dl), X);
+                            }
                         }
                     }
                     int c = 0;
 #pragma unroll
                     for (int seg = RMAX; seg >= 1; --seg) {
                         if (seg <= nr) {
-                            const int cend = r_w[seg - 1];
+                            const int cend = r_w(seg - 1);
                             for (; c < cend; ++c) {
 #pragma unroll
                                 for (int r = 0; r < seg; ++r) {
@@ -1344,17 +1372,19 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                                     if constexpr (CPLX) {
                                         const ValC v = s_val[e];
                                         const f2x XS = swap2(X);
-                                        kahan_add2(Y[r], C[r], mul2(f2pk(v.rh, v.rh), X));
-                                        kahan_add2(Y[r], C[r], mul2(f2pk(-v.ih, v.ih), XS));
-                                        Lo[r] = fma2(f2pk(v.rl, v.rl), X, Lo[r]);
-                                        Lo[r] = fma2(f2pk(-v.il, v.il), XS, Lo[r]);
+                                        kahan_add2l(Y[r], Lw[r], mul2(f2pk(v.rh, v.rh), X));
+                                        kahan_add2l(Y[r], Lw[r], mul2(f2pk(-v.ih, v.ih), XS));
+                                        f2x &Ls = FOLD ? Lw[r] : Lp[r];
+                                        Ls = fma2(f2pk(v.rl, v.rl), X, Ls);
+                                        Ls = fma2(f2pk(-v.il, v.il), XS, Ls);
                                     } else {
                                         const Val v = s_val[e];
+                                        kahan_add2l(Y[r], Lw[r], mul2(f2pk(v.hi, v.hi), X));
                                         float lo;
                                         if constexpr (PACKED) lo = __half2float(v.lo);
                                         else lo = v.lo;
-                                        kahan_add2(Y[r], C[r], mul2(f2pk(v.hi, v.hi), X));
-                                        Lo[r] = fma2(f2pk(lo, lo), X, Lo[r]);
+                                        f2x &Ls = FOLD ? Lw[r] : Lp[r];
+                                        Ls = fma2(f2pk(lo, lo), X, Ls);
                                     }
                                 }
                             }
@@ -1364,13 +1394,20 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 #pragma unroll
                     for (int r = 0; r < RMAX; ++r) {
                         if (r < nr) {
-                            // t_k = TW * (Y + (Lo - C)) - t_{k-2}
-                            const f2x LoR = PACKED ? mul2(Lo[r], f2pk(5.9604644775390625e-8f, 5.9604644775390625e-8f)) : Lo[r];
-                            const f2x T = sub2(fma2(TW, Y[r], mul2(TW, sub2(LoR, C[r]))), tp[r]);
-                            tp[r] = tc[r];
+                            // t_k = TW * (Y + Lw) - t_{k-2}
+                            f2x Lr = Lw[r];
+                            if constexpr (PACKED) Lr = fma2(Lp[r], f2pk(5.9604644775390625e-8f, 5.9604644775390625e-8f), Lr);
+                            else if constexpr (!FOLD) Lr = add2(Lp[r], Lr);
+                            // t_{k-2} of this row: in a register, or (6 rows per
+                            // lane) read back from the buffer term k overwrites
+                            f2x TP;
+                            if constexpr (FOLD) TP = (k == 1) ? 0ull : dst[r_row(r)];
+                            else TP = tp[r];
+                            const f2x T = sub2(fma2(TW, Y[r], mul2(TW, Lr)), TP);
+                            if constexpr (!FOLD) tp[r] = tc[r];
                             tc[r] = T;
-                            dst[r_row[r]] = T;
-                            push_peers<CLU>(dst + r_row[r], T, crank, CL);
+                            dst[r_row(r)] = T;
+                            push_peers<CLU>(dst + r_row(r), T, crank, CL);
                             if (!scoil) {
                                 MOM = fma2(crr[r], T, MOM);
                                 MOM = fma2(cim[r], swap2(T), MOM);
@@ -1383,7 +1420,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                                 ac[r] = S;
                             }
                             if (TRJ && TM1 > 0)
-                                traj_accumulate(s_tacc + (r_row[r] - row0), nrow_loc, s_tco + k * TM1, TM1, f2up(T), false);
+                                traj_accumulate(s_tacc + (r_row(r) - row0), nrow_loc, s_tco + k * TM1, TM1, f2up(T), false);
                         }
                     }
                     if (!scoil) {
@@ -1408,8 +1445,8 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 for (int r = 0; r < RMAX; ++r) {
                     if (r < nr) {
                         for (int j = 1; j <= jn; ++j) {
-                            const Vec v = s_tacc[(size_t)(j - 1) * nrow_loc + (r_row[r] - row0)];
-                            run.traj_out[((size_t)o * (nsteps + 1) + (size_t)a * Mo + j) * sys.n_pad + r_row[r]] =
+                            const Vec v = s_tacc[(size_t)(j - 1) * nrow_loc + (r_row(r) - row0)];
+                            run.traj_out[((size_t)o * (nsteps + 1) + (size_t)a * Mo + j) * sys.n_pad + r_row(r)] =
                                 make_double2((double)v.x, (double)v.y);
                         }
                     }
@@ -1528,7 +1565,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                     double2 v;
                     if constexpr (F64) v = tod(t_cur[r]);
                     else v = tod(f2up(tc[r]));
-                    run.state_out[(size_t)o * sys.n_pad + r_row[r]] = v;
+                    run.state_out[(size_t)o * sys.n_pad + r_row(r)] = v;
                 }
             }
         }

@@ -161,6 +161,11 @@ def c2(seed: int = 2, n_systems: int = 64) -> list:
     return out
 
 
+def c2_4096(seed: int = 2) -> Workload:
+    """The first dim-4096 system of c2 (six spins, full basis)."""
+    return next(w for w in c2(seed) if len(w.isotopes) == 6)
+
+
 def c4(seed: int = 4) -> Workload:
     """X-band nitroxide-like radical (0.34 T): electron with an axial g tensor,
     one 14N and ten 1H hyperfine couplings, T2 on the electron."""
