@@ -220,8 +220,8 @@ spx_status spx_run_powder_device(spx_handle *handle, int64_t n_orient,
  * orientations in FP32 and 0.9k in FP64: the Bessel tables of the 152 CTAs
  * take about 35 MB of the array).  Chunks are capped at 64 steps.  The
  * first call on a device (and the first after the device's context was reset)
- * looks up the array's address and should therefore come before any stream
- * capture.  The call waits for its stream before it returns.  Calls share the
+ * looks up the array's address.  The call waits for its stream before it
+ * returns, so it cannot be captured into a CUDA graph.  Calls share the
  * array, which keeps the last call's contents: calls that overlap on the GPU
  * (other threads or handles on the same device) race.  If an orientation fails
  * its series checks the call returns SPX_ERR_SERIES and d_fid holds no usable
