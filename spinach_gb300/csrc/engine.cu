@@ -565,41 +565,45 @@ size_t smem_for(const spx_handle *h, bool f64, int nsl_loc, int ell_loc, int Kma
 }  // namespace
 // Kernel addresses from the translation units that instantiate them
 // (kern_<precision><value type>_<sc: listed coil | dc: dense coil>.cu).
-const void *spx_kernel_f32r_sc(int rmax, bool cluster);
-const void *spx_kernel_f32c_sc(int rmax, bool cluster);
-const void *spx_kernel_f64r_sc(int rmax, bool cluster);
-const void *spx_kernel_f64c_sc(int rmax, bool cluster);
-const void *spx_kernel_f32r_dc(int rmax, bool cluster);
-const void *spx_kernel_f32c_dc(int rmax, bool cluster);
-const void *spx_kernel_f64r_dc(int rmax, bool cluster);
-const void *spx_kernel_f64c_dc(int rmax, bool cluster);
-const void *spx_kernel_f32r_sc_t(int rmax, bool cluster);     // with trajectory outputs
-const void *spx_kernel_f32c_sc_t(int rmax, bool cluster);
-const void *spx_kernel_f64r_sc_t(int rmax, bool cluster);
-const void *spx_kernel_f64c_sc_t(int rmax, bool cluster);
-const void *spx_kernel_f32r_dc_t(int rmax, bool cluster);
-const void *spx_kernel_f32c_dc_t(int rmax, bool cluster);
-const void *spx_kernel_f64r_dc_t(int rmax, bool cluster);
-const void *spx_kernel_f64c_dc_t(int rmax, bool cluster);
+const void *spx_kernel_f32r_sc(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f32c_sc(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f64r_sc(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f64c_sc(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f32r_dc(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f32c_dc(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f64r_dc(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f64c_dc(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f32r_sc_t(int rmax, bool cluster, bool wide);     // with trajectory outputs
+const void *spx_kernel_f32c_sc_t(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f64r_sc_t(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f64c_sc_t(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f32r_dc_t(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f32c_dc_t(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f64r_dc_t(int rmax, bool cluster, bool wide);
+const void *spx_kernel_f64c_dc_t(int rmax, bool cluster, bool wide);
 namespace {
 
 // Single-CTA kernels for RMAX 1, 2, 4, 6; cluster kernels for RMAX 1, 2, 4;
 // sc: the coil is listed (at most 32 non-zeros), else the dense projection.
-const void *select_kernel(bool f64, bool cplx, int rmax, bool clu, bool sc, bool traj = false) {
+const void *select_kernel(bool f64, bool cplx, int rmax, bool clu, bool sc, bool traj = false, bool wide = false) {
+    const void *k;
     if (traj) {
         if (sc) {
-            if (f64) return cplx ? spx_kernel_f64c_sc_t(rmax, clu) : spx_kernel_f64r_sc_t(rmax, clu);
-            return cplx ? spx_kernel_f32c_sc_t(rmax, clu) : spx_kernel_f32r_sc_t(rmax, clu);
+            if (f64) k = cplx ? spx_kernel_f64c_sc_t(rmax, clu, wide) : spx_kernel_f64r_sc_t(rmax, clu, wide);
+            else k = cplx ? spx_kernel_f32c_sc_t(rmax, clu, wide) : spx_kernel_f32r_sc_t(rmax, clu, wide);
+        } else {
+            if (f64) k = cplx ? spx_kernel_f64c_dc_t(rmax, clu, wide) : spx_kernel_f64r_dc_t(rmax, clu, wide);
+            else k = cplx ? spx_kernel_f32c_dc_t(rmax, clu, wide) : spx_kernel_f32r_dc_t(rmax, clu, wide);
         }
-        if (f64) return cplx ? spx_kernel_f64c_dc_t(rmax, clu) : spx_kernel_f64r_dc_t(rmax, clu);
-        return cplx ? spx_kernel_f32c_dc_t(rmax, clu) : spx_kernel_f32r_dc_t(rmax, clu);
+    } else if (sc) {
+        if (f64) k = cplx ? spx_kernel_f64c_sc(rmax, clu, wide) : spx_kernel_f64r_sc(rmax, clu, wide);
+        else k = cplx ? spx_kernel_f32c_sc(rmax, clu, wide) : spx_kernel_f32r_sc(rmax, clu, wide);
+    } else {
+        if (f64) k = cplx ? spx_kernel_f64c_dc(rmax, clu, wide) : spx_kernel_f64r_dc(rmax, clu, wide);
+        else k = cplx ? spx_kernel_f32c_dc(rmax, clu, wide) : spx_kernel_f32r_dc(rmax, clu, wide);
     }
-    if (sc) {
-        if (f64) return cplx ? spx_kernel_f64c_sc(rmax, clu) : spx_kernel_f64r_sc(rmax, clu);
-        return cplx ? spx_kernel_f32c_sc(rmax, clu) : spx_kernel_f32r_sc(rmax, clu);
-    }
-    if (f64) return cplx ? spx_kernel_f64c_dc(rmax, clu) : spx_kernel_f64r_dc(rmax, clu);
-    return cplx ? spx_kernel_f32c_dc(rmax, clu) : spx_kernel_f32r_dc(rmax, clu);
+    if (!k) throw SpxError(SPX_ERR_INTERNAL, "no kernel for this launch shape");
+    return k;
 }
 
 // Split the slices into cl contiguous blocks of about equal cost (ELL entries
@@ -665,17 +669,25 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
         // clusters: 16 warps 536 ms, 9 warps 584 ms)
         // a smaller CTA is tried before a larger cluster (its reconstruction
         // scratch is smaller), if the rows per lane stay within the limit
+        // FP32 on one CTA with 33-46 slices: 2 rows per lane on up to 24 warps
+        // (the wide kernel; one warp more than the rows need, for the warp
+        // that also folds the moments) before 3 rows on 16
+        const bool wide_ok = !f64 && cl == 1 && !traj;
         std::vector<int> nws = {std::min(16, std::max(1, c.nsl_loc))};
-        if (opt.threads > 0) nws = {std::max(1, std::min(16, opt.threads / 32))};
-        else if (nws[0] > 4) nws.push_back((nws[0] + 1) / 2);
+        if (opt.threads > 0) nws = {std::max(1, std::min(wide_ok ? 24 : 16, opt.threads / 32))};
+        else {
+            if (nws[0] > 4) nws.push_back((nws[0] + 1) / 2);
+            if (wide_ok && c.nsl_loc > 32 && c.nsl_loc <= 46) nws.insert(nws.begin(), std::min(24, c.nsl_loc / 2 + 2));
+        }
         for (int nwarps : nws) {
         const int rows = (c.nsl_loc + nwarps - 1) / nwarps;
         if (rows > (cl > 1 ? 4 : 6)) continue;
+        if (nwarps > 16 && rows > 2) continue;                       // the wide kernel has 2 rows per lane
         c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 6;
         c.threads = nwarps * 32;
         // dynamic shared memory may use what the kernel's static arrays leave
         cudaFuncAttributes fa{};
-        SPX_CUDA(cudaFuncGetAttributes(&fa, select_kernel(f64, h->cplx, c.rmax, cl > 1, h->ncoil > 0, traj)));
+        SPX_CUDA(cudaFuncGetAttributes(&fa, select_kernel(f64, h->cplx, c.rmax, cl > 1, h->ncoil > 0, traj, c.threads > 512)));
         const size_t budget = h->smem_optin > fa.sharedSizeBytes ? h->smem_optin - fa.sharedSizeBytes : 0;
         for (double tx : targets) {
             c.chunk_x = tx;
@@ -701,7 +713,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     if (!placed)
         throw SpxError(SPX_ERR_UNSUPPORTED, "system does not fit the shared memory of a cluster of 8 SMs (" +
                                                 std::to_string(c.smem) + " bytes per SM)");
-    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1, h->ncoil > 0, c.traj);
+    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1, h->ncoil > 0, c.traj, c.threads > 512);
     {
         // allow the whole budget: several configurations of one kernel may be
         // prepared before any of them launches (batched graphs)
@@ -744,7 +756,7 @@ void launch_chebyshev(spx_handle *h, bool f64, const Config &c, spx::DevSystem &
     run.nsl_loc = c.nsl_loc;
     run.ell_loc = c.ell_loc;
     for (int j = 0; j <= spx::kMaxCluster; ++j) run.cl_slices[j] = j <= c.cl ? c.slices[j] : 0;
-    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1, h->ncoil > 0, c.traj);
+    const void *kfn = select_kernel(f64, h->cplx, c.rmax, c.cl > 1, h->ncoil > 0, c.traj, c.threads > 512);
     void *args[] = {&sys, &run};
     ++h->launches;
     if (c.cl == 1) {
@@ -2437,7 +2449,8 @@ spx_status spx_batch_create(spx_batch **out, int32_t n, spx_handle *const *handl
             SPX_CUDA(cudaFuncGetAttributes(&fa, reinterpret_cast<const void *>(&spx::powder_combine_kernel)));
             for (int i = 0; i < n; ++i)
                 SPX_CUDA(cudaFuncGetAttributes(&fa, select_kernel(os[i].precision == SPX_FP64, handles[i]->cplx,
-                                                                  cfg[i].rmax, cfg[i].cl > 1, handles[i]->ncoil > 0)));
+                                                                  cfg[i].rmax, cfg[i].cl > 1, handles[i]->ncoil > 0,
+                                                                  false, cfg[i].threads > 512)));
         }
         b->marks.resize(n + 1, nullptr);
         for (auto &e : b->marks) SPX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));

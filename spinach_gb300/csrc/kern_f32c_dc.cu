@@ -4,4 +4,5 @@
 #define SPX_INST_CPLX true
 #define SPX_INST_SC false
 #define SPX_INST_FN spx_kernel_f32c_dc
+#define SPX_INST_WIDE
 #include "kern_inst.inc"

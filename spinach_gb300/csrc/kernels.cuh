@@ -721,8 +721,13 @@ static __device__ __noinline__ void traj_accumulate(Vec *acc, int stride, const 
 // TRJ: trajectory outputs (the state at every step, run.traj_out); compiled
 // into separate instantiations so that the other runs' term loop keeps its
 // registers (the out-of-line accumulation calls cost c1 5 % when present).
-template <bool F64, bool CPLX, int RMAX, bool CLU, bool SC, bool TRJ>
-__global__ void __launch_bounds__(512, 1)
+// WIDE: up to 24 warps (80 registers a thread) instead of 16 (128); used with
+// 2 rows per lane in FP32, where the rows' state fits (c1: 20 warps 60.2 ms,
+// 16 warps with 3 rows per lane 63.8 ms per powder).  The minimum of one
+// block per SM keeps ptxas from holding the 1- and 2-row kernels at 64
+// registers with spills.
+template <bool F64, bool CPLX, int RMAX, bool CLU, bool SC, bool TRJ, bool WIDE = false>
+__global__ void __launch_bounds__(WIDE ? 768 : 512, 1)
 powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     using P = Prec<F64, CPLX>;
     using Vec = typename P::Vec;
