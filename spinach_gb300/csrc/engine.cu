@@ -669,10 +669,10 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
         // clusters: 16 warps 536 ms, 9 warps 584 ms)
         // a smaller CTA is tried before a larger cluster (its reconstruction
         // scratch is smaller), if the rows per lane stay within the limit
-        // FP32 on one CTA with 33-46 slices: 2 rows per lane on up to 24 warps
-        // (the wide kernel; one warp more than the rows need, for the warp
+        // FP32 with 33-46 slices on a CTA: 2 rows per lane on up to 24 warps
+        // (the wide kernels; one warp more than the rows need, for the warp
         // that also folds the moments) before 3 rows on 16
-        const bool wide_ok = !f64 && cl == 1 && !traj;
+        const bool wide_ok = !f64 && !traj;
         std::vector<int> nws = {std::min(16, std::max(1, c.nsl_loc))};
         if (opt.threads > 0) nws = {std::max(1, std::min(wide_ok ? 24 : 16, opt.threads / 32))};
         else {
