@@ -1,0 +1,84 @@
+"""Launch shapes the engine picks for the benchmark systems, and parity across
+the shapes a system can run with.
+
+FP32 runs of 33-46 slices per CTA use the 768-thread 2-row kernel (one warp
+per two slices plus two); 5-6 rows per lane use the 6-row kernel with the
+low parts folded into the Kahan sums; cluster launches of real FP32 values
+use the packed layout (value and column in 8 bytes), which puts c2's
+dim-4096 systems on 4-CTA clusters.  Every shape of one system must give the
+same FID within the FP32 bar, and FP64 must keep its 16-warp shapes.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle_cases import rel_err
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), 'golden')
+
+
+def _engine(w):
+    from spinach_gb300 import engine as E, workloads as W
+    L = W.build(w)
+    eng = E.Engine(0)
+    eng.upload(L.I, L.terms, L.R, L.rho0, L.coil)
+    return eng
+
+
+def test_c1_fp32_runs_twenty_warps_and_every_warp_count_agrees(engine_lib):
+    from spinach_gb300 import engine as E, workloads as W
+    w = W.c1()
+    eng = _engine(w)
+    g = W.zcwn_grid(w.n_orient)
+    sel = slice(0, 152)
+    grid = [a[sel] for a in g]
+    r64 = eng.run(*grid, w.dt, w.nsteps, precision=E.FP64)
+    assert r64.stats['threads'] == 512 and r64.stats['cluster'] == 1
+    default = eng.run(*grid, w.dt, w.nsteps, precision=E.FP32, fp32_check=False)
+    assert default.stats['threads'] == 640 and default.stats['cluster'] == 1      # 37 slices: 20 warps
+    assert rel_err(default.fid, r64.fid) <= 1e-6
+    for threads in (512, 576, 704, 768):
+        r = eng.run(*grid, w.dt, w.nsteps, precision=E.FP32, fp32_check=False, threads=threads)
+        assert r.stats['threads'] == threads
+        assert rel_err(r.fid, r64.fid) <= 1e-6, threads
+    eng.close()
+
+
+def test_c4_fp32_one_cta_six_rows_matches_oracle(engine_lib):
+    from spinach_gb300 import engine as E, workloads as W
+    w = W.c4()
+    gold = np.load(os.path.join(GOLD, 'c4_orient_krylov_fp64.npz'))
+    al, be, ga, _ = W.zcwn_grid(w.n_orient)
+    s = gold['sel']
+    eng = _engine(w)
+    res = eng.run(al[s], be[s], ga[s], np.full(s.size, 1.0 / s.size), w.dt, w.nsteps, precision=E.FP32,
+                  per_orientation=True, fp32_check=False)
+    assert res.stats['cluster'] == 1 and res.stats['threads'] == 512          # 86 slices: 6 rows per lane
+    for i in range(s.size):
+        assert rel_err(res.fids[i], gold['fids'][i]) <= 1e-5, i
+    eng.close()
+
+
+def test_c2_dim4096_packed_clusters_of_four(engine_lib):
+    from spinach_gb300 import engine as E, workloads as W
+    gold = np.load(os.path.join(GOLD, 'c2_dim4096_orient_krylov_fp64.npz'))
+    w = W.c2()[int(gold['system'])]
+    al, be, ga, _ = W.zcwn_grid(w.n_orient)
+    s = gold['sel']
+    eng = _engine(w)
+    wt = np.full(s.size, 1.0 / s.size)
+    res = eng.run(al[s], be[s], ga[s], wt, w.dt, w.nsteps, precision=E.FP32, per_orientation=True,
+                  fp32_check=False)
+    assert res.stats['cluster'] == 4 and res.stats['threads'] > 512          # packed values, wide kernel
+    for i in range(s.size):
+        assert rel_err(res.fids[i], gold['fids'][i]) <= 1e-5, i
+    # the 8-CTA clusters (plain layout) and 16-warp 4-CTA clusters agree
+    for cluster, threads in ((8, 0), (4, 512)):
+        r = eng.run(al[s], be[s], ga[s], wt, w.dt, w.nsteps, precision=E.FP32, fp32_check=False,
+                    cluster=cluster, threads=threads)
+        assert r.stats['cluster'] == cluster
+        assert rel_err(r.fid, res.fid) <= 2e-6, (cluster, threads)
+    eng.close()
