@@ -735,6 +735,7 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     // (ValRP), which leaves room for larger systems per CTA
     constexpr bool PACKED = !F64 && !CPLX && CLU;
     constexpr bool FOLD = RMAX > 4 && !PACKED;     // see the FP32 term loop
+    constexpr bool TPR64 = F64 && (RMAX > 4 || (CLU && RMAX == 4));   // see the FP64 term loop
     using Val = std::conditional_t<PACKED, ValRP, typename P::Val>;
     // units of a packed entry's low part before the rescale to L~ (exact:
     // lo_scale is a power of two)
@@ -1271,8 +1272,16 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
 #pragma unroll
                     for (int r = 0; r < RMAX; ++r) {
                         if (r < nr) {
-                            const Vec tn = recur(y[r], two, t_prev[r]);
-                            t_prev[r] = t_cur[r];
+                            // t_{k-2}: with 6 rows per lane, or 4 on a cluster, read back
+                            // from the buffer this term overwrites (its own row, written two
+                            // terms earlier), which keeps the FP64 rows' state in registers
+                            // (c4 FP64 on 2-CTA clusters: no spills, 1238 ms per powder
+                            // against 1263; on one CTA with 4 rows the reload costs 0.5 %)
+                            Vec tpv;
+                            if constexpr (TPR64) tpv = (k == 1) ? vzero<Vec>() : dst[r_row(r)];
+                            else tpv = t_prev[r];
+                            const Vec tn = recur(y[r], two, tpv);
+                            if constexpr (!TPR64) t_prev[r] = t_cur[r];
                             t_cur[r] = tn;
                             dst[r_row(r)] = tn;
                             push_peers<CLU>(&dst[r_row(r)], tn, crank, CL);
