@@ -801,20 +801,19 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
     }
     // Slices to warps, longest-processing-time first: slices are stored in
     // non-increasing width, each goes to the least-loaded warp with room, so a
-    // warp's slices also come in non-increasing width.  Cost ~ width + 5; the
-    // last warp starts with 6, the detection moment it folds every term
-    // (c1: handicap 0 -> 67.5 ms, 3 -> 65.7, 6 -> 65.5, 10 -> 66.6, 24 -> 68.7;
-    // per-slice constant 2 -> 66.5, 10 -> 68.8).
+    // warp's slices also come in non-increasing width.  Cost ~ width + 3, no
+    // allowance for the detection moment the last warp folds every term (c1
+    // on 20 warps: 60.0 ms per powder, 60.2 with a handicap of 6, 60.5 with
+    // 12; c4: 194.8 ms against 198.1 with width + 5 and a handicap of 6).
     __shared__ short s_wsl[32 * 8];
     __shared__ int s_wcnt[32];
     __shared__ int s_wload[32];
     csync<CLU>();             // every CTA of the cluster has started before any remote access
     if (tid == 0) {
         for (int w = 0; w < nwarps; ++w) { s_wcnt[w] = 0; s_wload[w] = 0; }
-        if (nwarps > 1) s_wload[nwarps - 1] = 6;
         bool fits = true;
         for (int sl = 0; sl < nsl; ++sl) {
-            const int cost = ((s_soff[sl + 1] - s_soff[sl]) >> 5) + 5;
+            const int cost = ((s_soff[sl + 1] - s_soff[sl]) >> 5) + 3;
             int best = -1;
             for (int w = 0; w < nwarps; ++w)
                 if (s_wcnt[w] < RMAX && (best < 0 || s_wload[w] < s_wload[best])) best = w;
