@@ -223,16 +223,9 @@ static __device__ __forceinline__ f2x swap2(f2x a) { const float2 f = f2up(a); r
 static __device__ __forceinline__ f2x lo2(const float4 &v) { return f2pk(v.x, v.y); }
 static __device__ __forceinline__ f2x hi2(const float4 &v) { return f2pk(v.z, v.w); }
 
-// Kahan step: Y + (-C) += P, C the negated low part lost so far
-__device__ __forceinline__ void kahan_add2(f2x &Y, f2x &C, f2x P) {
-    const f2x y = sub2(P, C);
-    const f2x t = add2(Y, y);
-    C = sub2(sub2(t, Y), y);
-    Y = t;
-}
-// The same with the low-order part kept with the opposite sign: Y + L is the
-// sum, and products of the values' low parts can be added into L directly
-// (one accumulator per row fewer).
+// Kahan-compensated Y += P with the lost low-order part kept in L (Y + L is
+// the sum), so that products of the values' low parts can be added into L
+// directly (one accumulator per row fewer).
 __device__ __forceinline__ void kahan_add2l(f2x &Y, f2x &L, f2x P) {
     const f2x y = add2(P, L);
     const f2x t = add2(Y, y);
@@ -1304,9 +1297,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                 }
             } else {
                 // ---- FP32: packed (re, im) pairs, compensated row sums ----
-                // Row sums are Kahan-compensated: Y running sum, C its negated lost
-                // low part, L the products of the values' low parts; the row value
-                // Y + (L - C) is rounded once.
+                // Row sums are Kahan-compensated: Y the running sum, Lw its lost
+                // low-order part, Lp the products of the values' low parts (with
+                // 6 rows per lane folded into Lw); the row value Y + Lw + Lp is
+                // rounded once.
                 const f2x TWO = f2pk(2.f, 2.f), ONE = f2pk(1.f, 1.f);
                 f2x MOM = 0ull;
 #pragma unroll
