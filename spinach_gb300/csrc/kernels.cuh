@@ -67,13 +67,16 @@ enum DeviceStatus : int {
 //   ValC  complex value (re_hi, im_hi, re_lo, im_lo)               16 B
 //   DgS   diagonal (re_hi, re_lo, im, 0)                           16 B
 // Series coefficients are few and read by every row, so they stay pre-packed:
-//   PackA  h = (re_hi, re_hi, -im_hi, im_hi), l = same for the lo parts
+//   PackA  h = (re, re, -im, im) in float: a chunk-end sum of float-rounded
+//          coefficients loses about as much as storing the chunk-end state
+//          in float does (c1: 2.4e-7 -> 2.5e-7 from FP64), and drops two
+//          products per row and term
 struct __align__(8) ValR { float hi, lo; };
 struct __align__(8) ValRP { float hi; __half lo; uint16_t col; };
 static_assert(sizeof(ValRP) == sizeof(ValR), "packed values keep the layout's size");
 struct __align__(16) ValC { float rh, ih, rl, il; };
 struct __align__(16) DgS { float rh, rl, im, pad; };
-struct __align__(16) PackC { float4 h, l; };
+struct __align__(16) PackC { float4 h; };
 typedef PackC PackA;
 
 // ---------------------------------------------------------------------------
@@ -107,11 +110,8 @@ static __device__ __forceinline__ void pack(DgS &o, double re, double im) {
     o.pad = 0.f;
 }
 static __device__ __forceinline__ void pack(PackC &o, double re, double im) {
-    float rh, rl, ih, il;
-    split(re, rh, rl);
-    split(im, ih, il);
-    o.h = make_float4(rh, rh, -ih, ih);
-    o.l = make_float4(rl, rl, -il, il);
+    const float r = (float)re, i = (float)im;
+    o.h = make_float4(r, r, -i, i);
 }
 static __device__ __forceinline__ double2 unpack(const ValR &v) { return make_double2((double)v.hi + (double)v.lo, 0.0); }
 // value of a packed entry stored in units u
@@ -232,13 +232,9 @@ __device__ __forceinline__ void kahan_add2l(f2x &Y, f2x &L, f2x P) {
     L = sub2(y, sub2(t, Y));
     Y = t;
 }
-// a * t for a packed complex coefficient (PackC/PackA layout), hi and lo parts
+// a * t for a packed complex coefficient (PackC/PackA layout)
 static __device__ __forceinline__ f2x cmul_pk(const PackC &a, f2x T) {
-    const f2x TS = swap2(T);
-    f2x P = mul2(lo2(a.h), T);
-    P = fma2(hi2(a.h), TS, P);
-    P = fma2(lo2(a.l), T, P);
-    return fma2(hi2(a.l), TS, P);
+    return fma2(hi2(a.h), swap2(T), mul2(lo2(a.h), T));
 }
 
 // FP64 helpers of the generic propagation loop
@@ -1357,7 +1353,10 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                             const DgS d = s_diag[r_row(r) - row0];
                             const f2x X = tc[r];
                             Y[r] = mul2(f2pk(d.rh, d.rh), X);
-                            kahan_add2l(Y[r], Lw[r], mul2(f2pk(-d.im, d.im), swap2(X)));
+                            // the relaxation (imaginary) part of the diagonal goes into
+                            // the low-order sum, without a compensation step of its own
+                            // (c1: 2.4e-7 -> 2.6e-7 from FP64, 1.5 % faster)
+                            Lw[r] = fma2(f2pk(-d.im, d.im), swap2(X), Lw[r]);
                             if constexpr (FOLD) {
                                 Lw[r] = fma2(f2pk(d.rl, d.rl), X, Lw[r]);
                             } else {
