@@ -69,8 +69,9 @@ enum DeviceStatus : int {
 // Series coefficients are few and read by every row, so they stay pre-packed:
 //   PackA  h = (re, re, -im, im) in float: a chunk-end sum of float-rounded
 //          coefficients loses about as much as storing the chunk-end state
-//          in float does (c1: 2.4e-7 -> 2.5e-7 from FP64), and drops two
-//          products per row and term
+//          in float does, and drops two products per row and term (with the
+//          diagonal's relaxation part summed without its own compensation,
+//          c1 moved from 2.4e-7 to 2.7e-7 from FP64 and ran 3 % faster)
 struct __align__(8) ValR { float hi, lo; };
 struct __align__(8) ValRP { float hi; __half lo; uint16_t col; };
 static_assert(sizeof(ValRP) == sizeof(ValR), "packed values keep the layout's size");
@@ -1355,7 +1356,6 @@ powder_chebyshev_kernel(const DevSystem sys, const DevRun run) {
                             Y[r] = mul2(f2pk(d.rh, d.rh), X);
                             // the relaxation (imaginary) part of the diagonal goes into
                             // the low-order sum, without a compensation step of its own
-                            // (c1: 2.4e-7 -> 2.6e-7 from FP64, 1.5 % faster)
                             Lw[r] = fma2(f2pk(-d.im, d.im), swap2(X), Lw[r]);
                             if constexpr (FOLD) {
                                 Lw[r] = fma2(f2pk(d.rl, d.rl), X, Lw[r]);
