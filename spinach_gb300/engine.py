@@ -164,6 +164,41 @@ class _CscHolder:
 
 
 @dataclass
+class HostSystem:
+    """A spin system in the C ABI's host layout: I and every Q as
+    MATLAB-style CSC arrays (int64 column pointers and row indices,
+    interleaved complex values), R likewise or absent, rho0 and coil as
+    interleaved complex vectors."""
+    n: int
+    nterms: int
+    holders: list
+    Qarr: object
+    rank: np.ndarray
+    kk: np.ndarray
+    mm: np.ndarray
+    Rh: object
+    rho0: np.ndarray
+    coil: np.ndarray
+
+
+def host_system(I, terms: dict, R=None, rho0=None, coil=None) -> HostSystem:
+    """Lay out ``I``, the rotational-basis terms ``{(rank, k, m): Q}`` (0-based k,
+    m), ``R`` (or None) and the states as the C ABI takes them."""
+    n = I.shape[0]
+    keys = sorted(terms)
+    holders = [_CscHolder(I, n)] + [_CscHolder(terms[k], n) for k in keys]
+    Qarr = (SpxCsc * max(1, len(keys)))(*[h.struct for h in holders[1:]])
+    return HostSystem(
+        n=n, nterms=len(keys), holders=holders, Qarr=Qarr,
+        rank=np.array([k[0] for k in keys] or [0], np.int32),
+        kk=np.array([k[1] for k in keys] or [0], np.int32),
+        mm=np.array([k[2] for k in keys] or [0], np.int32),
+        Rh=_CscHolder(R, n) if R is not None else None,
+        rho0=np.ascontiguousarray(np.asarray(rho0, np.complex128).view(np.float64)),
+        coil=np.ascontiguousarray(np.asarray(coil, np.complex128).view(np.float64)))
+
+
+@dataclass
 class PowderResult:
     fid: np.ndarray                    # (nsteps+1,) complex128
     fids: np.ndarray | None            # (n_orient, nsteps+1) complex128 or None
@@ -199,21 +234,17 @@ class Engine:
     def upload(self, I, terms: dict, R=None, rho0=None, coil=None):
         """Upload ``I`` and the rotational-basis terms ``{(rank, k, m): Q}`` (0-based
         k, m), the relaxation superoperator ``R`` (or None), and the states."""
-        n = I.shape[0]
-        keys = sorted(terms)
-        self._holders = [_CscHolder(I, n)] + [_CscHolder(terms[k], n) for k in keys]
-        Qarr = (SpxCsc * max(1, len(keys)))(*[h.struct for h in self._holders[1:]])
-        rank = np.array([k[0] for k in keys] or [0], np.int32)
-        kk = np.array([k[1] for k in keys] or [0], np.int32)
-        mm = np.array([k[2] for k in keys] or [0], np.int32)
-        Rh = _CscHolder(R, n) if R is not None else None
-        rho0 = np.ascontiguousarray(np.asarray(rho0, np.complex128).view(np.float64))
-        coil = np.ascontiguousarray(np.asarray(coil, np.complex128).view(np.float64))
+        self.upload_host(host_system(I, terms, R, rho0, coil))
+
+    def upload_host(self, hs: 'HostSystem'):
+        """spx_upload_system from host buffers already in the C ABI's layout
+        (MATLAB-style CSC matrices, interleaved complex states)."""
         ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
         self._check(self.lib.spx_upload_system(
-            self.h, C.byref(self._holders[0].struct), len(keys), ip(rank), ip(kk), ip(mm), Qarr,
-            C.byref(Rh.struct) if Rh else None, _dptr(rho0), _dptr(coil)), self.h)
-        self.dim = n
+            self.h, C.byref(hs.holders[0].struct), hs.nterms, ip(hs.rank), ip(hs.kk), ip(hs.mm), hs.Qarr,
+            C.byref(hs.Rh.struct) if hs.Rh else None, _dptr(hs.rho0), _dptr(hs.coil)), self.h)
+        self._host_system = hs             # the library reads the buffers during the call only
+        self.dim = hs.n
         self.nchan = 1
 
     def build_system(self, hm, r_diag=None, rho0=None, coil=None) -> float:
