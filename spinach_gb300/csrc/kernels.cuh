@@ -22,12 +22,13 @@
 // the series is exact to the chosen tolerance, so the FID is the same
 // quantity the reference computes.
 //
-// FP32 mode stores Liouvillian values and series coefficients as hi+lo float
-// pairs (about 48 significant bits), keeps state vectors in complex float, and
-// sums every matvec row with a Kahan-compensated accumulator in packed f32x2
-// (re, im) arithmetic, rounding the row value once: that is what keeps the
-// phase from drifting over thousands of steps.  FP64 mode stores everything in
-// double.
+// FP32 mode stores Liouvillian values as hi+lo float pairs (about 48
+// significant bits; on clusters of real values hi + a half-precision low part
+// next to the column), keeps series coefficients and state vectors in
+// (complex) float, and sums every matvec row with a Kahan-compensated
+// accumulator in packed f32x2 (re, im) arithmetic, rounding the row value
+// once: that is what keeps the phase from drifting over thousands of steps.
+// FP64 mode stores everything in double.
 #pragma once
 
 #include <cuda_fp16.h>
