@@ -268,31 +268,59 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
         keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
     }
     const size_t nk = keys.size();
+    // row and column of every key (one division each, not one per use)
+    std::vector<int32_t> krow(nk), kcol(nk);
+    for (size_t p = 0; p < nk; ++p) {
+        krow[p] = (int32_t)(keys[p] / n);
+        kcol[p] = (int32_t)(keys[p] - (int64_t)krow[p] * n);
+    }
     // row start of each row in the key list; a position is found within its row
     std::vector<size_t> rstart(n + 1, 0);
-    for (size_t p = 0; p < nk; ++p) rstart[keys[p] / n + 1]++;
+    for (size_t p = 0; p < nk; ++p) rstart[krow[p] + 1]++;
     for (int64_t i = 0; i < n; ++i) rstart[i + 1] += rstart[i];
     auto pos = [&](int64_t r, int64_t c) -> size_t {
         return (size_t)(std::lower_bound(keys.begin() + rstart[r], keys.begin() + rstart[r + 1], r * n + c) -
                         keys.begin());
     };
+    // position of the transposed key: (c, r) for key p = (r, c).  Keys come
+    // row by row in column order, so the keys of one column c are met in
+    // increasing row r, the order of row c's keys (the pattern is symmetric).
+    std::vector<size_t> tpos(nk);
+    {
+        std::vector<size_t> cur(rstart.begin(), rstart.end() - 1);
+        for (size_t p = 0; p < nk; ++p) tpos[p] = cur[kcol[p]]++;
+    }
+    // every kept entry (r, c) of A with the positions p of key (r, c) and q of
+    // (c, r): the rows of column c are walked along row c's keys (MATLAB's CSC
+    // rows ascend; a binary search where they do not)
+    auto for_each_key = [&](const spx_csc *A, auto &&f) {
+        for (int64_t c = 0; c < n; ++c) {
+            size_t cur = rstart[c];
+            const size_t end = rstart[c + 1];
+            for (int64_t i = A->colptr[c]; i < A->colptr[c + 1]; ++i) {
+                const int64_t r = A->rowidx[i];
+                const Cplx v{A->values[2 * i], A->values[2 * i + 1]};
+                if (!kept(r, c, v)) continue;
+                while (cur < end && kcol[cur] < r) ++cur;
+                const size_t q = (cur < end && kcol[cur] == r) ? cur : pos(c, r);
+                f(tpos[q], q, r, c, v);
+            }
+        }
+    };
 
     // streams: 0 = Ih + iR (coefficient 1), then S_t, A_t per term
     const int nst_all = 1 + 2 * n_terms;
     std::vector<std::vector<Cplx>> st(nst_all, std::vector<Cplx>(nk));
-    for_each_entry(I, [&](int64_t r, int64_t c, Cplx v) {
-        if (!kept(r, c, v)) return;
-        Cplx &a = st[0][pos(r, c)];
+    for_each_key(I, [&](size_t p, size_t q, int64_t, int64_t, Cplx v) {
+        Cplx &a = st[0][p];
         a.re += 0.5 * v.re; a.im += 0.5 * v.im;
-        Cplx &b = st[0][pos(c, r)];
+        Cplx &b = st[0][q];
         b.re += 0.5 * v.re; b.im -= 0.5 * v.im;
     });
     for (int t = 0; t < n_terms; ++t) {
         auto &S = st[1 + 2 * t];
         auto &A = st[2 + 2 * t];
-        for_each_entry(&Q[t], [&](int64_t r, int64_t c, Cplx v) {
-            if (!kept(r, c, v)) return;
-            const size_t p = pos(r, c), q = pos(c, r);
+        for_each_key(&Q[t], [&](size_t p, size_t q, int64_t, int64_t, Cplx v) {
             // S = (Q + Q^H)/2,  A = 1i (Q - Q^H)/2
             S[p].re += 0.5 * v.re; S[p].im += 0.5 * v.im;
             S[q].re += 0.5 * v.re; S[q].im -= 0.5 * v.im;
@@ -321,8 +349,7 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
     bool cplx = false;
     for (auto &s : st)
         for (size_t p = 0; p < nk && !cplx; ++p) {
-            const int64_t r = keys[p] / n, c = keys[p] % n;
-            if (r != c && std::fabs(s[p].im) > im_tol) cplx = true;
+            if (krow[p] != kcol[p] && std::fabs(s[p].im) > im_tol) cplx = true;
         }
     // drop streams that are zero up to rounding (1e-14 of the largest value:
     // e.g. the anti-Hermitian part of a term whose commutators cancel only to
@@ -338,7 +365,7 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
     // rows: count off-diagonals, order by count (descending, stable)
     std::vector<int> cnt(n, 0);
     for (size_t p = 0; p < nk; ++p) {
-        const int64_t r = keys[p] / n, c = keys[p] % n;
+        const int32_t r = krow[p], c = kcol[p];
         if (r != c) ++cnt[r];
     }
     std::vector<int> perm(n);  // new -> old
@@ -371,7 +398,7 @@ void upload_system(spx_handle *h, const spx_csc *I, int32_t n_terms, const int32
             if (row < n) {
                 const int old = perm[row];
                 for (size_t p = rstart[old]; p < rstart[old + 1]; ++p) {
-                    const int64_t oc = keys[p] % n;
+                    const int64_t oc = kcol[p];
                     if (oc == old) {
                         for (int q = 0; q < nst; ++q) {
                             const Cplx v = st[keep[q]][p];
