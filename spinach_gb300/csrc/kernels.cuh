@@ -592,8 +592,8 @@ static __device__ int series_terms(double x, double lg, double tol, int kcap) {
 
 // Column j of the table T[k][j] = (2 - delta_k0) J_k(half * j * dt), k < K,
 // by Miller's backward recurrence J_{k-1} = (2k/x) J_k - J_{k+1}, normalised
-// with J_0 + 2 sum J_2k = 1.  Rescaling is only needed above the stored range;
-// tiny arguments use the leading terms of the power series.
+// with J_0 + 2 sum J_2k = 1; tiny arguments use the leading terms of the
+// power series.
 static __device__ void bessel_column(double *table, int M, int j, int K, double half, double dt) {
     double *col = table + j;
     const size_t ld = (size_t)(M + 1);
@@ -609,19 +609,30 @@ static __device__ void bessel_column(double *table, int M, int j, int K, double 
     const int base = max(kneed, (int)ceil(x));
     int kst = base + 20 + (int)sqrt(160.0 * base);
     kst += kst & 1;
-    double jp1 = 0.0, jk = 1e-30, norm = 0.0;
     const double two_over_x = 2.0 / x;                // one division per column
-    for (int k = kst; k >= 1; --k) {
+    // Above the stored range the recurrence only has to forget its start (the
+    // error it carries there decays towards k = 0), and those terms add below
+    // 1e-40 to the normalisation: it runs in float, rescaled well inside the
+    // float range (one step grows a value at most kst * 2/x-fold, below 1e9
+    // for the arguments x >= 1e-6 that reach it), and hands over to FP64 at
+    // the first stored term.
+    const float ftx = (float)two_over_x;
+    float fjp1 = 0.f, fjk = 1e-30f;
+    int k = kst;
+    for (; k > kneed; --k) {
+        const float fjm1 = ((float)k * ftx) * fjk - fjp1;
+        fjp1 = fjk;
+        fjk = fjm1;                                 // J_{k-1}, unnormalised
+        if (fabsf(fjk) > 1e20f) { fjk *= 1e-20f; fjp1 *= 1e-20f; }
+    }
+    double jp1 = fjp1, jk = fjk, norm = 0.0;
+    for (; k >= 1; --k) {
         const double jm1 = (k * two_over_x) * jk - jp1;
         jp1 = jk;
-        jk = jm1;                                   // J_{k-1}, unnormalised
+        jk = jm1;                                   // J_{k-1}, unnormalised, k-1 < kneed
         const int km1 = k - 1;
         if (km1 > 0 && (km1 & 1) == 0) norm += 2.0 * jk;
-        if (km1 < kneed) {
-            col[km1 * ld] = jk;
-        } else if (fabs(jk) > 1e200) {
-            jk *= 1e-200; jp1 *= 1e-200; norm *= 1e-200;
-        }
+        col[km1 * ld] = jk;
     }
     norm += jk;                                     // + J_0
     const double inv = 1.0 / norm;
