@@ -686,19 +686,20 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
     bool placed = false;
     const int cls[] = {1, 2, 4, 8};
     // up to 6 rows per lane on one CTA, at most 4 on a cluster (c4 on one CTA
-    // with 6 rows per lane: 195 ms per powder, on 2-CTA clusters with 3:
-    // 344 ms -- a cluster pays a barrier across SMs per term)
+    // with 6 rows per lane: 323 ms per powder when compared, 183 ms since; on
+    // 2-CTA clusters with 3: 344 ms -- a cluster pays a barrier across SMs
+    // per term)
     for (int cl : cls) {
         if (opt.cluster > 0 && cl != opt.cluster) continue;       // cluster size set by the caller
         if (!partition_slices(h, cl, c)) continue;
-        // warps: one per 32-row slice, at most 16 (c1: 16 warps 118.9 ms,
-        // 13 warps 121.3 ms per 1000-orientation powder; c2 dim 4096 on 8-CTA
-        // clusters: 16 warps 536 ms, 9 warps 584 ms)
-        // a smaller CTA is tried before a larger cluster (its reconstruction
-        // scratch is smaller), if the rows per lane stay within the limit
-        // FP32 with 33-46 slices on a CTA: 2 rows per lane on up to 24 warps
-        // (the wide kernels; one warp more than the rows need, for the warp
-        // that also folds the moments) before 3 rows on 16
+        // warps: one per 32-row slice, at most 16 (c1 on an older kernel: 16
+        // warps 118.9 ms, 13 warps 121.3 ms per 1000-orientation powder; c2
+        // dim 4096 on 8-CTA clusters: 16 warps 536 ms, 9 warps 584 ms), then
+        // half as many; a smaller CTA is tried before a larger cluster (its
+        // reconstruction scratch is smaller), if the rows per lane stay within
+        // the limit.  FP32 with 33-46 slices on a CTA first tries 2 rows per
+        // lane on up to 24 warps (the wide kernels; one warp more than the
+        // rows need: c1 on 20 warps 60.4 ms against 63.8 on 16 with 3 rows)
         const bool wide_ok = !f64 && !traj;
         std::vector<int> nws = {std::min(16, std::max(1, c.nsl_loc))};
         if (opt.threads > 0) nws = {std::max(1, std::min(wide_ok ? 24 : 16, opt.threads / 32))};
