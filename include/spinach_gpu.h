@@ -57,7 +57,7 @@ typedef struct {
 typedef struct {
     int32_t precision;         /* spx_precision: storage/arithmetic of the propagation */
     int32_t chunk_steps;       /* time steps covered by one series expansion, 0 = auto */
-    int32_t threads;           /* CTA size, 0 = auto */
+    int32_t threads;           /* CTA size, 0 = auto; up to 512 (FP32 with at most two 32-row slices per warp: 768) */
     int32_t cluster;           /* CTAs sharing one orientation (1, 2, 4, 8), 0 = auto:
                                   the smallest whose per-CTA share of L fits shared memory */
     double series_tol;         /* truncation tolerance of the series, 0 = auto */
