@@ -711,7 +711,7 @@ Config choose_config(spx_handle *h, int64_t n_orient, double dt, int64_t nsteps,
         const int rows = (c.nsl_loc + nwarps - 1) / nwarps;
         if (rows > (cl > 1 ? 4 : 6)) continue;
         if (nwarps > 16 && rows > 2) continue;                       // the wide kernel has 2 rows per lane
-        c.rmax = rows <= 1 ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 6;
+        c.rmax = (rows <= 1 && nwarps <= 16) ? 1 : rows <= 2 ? 2 : rows <= 4 ? 4 : 6;   // wide: always RMAX 2
         c.threads = nwarps * 32;
         // dynamic shared memory may use what the kernel's static arrays leave
         cudaFuncAttributes fa{};

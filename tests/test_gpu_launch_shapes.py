@@ -82,3 +82,20 @@ def test_c2_dim4096_packed_clusters_of_four(engine_lib):
         assert r.stats['cluster'] == cluster
         assert rel_err(r.fid, res.fid) <= 2e-6, (cluster, threads)
     eng.close()
+
+
+def test_forced_shapes_of_the_six_row_and_wide_kernels(engine_lib):
+    """Shapes the defaults do not reach on the benchmark systems: c1 on 7 and 9
+    warps (6 rows per lane: low parts folded into the Kahan sums, t_{k-2} read
+    back from shared memory) and a complex EPR system (18 slices) on 20 and 24
+    warps (the wide kernel with one row per lane), each against FP64."""
+    from spinach_gb300 import engine as E, workloads as W
+    for w, shapes in ((W.c1(), (224, 288)), (W.c4_small(n_protons=2), (640, 768))):
+        eng = _engine(w)
+        g = [a[:64] for a in W.zcwn_grid(w.n_orient)]
+        r64 = eng.run(*g, w.dt, w.nsteps, precision=E.FP64)
+        for threads in shapes:
+            r = eng.run(*g, w.dt, w.nsteps, precision=E.FP32, fp32_check=False, threads=threads)
+            assert r.stats['threads'] == threads and r.stats['cluster'] == 1, (threads, r.stats['cluster'])
+            assert rel_err(r.fid, r64.fid) <= 1e-5, threads
+        eng.close()
