@@ -99,3 +99,27 @@ def test_forced_shapes_of_the_six_row_and_wide_kernels(engine_lib):
             assert r.stats['threads'] == threads and r.stats['cluster'] == 1, (threads, r.stats['cluster'])
             assert rel_err(r.fid, r64.fid) <= 1e-5, threads
         eng.close()
+
+
+@pytest.mark.parametrize('scale', [1e-4, 1e4])
+def test_packed_cluster_values_at_any_magnitude(engine_lib, scale):
+    """The packed cluster layout stores each value's low part as a half in
+    units set by the system's bound on its entries: the c1 Liouvillian scaled
+    by 1e4 (EPR-sized entries, ~1e9 rad/s) or 1e-4, with the time step scaled
+    the other way, is the same dynamics and must give the same FIDs on 2- and
+    4-CTA clusters as on one CTA."""
+    from spinach_gb300 import engine as E, workloads as W
+    w = W.c1()
+    L = W.build(w)
+    eng = E.Engine(0)
+    eng.upload(L.I * scale, {k: q * scale for k, q in L.terms.items()}, L.R * scale, L.rho0, L.coil)
+    g = [a[:48] for a in W.zcwn_grid(w.n_orient)]
+    dt = w.dt / scale
+    ref = eng.run(*g, dt, w.nsteps, precision=E.FP64)
+    one = eng.run(*g, dt, w.nsteps, precision=E.FP32, fp32_check=False, cluster=1)
+    assert rel_err(one.fid, ref.fid) <= 1e-6
+    for cluster in (2, 4):
+        r = eng.run(*g, dt, w.nsteps, precision=E.FP32, fp32_check=False, cluster=cluster)
+        assert r.stats['cluster'] == cluster and r.stats['real_offdiag'] == 1
+        assert rel_err(r.fid, ref.fid) <= 1e-6, cluster
+    eng.close()
